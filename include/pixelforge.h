@@ -370,9 +370,16 @@ typedef struct {
     PFuint64 rasterized;       /* sub-triangles that survived clip and cull */
     PFuint64 flushes;          /* GPU flushes executed */
     PFuint64 bin_overflows;    /* flushes re-binned because a tile bin overflowed */
+    PFdouble device_ms;        /* with pfEnableTiming: GPU time of the pipeline kernels */
+    PFdouble raster_ms;        /* with pfEnableTiming: GPU time of the tile-raster kernel */
+    PFuint64 raster_launches;  /* tile-raster kernel launches */
+    PFuint64 kernel_launches;  /* all kernels launched by this library */
 } PFstats;
 
 PF_API void pfGetStats(PFstats* stats);
+/* Time the pipeline with CUDA events on the context's stream (adds a few
+ * event records per flush; off by default). */
+PF_API void pfEnableTiming(PFboolean enable);
 PF_API void pfResetStats(void);
 
 /* Device status of the last flush: 0 = no error, otherwise a bit set of

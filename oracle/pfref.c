@@ -1478,6 +1478,7 @@ void pfref_set_fog(const PFhookfog *f) { g_fog = *f; }
 void pfGetStats(PFstats *s) { *s = G->stats; }
 void pfResetStats(void) { memset(&G->stats, 0, sizeof G->stats); }
 PFuint pfGetDeviceStatus(void) { return 0; }
+void pfEnableTiming(PFboolean enable) { (void)enable; }
 
 PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
 {
@@ -1564,6 +1565,9 @@ void *pfGetTexturePixels(const PFtexture tex, PFsizei *w, PFsizei *h, PFpixelfor
 {
     const RTex *x = (const RTex *)tex;
     if (!x) return NULL;
-    if (w) *w = x->w; if (h) *h = x->h; if (f) *f = x->format; if (t) *t = x->type;
+    if (w) *w = x->w;
+    if (h) *h = x->h;
+    if (f) *f = x->format;
+    if (t) *t = x->type;
     return x->pixels;
 }

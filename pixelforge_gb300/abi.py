@@ -33,7 +33,9 @@ class PFframebuffer(C.Structure):
 class PFstats(C.Structure):
     _fields_ = [("fragments", C.c_uint64), ("primitives", C.c_uint64),
                 ("rasterized", C.c_uint64), ("flushes", C.c_uint64),
-                ("bin_overflows", C.c_uint64)]
+                ("bin_overflows", C.c_uint64), ("device_ms", C.c_double),
+                ("raster_ms", C.c_double), ("raster_launches", C.c_uint64),
+                ("kernel_launches", C.c_uint64)]
 
 
 class PFhookfog(C.Structure):
@@ -156,6 +158,8 @@ PROTOTYPES = {
     "pfGetStats": (_V, [C.POINTER(PFstats)]),
     "pfResetStats": (_V, []),
     "pfGetDeviceStatus": (PFuint, []),
+    "pfEnableTiming": (_V, [PFbool]),
+    "pfGetTexturePixels": (PFptr, [PFptr, PFptr, PFptr, PFptr, PFptr]),
 }
 
 

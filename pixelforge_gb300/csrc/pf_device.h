@@ -1,0 +1,52 @@
+/*
+ * pf_device.h -- launchers of the device pipeline (pf_kernels.cu), called by
+ * the host front end (pf_host.cpp).  Internal to libpixelforge_gb300.so.
+ */
+#ifndef PF_DEVICE_H
+#define PF_DEVICE_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "pf_layout.h"
+
+struct PFHookParams {
+    float znear, zfar, start, end;
+    uint32_t color;
+};
+
+/* Device pointers and sizes of one raster batch (a run of draw segments on
+ * one framebuffer). */
+struct PFBatchLaunch {
+    const PFSegment *segs;
+    int nSegs;
+    const PFDrawState *states;
+    PFVertexOut *vout;
+    uint32_t nVerts;
+    uint32_t nItems;
+    PFPrim *prims;            /* nItems records (sub-triangle 0 of each item) */
+    PFPrimPhong *primsPh;
+    PFPrim *pool;             /* clipped sub-triangles >= 1 */
+    PFPrimPhong *poolPh;
+    uint32_t poolCap;
+    uint32_t *clipQueue;      /* nItems entries */
+    uint32_t *clipQueueCount;
+    uint32_t *binCount;       /* tilesX * tilesY */
+    uint32_t *bins;           /* tilesX * tilesY * cap */
+    uint32_t cap;
+    uint32_t *color;
+    float *depth;
+    uint32_t W, H, tilesX, tilesY;
+    PFDevCounters *cnt;
+    uint32_t command;
+};
+
+cudaError_t pfd_launch_vertex(const PFSegment *segs, int nSegs, const PFDrawState *states, PFVertexOut *out,
+                              uint32_t nVerts, const PFDevCounters *cnt, cudaStream_t st);
+cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
+cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);
+cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
+                             const PFDevCounters *cnt, uint32_t command, cudaStream_t st);
+cudaError_t pfd_launch_hook(uint32_t *color, const float *depth, size_t n, int hook, const PFHookParams &hp,
+                            const PFDevCounters *cnt, uint32_t command, cudaStream_t st);
+
+#endif /* PF_DEVICE_H */

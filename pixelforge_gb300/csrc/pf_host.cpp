@@ -1,0 +1,1643 @@
+// pf_host.cpp -- host front end of libpixelforge_gb300.so.
+//
+// Implements the PixelForge C API (include/pixelforge.h) on top of the
+// device pipeline in pf_kernels.cu.  The state machine (matrices, lights,
+// materials, vertex capture, error codes) follows the reference's
+// src/context.c; what changes is *when* primitives are rasterized.  The
+// reference processes each primitive synchronously inside pfVertex /
+// pfDrawElements; here every draw is recorded -- its state snapshotted into
+// a PFDrawState, its vertices and indices copied into one pinned staging
+// block -- and the whole recording is rendered by the GPU at an observation
+// point (pfFinish, pfReadPixels, pfPostProcess, ...).  The recorded order of
+// primitives, face passes and clears is the reference's order, and the tile
+// rasterizer applies fragments per pixel in that order.
+//
+// Built with -ffp-contract=off: the matrix arithmetic must round exactly as
+// the reference's (src/pfm.h) does.
+
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <algorithm>
+#include <unordered_map>
+#include <vector>
+
+#include "pixelforge.h"
+#include "pf_layout.h"
+#include "pf_device.h"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kDeg2Rad = kPi / 180.0;
+constexpr uint32_t kCapMax = 16384;       // largest tile bin the rasterizer sorts in shared memory
+
+// ---------------------------------------------------------------------------
+// matrix arithmetic in the order of src/pfm.h
+// ---------------------------------------------------------------------------
+using Mat = float[16];
+
+void m_identity(float *d) { std::memset(d, 0, 64); d[0] = d[5] = d[10] = d[15] = 1.0f; }
+
+void m_mul(float *dst, const float *l, const float *r)               // pfm.h:2176-2199
+{
+    float res[16];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            float s = 0.0f;
+            for (int k = 0; k < 4; k++) s += l[i * 4 + k] * r[k * 4 + j];
+            res[i * 4 + j] = s;
+        }
+    std::memcpy(dst, res, 64);
+}
+
+void m_invert(float *dst, const float *s)                            // pfm.h:2082-2121
+{
+    float a00 = s[0], a01 = s[1], a02 = s[2], a03 = s[3], a10 = s[4], a11 = s[5], a12 = s[6], a13 = s[7];
+    float a20 = s[8], a21 = s[9], a22 = s[10], a23 = s[11], a30 = s[12], a31 = s[13], a32 = s[14], a33 = s[15];
+    float b00 = a00*a11 - a01*a10, b01 = a00*a12 - a02*a10, b02 = a00*a13 - a03*a10;
+    float b03 = a01*a12 - a02*a11, b04 = a01*a13 - a03*a11, b05 = a02*a13 - a03*a12;
+    float b06 = a20*a31 - a21*a30, b07 = a20*a32 - a22*a30, b08 = a20*a33 - a23*a30;
+    float b09 = a21*a32 - a22*a31, b10 = a21*a33 - a23*a31, b11 = a22*a33 - a23*a32;
+    float inv = 1.0f/(b00*b11 - b01*b10 + b02*b09 + b03*b08 - b04*b07 + b05*b06);
+    float d[16] = {
+        (a11*b11 - a12*b10 + a13*b09)*inv, (-a01*b11 + a02*b10 - a03*b09)*inv,
+        (a31*b05 - a32*b04 + a33*b03)*inv, (-a21*b05 + a22*b04 - a23*b03)*inv,
+        (-a10*b11 + a12*b08 - a13*b07)*inv, (a00*b11 - a02*b08 + a03*b07)*inv,
+        (-a30*b05 + a32*b02 - a33*b01)*inv, (a20*b05 - a22*b02 + a23*b01)*inv,
+        (a10*b10 - a11*b08 + a13*b06)*inv, (-a00*b10 + a01*b08 - a03*b06)*inv,
+        (a30*b04 - a31*b02 + a33*b00)*inv, (-a20*b04 + a21*b02 - a23*b00)*inv,
+        (-a10*b09 + a11*b07 - a12*b06)*inv, (a00*b09 - a01*b07 + a02*b06)*inv,
+        (-a30*b03 + a31*b01 - a32*b00)*inv, (a20*b03 - a21*b01 + a22*b00)*inv };
+    std::memcpy(dst, d, 64);
+}
+
+void m_transpose(float *dst, const float *s)
+{
+    float r[16];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) r[i * 4 + j] = s[j * 4 + i];
+    std::memcpy(dst, r, 64);
+}
+
+void v3_normalize(float *v)                                         // pfm.h:1183-1197
+{
+    float sq = v[0]*v[0] + v[1]*v[1] + v[2]*v[2];
+    if (sq == 0.0f) return;
+    float inv = 1.0f / std::sqrt(sq);
+    for (int i = 0; i < 3; i++) v[i] = v[i] * inv;
+}
+
+// (PFubyte)(float) as the reference's x86-64 build converts it: truncate to
+// int32 (0x80000000 out of range), keep the low 8 bits.
+inline uint8_t ftoub(float x)
+{
+    if (!(x > -2147483649.0f && x < 2147483648.0f)) return 0;
+    return (uint8_t)(uint32_t)(int32_t)x;
+}
+inline uint8_t dtoub(double x)
+{
+    if (!(x > -2147483649.0 && x < 2147483648.0)) return 0;
+    return (uint8_t)(uint32_t)(int32_t)x;
+}
+inline uint32_t pack(PFcolor c) { uint32_t u; std::memcpy(&u, &c, 4); return u; }
+inline PFcolor unpack(uint32_t u) { PFcolor c; std::memcpy(&c, &u, 4); return c; }
+
+// ---------------------------------------------------------------------------
+// objects
+// ---------------------------------------------------------------------------
+struct Tex {
+    void *pixels;
+    PFsizei w, h;
+    PFpixelformat format;
+    PFdatatype type;
+    float tx, ty;
+    int wrap, filter;
+    bool ownsPinned;     // colour of a pfGenFramebuffer framebuffer (pinned host memory)
+};
+
+struct Light {
+    float position[3] = { 0, 0, 0 }, direction[3] = { 0, 0, 0 };
+    float inner = (float)kPi, outer = (float)kPi;
+    float attC = 1, attL = 0, attQ = 0;
+    PFcolor ambient{ 51, 51, 51, 255 }, diffuse{ 255, 255, 255, 255 }, specular{ 255, 255, 255, 255 };
+};
+
+struct Material {
+    PFcolor ambient{ 255, 255, 255, 255 }, diffuse{ 255, 255, 255, 255 };
+    PFcolor specular{ 255, 255, 255, 255 }, emission{ 0, 0, 0, 255 };
+    float shininess = 64.0f;
+};
+
+struct Attrib { const void *buf = nullptr; PFsizei stride = 0; PFint size = 0; PFenum type = 0; };
+
+// Device mirror of one framebuffer (main or pfGenFramebuffer).
+struct FBMirror {
+    Tex *tex = nullptr;
+    float *hostDepth = nullptr;
+    bool depthUserVisible = false;     // pfGenFramebuffer: zbuffer is a public host pointer
+    uint32_t *dColor = nullptr;
+    float *dDepth = nullptr;
+    size_t w = 0, h = 0;
+    bool depthOnDevice = false;        // device depth already holds the authoritative copy
+    void *registered = nullptr;        // host colour registered with cudaHostRegister
+    size_t registeredBytes = 0;
+};
+
+enum CmdKind { CMD_CLEAR, CMD_FILL, CMD_DRAW, CMD_HOOK };
+struct Cmd {
+    CmdKind kind;
+    PFframebuffer *fb;
+    uint32_t color;
+    float depth;
+    int hook;
+    PFHookParams hp;
+    int segBegin, segEnd;              // CMD_DRAW: segments [segBegin, segEnd)
+};
+
+// Segment as recorded on the host: staging offsets instead of pointers.
+struct SegRec {
+    PFSegment seg;                     // pointer fields left null until the flush
+    int64_t recordsOff = -1, posOff = -1, nrmOff = -1, uvOff = -1, colOff = -1, idxOff = -1, itemsOff = -1;
+    std::vector<int32_t> explicitItems;   // immediate / non-triangle modes, grown while recording
+    std::vector<PFVertexIn> records;       // immediate mode vertices
+};
+
+struct StateRec {
+    PFDrawState st;
+    int64_t texOff = -1;
+};
+
+// Pinned host staging block, bump-allocated, uploaded with one copy per flush.
+struct Staging {
+    uint8_t *base = nullptr;
+    size_t cap = 0, used = 0;
+    bool pinned = false;
+    void reserve(size_t need)
+    {
+        if (need <= cap) return;
+        size_t nc = std::max(need, cap ? cap * 2 : (size_t)64 << 20);
+        uint8_t *nb = nullptr;
+        bool np = cudaMallocHost((void **)&nb, nc) == cudaSuccess;
+        if (!np) { cudaGetLastError(); nb = (uint8_t *)std::malloc(nc); }
+        if (base && used) std::memcpy(nb, base, used);
+        release();
+        base = nb; cap = nc; pinned = np;
+    }
+    void release()
+    {
+        if (!base) return;
+        if (pinned) cudaFreeHost(base); else std::free(base);
+        base = nullptr; cap = 0;
+    }
+    int64_t alloc(size_t bytes)
+    {
+        size_t off = (used + 255) & ~(size_t)255;
+        reserve(off + bytes);
+        used = off + bytes;
+        return (int64_t)off;
+    }
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    bool ensure(size_t bytes)
+    {
+        if (bytes <= cap) return true;
+        if (p) cudaFree(p);
+        size_t nc = std::max(bytes, cap + cap / 2);
+        nc = (nc + 4095) & ~(size_t)4095;
+        if (cudaMalloc(&p, nc) != cudaSuccess) { cudaGetLastError(); p = nullptr; cap = 0; return false; }
+        cap = nc;
+        return true;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+
+struct Ctx {
+    PFframebuffer mainFB{ nullptr, nullptr };
+    PFframebuffer *current = nullptr;
+    PFframebuffer *bound = nullptr;
+    Tex *texture = nullptr;
+    void *aux = nullptr;
+
+    PFint vpPos[2]{ 0, 0 }; PFsizei vpDim[2]{ 0, 0 }; PFint vpMin[2]{ 0, 0 }; PFint vpMax[2]{ 0, 0 };
+    Attrib positions, normals, colors, texcoords;
+
+    // immediate-mode capture: the reference's 6-slot vertex buffer (context.c:1658-1685)
+    PFVertexIn slots[6];
+    PFsizei vcount = 0;
+    float curNormal[3]{ 0, 0, 0 }; float curTex[2]{ 0, 0 }; PFcolor curColor{ 255, 255, 255, 255 };
+
+    PFcolor clearColor{ 0, 0, 0, 255 }; float clearDepth = FLT_MAX;
+    PFdrawmode drawMode = PF_POINTS;
+    PFpolygonmode polygonMode[2]{ PF_FILL, PF_FILL };
+    Material mat[2];
+    PFface colMatFace = PF_FRONT_AND_BACK; PFenum colMatMode = PF_AMBIENT_AND_DIFFUSE;
+    Light lights[PF_MAX_LIGHTS];
+    std::vector<int> activeLights;       // insertion order, as the reference's linked list
+
+    Mat proj, tex, model, view, mvp, normal;
+    Mat stackProj[2], stackMV[8], stackTex[4];
+    PFsizei nProj = 0, nMV = 0, nTex = 0;
+    PFmatrixmode matMode = PF_MODELVIEW; bool modelUsed = false;
+    float *cur = nullptr;
+
+    PFshademode shade = PF_SMOOTH; PFlightmode lightMode = PF_GOURAUD; PFface cullFace = PF_BACK;
+    PFblendmode blend = PF_BLEND_ALPHA; PFdepthmode depthFunc = PF_LESS;
+    PFerrcode err = PF_NO_ERROR; PFuint state = PF_CULL_FACE;
+    bool depthMask = true;
+    PFfloat pointSize = 1.0f, lineWidth = 1.0f;
+
+    // recording
+    Staging staging;
+    std::vector<StateRec> states;
+    std::vector<SegRec> segs;
+    std::vector<Cmd> cmds;
+    bool stateDirty = true;
+    int openImmSeg = -1;                 // immediate-mode segment accepting primitives
+    struct SnapKey { const void *p; size_t bytes; int64_t off; };
+    std::vector<SnapKey> snaps;          // dedup of texture / array snapshots in this recording
+
+    // device
+    bool devInit = false, devOk = false;
+    cudaStream_t stream = nullptr;
+    DevBuf arena, vout, prims, primsPh, pool, poolPh, clipQueue, binCount, bins, counters, misc;
+    uint32_t cap = 256, poolCap = 4096;
+    std::unordered_map<const void *, FBMirror> mirrors;     // keyed by framebuffer texture
+    PFDevCounters *hostCounters = nullptr;
+    PFstats stats{};
+    PFuint devStatus = 0;
+    bool timing = false;
+    cudaEvent_t evStart = nullptr, evEnd = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rasterEv;   // per raster launch, reused
+};
+
+thread_local Ctx *G = nullptr;
+
+void set_err(PFerrcode e) { if (G) G->err = e; }
+
+void report_device_failure(const char *what, cudaError_t e)
+{
+    static bool once = false;
+    if (!once) {
+        std::fprintf(stderr, "pixelforge_gb300: %s failed: %s -- nothing is rendered without a CUDA device\n",
+                     what, cudaGetErrorString(e));
+        once = true;
+    }
+}
+
+Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
+{
+    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { set_err(PF_INVALID_ENUM); return nullptr; }
+    Tex *x = new Tex();
+    x->pixels = pixels; x->w = w; x->h = h; x->format = f; x->type = t;
+    x->tx = 1.0f / (float)w; x->ty = 1.0f / (float)h;
+    x->wrap = PF_REPEAT; x->filter = PF_NEAREST; x->ownsPinned = false;
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// recording
+// ---------------------------------------------------------------------------
+// Copy `bytes` of caller memory into staging, reusing an identical snapshot
+// taken earlier in the same recording.
+int64_t snapshot(Ctx *c, const void *p, size_t bytes)
+{
+    for (auto &s : c->snaps)
+        if (s.p == p && s.bytes == bytes && std::memcmp(c->staging.base + s.off, p, bytes) == 0) return s.off;
+    int64_t off = c->staging.alloc(bytes);
+    std::memcpy(c->staging.base + off, p, bytes);
+    c->snaps.push_back({ p, bytes, off });
+    return off;
+}
+
+void update_matrices(Ctx *c, bool withNormal)                      // context.c:96-111
+{
+    if (c->modelUsed) {
+        m_mul(c->mvp, c->model, c->view);
+        m_mul(c->mvp, c->mvp, c->proj);
+        if (withNormal && (c->state & PF_LIGHTING)) { m_invert(c->normal, c->model); m_transpose(c->normal, c->normal); }
+    } else {
+        m_mul(c->mvp, c->view, c->proj);
+        if (withNormal && (c->state & PF_LIGHTING)) m_identity(c->normal);
+    }
+}
+
+// Snapshot the state every primitive of the next segment is processed with.
+int snapshot_state(Ctx *c)
+{
+    StateRec r;
+    PFDrawState &s = r.st;
+    std::memset(&s, 0, sizeof s);
+    std::memcpy(s.mvp, c->mvp, 64);
+    std::memcpy(s.normal, c->normal, 64);
+    const bool lighting = (c->state & PF_LIGHTING) && !c->activeLights.empty();
+    if (lighting) {
+        float inv[16]; m_invert(inv, c->view);                        // triangles.c:84-86
+        s.viewPos[0] = inv[12]; s.viewPos[1] = inv[13]; s.viewPos[2] = inv[14];
+    }
+    s.view8[0] = c->view[8]; s.view8[1] = c->view[9]; s.view8[2] = c->view[10];
+    uint32_t fl = 0;
+    if (lighting) fl |= PFS_LIGHTING;
+    if (lighting && c->lightMode == PF_PHONG) fl |= PFS_PHONG;
+    Tex *t = ((c->state & PF_TEXTURE_2D) && c->texture) ? c->texture : nullptr;
+    if (t) {
+        fl |= PFS_TEXTURE;
+        r.texOff = snapshot(c, t->pixels, (size_t)t->w * t->h * 4);
+        s.texW = t->w; s.texH = t->h; s.texWrap = t->wrap; s.texFilter = t->filter; s.texTx = t->tx; s.texTy = t->ty;
+    }
+    if (c->state & PF_BLEND) fl |= PFS_BLEND;
+    if (c->state & PF_DEPTH_TEST) fl |= PFS_DEPTH_TEST;
+    if (c->depthMask) fl |= PFS_DEPTH_MASK;
+    if (c->shade == PF_SMOOTH) fl |= PFS_SMOOTH;
+    s.flags = fl;
+    s.blendMode = c->blend; s.depthFunc = c->depthFunc;
+    for (int i = 0; i < 2; i++) {
+        s.vpPos[i] = c->vpPos[i]; s.vpDim[i] = c->vpDim[i]; s.vpMin[i] = c->vpMin[i]; s.vpMax[i] = c->vpMax[i];
+    }
+    s.nLights = lighting ? (int)c->activeLights.size() : 0;
+    for (int i = 0; i < s.nLights; i++) {
+        const Light &l = c->lights[c->activeLights[i]];
+        PFDevLight &d = s.lights[i];
+        std::memcpy(d.pos, l.position, 12); std::memcpy(d.dir, l.direction, 12);
+        d.inner = l.inner; d.outer = l.outer; d.attC = l.attC; d.attL = l.attL; d.attQ = l.attQ;
+        d.amb = pack(l.ambient); d.diff = pack(l.diffuse); d.spec = pack(l.specular);
+    }
+    for (int f = 0; f < 2; f++) {
+        s.mat[f].amb = pack(c->mat[f].ambient); s.mat[f].diff = pack(c->mat[f].diffuse);
+        s.mat[f].spec = pack(c->mat[f].specular); s.mat[f].emis = pack(c->mat[f].emission);
+        s.mat[f].shininess = c->mat[f].shininess;
+    }
+    c->states.push_back(r);
+    return (int)c->states.size() - 1;
+}
+
+// Append a DRAW of segment `si` to the command list, merging with the
+// previous DRAW when it targets the same framebuffer.
+void push_draw(Ctx *c, int si)
+{
+    if (!c->cmds.empty() && c->cmds.back().kind == CMD_DRAW && c->cmds.back().fb == c->current &&
+        c->cmds.back().segEnd == si) {
+        c->cmds.back().segEnd = si + 1;
+        return;
+    }
+    Cmd cmd{};
+    cmd.kind = CMD_DRAW; cmd.fb = c->current; cmd.segBegin = si; cmd.segEnd = si + 1;
+    c->cmds.push_back(cmd);
+}
+
+int new_segment(Ctx *c, int srcKind, int itemKind)
+{
+    SegRec r;
+    std::memset(&r.seg, 0, sizeof r.seg);
+    r.seg.state = snapshot_state(c);
+    r.seg.srcKind = srcKind;
+    r.seg.itemKind = itemKind;
+    c->segs.push_back(std::move(r));
+    int si = (int)c->segs.size() - 1;
+    push_draw(c, si);
+    c->stateDirty = false;
+    return si;
+}
+
+// Face passes of one primitive (internal/context/context.c:95-244): returns
+// the faces to fill, in order.
+int faces_for(const Ctx *c, PFdrawmode mode, int faces[2])
+{
+    const bool cull = (c->state & PF_CULL_FACE) != 0;
+    const PFface f = cull ? (PFface)!c->cullFace : PF_FRONT_AND_BACK;
+    const bool usesPolyMode = (mode == PF_TRIANGLES || mode == PF_QUADS);
+    int n = 0;
+    if (f == PF_FRONT_AND_BACK) {
+        for (int i = 0; i < 2; i++)
+            if (!usesPolyMode || c->polygonMode[i] == PF_FILL) faces[n++] = i;
+    } else if (!usesPolyMode || c->polygonMode[f] == PF_FILL) faces[n++] = f;
+    if (usesPolyMode && n < (f == PF_FRONT_AND_BACK ? 2 : 1)) set_err(PF_INVALID_OPERATION);   // point/line modes
+    return n;
+}
+
+// Items of one completed primitive of `mode` whose vertices are the slot
+// sequence positions s[0..count).  Order: the reference's per-face loops
+// (triangles.c:118-152 and internal/context/context.c:104-243).
+void emit_items(std::vector<int32_t> &out, PFdrawmode mode, const uint32_t *s, const int *faces, int nf)
+{
+    auto tri = [&](int a, int b, int d, int face) {
+        out.push_back((int32_t)s[a]); out.push_back((int32_t)s[b]); out.push_back((int32_t)s[d]); out.push_back(face);
+    };
+    auto fan = [&](int face, int n) { for (int i = 0; i < n; i++) tri(0, i + 1, i + 2, face); };
+    auto strip = [&](int face, int n) {
+        for (int i = 0; i < n; i++) { if (i % 2 == 0) tri(i, i + 1, i + 2, face); else tri(i + 2, i + 1, i, face); }
+    };
+    for (int k = 0; k < nf; k++) {
+        switch (mode) {
+        case PF_TRIANGLES: tri(0, 1, 2, faces[k]); break;
+        case PF_TRIANGLE_FAN: case PF_QUADS: fan(faces[k], 2); break;
+        case PF_TRIANGLE_STRIP: strip(faces[k], 2); break;
+        case PF_QUAD_FAN: fan(faces[k], 4); break;
+        case PF_QUAD_STRIP: strip(faces[k], 4); break;
+        default: break;
+        }
+    }
+}
+
+PFsizei mode_count(PFdrawmode m)                                    // context.c:61-74
+{
+    switch (m) {
+    case PF_POINTS: return 1; case PF_LINES: return 2; case PF_TRIANGLES: return 3;
+    case PF_TRIANGLE_FAN: case PF_TRIANGLE_STRIP: case PF_QUADS: return 4;
+    case PF_QUAD_FAN: case PF_QUAD_STRIP: return 6;
+    }
+    return 0;
+}
+
+// After a primitive: which slots carry over (context.c:41-59); returns the
+// new vertex count and moves slot indices in `slot` accordingly.
+template <typename T> PFsizei reset_for_next(PFdrawmode mode, T *slot)
+{
+    switch (mode) {
+    case PF_TRIANGLE_FAN: case PF_TRIANGLE_STRIP: slot[0] = slot[3]; return 1;
+    case PF_QUAD_FAN: case PF_QUAD_STRIP: slot[0] = slot[4]; slot[1] = slot[5]; return 2;
+    default: return 0;
+    }
+}
+
+// pfVertex4fv path: a primitive completed in immediate mode.
+void immediate_primitive(Ctx *c)
+{
+    const PFdrawmode mode = c->drawMode;
+    const PFsizei n = mode_count(mode);
+    if (mode == PF_POINTS || mode == PF_LINES) { set_err(PF_INVALID_OPERATION); return; }
+    int faces[2];
+    const int nf = faces_for(c, mode, faces);
+    if (nf == 0) return;
+    if (c->openImmSeg < 0 || c->stateDirty) c->openImmSeg = new_segment(c, PF_SRC_RECORDS, PF_ITEMS_EXPLICIT);
+    SegRec &r = c->segs[c->openImmSeg];
+    uint32_t s[6];
+    for (PFsizei i = 0; i < n; i++) { s[i] = (uint32_t)r.records.size(); r.records.push_back(c->slots[i]); }
+    emit_items(r.explicitItems, mode, s, faces, nf);
+}
+
+// ---------------------------------------------------------------------------
+// device side
+// ---------------------------------------------------------------------------
+bool device_init(Ctx *c)
+{
+    if (c->devInit) return c->devOk;
+    c->devInit = true;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        report_device_failure("cudaGetDeviceCount", e == cudaSuccess ? cudaErrorNoDevice : e);
+        cudaGetLastError();
+        c->devStatus |= PF_DEVICE_NO_GPU;
+        return false;
+    }
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); c->devStatus |= PF_DEVICE_NO_GPU; return false; }
+    if (!c->counters.ensure(sizeof(PFDevCounters))) { c->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
+    if (cudaMallocHost((void **)&c->hostCounters, sizeof(PFDevCounters)) != cudaSuccess) {
+        cudaGetLastError(); c->devStatus |= PF_DEVICE_ALLOC_FAIL; return false;
+    }
+    c->devOk = true;
+    return true;
+}
+
+FBMirror *mirror_for(Ctx *c, PFframebuffer *fb)
+{
+    Tex *t = (Tex *)fb->texture;
+    FBMirror &m = c->mirrors[t];
+    const size_t w = t->w, h = t->h;
+    if (m.dColor && (m.w != w || m.h != h)) { cudaFree(m.dColor); cudaFree(m.dDepth); m.dColor = nullptr; m.dDepth = nullptr; }
+    if (!m.dColor) {
+        if (cudaMalloc((void **)&m.dColor, w * h * 4) != cudaSuccess ||
+            cudaMalloc((void **)&m.dDepth, w * h * 4) != cudaSuccess) {
+            cudaGetLastError(); c->devStatus |= PF_DEVICE_ALLOC_FAIL; return nullptr;
+        }
+        m.w = w; m.h = h; m.depthOnDevice = false;
+    }
+    m.tex = t;
+    m.hostDepth = fb->zbuffer;
+    m.depthUserVisible = (fb != &c->mainFB);
+    if (m.registered != t->pixels && !t->ownsPinned) {
+        if (m.registered) cudaHostUnregister(m.registered);
+        m.registered = nullptr;
+        if (cudaHostRegister(t->pixels, w * h * 4, cudaHostRegisterDefault) == cudaSuccess) m.registered = t->pixels;
+        else cudaGetLastError();
+    }
+    return &m;
+}
+
+void release_mirrors(Ctx *c)
+{
+    for (auto &kv : c->mirrors) {
+        if (kv.second.registered) cudaHostUnregister(kv.second.registered);
+        if (kv.second.dColor) cudaFree(kv.second.dColor);
+        if (kv.second.dDepth) cudaFree(kv.second.dDepth);
+    }
+    c->mirrors.clear();
+}
+
+void discard_recording(Ctx *c)
+{
+    c->states.clear(); c->segs.clear(); c->cmds.clear(); c->snaps.clear();
+    c->staging.used = 0; c->openImmSeg = -1; c->stateDirty = true;
+}
+
+// Render everything recorded, then write colour (and user-visible depth) back
+// to host memory.  Returns false if the device could not be used.
+bool flush(Ctx *c)
+{
+    if (c->cmds.empty()) { discard_recording(c); return true; }
+    if (!device_init(c)) { set_err(PF_INVALID_OPERATION); discard_recording(c); return false; }
+    cudaStream_t st = c->stream;
+    auto fail = [&](const char *what, cudaError_t e) {
+        report_device_failure(what, e);
+        c->devStatus |= PF_DEVICE_LAUNCH_FAIL;
+        set_err(PF_INVALID_OPERATION);
+        cudaGetLastError();
+        cudaStreamSynchronize(st);
+        discard_recording(c);
+        return false;
+    };
+
+    // --- staging: states, segments and explicit items join the block -------
+    const size_t nStates = c->states.size(), nSegs = c->segs.size();
+    int64_t statesOff = c->staging.alloc(nStates * sizeof(PFDrawState));
+    int64_t segsOff = c->staging.alloc(nSegs * sizeof(PFSegment));
+    for (auto &r : c->segs) {
+        if (!r.records.empty()) {
+            r.recordsOff = c->staging.alloc(r.records.size() * sizeof(PFVertexIn));
+            std::memcpy(c->staging.base + r.recordsOff, r.records.data(), r.records.size() * sizeof(PFVertexIn));
+            r.seg.nVerts = (uint32_t)r.records.size();
+        }
+        if (r.seg.itemKind == PF_ITEMS_EXPLICIT) {
+            r.itemsOff = c->staging.alloc(r.explicitItems.size() * 4 + 16);
+            if (!r.explicitItems.empty())
+                std::memcpy(c->staging.base + r.itemsOff, r.explicitItems.data(), r.explicitItems.size() * 4);
+            r.seg.nItems = (uint32_t)(r.explicitItems.size() / 4);
+        }
+    }
+    const size_t total = c->staging.used;
+    if (!c->arena.ensure(total)) { c->devStatus |= PF_DEVICE_ALLOC_FAIL; return fail("cudaMalloc(arena)", cudaErrorMemoryAllocation); }
+    uint8_t *dbase = (uint8_t *)c->arena.p;
+    auto dptr = [&](int64_t off) -> const void * { return off < 0 ? nullptr : (const void *)(dbase + off); };
+    PFDrawState *hs = (PFDrawState *)(c->staging.base + statesOff);
+    for (size_t i = 0; i < nStates; i++) {
+        hs[i] = c->states[i].st;
+        hs[i].tex = (const uint32_t *)dptr(c->states[i].texOff);
+    }
+    PFSegment *hseg = (PFSegment *)(c->staging.base + segsOff);
+    for (size_t i = 0; i < nSegs; i++) {
+        SegRec &r = c->segs[i];
+        PFSegment s = r.seg;
+        s.records = (const PFVertexIn *)dptr(r.recordsOff);
+        s.pos = (const float *)dptr(r.posOff);
+        s.nrm = (const float *)dptr(r.nrmOff);
+        s.uv = (const float *)dptr(r.uvOff);
+        s.col = (const uint8_t *)dptr(r.colOff);
+        s.idx = (const uint32_t *)dptr(r.idxOff);
+        s.explicitItems = (const int32_t *)dptr(r.itemsOff);
+        hseg[i] = s;
+    }
+    // --- scratch sizing -------------------------------------------------------
+    uint32_t maxVerts = 0, maxItems = 0, maxTiles = 0;
+    bool anyPhong = false;
+    for (auto &cmd : c->cmds) {
+        if (cmd.kind != CMD_DRAW) continue;
+        uint32_t v = 0, it = 0;
+        for (int si = cmd.segBegin; si < cmd.segEnd; si++) {
+            hseg[si].vtxBase = v; hseg[si].itemBase = it;
+            v += hseg[si].nVerts; it += hseg[si].nItems;
+            if (hs[hseg[si].state].flags & PFS_PHONG) anyPhong = true;
+        }
+        Tex *t = (Tex *)cmd.fb->texture;
+        uint32_t tiles = ((t->w + PF_TILE - 1) / PF_TILE) * ((t->h + PF_TILE - 1) / PF_TILE);
+        maxVerts = std::max(maxVerts, v); maxItems = std::max(maxItems, it); maxTiles = std::max(maxTiles, tiles);
+    }
+
+    cudaError_t e = cudaMemcpyAsync(dbase, c->staging.base, total, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail("cudaMemcpyAsync(staging)", e);
+    const PFDrawState *dStates = (const PFDrawState *)(dbase + statesOff);
+
+    // --- framebuffers used: bring host content to the device ----------------
+    std::vector<PFframebuffer *> used;
+    for (auto &cmd : c->cmds)
+        if (std::find(used.begin(), used.end(), cmd.fb) == used.end()) used.push_back(cmd.fb);
+    for (PFframebuffer *fb : used) {
+        FBMirror *m = mirror_for(c, fb);
+        if (!m) return fail("cudaMalloc(framebuffer)", cudaErrorMemoryAllocation);
+        const size_t n = m->w * m->h;
+        const Cmd *first = nullptr;
+        for (auto &cmd : c->cmds) if (cmd.fb == fb) { first = &cmd; break; }
+        const bool uploadDepth = m->depthUserVisible || !m->depthOnDevice;
+        if (first->kind == CMD_FILL) {
+            // every pixel is overwritten first
+        } else if (first->kind == CMD_CLEAR) {
+            // the clear leaves pixels 0..7 and reads pixel 0 for the tail
+            const size_t k = std::min<size_t>(8, n);
+            cudaMemcpyAsync(m->dColor, m->tex->pixels, k * 4, cudaMemcpyHostToDevice, st);
+            if (uploadDepth) cudaMemcpyAsync(m->dDepth, m->hostDepth, k * 4, cudaMemcpyHostToDevice, st);
+        } else {
+            cudaMemcpyAsync(m->dColor, m->tex->pixels, n * 4, cudaMemcpyHostToDevice, st);
+            if (uploadDepth) cudaMemcpyAsync(m->dDepth, m->hostDepth, n * 4, cudaMemcpyHostToDevice, st);
+        }
+        m->depthOnDevice = true;
+    }
+
+    PFDevCounters *dcnt = (PFDevCounters *)c->counters.p;
+    uint32_t startCmd = 0;
+    for (int attempt = 0;; attempt++) {
+        if (!c->vout.ensure((size_t)maxVerts * sizeof(PFVertexOut) + 64) ||
+            !c->prims.ensure((size_t)maxItems * sizeof(PFPrim) + 128) ||
+            !c->primsPh.ensure(anyPhong ? (size_t)maxItems * sizeof(PFPrimPhong) + 128 : 128) ||
+            !c->pool.ensure((size_t)c->poolCap * sizeof(PFPrim)) ||
+            !c->poolPh.ensure(anyPhong ? (size_t)c->poolCap * sizeof(PFPrimPhong) : 128) ||
+            !c->clipQueue.ensure((size_t)maxItems * 4 + 64) ||
+            !c->binCount.ensure((size_t)maxTiles * 4 + 64) ||
+            !c->bins.ensure((size_t)maxTiles * c->cap * 4 + 64) ||
+            !c->misc.ensure(64)) {
+            c->devStatus |= PF_DEVICE_ALLOC_FAIL;
+            return fail("cudaMalloc(scratch)", cudaErrorMemoryAllocation);
+        }
+        // counters: abortCommand = none
+        PFDevCounters init{};
+        init.abortCommand = 0xffffffffu;
+        *c->hostCounters = init;
+        e = cudaMemcpyAsync(dcnt, c->hostCounters, sizeof(PFDevCounters), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return fail("cudaMemcpyAsync(counters)", e);
+
+        size_t nRaster = 0;
+        if (c->timing) {
+            if (!c->evStart) { cudaEventCreate(&c->evStart); cudaEventCreate(&c->evEnd); }
+            cudaEventRecord(c->evStart, st);
+        }
+        for (size_t ci = startCmd; ci < c->cmds.size(); ci++) {
+            const Cmd &cmd = c->cmds[ci];
+            FBMirror *m = &c->mirrors[(Tex *)cmd.fb->texture];
+            const size_t n = m->w * m->h;
+            c->stats.kernel_launches += (cmd.kind == CMD_DRAW) ? 4 : 1;
+            if (cmd.kind == CMD_CLEAR || cmd.kind == CMD_FILL) {
+                e = pfd_launch_clear(m->dColor, m->dDepth, n, cmd.color, cmd.depth, cmd.kind == CMD_FILL, dcnt, (uint32_t)ci, st);
+            } else if (cmd.kind == CMD_HOOK) {
+                e = pfd_launch_hook(m->dColor, m->dDepth, n, cmd.hook, cmd.hp, dcnt, (uint32_t)ci, st);
+            } else {
+                const PFSegment *dsegs = (const PFSegment *)(dbase + segsOff) + cmd.segBegin;
+                const int ns = cmd.segEnd - cmd.segBegin;
+                const PFSegment &lastSeg = hseg[cmd.segEnd - 1];
+                const uint32_t nV = lastSeg.vtxBase + lastSeg.nVerts, nI = lastSeg.itemBase + lastSeg.nItems;
+                PFBatchLaunch L{};
+                L.segs = dsegs; L.nSegs = ns; L.states = dStates;
+                L.vout = (PFVertexOut *)c->vout.p; L.nVerts = nV; L.nItems = nI;
+                L.prims = (PFPrim *)c->prims.p; L.primsPh = (PFPrimPhong *)c->primsPh.p;
+                L.pool = (PFPrim *)c->pool.p; L.poolPh = (PFPrimPhong *)c->poolPh.p; L.poolCap = c->poolCap;
+                L.clipQueue = (uint32_t *)c->clipQueue.p; L.clipQueueCount = (uint32_t *)c->misc.p;
+                L.binCount = (uint32_t *)c->binCount.p; L.bins = (uint32_t *)c->bins.p; L.cap = c->cap;
+                L.color = m->dColor; L.depth = m->dDepth;
+                L.W = (uint32_t)m->w; L.H = (uint32_t)m->h;
+                L.tilesX = (L.W + PF_TILE - 1) / PF_TILE; L.tilesY = (L.H + PF_TILE - 1) / PF_TILE;
+                L.cnt = dcnt; L.command = (uint32_t)ci;
+                e = pfd_launch_vertex(L.segs, ns, dStates, L.vout, nV, dcnt, st);
+                if (e == cudaSuccess) e = cudaMemsetAsync(L.binCount, 0, (size_t)L.tilesX * L.tilesY * 4, st);
+                if (e == cudaSuccess) e = cudaMemsetAsync(L.clipQueueCount, 0, 4, st);
+                if (e == cudaSuccess) e = cudaMemsetAsync(&dcnt->clipCount, 0, 4, st);
+                if (e == cudaSuccess) e = cudaMemsetAsync(&dcnt->batchRasterized, 0, 8, st);
+                if (e == cudaSuccess) e = pfd_launch_items(L, st);
+                if (c->timing) {
+                    if (c->rasterEv.size() <= nRaster) {
+                        cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b);
+                        c->rasterEv.push_back({ a, b });
+                    }
+                    cudaEventRecord(c->rasterEv[nRaster].first, st);
+                }
+                if (e == cudaSuccess) e = pfd_launch_raster(L, st);
+                if (c->timing) cudaEventRecord(c->rasterEv[nRaster].second, st);
+                nRaster++;
+            }
+            if (e != cudaSuccess) return fail("kernel launch", e);
+        }
+        if (c->timing) cudaEventRecord(c->evEnd, st);
+        e = cudaMemcpyAsync(c->hostCounters, dcnt, sizeof(PFDevCounters), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail("pipeline", e);
+        if (c->timing) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, c->evStart, c->evEnd);
+            c->stats.device_ms += ms;
+            for (size_t k = 0; k < nRaster; k++) {
+                cudaEventElapsedTime(&ms, c->rasterEv[k].first, c->rasterEv[k].second);
+                c->stats.raster_ms += ms;
+            }
+        }
+        c->stats.raster_launches += nRaster;
+        const PFDevCounters hc = *c->hostCounters;
+        if (hc.abortCommand == 0xffffffffu) {
+            c->stats.fragments += hc.fragments;
+            c->stats.rasterized += hc.rasterized;
+            break;
+        }
+        // A bin or the clip pool overflowed in command hc.abortCommand.  The
+        // commands before it completed; it and every later one wrote nothing
+        // to any framebuffer.  Grow the capacity and resume from it.
+        c->stats.fragments += hc.fragments;
+        c->stats.rasterized += hc.rasterized;
+        c->stats.bin_overflows += 1;
+        if (hc.status & PFD_BIN_OVERFLOW) {
+            uint32_t need = std::max(hc.maxBin, c->cap * 2);
+            uint32_t nc = 1; while (nc < need) nc <<= 1;
+            if (nc > kCapMax) {
+                c->devStatus |= PF_DEVICE_BIN_LIMIT;
+                return fail("tile bin capacity", cudaErrorMemoryAllocation);
+            }
+            c->cap = nc;
+        }
+        if (hc.status & PFD_CLIP_OVERFLOW) c->poolCap = std::max(c->poolCap * 4, hc.clipCount * 2);
+        if (attempt > 8) return fail("overflow retries", cudaErrorUnknown);
+        startCmd = hc.abortCommand;
+    }
+
+    // --- write back -------------------------------------------------------------
+    for (PFframebuffer *fb : used) {
+        FBMirror *m = &c->mirrors[(Tex *)fb->texture];
+        const size_t n = m->w * m->h;
+        e = cudaMemcpyAsync(m->tex->pixels, m->dColor, n * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && m->depthUserVisible)
+            e = cudaMemcpyAsync(m->hostDepth, m->dDepth, n * 4, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return fail("cudaMemcpyAsync(write-back)", e);
+    }
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail("write-back", e);
+    c->stats.flushes += 1;
+    discard_recording(c);
+    return true;
+}
+
+// Bring the main framebuffer's internal depth back to the host (it stays on
+// the device otherwise: the reference exposes it only to pfPostProcess).
+void pull_main_depth(Ctx *c)
+{
+    auto it = c->mirrors.find(c->mainFB.texture);
+    if (it == c->mirrors.end() || !it->second.depthOnDevice) return;
+    FBMirror &m = it->second;
+    cudaMemcpy(m.hostDepth, m.dDepth, m.w * m.h * 4, cudaMemcpyDeviceToHost);
+    m.depthOnDevice = false;    // host copy authoritative again
+}
+
+void sync_host(Ctx *c) { flush(c); }
+
+}  // namespace
+
+// ===========================================================================
+// C API
+// ===========================================================================
+extern "C" {
+
+PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
+{
+    Ctx *c = new Ctx();
+    Ctx *prev = G; G = c;
+    c->mainFB.texture = tex_new(buf, w, h, f, t);
+    G = prev;
+    if (!c->mainFB.texture) { delete c; return nullptr; }
+    c->mainFB.zbuffer = (float *)std::malloc((size_t)w * h * sizeof(float));
+    if (!c->mainFB.zbuffer) { delete (Tex *)c->mainFB.texture; delete c; return nullptr; }
+    for (size_t i = 0; i < (size_t)w * h; i++) c->mainFB.zbuffer[i] = FLT_MAX;
+    c->current = &c->mainFB;
+    c->vpDim[0] = w - 1; c->vpMax[0] = (PFint)w - 1;
+    c->vpDim[1] = h - 1; c->vpMax[1] = (PFint)h - 1;
+    std::memset(c->proj, 0, 64);                                     // pfmMat4Ortho(-1,1,-1,1,-1,1)
+    c->proj[0] = 2.0f / 2.0f; c->proj[5] = 2.0f / 2.0f; c->proj[10] = -2.0f / 2.0f;
+    c->proj[12] = -(-1.0f + 1.0f) / 2.0f; c->proj[13] = -(1.0f + -1.0f) / 2.0f;
+    c->proj[14] = -(1.0f + -1.0f) / 2.0f; c->proj[15] = 1.0f;
+    m_identity(c->tex); m_identity(c->normal); m_identity(c->model); m_identity(c->view); m_identity(c->mvp);
+    c->cur = c->view;
+    std::memset(c->slots, 0, sizeof c->slots);
+    return c;
+}
+
+void pfDeleteContext(PFcontext ctx)
+{
+    Ctx *c = (Ctx *)ctx;
+    if (!c) return;
+    Ctx *prev = G; G = c;
+    flush(c);
+    G = (prev == c) ? nullptr : prev;
+    release_mirrors(c);
+    if (c->devOk) {
+        c->arena.release(); c->vout.release(); c->prims.release(); c->primsPh.release(); c->pool.release();
+        c->poolPh.release(); c->clipQueue.release(); c->binCount.release(); c->bins.release();
+        c->counters.release(); c->misc.release();
+        if (c->hostCounters) cudaFreeHost(c->hostCounters);
+        if (c->evStart) { cudaEventDestroy(c->evStart); cudaEventDestroy(c->evEnd); }
+        for (auto &pr : c->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        if (c->stream) cudaStreamDestroy(c->stream);
+    }
+    c->staging.release();
+    std::free(c->mainFB.zbuffer);
+    delete (Tex *)c->mainFB.texture;
+    delete c;
+}
+
+void pfSetMainBuffer(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
+{
+    if (!buf || !w || !h) { G->err = PF_INVALID_VALUE; return; }
+    flush(G);
+    pull_main_depth(G);
+    Tex *old = (Tex *)G->mainFB.texture;
+    if (old->w != w || old->h != h) {
+        std::free(G->mainFB.zbuffer);
+        G->mainFB.zbuffer = (float *)std::malloc((size_t)w * h * sizeof(float));
+        for (size_t i = 0; i < (size_t)w * h; i++) G->mainFB.zbuffer[i] = G->clearDepth;
+    }
+    auto it = G->mirrors.find(old);
+    if (it != G->mirrors.end()) {
+        if (it->second.registered) cudaHostUnregister(it->second.registered);
+        if (it->second.dColor) cudaFree(it->second.dColor);
+        if (it->second.dDepth) cudaFree(it->second.dDepth);
+        G->mirrors.erase(it);
+    }
+    delete old;
+    G->mainFB.texture = tex_new(buf, w, h, f, t);
+    G->aux = nullptr;
+}
+
+void pfSetAuxBuffer(void *aux) { G->aux = aux; }
+
+void pfSwapBuffers(void)
+{
+    if (!G->aux) { G->err = PF_INVALID_OPERATION; return; }
+    flush(G);
+    Tex *t = (Tex *)G->current->texture;
+    void *tmp = t->pixels; t->pixels = G->aux; G->aux = tmp;
+}
+
+PFcontext pfGetCurrentContext(void) { return G; }
+
+void pfMakeCurrent(PFcontext ctx)
+{
+    if (G && G != (Ctx *)ctx) flush(G);
+    G = (Ctx *)ctx;
+}
+
+PFboolean pfIsEnabled(PFstate s) { return (G->state & s) != 0; }
+void pfEnable(PFstate s)
+{
+    G->state |= s; G->stateDirty = true;
+    if (s & PF_FRAMEBUFFER) G->current = G->bound ? G->bound : &G->mainFB;
+}
+void pfDisable(PFstate s)
+{
+    G->state &= ~(PFuint)s; G->stateDirty = true;
+    if (s & PF_FRAMEBUFFER) G->current = &G->mainFB;
+}
+
+PFerrcode pfGetError(void) { PFerrcode e = G->err; G->err = PF_NO_ERROR; return e; }
+
+void pfGetBooleanv(PFenum p, PFboolean *v)                            // getter.c:24-113
+{
+    switch (p) {
+    case PF_TEXTURE_2D: case PF_FRAMEBUFFER: case PF_BLEND: case PF_DEPTH_TEST: case PF_CULL_FACE:
+    case PF_NORMALIZE: case PF_LIGHTING: case PF_COLOR_MATERIAL: case PF_VERTEX_ARRAY: case PF_NORMAL_ARRAY:
+    case PF_COLOR_ARRAY: case PF_TEXTURE_COORD_ARRAY:
+        *v = (G->state & p) != 0; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfGetIntegerv(PFenum p, PFint *v)
+{
+    switch (p) {
+    case PF_VIEWPORT: v[0] = G->vpPos[0]; v[1] = G->vpPos[1]; v[2] = (PFint)G->vpDim[0] + 1; v[3] = (PFint)G->vpDim[1] + 1; break;
+    case PF_BLEND_FUNC: v[0] = G->blend; break;
+    case PF_DEPTH_FUNC: v[0] = G->depthFunc; break;
+    case PF_CULL_FACE_MODE: v[0] = G->cullFace; break;
+    case PF_SHADE_MODEL: v[0] = G->shade; break;
+    case PF_MATRIX_MODE: v[0] = G->matMode; break;
+    case PF_POLYGON_MODE: v[0] = G->polygonMode[0]; v[1] = G->polygonMode[1]; break;
+    case PF_MAX_LIGHTS: v[0] = PF_MAX_LIGHTS; break;
+    case PF_MAX_PROJECTION_STACK_DEPTH: v[0] = 2; break;
+    case PF_MAX_MODELVIEW_STACK_DEPTH: v[0] = 8; break;
+    case PF_MAX_TEXTURE_STACK_DEPTH: v[0] = 4; break;
+    case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r; v[1] = G->clearColor.g; v[2] = G->clearColor.b; v[3] = G->clearColor.a; break;
+    case PF_CURRENT_COLOR: v[0] = G->curColor.r; v[1] = G->curColor.g; v[2] = G->curColor.b; v[3] = G->curColor.a; break;
+    case PF_VERTEX_ARRAY_SIZE: v[0] = G->positions.size; break;
+    case PF_VERTEX_ARRAY_STRIDE: v[0] = (PFint)G->positions.stride; break;
+    case PF_VERTEX_ARRAY_TYPE: v[0] = (PFint)G->positions.type; break;
+    case PF_NORMAL_ARRAY_STRIDE: v[0] = (PFint)G->normals.stride; break;
+    case PF_NORMAL_ARRAY_TYPE: v[0] = (PFint)G->normals.type; break;
+    case PF_TEXTURE_COORD_ARRAY_STRIDE: v[0] = (PFint)G->texcoords.stride; break;
+    case PF_TEXTURE_COORD_ARRAY_TYPE: v[0] = (PFint)G->texcoords.type; break;
+    case PF_COLOR_ARRAY_SIZE: v[0] = G->colors.size; break;
+    case PF_COLOR_ARRAY_STRIDE: v[0] = (PFint)G->colors.stride; break;
+    case PF_COLOR_ARRAY_TYPE: v[0] = (PFint)G->colors.type; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfGetFloatv(PFenum p, PFfloat *v)
+{
+    switch (p) {
+    case PF_DEPTH_CLEAR_VALUE: v[0] = G->clearDepth; break;
+    case PF_POINT_SIZE: v[0] = G->pointSize; break;
+    case PF_LINE_WIDTH: v[0] = G->lineWidth; break;
+    case PF_CURRENT_NORMAL: std::memcpy(v, G->curNormal, 12); break;
+    case PF_CURRENT_TEXTURE_COORDS: std::memcpy(v, G->curTex, 8); break;
+    case PF_PROJECTION_MATRIX: std::memcpy(v, G->proj, 64); break;
+    case PF_MODELVIEW_MATRIX: std::memcpy(v, G->modelUsed ? G->model : G->view, 64); break;
+    case PF_TEXTURE_MATRIX: std::memcpy(v, G->tex, 64); break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfGetDoublev(PFenum p, PFdouble *v)
+{
+    float f[16];
+    int n = (p == PF_PROJECTION_MATRIX || p == PF_MODELVIEW_MATRIX || p == PF_TEXTURE_MATRIX) ? 16 :
+            (p == PF_CURRENT_NORMAL) ? 3 : (p == PF_CURRENT_TEXTURE_COORDS) ? 2 : 1;
+    PFerrcode before = G->err; G->err = PF_NO_ERROR;
+    pfGetFloatv(p, f);
+    if (G->err != PF_NO_ERROR) return;
+    G->err = before;
+    for (int i = 0; i < n; i++) v[i] = f[i];
+}
+void pfGetPointerv(PFenum p, const void **v)                          // getter.c:493-521
+{
+    switch (p) {
+    case PF_TEXTURE_2D: *v = G->texture; break;
+    case PF_FRAMEBUFFER: *v = G->bound; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+
+// --- matrices (context.c:392-548) -------------------------------------------
+void pfMatrixMode(PFmatrixmode m)
+{
+    switch (m) {
+    case PF_PROJECTION: G->cur = G->proj; break;
+    case PF_MODELVIEW: G->cur = G->modelUsed ? G->model : G->view; break;
+    case PF_TEXTURE: G->cur = G->tex; break;
+    default: G->err = PF_INVALID_ENUM; return;
+    }
+    G->matMode = m;
+}
+void pfPushMatrix(void)
+{
+    switch (G->matMode) {
+    case PF_PROJECTION:
+        if (G->nProj >= 2) { G->err = PF_STACK_OVERFLOW; return; }
+        std::memcpy(G->stackProj[G->nProj++], G->proj, 64); break;
+    case PF_MODELVIEW:
+        if (G->nMV >= 8) { G->err = PF_STACK_OVERFLOW; return; }
+        if (G->modelUsed) std::memcpy(G->stackMV[G->nMV++], G->model, 64);
+        else { G->cur = G->model; G->modelUsed = true; }
+        break;
+    case PF_TEXTURE:
+        if (G->nTex >= 4) { G->err = PF_STACK_OVERFLOW; return; }
+        std::memcpy(G->stackTex[G->nTex++], G->tex, 64); break;
+    }
+}
+void pfPopMatrix(void)
+{
+    switch (G->matMode) {
+    case PF_PROJECTION:
+        if (G->nProj == 0) { G->err = PF_STACK_UNDERFLOW; return; }
+        std::memcpy(G->proj, G->stackProj[--G->nProj], 64); break;
+    case PF_MODELVIEW:
+        if (G->nMV == 0) {
+            if (!G->modelUsed) { G->err = PF_STACK_UNDERFLOW; return; }
+            m_identity(G->model); G->modelUsed = false; G->cur = G->view;
+        } else std::memcpy(G->model, G->stackMV[--G->nMV], 64);
+        break;
+    case PF_TEXTURE:
+        if (G->nTex == 0) { G->err = PF_STACK_UNDERFLOW; return; }
+        std::memcpy(G->tex, G->stackTex[--G->nTex], 64); break;
+    }
+}
+void pfLoadIdentity(void) { m_identity(G->cur); G->stateDirty = true; }
+void pfTranslatef(PFfloat x, PFfloat y, PFfloat z)
+{
+    float t[16]; m_identity(t); t[12] = x; t[13] = y; t[14] = z;
+    m_mul(G->cur, t, G->cur); G->stateDirty = true;
+}
+void pfRotatef(PFfloat angle, PFfloat x, PFfloat y, PFfloat z)        // pfm.h:2227-2262
+{
+    float a = (float)(angle * kDeg2Rad);
+    float r[16]; m_identity(r);
+    float lsq = x*x + y*y + z*z;
+    if (lsq != 1.0f && lsq != 0.0f) { float il = 1.0f / std::sqrt(lsq); x *= il; y *= il; z *= il; }
+    float s = sinf(a), co = cosf(a), t = 1.0f - co;
+    r[0] = x*x*t + co; r[1] = y*x*t + z*s; r[2] = z*x*t - y*s;
+    r[4] = x*y*t - z*s; r[5] = y*y*t + co; r[6] = z*y*t + x*s;
+    r[8] = x*z*t + y*s; r[9] = y*z*t - x*s; r[10] = z*z*t + co;
+    m_mul(G->cur, r, G->cur); G->stateDirty = true;
+}
+void pfScalef(PFfloat x, PFfloat y, PFfloat z)
+{
+    float s[16]; std::memset(s, 0, 64); s[0] = x; s[5] = y; s[10] = z; s[15] = 1.0f;
+    m_mul(G->cur, s, G->cur); G->stateDirty = true;
+}
+void pfMultMatrixf(const PFfloat *m) { m_mul(G->cur, G->cur, m); G->stateDirty = true; }
+void pfFrustum(PFfloat l, PFfloat r, PFfloat b, PFfloat t, PFfloat n, PFfloat f)   // pfm.h:2375-2393
+{
+    float m[16]; std::memset(m, 0, 64);
+    float rl = r - l, tb = t - b, fn = f - n;
+    m[0] = (n*2.0f)/rl; m[5] = (n*2.0f)/tb; m[8] = (r + l)/rl; m[9] = (t + b)/tb;
+    m[10] = -(f + n)/fn; m[11] = -1.0f; m[14] = -(f*n*2.0f)/fn;
+    m_mul(G->cur, G->cur, m); G->stateDirty = true;
+}
+void pfOrtho(PFfloat l, PFfloat r, PFfloat b, PFfloat t, PFfloat n, PFfloat f)     // pfm.h:2422-2440
+{
+    float m[16]; std::memset(m, 0, 64);
+    float rl = r - l, tb = t - b, fn = f - n;
+    m[0] = 2.0f/rl; m[5] = 2.0f/tb; m[10] = -2.0f/fn;
+    m[12] = -(l + r)/rl; m[13] = -(t + b)/tb; m[14] = -(f + n)/fn; m[15] = 1.0f;
+    m_mul(G->cur, G->cur, m); G->stateDirty = true;
+}
+
+// --- render configuration (context.c:553-797) --------------------------------
+void pfViewport(PFint x, PFint y, PFsizei w, PFsizei h)
+{
+    if (x <= -(PFint)w || y <= -(PFint)h) { G->err = PF_INVALID_OPERATION; return; }
+    Tex *mt = (Tex *)G->mainFB.texture;
+    G->vpPos[0] = x; G->vpPos[1] = y; G->vpDim[0] = w - 1; G->vpDim[1] = h - 1;
+    G->vpMin[0] = std::max(x, 0); G->vpMin[1] = std::max(y, 0);
+    G->vpMax[0] = (PFint)std::min((PFsizei)(x + (PFint)w), mt->w - 1);
+    G->vpMax[1] = (PFint)std::min((PFsizei)(y + (PFint)h), mt->h - 1);
+    G->stateDirty = true;
+}
+void pfPolygonMode(PFface f, PFpolygonmode m)
+{
+    if (!(m == PF_POINT || m == PF_LINE || m == PF_FILL)) { G->err = PF_INVALID_ENUM; return; }
+    switch (f) {
+    case PF_FRONT: G->polygonMode[0] = m; break;
+    case PF_BACK: G->polygonMode[1] = m; break;
+    case PF_FRONT_AND_BACK: G->polygonMode[0] = G->polygonMode[1] = m; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfShadeModel(PFshademode m) { G->shade = m; G->stateDirty = true; }
+void pfLightModel(PFlightmode m) { G->lightMode = m; G->stateDirty = true; }
+void pfLineWidth(PFfloat w) { if (w <= 0.0f) { G->err = PF_INVALID_VALUE; return; } G->lineWidth = w; }
+void pfPointSize(PFfloat s) { if (s <= 0.0f) { G->err = PF_INVALID_VALUE; return; } G->pointSize = s; }
+void pfCullFace(PFface f)
+{
+    if (f < PF_FRONT || f > PF_BACK) { G->err = PF_INVALID_ENUM; return; }
+    G->cullFace = f;
+}
+void pfBlendFunc(PFblendmode m)
+{
+    if (m < PF_BLEND_AVERAGE || m > PF_BLEND_DARKEN) { G->err = PF_INVALID_ENUM; return; }
+    G->blend = m; G->stateDirty = true;
+}
+void pfDepthFunc(PFdepthmode m)
+{
+    if (m < PF_EQUAL || m > PF_GEQUAL) { G->err = PF_INVALID_ENUM; return; }
+    G->depthFunc = m; G->stateDirty = true;
+}
+void pfDepthMask(PFboolean f) { G->depthMask = f; G->stateDirty = true; }
+void pfBindFramebuffer(PFframebuffer *fb)
+{
+    G->bound = fb;
+    if (G->state & PF_FRAMEBUFFER) G->current = fb ? fb : &G->mainFB;
+    G->stateDirty = true;
+}
+void pfBindTexture(PFtexture t) { G->texture = (Tex *)t; G->stateDirty = true; }
+
+void pfClear(PFclearflag flag)
+{
+    if (!flag) return;
+    Cmd cmd{};
+    cmd.kind = CMD_CLEAR; cmd.fb = G->current; cmd.color = pack(G->clearColor); cmd.depth = G->clearDepth;
+    G->cmds.push_back(cmd);
+    G->openImmSeg = -1;
+}
+void pfClearDepth(PFfloat d) { G->clearDepth = d; }
+void pfClearColor(PFubyte r, PFubyte g, PFubyte b, PFubyte a) { G->clearColor = PFcolor{ r, g, b, a }; }
+
+// --- lights and materials (context.c:802-1156) --------------------------------
+void pfEnableLight(PFsizei l)
+{
+    if (l >= PF_MAX_LIGHTS) { G->err = PF_INVALID_VALUE; return; }
+    for (int a : G->activeLights) if (a == (int)l) { G->err = PF_INVALID_OPERATION; return; }
+    G->activeLights.push_back((int)l); G->stateDirty = true;
+}
+void pfDisableLight(PFsizei l)
+{
+    if (l >= PF_MAX_LIGHTS) { G->err = PF_INVALID_VALUE; return; }
+    auto it = std::find(G->activeLights.begin(), G->activeLights.end(), (int)l);
+    if (it == G->activeLights.end()) { G->err = PF_INVALID_OPERATION; return; }
+    G->activeLights.erase(it); G->stateDirty = true;
+}
+PFboolean pfIsEnabledLight(PFsizei l)
+{
+    if (l >= PF_MAX_LIGHTS) { G->err = PF_INVALID_VALUE; return PF_FALSE; }
+    return std::find(G->activeLights.begin(), G->activeLights.end(), (int)l) != G->activeLights.end();
+}
+static PFcolor f3_color(const float *v) { return PFcolor{ ftoub(v[0]*255.0f), ftoub(v[1]*255.0f), ftoub(v[2]*255.0f), 255 }; }
+static bool cutoff_ok(float v) { return (v >= 0 && v <= 90) || v == 180; }
+void pfLightf(PFsizei li, PFenum p, PFfloat v)
+{
+    if (li >= PF_MAX_LIGHTS) { G->err = PF_STACK_OVERFLOW; return; }
+    Light &l = G->lights[li];
+    switch (p) {
+    case PF_SPOT_INNER_CUTOFF: if (cutoff_ok(v)) l.inner = cosf((float)(v * kDeg2Rad)); else G->err = PF_INVALID_VALUE; break;
+    case PF_SPOT_OUTER_CUTOFF: if (cutoff_ok(v)) l.outer = cosf((float)(v * kDeg2Rad)); else G->err = PF_INVALID_VALUE; break;
+    case PF_CONSTANT_ATTENUATION: l.attC = v; break;
+    case PF_LINEAR_ATTENUATION: l.attL = v; break;
+    case PF_QUADRATIC_ATTENUATION: l.attQ = v; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+    G->stateDirty = true;
+}
+void pfLightfv(PFsizei li, PFenum p, const void *value)
+{
+    if (li >= PF_MAX_LIGHTS) { G->err = PF_STACK_OVERFLOW; return; }
+    Light &l = G->lights[li];
+    const float *v = (const float *)value;
+    switch (p) {
+    case PF_POSITION: std::memcpy(l.position, v, 12); break;
+    case PF_SPOT_DIRECTION: std::memcpy(l.direction, v, 12); break;
+    case PF_SPOT_INNER_CUTOFF: case PF_SPOT_OUTER_CUTOFF: case PF_CONSTANT_ATTENUATION:
+    case PF_LINEAR_ATTENUATION: case PF_QUADRATIC_ATTENUATION: pfLightf(li, p, v[0]); break;
+    case PF_AMBIENT: l.ambient = f3_color(v); break;
+    case PF_DIFFUSE: l.diffuse = f3_color(v); break;
+    case PF_SPECULAR: l.specular = f3_color(v); break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+    G->stateDirty = true;
+}
+static void mat_set(PFface f, PFenum p, const float *v)
+{
+    Material *a, *b;
+    switch (f) {
+    case PF_FRONT: a = b = &G->mat[0]; break;
+    case PF_BACK: a = b = &G->mat[1]; break;
+    case PF_FRONT_AND_BACK: a = &G->mat[0]; b = &G->mat[1]; break;
+    default: G->err = PF_INVALID_ENUM; return;
+    }
+    PFcolor c = f3_color(v);
+    switch (p) {
+    case PF_AMBIENT: a->ambient = b->ambient = c; break;
+    case PF_DIFFUSE: a->diffuse = b->diffuse = c; break;
+    case PF_SPECULAR: a->specular = b->specular = c; break;
+    case PF_EMISSION: a->emission = b->emission = c; break;
+    case PF_SHININESS: a->shininess = b->shininess = v[0]; break;
+    case PF_AMBIENT_AND_DIFFUSE: a->ambient = b->ambient = c; a->diffuse = b->diffuse = c; break;
+    default: G->err = PF_INVALID_ENUM; return;
+    }
+    G->stateDirty = true;
+}
+void pfMaterialf(PFface f, PFenum p, PFfloat v) { float vv[3] = { v, v, v }; mat_set(f, p, vv); }
+void pfMaterialfv(PFface f, PFenum p, const void *v) { mat_set(f, p, (const float *)v); }
+void pfColorMaterial(PFface f, PFenum m)
+{
+    if (f < PF_FRONT || f > PF_FRONT_AND_BACK) { G->err = PF_INVALID_ENUM; return; }
+    if (m < PF_AMBIENT_AND_DIFFUSE || m > PF_EMISSION) { G->err = PF_INVALID_ENUM; return; }
+    G->colMatFace = f; G->colMatMode = m;
+}
+
+// --- vertex arrays and draws (context.c:1161-1575) ----------------------------
+void pfVertexPointer(PFint size, PFenum type, PFsizei stride, const void *p)
+{
+    if (size < 2 || size > 4) { G->err = PF_INVALID_VALUE; return; }
+    if (!(type == PF_SHORT || type == PF_INT || type == PF_FLOAT || type == PF_DOUBLE)) { G->err = PF_INVALID_ENUM; return; }
+    G->positions = Attrib{ p, stride, size, type };
+}
+void pfNormalPointer(PFenum type, PFsizei stride, const void *p)
+{
+    if (!(type == PF_FLOAT || type == PF_DOUBLE)) { G->err = PF_INVALID_ENUM; return; }
+    G->normals = Attrib{ p, stride, 3, type };
+}
+void pfTexCoordPointer(PFenum type, PFsizei stride, const void *p)
+{
+    if (!(type == PF_FLOAT || type == PF_DOUBLE)) { G->err = PF_INVALID_ENUM; return; }
+    G->texcoords = Attrib{ p, stride, 2, type };
+}
+void pfColorPointer(PFint size, PFenum type, PFsizei stride, const void *p)
+{
+    if (size < 3 || size > 4) { G->err = PF_INVALID_VALUE; return; }
+    if (!(type == PF_UNSIGNED_BYTE || type == PF_UNSIGNED_SHORT || type == PF_UNSIGNED_INT ||
+          type == PF_FLOAT || type == PF_DOUBLE)) { G->err = PF_INVALID_ENUM; return; }
+    G->colors = Attrib{ p, stride, size, type };
+}
+
+static float attr_f(const Attrib &a, size_t i)
+{
+    switch (a.type) {
+    case PF_SHORT: return (float)((const PFshort *)a.buf)[i];
+    case PF_INT: return (float)((const PFint *)a.buf)[i];
+    case PF_FLOAT: return ((const PFfloat *)a.buf)[i];
+    case PF_DOUBLE: return (float)((const PFdouble *)a.buf)[i];
+    }
+    return 0.0f;
+}
+
+// Snapshot `count` elements of one attribute array as floats (positions,
+// normals, texcoords) starting at element `first`.
+static int64_t stage_float_attr(Ctx *c, const Attrib &a, int comps, size_t first, size_t count)
+{
+    if (a.type == PF_FLOAT) return snapshot(c, (const float *)a.buf + first * comps, count * comps * 4);
+    int64_t off = c->staging.alloc(count * comps * 4);
+    float *dst = (float *)(c->staging.base + off);
+    for (size_t i = 0; i < count * comps; i++) dst[i] = attr_f(a, first * comps + i);
+    return off;
+}
+
+static int64_t stage_color_attr(Ctx *c, const Attrib &a, size_t first, size_t count)
+{
+    const size_t k = (size_t)a.size;
+    if (a.type == PF_UNSIGNED_BYTE) return snapshot(c, (const uint8_t *)a.buf + first * k, count * k);
+    int64_t off = c->staging.alloc(count * k);
+    uint8_t *dst = c->staging.base + off;
+    for (size_t i = 0; i < count * k; i++) {
+        const size_t o = first * k + i;
+        switch (a.type) {
+        case PF_UNSIGNED_SHORT: dst[i] = (uint8_t)(((const PFushort *)a.buf)[o] >> 8); break;
+        case PF_UNSIGNED_INT: dst[i] = (uint8_t)(((const PFuint *)a.buf)[o] >> 24); break;
+        case PF_FLOAT: dst[i] = ftoub(((const PFfloat *)a.buf)[o] * 255); break;
+        case PF_DOUBLE: dst[i] = dtoub(((const PFdouble *)a.buf)[o] * 255); break;
+        }
+    }
+    return off;
+}
+
+// pfDrawElements / pfDrawArrays: one segment whose vertices are the arrays'
+// elements [first, first + nverts) and whose primitives follow `indices`
+// (or the sequence 0..count-1).
+static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first)
+{
+    Ctx *c = G;
+    update_matrices(c, !(mode == PF_POINTS || mode == PF_LINES));     // pfBegin inside the draw
+    c->drawMode = mode; c->vcount = 0;
+    c->stateDirty = true;
+    c->openImmSeg = -1;
+    if (mode > PF_QUAD_STRIP) { c->err = PF_INVALID_ENUM; return; }
+    if (mode == PF_POINTS || mode == PF_LINES) { c->err = PF_INVALID_OPERATION; return; }
+    const PFsizei nv = mode_count(mode);
+    const PFsizei nprim = count / nv;
+    int faces[2];
+    const int nf = faces_for(c, mode, faces);
+    if (nprim == 0 || nf == 0) return;
+
+    // indices: stage as u32 and find the vertex range
+    int64_t idxOff = -1;
+    size_t nverts;
+    if (indices) {
+        idxOff = c->staging.alloc((size_t)count * 4);
+        uint32_t *dst = (uint32_t *)(c->staging.base + idxOff);
+        uint32_t mx = 0;
+        if (itype == PF_UNSIGNED_INT) {
+            const uint32_t *s = (const uint32_t *)indices;
+            std::memcpy(dst, s, (size_t)count * 4);
+            for (PFsizei i = 0; i < count; i++) mx = std::max(mx, s[i]);
+        } else if (itype == PF_UNSIGNED_SHORT) {
+            const uint16_t *s = (const uint16_t *)indices;
+            for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
+        } else {
+            const uint8_t *s = (const uint8_t *)indices;
+            for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
+        }
+        nverts = (size_t)mx + 1;
+        first = 0;
+    } else {
+        nverts = count;
+    }
+    const bool useT = (c->state & PF_TEXTURE_COORD_ARRAY) && c->texcoords.buf;
+    const bool useN = (c->state & PF_NORMAL_ARRAY) && c->normals.buf;
+    const bool useC = (c->state & PF_COLOR_ARRAY) && c->colors.buf;
+
+    const int si = new_segment(c, PF_SRC_ARRAYS, mode == PF_TRIANGLES ? PF_ITEMS_TRIS : PF_ITEMS_EXPLICIT);
+    SegRec &r = c->segs[si];
+    r.posOff = stage_float_attr(c, c->positions, c->positions.size, (size_t)first, nverts);
+    if (useN) r.nrmOff = stage_float_attr(c, c->normals, 3, (size_t)first, nverts);
+    if (useT) r.uvOff = stage_float_attr(c, c->texcoords, 2, (size_t)first, nverts);
+    if (useC) r.colOff = stage_color_attr(c, c->colors, (size_t)first, nverts);
+    r.idxOff = idxOff;
+    PFSegment &s = r.seg;
+    s.nVerts = (uint32_t)nverts;
+    s.posSize = c->positions.size;
+    s.colSize = c->colors.size;
+    s.constColor = pack(c->curColor);
+    if (mode == PF_TRIANGLES) {
+        s.nFaces = nf; s.face0 = faces[0];
+        s.nItems = nprim * (uint32_t)nf;
+    } else {
+        // simulate the reference's vertex-buffer slots over sequence positions
+        uint32_t slot[6];
+        PFsizei vc = 0;
+        for (PFsizei i = 0; i < count; i++) {
+            slot[vc++] = i;
+            if (vc == nv) { emit_items(r.explicitItems, mode, slot, faces, nf); vc = reset_for_next(mode, slot); }
+        }
+    }
+    c->stateDirty = true;
+}
+
+void pfDrawElements(PFdrawmode mode, PFsizei count, PFdatatype type, const void *indices)
+{
+    if (!(type == PF_UNSIGNED_BYTE || type == PF_UNSIGNED_SHORT || type == PF_UNSIGNED_INT)) { G->err = PF_INVALID_ENUM; return; }
+    if (!(G->state & PF_VERTEX_ARRAY)) { G->err = PF_INVALID_OPERATION; return; }
+    draw_arrays(mode, count, indices, type, 0);
+}
+void pfDrawArrays(PFdrawmode mode, PFint first, PFsizei count)
+{
+    if (!(G->state & PF_VERTEX_ARRAY)) { G->err = PF_INVALID_OPERATION; return; }
+    draw_arrays(mode, count, nullptr, PF_UNSIGNED_INT, first);
+}
+
+void pfBegin(PFdrawmode mode)
+{
+    if (mode > PF_QUAD_STRIP) { G->err = PF_INVALID_ENUM; return; }
+    update_matrices(G, !(mode == PF_POINTS || mode == PF_LINES));
+    G->drawMode = mode; G->vcount = 0;
+    G->stateDirty = true;
+}
+void pfEnd(void) { G->vcount = 0; }
+
+void pfVertex4fv(const PFfloat *v)
+{
+    Ctx *c = G;
+    PFVertexIn &x = c->slots[c->vcount++];
+    std::memcpy(x.pos, v, 16);
+    std::memcpy(x.normal, c->curNormal, 12);
+    std::memcpy(x.uv, c->curTex, 8);
+    x.color = pack(c->curColor);
+    x.pad[0] = x.pad[1] = 0;
+    if (c->vcount == mode_count(c->drawMode)) {
+        immediate_primitive(c);
+        c->vcount = reset_for_next(c->drawMode, c->slots);
+    }
+}
+void pfVertex2i(PFint x, PFint y) { float v[4] = { (float)x, (float)y, 0.0f, 1.0f }; pfVertex4fv(v); }
+void pfVertex2f(PFfloat x, PFfloat y) { float v[4] = { x, y, 0.0f, 1.0f }; pfVertex4fv(v); }
+void pfVertex2fv(const PFfloat *p) { float v[4] = { p[0], p[1], 0.0f, 1.0f }; pfVertex4fv(v); }
+void pfVertex3i(PFint x, PFint y, PFint z) { float v[4] = { (float)x, (float)y, (float)z, 1.0f }; pfVertex4fv(v); }
+void pfVertex3f(PFfloat x, PFfloat y, PFfloat z) { float v[4] = { x, y, z, 1.0f }; pfVertex4fv(v); }
+void pfVertex3fv(const PFfloat *p) { float v[4] = { p[0], p[1], p[2], 1.0f }; pfVertex4fv(v); }
+void pfVertex4i(PFint x, PFint y, PFint z, PFint w) { float v[4] = { (float)x, (float)y, (float)z, (float)w }; pfVertex4fv(v); }
+void pfVertex4f(PFfloat x, PFfloat y, PFfloat z, PFfloat w) { float v[4] = { x, y, z, w }; pfVertex4fv(v); }
+
+void pfColor(PFcolor col)                                           // context.c:1687-1717
+{
+    if (G->state & PF_COLOR_MATERIAL) {
+        Material *m1 = &G->mat[0], *m2 = &G->mat[1];
+        if (G->colMatFace == PF_FRONT) m2 = m1; else if (G->colMatFace == PF_BACK) m1 = m2;
+        switch (G->colMatMode) {
+        case PF_AMBIENT_AND_DIFFUSE: m1->ambient = m2->ambient = col; m1->diffuse = m2->diffuse = col; break;
+        case PF_AMBIENT: m1->ambient = m2->ambient = col; break;
+        case PF_DIFFUSE: m1->diffuse = m2->diffuse = col; break;
+        case PF_SPECULAR: m1->specular = m2->specular = col; break;
+        case PF_EMISSION: m1->emission = m2->emission = col; break;
+        }
+        G->stateDirty = true;
+    } else G->curColor = col;
+}
+void pfColor1ui(PFuint u) { pfColor(unpack(u)); }
+void pfColor3ub(PFubyte r, PFubyte g, PFubyte b) { pfColor(PFcolor{ r, g, b, 255 }); }
+void pfColor3ubv(const PFubyte *v) { pfColor3ub(v[0], v[1], v[2]); }
+void pfColor3us(PFushort r, PFushort g, PFushort b) { pfColor3ub((PFubyte)(r >> 8), (PFubyte)(g >> 8), (PFubyte)(b >> 8)); }
+void pfColor3usv(const PFushort *v) { pfColor3us(v[0], v[1], v[2]); }
+void pfColor3ui(PFuint r, PFuint g, PFuint b) { pfColor3ub((PFubyte)(r >> 24), (PFubyte)(g >> 24), (PFubyte)(b >> 24)); }
+void pfColor3uiv(const PFuint *v) { pfColor3ui(v[0], v[1], v[2]); }
+void pfColor3f(PFfloat r, PFfloat g, PFfloat b) { pfColor3ub(ftoub(r*255), ftoub(g*255), ftoub(b*255)); }
+void pfColor3fv(const PFfloat *v) { pfColor3f(v[0], v[1], v[2]); }
+void pfColor4ub(PFubyte r, PFubyte g, PFubyte b, PFubyte a) { pfColor(PFcolor{ r, g, b, a }); }
+void pfColor4ubv(const PFubyte *v) { pfColor4ub(v[0], v[1], v[2], v[3]); }
+void pfColor4us(PFushort r, PFushort g, PFushort b, PFushort a) { pfColor4ub((PFubyte)(r >> 8), (PFubyte)(g >> 8), (PFubyte)(b >> 8), (PFubyte)(a >> 8)); }
+void pfColor4usv(const PFushort *v) { pfColor4us(v[0], v[1], v[2], v[3]); }
+void pfColor4ui(PFuint r, PFuint g, PFuint b, PFuint a) { pfColor4ub((PFubyte)(r >> 24), (PFubyte)(g >> 24), (PFubyte)(b >> 24), (PFubyte)(a >> 24)); }
+void pfColor4uiv(const PFuint *v) { pfColor4ui(v[0], v[1], v[2], v[3]); }
+void pfColor4f(PFfloat r, PFfloat g, PFfloat b, PFfloat a) { pfColor4ub(ftoub(r*255), ftoub(g*255), ftoub(b*255), ftoub(a*255)); }
+void pfColor4fv(const PFfloat *v) { pfColor4f(v[0], v[1], v[2], v[3]); }
+void pfTexCoord2f(PFfloat u, PFfloat v)                              // context.c:1874-1893
+{
+    const float *m = G->tex;
+    float t0 = m[0]*u + m[4]*v + m[12], t1 = m[1]*u + m[5]*v + m[13];
+    G->curTex[0] = t0; G->curTex[1] = t1;
+}
+void pfTexCoordfv(const PFfloat *v) { pfTexCoord2f(v[0], v[1]); }
+void pfNormal3f(PFfloat x, PFfloat y, PFfloat z)
+{
+    G->curNormal[0] = x; G->curNormal[1] = y; G->curNormal[2] = z;
+    if (G->state & PF_NORMALIZE) v3_normalize(G->curNormal);
+}
+void pfNormal3fv(const PFfloat *v) { pfNormal3f(v[0], v[1], v[2]); }
+
+// --- outside the triangle pipeline -------------------------------------------
+#define PF_UNSUPPORTED { if (G) G->err = PF_INVALID_OPERATION; }
+void pfRects(PFshort, PFshort, PFshort, PFshort) PF_UNSUPPORTED
+void pfRectsv(const PFshort *, const PFshort *) PF_UNSUPPORTED
+void pfRectf(PFfloat, PFfloat, PFfloat, PFfloat) PF_UNSUPPORTED
+void pfRectfv(const PFfloat *, const PFfloat *) PF_UNSUPPORTED
+void pfDrawPixels(PFsizei, PFsizei, PFpixelformat, PFdatatype, const void *) PF_UNSUPPORTED
+void pfPixelZoom(PFfloat, PFfloat) PF_UNSUPPORTED
+void pfRasterPos2i(PFint, PFint) PF_UNSUPPORTED
+void pfRasterPos2f(PFfloat, PFfloat) PF_UNSUPPORTED
+void pfRasterPos2fv(const PFfloat *) PF_UNSUPPORTED
+void pfRasterPos3i(PFint, PFint, PFint) PF_UNSUPPORTED
+void pfRasterPos3f(PFfloat, PFfloat, PFfloat) PF_UNSUPPORTED
+void pfRasterPos3fv(const PFfloat *) PF_UNSUPPORTED
+void pfRasterPos4i(PFint, PFint, PFint, PFint) PF_UNSUPPORTED
+void pfRasterPos4f(PFfloat, PFfloat, PFfloat, PFfloat) PF_UNSUPPORTED
+void pfRasterPos4fv(const PFfloat *) PF_UNSUPPORTED
+void pfFogi(PFfogparam, PFint) PF_UNSUPPORTED
+void pfFogf(PFfogparam, PFfloat) PF_UNSUPPORTED
+void pfFogiv(PFfogparam, PFint *) PF_UNSUPPORTED
+void pfFogfv(PFfogparam, PFfloat *) PF_UNSUPPORTED
+void pfFogProcess(void) PF_UNSUPPORTED
+PFrenderlist pfGenList(void) { PF_UNSUPPORTED return nullptr; }
+void pfDeleteList(PFrenderlist *) PF_UNSUPPORTED
+void pfNewList(PFrenderlist) PF_UNSUPPORTED
+void pfEndList(void) PF_UNSUPPORTED
+void pfCallList(const PFrenderlist) PF_UNSUPPORTED
+
+// --- readback, post-process -----------------------------------------------------
+void pfFinish(void) { if (G) flush(G); }
+
+void pfReadPixels(PFint x, PFint y, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, void *pixels)
+{
+    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { G->err = PF_INVALID_ENUM; return; }
+    sync_host(G);
+    const Tex *s = (const Tex *)G->current->texture;
+    auto cl = [](PFint v, PFint lo, PFint hi) { return v < lo ? lo : (v > hi ? hi : v); };
+    PFint xMin = cl(x, 0, (PFint)s->w - 1), yMin = cl(y, 0, (PFint)s->h - 1);
+    PFint xMax = cl(x + (PFint)w, 0, (PFint)s->w), yMax = cl(y + (PFint)h, 0, (PFint)s->h);
+    const uint32_t *src = (const uint32_t *)s->pixels;
+    uint32_t *dst = (uint32_t *)pixels;
+    for (PFint yy = yMin; yy < yMax; yy++)
+        for (PFint xx = xMin; xx < xMax; xx++)
+            dst[(size_t)(yy - yMin) * w + (size_t)(xx - xMin)] = src[(size_t)yy * s->w + (size_t)xx];
+}
+
+void pfPostProcess(PFpostprocessfunc fn)                             // context.c:2397-2441
+{
+    sync_host(G);
+    if (G->current == &G->mainFB) pull_main_depth(G);
+    Tex *t = (Tex *)G->current->texture;
+    uint32_t *pb = (uint32_t *)t->pixels;
+    const float *zb = G->current->zbuffer;
+    for (PFint y = 0; y < (PFint)t->h; y++)
+        for (PFint x = 0; x < (PFint)t->w; x++) {
+            size_t o = (size_t)y * t->w + (size_t)x;
+            pb[o] = pack(fn(x, y, zb[o], unpack(pb[o])));
+        }
+}
+
+void pfPostProcessDevice(PFuint hookId, const void *params, PFsizei size)
+{
+    Cmd cmd{};
+    cmd.kind = CMD_HOOK; cmd.fb = G->current; cmd.hook = (int)hookId;
+    switch (hookId) {
+    case PF_HOOK_IDENTITY: case PF_HOOK_GRAYSCALE: break;
+    case PF_HOOK_FOG_LINEAR: {
+        if (!params || size < sizeof(PFhookfog)) { G->err = PF_INVALID_VALUE; return; }
+        PFhookfog f; std::memcpy(&f, params, sizeof f);
+        cmd.hp.znear = f.znear; cmd.hp.zfar = f.zfar; cmd.hp.start = f.start; cmd.hp.end = f.end;
+        cmd.hp.color = pack(f.color);
+    } break;
+    default: G->err = PF_INVALID_ENUM; return;
+    }
+    G->cmds.push_back(cmd);
+    G->openImmSeg = -1;
+}
+
+void pfGetStats(PFstats *s) { *s = G->stats; }
+void pfResetStats(void) { G->stats = PFstats{}; }
+void pfEnableTiming(PFboolean enable) { G->timing = enable; }
+PFuint pfGetDeviceStatus(void) { return G ? G->devStatus : 0; }
+
+// --- framebuffers (framebuffer.c) ----------------------------------------------
+PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
+{
+    PFframebuffer fb{ nullptr, nullptr };
+    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { set_err(PF_INVALID_ENUM); return fb; }
+    const size_t n = (size_t)w * h;
+    void *px = nullptr;
+    bool pinned = cudaMallocHost(&px, n * 4) == cudaSuccess;
+    if (!pinned) { cudaGetLastError(); px = std::malloc(n * 4); }
+    if (!px) { set_err(PF_ERROR_OUT_OF_MEMORY); return fb; }
+    std::memset(px, 0, n * 4);
+    Tex *tx = tex_new(px, w, h, f, t);
+    tx->ownsPinned = pinned;
+    float *z = nullptr;
+    bool zp = cudaMallocHost((void **)&z, n * 4) == cudaSuccess;
+    if (!zp) { cudaGetLastError(); z = (float *)std::malloc(n * 4); }
+    for (size_t i = 0; i < n; i++) z[i] = FLT_MAX;
+    fb.texture = tx; fb.zbuffer = z;
+    return fb;
+}
+
+void pfDeleteFramebuffer(PFframebuffer *fb)
+{
+    if (!fb) return;
+    if (G) flush(G);
+    Tex *t = (Tex *)fb->texture;
+    if (t) {
+        if (G) {
+            auto it = G->mirrors.find(t);
+            if (it != G->mirrors.end()) {
+                if (it->second.registered) cudaHostUnregister(it->second.registered);
+                cudaFree(it->second.dColor); cudaFree(it->second.dDepth);
+                G->mirrors.erase(it);
+            }
+        }
+        if (t->ownsPinned) cudaFreeHost(t->pixels); else std::free(t->pixels);
+        if (fb->zbuffer) { if (cudaFreeHost(fb->zbuffer) != cudaSuccess) { cudaGetLastError(); std::free(fb->zbuffer); } }
+        delete t;
+    }
+    fb->texture = nullptr; fb->zbuffer = nullptr;
+}
+
+PFboolean pfIsValidFramebuffer(PFframebuffer *fb)
+{
+    const Tex *t = (const Tex *)fb->texture;
+    return t && fb->zbuffer && t->w > 0 && t->h > 0 && t->pixels;
+}
+
+void pfClearFramebuffer(PFframebuffer *fb, PFcolor color, PFfloat depth)
+{
+    Cmd cmd{};
+    cmd.kind = CMD_FILL; cmd.fb = fb; cmd.color = pack(color); cmd.depth = depth;
+    if (G) { G->cmds.push_back(cmd); G->openImmSeg = -1; }
+}
+
+PFcolor pfGetFramebufferPixel(const PFframebuffer *fb, PFsizei x, PFsizei y)
+{
+    if (G) sync_host(G);
+    const Tex *t = (const Tex *)fb->texture;
+    return unpack(((const uint32_t *)t->pixels)[(size_t)y * t->w + x]);
+}
+PFfloat pfGetFramebufferDepth(const PFframebuffer *fb, PFsizei x, PFsizei y)
+{
+    if (G) { sync_host(G); if (fb == &G->mainFB) pull_main_depth(G); }
+    const Tex *t = (const Tex *)fb->texture;
+    return fb->zbuffer[(size_t)y * t->w + x];
+}
+void pfSetFramebufferPixelDepthTest(PFframebuffer *fb, PFsizei x, PFsizei y, PFfloat z, PFcolor col, PFdepthmode m)
+{
+    if (m > PF_GEQUAL) { set_err(PF_INVALID_ENUM); return; }
+    if (G) { sync_host(G); if (fb == &G->mainFB) pull_main_depth(G); }
+    Tex *t = (Tex *)fb->texture;
+    size_t o = (size_t)y * t->w + x;
+    bool pass;
+    switch (m) {                                                    // depth.h:30-70
+    case PF_EQUAL: pass = z == fb->zbuffer[o]; break;
+    case PF_NOTEQUAL: pass = z != fb->zbuffer[o]; break;
+    case PF_LESS: pass = z < fb->zbuffer[o]; break;
+    case PF_LEQUAL: pass = z <= fb->zbuffer[o]; break;
+    case PF_GREATER: pass = z > fb->zbuffer[o]; break;
+    default: pass = z >= fb->zbuffer[o]; break;
+    }
+    if (pass) { ((uint32_t *)t->pixels)[o] = pack(col); fb->zbuffer[o] = z; }
+}
+void pfSetFramebufferPixelDepth(PFframebuffer *fb, PFsizei x, PFsizei y, PFfloat z, PFcolor col)
+{
+    if (G) { sync_host(G); if (fb == &G->mainFB) pull_main_depth(G); }
+    Tex *t = (Tex *)fb->texture;
+    size_t o = (size_t)y * t->w + x;
+    ((uint32_t *)t->pixels)[o] = pack(col); fb->zbuffer[o] = z;
+}
+void pfSetFramebufferPixel(PFframebuffer *fb, PFsizei x, PFsizei y, PFcolor col)
+{
+    if (G) sync_host(G);
+    Tex *t = (Tex *)fb->texture;
+    ((uint32_t *)t->pixels)[(size_t)y * t->w + x] = pack(col);
+}
+
+// --- textures (texture.c) --------------------------------------------------------
+PFtexture pfGenTexture(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t) { return tex_new(pixels, w, h, f, t); }
+void pfDeleteTexture(PFtexture *tex, PFboolean freeBuffer)
+{
+    Tex *t = (Tex *)*tex;
+    if (!t) return;
+    if (G && G->texture == t) G->texture = nullptr;   // snapshots already hold the texels
+    if (freeBuffer) std::free(t->pixels);
+    delete t;
+    *tex = nullptr;
+}
+PFboolean pfIsValidTexture(const PFtexture tex)
+{
+    const Tex *t = (const Tex *)tex;
+    return t && t->pixels && t->w > 0 && t->h > 0;
+}
+void pfTextureParameter(PFtexture tex, PFtexturewrap wrap, PFtexturefilter filter)
+{
+    if (!(wrap <= PF_CLAMP_TO_EDGE && filter <= PF_BILINEAR)) { set_err(PF_INVALID_ENUM); return; }
+    Tex *t = (Tex *)tex; t->wrap = wrap; t->filter = filter;
+    if (G) G->stateDirty = true;
+}
+void *pfGetTexturePixels(const PFtexture tex, PFsizei *w, PFsizei *h, PFpixelformat *f, PFdatatype *t)
+{
+    const Tex *x = (const Tex *)tex;
+    if (!x) return nullptr;
+    if (G) sync_host(G);
+    if (w) *w = x->w;
+    if (h) *h = x->h;
+    if (f) *f = x->format;
+    if (t) *t = x->type;
+    return x->pixels;
+}
+
+}  // extern "C"

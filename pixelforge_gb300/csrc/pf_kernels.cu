@@ -1,0 +1,1048 @@
+// pf_kernels.cu -- sm_103a kernels of the PixelForge triangle pipeline.
+//
+//   k_vertex   one thread per vertex: transform, Gouraud lighting
+//              (src/internal/primitives/triangles.c:72-104, lighting.c:24-134)
+//   k_items    one thread per triangle-face item, in submission order:
+//              2D/3D decision, unclipped projection, setup, cull and
+//              order-keyed binning into 16x16 tiles (triangles.c:246-339);
+//              items that cross a clip plane are queued for k_clip
+//   k_clip     polygon clipping of queued items (triangles.c:157-244)
+//   k_raster   one CTA per tile: sorts the tile's bin keys (submission
+//              order), then evaluates every sub-triangle for the tile's 256
+//              pixels with the reference's integer edge functions, depth
+//              test, texturing, Phong, blending (triangles.c:398-557)
+//   k_clear, k_fill, k_hook  framebuffer-wide passes (pfClear,
+//              pfClearFramebuffer, device post-process hooks)
+//
+// Arithmetic parity.  The file is compiled with -fmad=false so that no
+// multiply-add is contracted (the reference is built for AVX2 without FMA);
+// every floating-point expression keeps the reference's operation order.
+// x86 conversion and min/max rules are restated explicitly (see x86_* below).
+// Depth and Phong use exact 1/x and 1/sqrt(x) where the reference uses the
+// approximate rcp/rsqrt instructions.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "pf_layout.h"
+#include "pf_device.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// x86 rules
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float x86_min(float a, float b) { return (a < b) ? a : b; }   // MINPS
+__device__ __forceinline__ float x86_max(float a, float b) { return (a > b) ? a : b; }   // MAXPS
+
+// CVTPS2DQ: round to nearest even, 0x80000000 for NaN / out of range.
+__device__ __forceinline__ int32_t x86_cvt_rne(float x)
+{
+    if (!(x > -2147483648.0f && x < 2147483648.0f)) return INT32_MIN;
+    return __float2int_rn(x);
+}
+// CVTTPS2DQ / CVTTSS2SI: truncation, 0x80000000 for NaN / out of range.
+__device__ __forceinline__ int32_t x86_cvt_trunc(float x)
+{
+    if (!(x > -2147483649.0f && x < 2147483648.0f)) return INT32_MIN;
+    return __float2int_rz(x);
+}
+// (unsigned char)(float) as GCC emits it on x86-64.
+__device__ __forceinline__ uint32_t x86_ftoub(float x) { return (uint32_t)x86_cvt_trunc(x) & 255u; }
+
+__device__ __forceinline__ uint32_t chn(uint32_t p, int i) { return (p >> (8 * i)) & 255u; }
+
+// ---------------------------------------------------------------------------
+// pfm.h arithmetic in the reference's order
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void v4_transform(float *d, const float *v, const float *m)
+{
+    float t0 = m[0]*v[0] + m[4]*v[1] + m[8]*v[2] + m[12]*v[3];
+    float t1 = m[1]*v[0] + m[5]*v[1] + m[9]*v[2] + m[13]*v[3];
+    float t2 = m[2]*v[0] + m[6]*v[1] + m[10]*v[2] + m[14]*v[3];
+    float t3 = m[3]*v[0] + m[7]*v[1] + m[11]*v[2] + m[15]*v[3];
+    d[0] = t0; d[1] = t1; d[2] = t2; d[3] = t3;
+}
+__device__ __forceinline__ void v3_transform(float *d, const float *v, const float *m)
+{
+    float t0 = m[0]*v[0] + m[4]*v[1] + m[8]*v[2] + m[12];
+    float t1 = m[1]*v[0] + m[5]*v[1] + m[9]*v[2] + m[13];
+    float t2 = m[2]*v[0] + m[6]*v[1] + m[10]*v[2] + m[14];
+    d[0] = t0; d[1] = t1; d[2] = t2;
+}
+__device__ __forceinline__ void v3_normalize(float *v)          // pfm.h:1183-1197
+{
+    float sq = v[0]*v[0] + v[1]*v[1] + v[2]*v[2];
+    if (sq == 0.0f) return;
+    float inv = 1.0f / sqrtf(sq);
+    v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
+}
+__device__ __forceinline__ float v3_dot(const float *a, const float *b) { return a[0]*b[0] + a[1]*b[1] + a[2]*b[2]; }
+
+// ---------------------------------------------------------------------------
+// Gouraud lighting, ubyte arithmetic (lighting.c:24-134), Blinn-Phong
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t min255(int32_t n) { return (uint32_t)(n | ((255 - n) >> 31)) & 255u; }
+
+__device__ uint32_t light_gouraud(const PFDrawState &S, const PFDevMaterial &m, uint32_t diffuse,
+                                  const float *P, const float *N)
+{
+    uint32_t R = chn(m.emis, 0), G = chn(m.emis, 1), B = chn(m.emis, 2);
+    const uint32_t dR = chn(diffuse, 0), dG = chn(diffuse, 1), dB = chn(diffuse, 2);
+    const uint32_t aR = (chn(m.amb, 0) * dR) / 255, aG = (chn(m.amb, 1) * dG) / 255, aB = (chn(m.amb, 2) * dB) / 255;
+    float V[3];
+    {
+        float lsq = 0.0f;
+        for (int i = 0; i < 3; i++) { V[i] = S.viewPos[i] - P[i]; lsq += V[i]*V[i]; }
+        float inv = 1.0f / sqrtf(lsq);
+        for (int i = 0; i < 3; i++) V[i] = V[i] * inv;
+    }
+    const float shin = m.shininess;
+    for (int li = 0; li < S.nLights; li++) {
+        const PFDevLight &l = S.lights[li];
+        uint32_t lR = 0, lG = 0, lB = 0;
+        float L[3] = { l.pos[0] - P[0], l.pos[1] - P[1], l.pos[2] - P[2] };
+        float dsq = L[0]*L[0] + L[1]*L[1] + L[2]*L[2];
+        float dist = 0.0f;
+        if (dsq != 0.0f) {
+            dist = sqrtf(dsq);
+            float inv = 1.0f / dist;
+            L[0] = L[0] * inv; L[1] = L[1] * inv; L[2] = L[2] * inv;
+        }
+        uint32_t intensity = 255;
+        bool skip = false;
+        if ((double)l.inner < 3.14159265358979323846) {
+            float nd[3] = { -l.dir[0], -l.dir[1], -l.dir[2] };
+            float theta = v3_dot(L, nd);
+            float eps = l.inner - l.outer;
+            int32_t iv = x86_cvt_trunc(255.0f*(theta - l.outer)/eps);
+            intensity = (uint32_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
+            if (intensity == 0) skip = true;
+        }
+        if (!skip) {
+            uint32_t att = 255;
+            if (l.attL != 0.0f || l.attQ != 0.0f) {
+                att = x86_ftoub(255.0f / (l.attC + l.attL*dist + l.attQ*dsq));
+                if (att == 0) skip = true;
+            }
+            if (!skip) {
+                uint32_t factor = (intensity * att) / 255;
+                int32_t dI = x86_cvt_trunc(255.0f * v3_dot(N, L));
+                uint32_t diff = (uint32_t)(dI > 0 ? dI : 0) & 255u;
+                lR = min255((int32_t)(lR + (dR * chn(l.diff, 0) * diff) / (255 * 255)));
+                lG = min255((int32_t)(lG + (dG * chn(l.diff, 1) * diff) / (255 * 255)));
+                lB = min255((int32_t)(lB + (dB * chn(l.diff, 2) * diff) / (255 * 255)));
+                float H[3] = { L[0] + V[0], L[1] + V[1], L[2] + V[2] };
+                v3_normalize(H);
+                float nh = fmaxf(v3_dot(N, H), 0.0f);
+                float pw = (float)pow((double)nh, (double)shin);
+                uint32_t spec = x86_ftoub(255.0f * pw);
+                lR = min255((int32_t)(lR + (chn(m.spec, 0) * chn(l.spec, 0) * spec) / (255 * 255)));
+                lG = min255((int32_t)(lG + (chn(m.spec, 1) * chn(l.spec, 1) * spec) / (255 * 255)));
+                lB = min255((int32_t)(lB + (chn(m.spec, 2) * chn(l.spec, 2) * spec) / (255 * 255)));
+                lR = (lR * factor) / 255; lG = (lG * factor) / 255; lB = (lB * factor) / 255;
+            }
+        }
+        R = min255((int32_t)(R + lR + (aR * chn(l.amb, 0)) / 255));
+        G = min255((int32_t)(G + lG + (aG * chn(l.amb, 1)) / 255));
+        B = min255((int32_t)(B + lB + (aB * chn(l.amb, 2)) / 255));
+    }
+    return R | (G << 8) | (B << 16) | (diffuse & 0xff000000u);
+}
+
+// scalar pfiBlendMultiplicative (blend.h:77-86)
+__device__ __forceinline__ uint32_t blend_mul_scalar(uint32_t s, uint32_t d)
+{
+    uint32_t r = 0;
+    for (int i = 0; i < 4; i++) r |= ((chn(s, i) * chn(d, i)) / 255) << (8 * i);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// per-fragment operations, SIMD semantics
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack4(const int32_t *v)
+{
+    return (uint32_t)v[0] | ((uint32_t)v[1] << 8) | ((uint32_t)v[2] << 16) | ((uint32_t)v[3] << 24);
+}
+
+// blend.h:140-277 (SUB adds; channels are ORed without masks when packed)
+__device__ uint32_t blend_simd(int mode, uint32_t src, uint32_t dst)
+{
+    int32_t s[4], d[4], o[4];
+    for (int i = 0; i < 4; i++) { s[i] = (int32_t)chn(src, i); d[i] = (int32_t)chn(dst, i); }
+    switch (mode) {
+    case 0: for (int i = 0; i < 4; i++) o[i] = (s[i] + d[i]) >> 1; break;
+    case 1: { int32_t a = s[3] + 1, ia = 256 - a;
+              for (int i = 0; i < 3; i++) o[i] = (s[i]*a + d[i]*ia) >> 8;
+              o[3] = (255*a + d[3]*ia) >> 8; } break;
+    case 2: for (int i = 0; i < 4; i++) { int32_t t = s[i] + d[i]; o[i] = t < 255 ? t : 255; } break;
+    case 3: for (int i = 0; i < 4; i++) { int32_t t = s[i] + d[i]; o[i] = t > 0 ? t : 0; } break;
+    case 4: for (int i = 0; i < 4; i++) o[i] = (s[i]*d[i]) >> 8; break;
+    case 5: for (int i = 0; i < 4; i++) { int32_t t = ((d[i]*(255 - s[i])) >> 8) + s[i]; o[i] = t < 255 ? t : 255; } break;
+    case 6: for (int i = 0; i < 4; i++) o[i] = s[i] > d[i] ? s[i] : d[i]; break;
+    case 7: for (int i = 0; i < 4; i++) o[i] = s[i] < d[i] ? s[i] : d[i]; break;
+    default: return src;
+    }
+    return pack4(o);
+}
+
+// depth.h:80-124 (NOTEQUAL compares equal there)
+__device__ __forceinline__ bool depth_simd(int f, float src, float dst)
+{
+    switch (f) {
+    case 0: case 1: return src == dst;
+    case 2: return src < dst;
+    case 3: return src <= dst;
+    case 4: return src > dst;
+    default: return src >= dst;
+    }
+}
+
+// sampler.h:203-258 (SIMD texture maps)
+__device__ __forceinline__ void tex_map(const PFDrawState &S, float u, float v, int32_t &x, int32_t &y)
+{
+    const float wm1 = (float)(S.texW - 1), hm1 = (float)(S.texH - 1);
+    if (S.texWrap == 0) {                 // REPEAT
+        u = (u - truncf(u)) * wm1;
+        v = (v - truncf(v)) * hm1;
+        int32_t a = x86_cvt_rne(u), b = x86_cvt_rne(v);
+        x = (a < 0) ? (int32_t)(0u - (uint32_t)a) : a;
+        y = (b < 0) ? (int32_t)(0u - (uint32_t)b) : b;
+    } else if (S.texWrap == 1) {          // MIRRORED_REPEAT; pfiSimdMod_F32 = x - floor(x/2)*2
+        u = fabsf(u); v = fabsf(v);
+        u = u - floorf(u / 2.0f) * 2.0f;
+        v = v - floorf(v / 2.0f) * 2.0f;
+        float um = 1.0f - (u - 1.0f), vm = 1.0f - (v - 1.0f);
+        u = (u > 1.0f) ? um : u;
+        v = (v > 1.0f) ? vm : v;
+        u = u * wm1; v = v * hm1;
+        x = x86_cvt_rne(u + 0.5f);
+        y = x86_cvt_rne(v + 0.5f);
+    } else {                              // CLAMP_TO_EDGE
+        u = x86_min(x86_max(u, 0.0f), 1.0f) * wm1;
+        v = x86_min(x86_max(v, 0.0f), 1.0f) * hm1;
+        x = x86_cvt_rne(u + 0.5f);
+        y = x86_cvt_rne(v + 0.5f);
+    }
+}
+
+// Texel at linear offset y*w + x; offsets outside the texture read as 0
+// (the reference reads past its buffer there).
+__device__ __forceinline__ uint32_t tex_fetch(const PFDrawState &S, int32_t x, int32_t y)
+{
+    int32_t off = (int32_t)((uint32_t)y * S.texW + (uint32_t)x);
+    if (off < 0 || (uint32_t)off >= S.texW * S.texH) return 0u;
+    return __ldg(S.tex + off);
+}
+
+__device__ __forceinline__ uint32_t lerp_color(uint32_t a, uint32_t b, float t)
+{
+    const float inv255 = 1.0f / 255.0f;
+    int32_t o[4];
+    for (int i = 0; i < 4; i++) {
+        float af = (float)chn(a, i) * inv255;
+        float bf = (float)chn(b, i) * inv255;
+        float r = af + t * (bf - af);
+        o[i] = x86_cvt_rne(x86_min(x86_max(r, 0.0f), 1.0f) * 255.0f);
+    }
+    return pack4(o);
+}
+
+__device__ uint32_t tex_sample(const PFDrawState &S, float u, float v)
+{
+    int32_t x0, y0;
+    tex_map(S, u, v, x0, y0);
+    if (S.texFilter == 0) return tex_fetch(S, x0, y0);
+    int32_t x1, y1;
+    tex_map(S, u + S.texTx, v + S.texTy, x1, y1);
+    float fx = u * (float)S.texW - (float)x0;
+    float fy = v * (float)S.texH - (float)y0;
+    fx = x86_min(x86_max(fx, 0.0f), 1.0f);
+    fy = x86_min(x86_max(fy, 0.0f), 1.0f);
+    uint32_t c00 = tex_fetch(S, x0, y0), c10 = tex_fetch(S, x1, y0);
+    uint32_t c01 = tex_fetch(S, x0, y1), c11 = tex_fetch(S, x1, y1);
+    return lerp_color(lerp_color(c00, c10, fx), lerp_color(c01, c11, fx), fy);
+}
+
+// Cephes log/exp as adapted for SSE/AVX by J. Pommier and G. Garberoglio
+// (zlib licence), the reference's per-fragment power (simd.h:183-300, 1158-1170).
+__device__ float cephes_log(float x)
+{
+    const bool invalid = (x <= 0.0f);
+    x = x86_max(x, __uint_as_float(0x00800000u));
+    int32_t e_i = (int32_t)(__float_as_uint(x) >> 23);
+    x = __uint_as_float((__float_as_uint(x) & ~0x7f800000u) | __float_as_uint(0.5f));
+    e_i -= 0x7f;
+    float e = (float)e_i;
+    e = e + 1.0f;
+    const bool lt = (x < 0.707106781186547524f);
+    float tmp = lt ? x : 0.0f;
+    x = x - 1.0f;
+    e = e - (lt ? 1.0f : 0.0f);
+    x = x + tmp;
+    float z = x * x;
+    float y = 7.0376836292E-2f;
+    y = y * x; y = y + -1.1514610310E-1f;
+    y = y * x; y = y + 1.1676998740E-1f;
+    y = y * x; y = y + -1.2420140846E-1f;
+    y = y * x; y = y + 1.4249322787E-1f;
+    y = y * x; y = y + -1.6668057665E-1f;
+    y = y * x; y = y + 2.0000714765E-1f;
+    y = y * x; y = y + -2.4999993993E-1f;
+    y = y * x; y = y + 3.3333331174E-1f;
+    y = y * x;
+    y = y * z;
+    tmp = e * -2.12194440e-4f;
+    y = y + tmp;
+    tmp = z * 0.5f;
+    y = y - tmp;
+    tmp = e * 0.693359375f;
+    x = x + y;
+    x = x + tmp;
+    return invalid ? __uint_as_float(0xffffffffu) : x;
+}
+
+__device__ float cephes_exp(float x)
+{
+    x = x86_min(x, 88.3762626647949f);
+    x = x86_max(x, -88.3762626647949f);
+    float fx = x * 1.44269504088896341f;
+    fx = fx + 0.5f;
+    float tmp = floorf(fx);
+    fx = tmp - ((tmp > fx) ? 1.0f : 0.0f);
+    tmp = fx * 0.693359375f;
+    float z = fx * -2.12194440e-4f;
+    x = x - tmp;
+    x = x - z;
+    z = x * x;
+    float y = 1.9875691500E-4f;
+    y = y * x; y = y + 1.3981999507E-3f;
+    y = y * x; y = y + 8.3334519073E-3f;
+    y = y * x; y = y + 4.1665795894E-2f;
+    y = y * x; y = y + 1.6666665459E-1f;
+    y = y * x; y = y + 5.0000001201E-1f;
+    y = y * z;
+    y = y + x;
+    y = y + 1.0f;
+    int32_t n = x86_cvt_trunc(fx) + 0x7f;
+    return y * __uint_as_float((uint32_t)n << 23);
+}
+
+__device__ __forceinline__ void dir_simd(float *d, const float *a, const float *b)   // simd.h:2469-2490
+{
+    d[0] = a[0] - b[0]; d[1] = a[1] - b[1]; d[2] = a[2] - b[2];
+    float lsq = d[0]*d[0] + d[1]*d[1];
+    lsq = lsq + d[2]*d[2];
+    lsq = x86_max(lsq, 1e-5f);
+    float inv = 1.0f / sqrtf(lsq);
+    d[0] = d[0] * inv; d[1] = d[1] * inv; d[2] = d[2] * inv;
+}
+__device__ __forceinline__ float dot_simd(const float *a, const float *b)
+{
+    float d = a[0]*b[0] + a[1]*b[1];
+    return d + a[2]*b[2];
+}
+
+// pfiSimdLightingProcess (lighting.c:149-258), one lane
+__device__ uint32_t light_phong(const PFDrawState &S, uint32_t frag, const PFDevMaterial &m,
+                                const float *P, const float *N)
+{
+    const float inv255 = 1.0f / 255.0f;
+    float cd[3], ca[3], cs[3];
+    for (int i = 0; i < 3; i++) {
+        cd[i] = (float)chn(frag, i) * inv255;
+        ca[i] = (float)chn(m.amb, i) * inv255;
+        cs[i] = (float)chn(m.spec, i) * inv255;
+    }
+    for (int i = 0; i < 3; i++) ca[i] = ca[i] * cd[i];
+    float V[3]; dir_simd(V, S.viewPos, P);
+    float acc[3] = { 0.0f, 0.0f, 0.0f };
+    for (int li = 0; li < S.nLights; li++) {
+        const PFDevLight &l = S.lights[li];
+        float la[3], ld[3], ls[3];
+        for (int i = 0; i < 3; i++) {
+            la[i] = (float)chn(l.amb, i) * inv255;
+            ld[i] = (float)chn(l.diff, i) * inv255;
+            ls[i] = (float)chn(l.spec, i) * inv255;
+        }
+        float L[3]; dir_simd(L, l.pos, P);
+        float amb[3], dif[3], spe[3];
+        for (int i = 0; i < 3; i++) amb[i] = la[i] * ca[i];
+        float diff = x86_max(dot_simd(N, L), 0.0f);
+        for (int i = 0; i < 3; i++) { dif[i] = ld[i] * diff; dif[i] = dif[i] * cd[i]; }
+        float H[3] = { L[0] + V[0], L[1] + V[1], L[2] + V[2] };
+        float hs = H[0]*H[0] + H[1]*H[1];
+        hs = hs + H[2]*H[2];
+        float hinv = 1.0f / sqrtf(hs);
+        for (int i = 0; i < 3; i++) H[i] = H[i] * hinv;
+        float spec = x86_max(dot_simd(N, H), 0.0f);
+        spec = cephes_exp(cephes_log(spec) * m.shininess);
+        for (int i = 0; i < 3; i++) { spe[i] = ls[i] * spec; spe[i] = spe[i] * cs[i]; }
+        if ((double)l.inner < 3.14159265358979323846) {
+            float nd[3] = { -l.dir[0], -l.dir[1], -l.dir[2] };
+            float theta = dot_simd(L, nd);
+            float eps = l.inner - l.outer;
+            float it = (theta - l.outer) / eps;
+            it = x86_min(x86_max(it, 0.0f), 1.0f);
+            for (int i = 0; i < 3; i++) { dif[i] = dif[i] * it; spe[i] = spe[i] * it; }
+        }
+        if (l.attL != 0.0f || l.attQ != 0.0f) {
+            // pfiVec3DistanceSq_simd reads y for z (simd.h:2423-2442)
+            float d0 = l.pos[0] - P[0], d1 = l.pos[1] - P[1], d2 = l.pos[1] - P[1];
+            float dsq = d0*d0 + (d1*d1 + d2*d2);
+            float dist = sqrtf(dsq);
+            float att = 1.0f / (l.attC + (l.attL*dist + l.attQ*dsq));
+            for (int i = 0; i < 3; i++) { amb[i] = amb[i] * att; dif[i] = dif[i] * att; spe[i] = spe[i] * att; }
+        }
+        for (int i = 0; i < 3; i++) { acc[i] = acc[i] + amb[i]; acc[i] = acc[i] + dif[i]; acc[i] = acc[i] + spe[i]; }
+    }
+    int32_t o[4] = { 0, 0, 0, 0 };
+    for (int i = 0; i < 3; i++) o[i] = x86_cvt_rne(x86_min(x86_max(acc[i], 0.0f), 1.0f) * 255.0f);
+    return pack4(o);
+}
+
+// ---------------------------------------------------------------------------
+// k_vertex
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int seg_of_vertex(const PFSegment *segs, int nSegs, uint32_t g)
+{
+    int lo = 0, hi = nSegs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (segs[mid].vtxBase <= g) lo = mid; else hi = mid - 1; }
+    return lo;
+}
+__device__ __forceinline__ int seg_of_item(const PFSegment *segs, int nSegs, uint32_t g)
+{
+    int lo = 0, hi = nSegs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (segs[mid].itemBase <= g) lo = mid; else hi = mid - 1; }
+    return lo;
+}
+
+__global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
+                         PFVertexOut *__restrict__ out, uint32_t nVerts, const PFDevCounters *cnt)
+{
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nVerts || cnt->abortCommand != 0xffffffffu) return;
+    const PFSegment &sg = segs[seg_of_vertex(segs, nSegs, g)];
+    const PFDrawState &S = states[sg.state];
+    const uint32_t j = g - sg.vtxBase;
+    float pos[4], nrm[3], uv[2];
+    uint32_t col;
+    if (sg.srcKind == PF_SRC_RECORDS) {
+        const PFVertexIn &r = sg.records[j];
+        for (int i = 0; i < 4; i++) pos[i] = r.pos[i];
+        for (int i = 0; i < 3; i++) nrm[i] = r.normal[i];
+        uv[0] = r.uv[0]; uv[1] = r.uv[1];
+        col = r.color;
+    } else {
+        pos[0] = pos[1] = pos[2] = 0.0f; pos[3] = 1.0f;
+        for (int k = 0; k < sg.posSize; k++) pos[k] = sg.pos[(size_t)j * sg.posSize + k];
+        if (sg.nrm) { for (int k = 0; k < 3; k++) nrm[k] = sg.nrm[(size_t)j * 3 + k]; }
+        else { nrm[0] = sg.constNormal[0]; nrm[1] = sg.constNormal[1]; nrm[2] = sg.constNormal[2]; }
+        if (sg.uv) { uv[0] = sg.uv[(size_t)j * 2]; uv[1] = sg.uv[(size_t)j * 2 + 1]; }
+        else { uv[0] = sg.constUv[0]; uv[1] = sg.constUv[1]; }
+        if (sg.col) {
+            col = 0xffffffffu;
+            for (int k = 0; k < sg.colSize; k++) {
+                uint32_t b = sg.col[(size_t)j * sg.colSize + k];
+                col = (col & ~(255u << (8 * k))) | (b << (8 * k));
+            }
+        } else col = sg.constColor;
+    }
+    PFVertexOut o;
+    uint32_t c0 = col, c1 = col;
+    float n[3] = { nrm[0], nrm[1], nrm[2] };
+    if (S.flags & PFS_LIGHTING) {
+        v3_transform(n, nrm, S.normal);
+        v3_normalize(n);
+        uint32_t base[2] = { blend_mul_scalar(col, S.mat[0].diff), blend_mul_scalar(col, S.mat[1].diff) };
+        if (!(S.flags & PFS_PHONG)) {
+            float NdotV = v3_dot(n, S.view8);
+            const PFDevMaterial &lm = S.mat[(NdotV < 0.0f) ? 0 : 1];
+            base[0] = light_gouraud(S, lm, base[0], pos, n);
+            base[1] = (S.mat[0].diff == S.mat[1].diff) ? base[0] : light_gouraud(S, lm, base[1], pos, n);
+        }
+        c0 = base[0]; c1 = base[1];
+    }
+    v4_transform(o.h, pos, S.mvp);
+    o.uv[0] = uv[0]; o.uv[1] = uv[1];
+    o.col[0] = c0; o.col[1] = c1;
+    o.n[0] = n[0]; o.n[1] = n[1]; o.n[2] = n[2];
+    o.p[0] = pos[0]; o.p[1] = pos[1]; o.p[2] = pos[2];
+    o.pad[0] = o.pad[1] = 0;
+    out[g] = o;
+}
+
+// ---------------------------------------------------------------------------
+// setup + binning (shared by k_items and k_clip)
+// ---------------------------------------------------------------------------
+struct SVert {                 // a vertex after projection to the screen
+    float sx, sy, z, u, v;
+    uint32_t c;
+    float n[3], p[3];
+};
+
+// pfiHomogeneousToScreen (internal/context/context.c:52-65)
+__device__ __forceinline__ void to_screen(const PFDrawState &S, float hx, float hy, float &sx, float &sy)
+{
+    sx = ((float)S.vpPos[0] + (hx + 1.0f) * 0.5f * (float)S.vpDim[0]) + 0.5f;
+    sy = ((float)S.vpPos[1] + (1.0f - hy) * 0.5f * (float)S.vpDim[1]) + 0.5f;
+}
+
+struct BinArgs {
+    uint32_t *binCount;
+    uint32_t *bins;
+    uint32_t cap;
+    uint32_t W, H, tilesX;
+    PFDevCounters *cnt;
+    uint32_t command;
+};
+
+// Rasterize_Triangle set-up (triangles.c:287-349).  Returns false if culled.
+__device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVert &a, const SVert &b,
+                           const SVert &c, int stateIdx, PFPrim &P)
+{
+    int32_t x1 = x86_cvt_trunc(a.sx), y1 = x86_cvt_trunc(a.sy);
+    int32_t x2 = x86_cvt_trunc(b.sx), y2 = x86_cvt_trunc(b.sy);
+    int32_t x3 = x86_cvt_trunc(c.sx), y3 = x86_cvt_trunc(c.sy);
+    float area = (float)(int32_t)((uint32_t)(x2 - x1) * (uint32_t)(y3 - y1) - (uint32_t)(x3 - x1) * (uint32_t)(y2 - y1));
+    if ((face == 0 && area >= 0.0f) || (face == 1 && area <= 0.0f)) return false;
+    int32_t mnx = min(x1, min(x2, x3)), mny = min(y1, min(y2, y3));
+    int32_t mxx = max(x1, max(x2, x3)), mxy = max(y1, max(y2, y3));
+    if (!is3D) {
+        mnx = min(max(mnx, S.vpMin[0]), S.vpMax[0]); mny = min(max(mny, S.vpMin[1]), S.vpMax[1]);
+        mxx = min(max(mxx, S.vpMin[0]), S.vpMax[0]); mxy = min(max(mxy, S.vpMin[1]), S.vpMax[1]);
+    }
+    uint32_t xMin = (uint32_t)mnx, yMin = (uint32_t)mny;
+    int32_t w1X = y3 - y2, w1Y = x2 - x3, w2X = y1 - y3, w2Y = x3 - x1, w3X = y2 - y1, w3Y = x1 - x2;
+    if (face == 1) { w1X = -w1X; w1Y = -w1Y; w2X = -w2X; w2Y = -w2Y; w3X = -w3X; w3Y = -w3Y; }
+    uint32_t r1 = (xMin - (uint32_t)x2) * (uint32_t)w1X + (uint32_t)w1Y * (yMin - (uint32_t)y2);
+    uint32_t r2 = (xMin - (uint32_t)x3) * (uint32_t)w2X + (uint32_t)w2Y * (yMin - (uint32_t)y3);
+    uint32_t r3 = (xMin - (uint32_t)x1) * (uint32_t)w3X + (uint32_t)w3Y * (yMin - (uint32_t)y1);
+    P.x1 = x1; P.y1 = y1; P.x2 = x2; P.y2 = y2; P.x3 = x3; P.y3 = y3;
+    P.xMin = mnx; P.yMin = mny; P.xMax = mxx; P.yMax = mxy;
+    P.flags = (uint32_t)face | (is3D ? 2u : 0u) | ((uint32_t)stateIdx << 8);
+    P.poolBase = -1;
+    P.wInvSum = 1.0f / (float)(int32_t)(r1 + r2 + r3);
+    P.z1 = a.z; P.z2 = b.z; P.z3 = c.z;
+    P.c1 = a.c; P.c2 = b.c; P.c3 = c.c; P.pad0 = 0;
+    P.u1 = a.u; P.v1 = a.v; P.u2 = b.u; P.v2 = b.v; P.u3 = c.u; P.v3 = c.v;
+    P.pad1 = P.pad2 = 0.0f;
+    P.pad3[0] = P.pad3[1] = P.pad3[2] = P.pad3[3] = 0.0f;
+    return true;
+}
+
+__device__ void bin_prim(const BinArgs &B, const PFPrim &P, uint32_t key)
+{
+    // pixels: x in [xMin, xMax) and y in [yMin, yMax], compared as unsigned
+    // (the reference's PFsizei loop bounds), then clipped to the framebuffer.
+    uint32_t x0 = (uint32_t)P.xMin, x1 = (uint32_t)P.xMax, y0 = (uint32_t)P.yMin, y1 = (uint32_t)P.yMax;
+    if (x1 > B.W) x1 = B.W;
+    if (y1 >= B.H) y1 = B.H - 1;
+    if (x0 >= x1 || y0 > y1) return;
+    uint32_t tx0 = x0 / PF_TILE, tx1 = (x1 - 1) / PF_TILE, ty0 = y0 / PF_TILE, ty1 = y1 / PF_TILE;
+    for (uint32_t ty = ty0; ty <= ty1; ty++)
+        for (uint32_t tx = tx0; tx <= tx1; tx++) {
+            uint32_t t = ty * B.tilesX + tx;
+            uint32_t slot = atomicAdd(&B.binCount[t], 1u);
+            if (slot < B.cap) B.bins[(size_t)t * B.cap + slot] = key;
+            else {
+                atomicMax(&B.cnt->maxBin, slot + 1);
+                if (slot == B.cap) {
+                    atomicOr(&B.cnt->status, (unsigned)PFD_BIN_OVERFLOW);
+                    atomicMin(&B.cnt->abortCommand, B.command);
+                }
+            }
+        }
+}
+
+__device__ __forceinline__ void store_phong(PFPrimPhong *dst, const SVert &a, const SVert &b, const SVert &c)
+{
+    PFPrimPhong q;
+    for (int i = 0; i < 3; i++) {
+        q.n1[i] = a.n[i]; q.n2[i] = b.n[i]; q.n3[i] = c.n[i];
+        q.p1[i] = a.p[i]; q.p2[i] = b.p[i]; q.p3[i] = c.p[i];
+    }
+    q.pad[0] = q.pad[1] = 0.0f;
+    *dst = q;
+}
+
+// ---------------------------------------------------------------------------
+// k_items
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void item_vertices(const PFSegment &sg, uint32_t k, uint32_t v[3], int &face)
+{
+    uint32_t s[3];
+    if (sg.itemKind == PF_ITEMS_TRIS) {
+        uint32_t tri = (sg.nFaces == 2) ? (k >> 1) : k;
+        face = (sg.nFaces == 2) ? (int)(k & 1) : sg.face0;
+        s[0] = 3 * tri; s[1] = 3 * tri + 1; s[2] = 3 * tri + 2;
+    } else {
+        const int32_t *e = sg.explicitItems + 4 * (size_t)k;
+        s[0] = (uint32_t)e[0]; s[1] = (uint32_t)e[1]; s[2] = (uint32_t)e[2]; face = e[3];
+    }
+    for (int m = 0; m < 3; m++) {
+        uint32_t j = sg.idx ? sg.idx[s[m]] : s[m];
+        if (j >= sg.nVerts) j = sg.nVerts - 1;        // memory guard; the host sizes nVerts from the indices
+        v[m] = sg.vtxBase + j;
+    }
+}
+
+__global__ void k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
+                        const PFVertexOut *__restrict__ vout, uint32_t nItems,
+                        PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
+                        uint32_t *__restrict__ clipQueue, uint32_t *__restrict__ clipQueueCount, BinArgs B)
+{
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nItems || B.cnt->abortCommand != 0xffffffffu) return;
+    const PFSegment &sg = segs[seg_of_item(segs, nSegs, g)];
+    const PFDrawState &S = states[sg.state];
+    uint32_t vi[3]; int face;
+    item_vertices(sg, g - sg.itemBase, vi, face);
+    const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
+    float ws = 0.0f;
+    for (int m = 0; m < 3; m++) ws += V[m]->h[3];
+    const bool is2D = fabsf(ws - 3.0f) < 1e-5f;
+    if (!is2D) {
+        bool inside = true;
+        for (int m = 0; m < 3; m++) {
+            const float *h = V[m]->h;
+            inside = inside && !(h[3] < 1e-5f);
+            for (int ax = 0; ax < 3; ax++) inside = inside && (h[ax] <= h[3]) && (-h[ax] <= h[3]);
+        }
+        if (!inside) {                                   // clip plane crossed: k_clip handles it
+            uint32_t q = atomicAdd(clipQueueCount, 1u);
+            clipQueue[q] = g;
+            return;
+        }
+    }
+    SVert s[3];
+    for (int m = 0; m < 3; m++) {
+        const PFVertexOut &o = *V[m];
+        if (is2D) {
+            to_screen(S, o.h[0], o.h[1], s[m].sx, s[m].sy);
+            s[m].z = o.h[2]; s[m].u = o.uv[0]; s[m].v = o.uv[1];
+        } else {
+            float hz = 1.0f / o.h[2];
+            s[m].u = o.uv[0] * hz; s[m].v = o.uv[1] * hz;
+            float invW = 1.0f / o.h[3];
+            to_screen(S, o.h[0] * invW, o.h[1] * invW, s[m].sx, s[m].sy);
+            s[m].z = hz;
+        }
+        s[m].c = o.col[face];
+        for (int i = 0; i < 3; i++) { s[m].n[i] = o.n[i]; s[m].p[i] = o.p[i]; }
+    }
+    PFPrim P;
+    if (!setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P)) return;
+    atomicAdd(&B.cnt->batchRasterized, 1ull);
+    prims[g] = P;
+    if (S.flags & PFS_PHONG) store_phong(&primsPh[g], s[0], s[1], s[2]);
+    bin_prim(B, P, g << PF_SUB_BITS);
+}
+
+// ---------------------------------------------------------------------------
+// k_clip (triangles.c:157-280)
+// ---------------------------------------------------------------------------
+struct CVert { float h[4]; float pos[4]; float n[3]; float uv[2]; uint32_t c; };
+
+// pfiLerpVertex (internal/context/context.c:67-90)
+__device__ void lerp_vert(CVert &r, const CVert &s, const CVert &e, float t)
+{
+    uint32_t uT = x86_ftoub(255.0f * t);
+    r.c = 0;
+    for (int i = 0; i < 4; i++) {
+        r.h[i] = s.h[i] + t*(e.h[i] - s.h[i]);
+        r.pos[i] = s.pos[i] + t*(e.pos[i] - s.pos[i]);
+        int32_t sc = (int32_t)chn(s.c, i), ec = (int32_t)chn(e.c, i);
+        r.c |= ((uint32_t)(sc + ((int32_t)uT * (ec - sc)) / 255) & 255u) << (8 * i);
+    }
+    r.uv[0] = s.uv[0] + t*(e.uv[0] - s.uv[0]);
+    r.uv[1] = s.uv[1] + t*(e.uv[1] - s.uv[1]);
+    for (int i = 0; i < 3; i++) r.n[i] = s.n[i] + t*(e.n[i] - s.n[i]);
+}
+
+__device__ int clip_plane(CVert *poly, int n, CVert *tmp, int ax, int sign)
+{
+    // sign 0: w clip (w < eps is outside); sign +1: h[ax] <= w; sign -1: -h[ax] <= w
+    for (int i = 0; i < n; i++) tmp[i] = poly[i];
+    int m = 0;
+    int prev = n - 1;
+    auto inside = [&](const CVert &v) -> int {
+        if (sign == 0) return (v.h[3] < 1e-5f) ? -1 : 1;
+        if (sign > 0) return (v.h[ax] <= v.h[3]) ? 1 : -1;
+        return (-v.h[ax] <= v.h[3]) ? 1 : -1;
+    };
+    int pd = inside(tmp[prev]);
+    for (int i = 0; i < n; i++) {
+        int cd = inside(tmp[i]);
+        if (pd * cd < 0 && m < PF_CLIP_MAXV) {
+            const CVert &p = tmp[prev], &c = tmp[i];
+            float t;
+            if (sign == 0) t = (1e-5f - p.h[3]) / (c.h[3] - p.h[3]);
+            else if (sign > 0) t = (p.h[3] - p.h[ax]) / ((p.h[3] - p.h[ax]) - (c.h[3] - c.h[ax]));
+            else t = (p.h[3] + p.h[ax]) / ((p.h[3] + p.h[ax]) - (c.h[3] + c.h[ax]));
+            lerp_vert(poly[m++], p, c, t);
+        }
+        if (cd > 0 && m < PF_CLIP_MAXV) poly[m++] = tmp[i];
+        pd = cd; prev = i;
+    }
+    return m;
+}
+
+__device__ __noinline__ void clip_one(const PFSegment *__restrict__ segs, int nSegs,
+                                      const PFDrawState *__restrict__ states, const PFVertexOut *__restrict__ vout,
+                                      uint32_t g, PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
+                                      PFPrim *__restrict__ pool, PFPrimPhong *__restrict__ poolPh, uint32_t poolCap,
+                                      const BinArgs &B);
+
+__global__ void k_clip(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
+                       const PFVertexOut *__restrict__ vout, const uint32_t *__restrict__ clipQueue,
+                       const uint32_t *__restrict__ clipQueueCount,
+                       PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
+                       PFPrim *__restrict__ pool, PFPrimPhong *__restrict__ poolPh, uint32_t poolCap,
+                       BinArgs B)
+{
+    if (B.cnt->abortCommand != 0xffffffffu) return;
+    const uint32_t nq = *clipQueueCount;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+        clip_one(segs, nSegs, states, vout, clipQueue[q], prims, primsPh, pool, poolPh, poolCap, B);
+}
+
+__device__ __noinline__ void clip_one(const PFSegment *__restrict__ segs, int nSegs,
+                                      const PFDrawState *__restrict__ states, const PFVertexOut *__restrict__ vout,
+                                      uint32_t g, PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
+                                      PFPrim *__restrict__ pool, PFPrimPhong *__restrict__ poolPh, uint32_t poolCap,
+                                      const BinArgs &B)
+{
+    const PFSegment &sg = segs[seg_of_item(segs, nSegs, g)];
+    const PFDrawState &S = states[sg.state];
+    uint32_t vi[3]; int face;
+    item_vertices(sg, g - sg.itemBase, vi, face);
+    CVert poly[PF_CLIP_MAXV], tmp[PF_CLIP_MAXV];
+    for (int m = 0; m < 3; m++) {
+        const PFVertexOut &o = vout[vi[m]];
+        for (int i = 0; i < 4; i++) poly[m].h[i] = o.h[i];
+        poly[m].pos[0] = o.p[0]; poly[m].pos[1] = o.p[1]; poly[m].pos[2] = o.p[2];
+        poly[m].pos[3] = 1.0f;
+        for (int i = 0; i < 3; i++) poly[m].n[i] = o.n[i];
+        poly[m].uv[0] = o.uv[0]; poly[m].uv[1] = o.uv[1];
+        poly[m].c = o.col[face];
+    }
+    int n = clip_plane(poly, 3, tmp, 3, 0);
+    for (int ax = 0; ax < 3 && n > 0; ax++) {
+        n = clip_plane(poly, n, tmp, ax, +1);
+        if (n == 0) break;
+        n = clip_plane(poly, n, tmp, ax, -1);
+    }
+    if (n < 3) return;
+    SVert s[PF_CLIP_MAXV];
+    for (int i = 0; i < n; i++) {
+        float hz = 1.0f / poly[i].h[2];
+        s[i].u = poly[i].uv[0] * hz; s[i].v = poly[i].uv[1] * hz;
+        float invW = 1.0f / poly[i].h[3];
+        to_screen(S, poly[i].h[0] * invW, poly[i].h[1] * invW, s[i].sx, s[i].sy);
+        s[i].z = hz;
+        s[i].c = poly[i].c;
+        for (int k = 0; k < 3; k++) { s[i].n[k] = poly[i].n[k]; s[i].p[k] = poly[i].pos[k]; }
+    }
+    const int nsub = n - 2;
+    uint32_t base = 0;
+    if (nsub > 1) {
+        base = atomicAdd(&B.cnt->clipCount, (unsigned)(nsub - 1));
+        if (base + (uint32_t)(nsub - 1) > poolCap) {
+            atomicOr(&B.cnt->status, (unsigned)PFD_CLIP_OVERFLOW);
+            atomicMin(&B.cnt->abortCommand, B.command);
+            return;
+        }
+    }
+    PFPrim first;
+    bool firstSet = false;
+    for (int i = 0; i < nsub; i++) {
+        PFPrim P;
+        if (!setup_prim(S, face, true, s[0], s[i + 1], s[i + 2], sg.state, P)) continue;
+        atomicAdd(&B.cnt->batchRasterized, 1ull);
+        if (i == 0) { first = P; firstSet = true; }
+        else {
+            pool[base + i - 1] = P;
+            if (S.flags & PFS_PHONG) store_phong(&poolPh[base + i - 1], s[0], s[i + 1], s[i + 2]);
+        }
+        bin_prim(B, P, (g << PF_SUB_BITS) | (uint32_t)i);
+    }
+    // prims[g] carries the pool base for sub-triangles >= 1 even when
+    // sub-triangle 0 was culled.
+    if (!firstSet) { first.flags = 0; first.xMin = 1; first.xMax = 0; }
+    first.poolBase = (int32_t)base;
+    prims[g] = first;
+    if (firstSet && (S.flags & PFS_PHONG)) store_phong(&primsPh[g], s[0], s[1], s[2]);
+}
+
+// ---------------------------------------------------------------------------
+// k_raster
+// ---------------------------------------------------------------------------
+#define RASTER_THREADS PF_TILE_PIXELS
+#define PRIM_CHUNK 32
+
+struct RasterArgs {
+    const uint32_t *binCount;
+    const uint32_t *bins;
+    uint32_t cap;
+    const PFPrim *prims;
+    const PFPrimPhong *primsPh;
+    const PFPrim *pool;
+    const PFPrimPhong *poolPh;
+    const PFDrawState *states;
+    uint32_t *color;
+    float *depth;
+    uint32_t W, H, tilesX;
+    PFDevCounters *cnt;
+    uint32_t command;
+};
+
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster(RasterArgs a)
+{
+    extern __shared__ uint32_t skeys[];
+    __shared__ PFPrim sprim[PRIM_CHUNK];
+    __shared__ PFPrimPhong sph[PRIM_CHUNK];
+    __shared__ int sHasPhong;
+
+    if (a.cnt->abortCommand <= a.command) return;
+    // the batch completed set-up without overflow: its sub-triangles count
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.cnt->rasterized, a.cnt->batchRasterized);
+    const uint32_t tile = blockIdx.x;
+    const uint32_t n = min(a.binCount[tile], a.cap);
+    if (n == 0) return;
+    const int tid = threadIdx.x;
+    const uint32_t *bin = a.bins + (size_t)tile * a.cap;
+    for (uint32_t i = tid; i < n; i += RASTER_THREADS) skeys[i] = bin[i];
+    __syncthreads();
+    // keys arrive in atomic order; restore submission order
+    int unsorted = 0;
+    for (uint32_t i = tid; i + 1 < n; i += RASTER_THREADS) unsorted |= (skeys[i] > skeys[i + 1]);
+    if (__syncthreads_or(unsorted)) {
+        uint32_t N = 1; while (N < n) N <<= 1;
+        for (uint32_t i = n + tid; i < N; i += RASTER_THREADS) skeys[i] = 0xffffffffu;
+        __syncthreads();
+        for (uint32_t k = 2; k <= N; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = tid; i < N; i += RASTER_THREADS) {
+                    uint32_t ixj = i ^ j;
+                    if (ixj > i) {
+                        uint32_t x = skeys[i], y = skeys[ixj];
+                        bool up = (i & k) == 0;
+                        if ((x > y) == up) { skeys[i] = y; skeys[ixj] = x; }
+                    }
+                }
+                __syncthreads();
+            }
+    }
+    const uint32_t tx = tile % a.tilesX, ty = tile / a.tilesX;
+    const uint32_t px = tx * PF_TILE + (tid % PF_TILE), py = ty * PF_TILE + (tid / PF_TILE);
+    const bool inside = px < a.W && py < a.H;
+    const size_t pidx = (size_t)py * a.W + px;
+    uint32_t col = 0; float dep = 0.0f;
+    if (inside) { col = a.color[pidx]; dep = a.depth[pidx]; }
+    unsigned long long frags = 0;
+
+    for (uint32_t c0 = 0; c0 < n; c0 += PRIM_CHUNK) {
+        const uint32_t cn = min((uint32_t)PRIM_CHUNK, n - c0);
+        __syncthreads();
+        if (tid == 0) sHasPhong = 0;
+        __syncthreads();
+        // stage the chunk's records: 8 int4 per PFPrim, 5 int4 per PFPrimPhong
+        for (uint32_t w = tid; w < cn * 8; w += RASTER_THREADS) {
+            uint32_t pi = w >> 3, part = w & 7;
+            uint32_t key = skeys[c0 + pi];
+            uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+            const PFPrim *src = &a.prims[item];
+            if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
+            reinterpret_cast<int4 *>(&sprim[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
+        }
+        __syncthreads();
+        for (uint32_t w = tid; w < cn; w += RASTER_THREADS) {
+            uint32_t st = sprim[w].flags >> 8;
+            if (a.states[st].flags & PFS_PHONG) sHasPhong = 1;
+        }
+        __syncthreads();
+        if (sHasPhong) {
+            for (uint32_t w = tid; w < cn * 5; w += RASTER_THREADS) {
+                uint32_t pi = w / 5, part = w % 5;
+                uint32_t key = skeys[c0 + pi];
+                uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+                const PFPrimPhong *src = &a.primsPh[item];
+                if (sub != 0) src = &a.poolPh[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
+                reinterpret_cast<int4 *>(&sph[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
+            }
+            __syncthreads();
+        }
+        if (!inside) continue;
+        for (uint32_t k = 0; k < cn; k++) {
+            const PFPrim &P = sprim[k];
+            if (!(px >= (uint32_t)P.xMin && px < (uint32_t)P.xMax && py >= (uint32_t)P.yMin && py <= (uint32_t)P.yMax))
+                continue;
+            const int face = P.flags & 1;
+            int32_t w1X = P.y3 - P.y2, w1Y = P.x2 - P.x3, w2X = P.y1 - P.y3, w2Y = P.x3 - P.x1;
+            int32_t w3X = P.y2 - P.y1, w3Y = P.x1 - P.x2;
+            if (face) { w1X = -w1X; w1Y = -w1Y; w2X = -w2X; w2Y = -w2Y; w3X = -w3X; w3Y = -w3Y; }
+            const int32_t w1 = (int32_t)((px - (uint32_t)P.x2) * (uint32_t)w1X + (py - (uint32_t)P.y2) * (uint32_t)w1Y);
+            const int32_t w2 = (int32_t)((px - (uint32_t)P.x3) * (uint32_t)w2X + (py - (uint32_t)P.y3) * (uint32_t)w2Y);
+            const int32_t w3 = (int32_t)((px - (uint32_t)P.x1) * (uint32_t)w3X + (py - (uint32_t)P.y1) * (uint32_t)w3Y);
+            if ((w1 | w2 | w3) <= 0) continue;
+            frags++;
+            const PFDrawState &S = a.states[P.flags >> 8];
+            const float wn1 = (float)w1 * P.wInvSum, wn2 = (float)w2 * P.wInvSum, wn3 = (float)w3 * P.wInvSum;
+            float zs = P.z1 * wn1 + P.z2 * wn2;
+            zs = zs + P.z3 * wn3;
+            const float z = 1.0f / zs;
+            const uint32_t fl = S.flags;
+            if ((fl & PFS_DEPTH_TEST) && !depth_simd(S.depthFunc, z, dep)) continue;
+            uint32_t frag;
+            if (fl & PFS_SMOOTH) {
+                const uint32_t u1 = (uint32_t)x86_cvt_rne(wn1 * 255.0f), u2 = (uint32_t)x86_cvt_rne(wn2 * 255.0f);
+                const uint32_t u3 = (uint32_t)x86_cvt_rne(wn3 * 255.0f);
+                int32_t o[4];
+                for (int i = 0; i < 4; i++) {
+                    uint32_t s = u1 * chn(P.c1, i) + u2 * chn(P.c2, i);
+                    s = s + u3 * chn(P.c3, i);
+                    o[i] = (int32_t)((s * 257u) >> 16);
+                }
+                frag = pack4(o);
+            } else {
+                const float mx = x86_max(wn1, x86_max(wn2, wn3));
+                frag = ((mx == wn1) ? P.c1 : 0u) | (((mx == wn2) ? P.c2 : 0u) | ((mx == wn3) ? P.c3 : 0u));
+            }
+            if (fl & PFS_TEXTURE) {
+                float tu = P.u1 * wn1 + P.u2 * wn2;
+                tu = tu + P.u3 * wn3;
+                float tv = P.v1 * wn1 + P.v2 * wn2;
+                tv = tv + P.v3 * wn3;
+                if (P.flags & 2) { tu = tu * z; tv = tv * z; }
+                frag = blend_simd(4, tex_sample(S, tu, tv), frag);
+            }
+            if (fl & PFS_PHONG) {
+                const PFPrimPhong &Q = sph[k];
+                float N[3], Pp[3];
+                for (int i = 0; i < 3; i++) {
+                    float t0 = Q.n1[i] * wn1 + Q.n2[i] * wn2; N[i] = t0 + Q.n3[i] * wn3;
+                    float t1 = Q.p1[i] * wn1 + Q.p2[i] * wn2; Pp[i] = t1 + Q.p3[i] * wn3;
+                }
+                frag = light_phong(S, frag, S.mat[face], Pp, N);
+            }
+            if (fl & PFS_BLEND) frag = blend_simd(S.blendMode, frag, col);
+            col = frag;
+            if (fl & PFS_DEPTH_MASK) dep = z;
+        }
+    }
+    if (inside) { a.color[pidx] = col; a.depth[pidx] = dep; }
+    // fragment counter: warp reduce, one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
+    if ((tid & 31) == 0 && frags) atomicAdd(&a.cnt->fragments, frags);
+}
+
+// ---------------------------------------------------------------------------
+// framebuffer-wide passes
+// ---------------------------------------------------------------------------
+// pfClear, SIMD build (context.c:680-745): pixels [8, n - n%8) take the clear
+// values, the tail copies pixel 0, pixels 0..7 are left as they are.
+__global__ void k_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd,
+                        const PFDevCounters *cnt, uint32_t command)
+{
+    if (cnt->abortCommand <= command) return;
+    const size_t aligned = n - (n % 8);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (i < 8) continue;
+        if (i < aligned) { color[i] = cc; depth[i] = cd; }
+        else { color[i] = color[0]; depth[i] = depth[0]; }
+    }
+}
+
+// pfClearFramebuffer (framebuffer.c:89-102): every pixel.
+__global__ void k_fill(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd,
+                       const PFDevCounters *cnt, uint32_t command)
+{
+    if (cnt->abortCommand <= command) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        color[i] = cc; depth[i] = cd;
+    }
+}
+
+__global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, PFHookParams hp,
+                       const PFDevCounters *cnt, uint32_t command)
+{
+    if (cnt->abortCommand <= command) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t c = color[i];
+        if (hook == 1) {          // linear fog on depth
+            float d = (depth[i] + hp.znear) / (hp.zfar + hp.znear);
+            float f = (hp.end - d) / (hp.end - hp.start);
+            f = x86_min(x86_max(f, 0.0f), 1.0f);
+            uint32_t k = (uint32_t)x86_cvt_trunc(f * 255.0f);
+            uint32_t r = 0;
+            for (int ch = 0; ch < 4; ch++) r |= (((chn(c, ch) * k + chn(hp.color, ch) * (255u - k)) / 255u) & 255u) << (8 * ch);
+            c = r;
+        } else if (hook == 2) {   // grayscale
+            uint32_t gy = (77u * chn(c, 0) + 150u * chn(c, 1) + 29u * chn(c, 2)) >> 8;
+            c = gy | (gy << 8) | (gy << 16) | (c & 0xff000000u);
+        }
+        color[i] = c;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers (called by pf_host.cpp)
+// ---------------------------------------------------------------------------
+static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+cudaError_t pfd_launch_vertex(const PFSegment *segs, int nSegs, const PFDrawState *states, PFVertexOut *out,
+                              uint32_t nVerts, const PFDevCounters *cnt, cudaStream_t st)
+{
+    if (nVerts == 0) return cudaSuccess;
+    k_vertex<<<grid_for(nVerts, 128), 128, 0, st>>>(segs, nSegs, states, out, nVerts, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
+{
+    if (L.nItems == 0) return cudaSuccess;
+    BinArgs B{ L.binCount, L.bins, L.cap, L.W, L.H, L.tilesX, L.cnt, L.command };
+    k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, L.prims,
+                                                    L.primsPh, L.clipQueue, L.clipQueueCount, B);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_clip<<<152 * 4, 64, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.clipQueue, L.clipQueueCount,
+                                                  L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, B);
+    return cudaGetLastError();
+}
+
+cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
+{
+    RasterArgs a{ L.binCount, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.color, L.depth,
+                  L.W, L.H, L.tilesX, L.cnt, L.command };
+    uint32_t N = 1; while (N < L.cap) N <<= 1;
+    size_t smem = (size_t)N * sizeof(uint32_t);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_raster<<<L.tilesX * L.tilesY, RASTER_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
+                             const PFDevCounters *cnt, uint32_t command, cudaStream_t st)
+{
+    unsigned grid = (unsigned)min((size_t)152 * 8, (n + 255) / 256);
+    if (grid == 0) return cudaSuccess;
+    if (all) k_fill<<<grid, 256, 0, st>>>(color, depth, n, cc, cd, cnt, command);
+    else k_clear<<<grid, 256, 0, st>>>(color, depth, n, cc, cd, cnt, command);
+    return cudaGetLastError();
+}
+
+cudaError_t pfd_launch_hook(uint32_t *color, const float *depth, size_t n, int hook, const PFHookParams &hp,
+                            const PFDevCounters *cnt, uint32_t command, cudaStream_t st)
+{
+    unsigned grid = (unsigned)min((size_t)152 * 8, (n + 255) / 256);
+    if (grid == 0) return cudaSuccess;
+    k_hook<<<grid, 256, 0, st>>>(color, depth, n, hook, hp, cnt, command);
+    return cudaGetLastError();
+}

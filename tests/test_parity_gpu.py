@@ -1,0 +1,107 @@
+"""GPU parity: libpixelforge_gb300.so against the CPU oracle, through the C ABI.
+
+Bar (per the reference's own arithmetic): depth buffers -- hence coverage and
+depth-test outcomes -- bit-exact; RGBA8 colour within 1 LSB per channel
+(the only differing step is the Gouraud specular power, libm powf on the
+host versus the device's pow, which can round the 8-bit specular term
+differently).  Every other pixel is expected to match exactly and the tests
+report how many do not.
+"""
+import numpy as np
+import pytest
+
+from pixelforge_gb300 import abi as A
+from pixelforge_gb300.scenes import PhongScene, SoupScene, SphereScene
+from mixscenes import mix_case, run_mix
+
+pytestmark = pytest.mark.gpu
+
+COLOR_TOL = 1
+
+
+def assert_parity(got, ref, exact_color=False, label=""):
+    assert got.color.shape == ref.color.shape
+    if ref.depth is not None:
+        gd, rd = got.depth.view(np.uint32), ref.depth.view(np.uint32)
+        nd = int((gd != rd).sum())
+        assert nd == 0, f"{label}: {nd} depth values differ"
+    diff = np.abs(got.color.astype(np.int32) - ref.color.astype(np.int32))
+    worst = int(diff.max()) if diff.size else 0
+    ndiff = int((diff.max(-1) > 0).sum())
+    tol = 0 if exact_color else COLOR_TOL
+    assert worst <= tol, f"{label}: colour differs by up to {worst} LSB on {ndiff} pixels"
+    return ndiff
+
+
+def test_soup256_config(gpu, oracle):
+    sc = SoupScene()
+    got, ref = sc.render(gpu), sc.render(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert_parity(got, ref, exact_color=True, label="soup256")
+    assert got.stats["fragments"] == ref.stats["fragments"]
+    assert got.stats["rasterized"] == ref.stats["rasterized"]
+
+
+@pytest.mark.parametrize("kw", [
+    dict(cull=False), dict(shade=A.PF_FLAT), dict(depth_func=A.PF_GREATER, clear_depth=-5.0),
+    dict(depth_func=A.PF_NOTEQUAL), dict(blend=A.PF_BLEND_ALPHA), dict(blend=A.PF_BLEND_SUB),
+    dict(blend=A.PF_BLEND_SCREEN, cull=False), dict(width=250, height=131, ntris=500),
+    dict(xy_range=(-3.0, 3.0), ntris=400),
+])
+def test_soup_variants(gpu, oracle, kw):
+    sc = SoupScene(**kw)
+    assert_parity(sc.render(gpu), sc.render(oracle), exact_color=True, label=str(kw))
+
+
+def test_soup_main_target(gpu, oracle):
+    sc = SoupScene(ntris=700)
+    got, ref = sc.render(gpu, "main"), sc.render(oracle, "main")
+    assert_parity(got, ref, exact_color=True, label="main target")
+
+
+@pytest.mark.parametrize("filt", [A.PF_NEAREST, A.PF_BILINEAR])
+def test_sphere1080(gpu, oracle, filt):
+    sc = SphereScene(filt=filt)
+    got, ref = sc.render(gpu), sc.render(oracle)
+    n = assert_parity(got, ref, label=f"sphere1080 filter={filt}")
+    assert n <= 0.001 * got.color.shape[0] * got.color.shape[1]
+    assert got.stats["fragments"] == ref.stats["fragments"]
+
+
+def test_phong_fog_540(gpu, oracle):
+    sc = PhongScene(subdiv=6, width=960, height=540, tex_size=512)
+    got, ref = sc.render(gpu), sc.render(oracle)
+    assert_parity(got, ref, exact_color=True, label="phong fog")
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_feature_mix(gpu, oracle, seed):
+    case = mix_case(seed, bilinear=True)
+    assert_parity(run_mix(gpu, case), run_mix(oracle, case), label=f"mix {seed} {case}")
+
+
+def test_clear_leaves_first_pixels(gpu, oracle):
+    # pfClear's vector loop starts at pixel 8 and the tail copies pixel 0
+    # (context.c:705-723): a 13x7 buffer (91 pixels, tail of 3).
+    init = np.arange(13 * 7 * 4, dtype=np.uint32).astype(np.uint8).reshape(7, 13, 4)
+    outs = []
+    for lib in (gpu, oracle):
+        from pixelforge_gb300.scenes import Target
+        tg = Target(lib, 13, 7, "main", init=init)
+        lib.pfClearColor(10, 20, 30, 40)
+        lib.pfClear(A.PF_COLOR_BUFFER_BIT)
+        outs.append(tg.finish().color)
+        tg.close()
+    assert np.array_equal(outs[0], outs[1])
+    flat = outs[0].reshape(-1, 4)
+    assert np.array_equal(flat[:8], init.reshape(-1, 4)[:8])
+    assert (flat[8:88] == [10, 20, 30, 40]).all()
+    assert np.array_equal(flat[88:], np.repeat(flat[:1], 3, 0))
+
+
+def test_bin_overflow_replay(gpu, oracle):
+    # thousands of full-screen triangles overflow the first tile-bin capacity;
+    # the flush must grow it and replay from the failing command
+    sc = SoupScene(ntris=3000, xy_range=(-6.0, 6.0), cull=False, width=64, height=64)
+    got, ref = sc.render(gpu), sc.render(oracle)
+    assert_parity(got, ref, exact_color=True, label="overflow")
