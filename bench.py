@@ -134,14 +134,17 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clocks = ClockSampler()
     clocks.start()
-    wall = 0.0
+    wall = rec = 0.0
     for _ in range(args.steps):
         l2_flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         scene.frame(lib)
+        t1 = time.perf_counter()
         lib.pfFinish()
-        wall += time.perf_counter() - t0
+        t2 = time.perf_counter()
+        wall += t2 - t0
+        rec += t1 - t0
     torch.cuda.synchronize()
     ck = clocks.stop()
     st = stats()
@@ -172,6 +175,8 @@ def run_gpu(args):
                    "fragments_per_frame": frags / args.steps,
                    "l2": "flushed between frames (512 MiB write)", "parallelism": "single GPU"},
         "e2e": {"value": frags / wall, "unit": "fragments/s", "ms_per_step": wall * 1e3 / args.steps,
+                "record_ms_per_step": rec * 1e3 / args.steps,
+                "flush_ms_per_step": (wall - rec) * 1e3 / args.steps,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": st["kernel_launches"],
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,

@@ -28,8 +28,6 @@ struct PFBatchLaunch {
     PFPrim *pool;             /* clipped sub-triangles >= 1 */
     PFPrimPhong *poolPh;
     uint32_t poolCap;
-    uint32_t *clipQueue;      /* nItems entries */
-    uint32_t *clipQueueCount;
     uint32_t *binCount;       /* tilesX * tilesY */
     uint32_t *bins;           /* tilesX * tilesY * cap */
     uint32_t cap;
@@ -40,10 +38,14 @@ struct PFBatchLaunch {
     uint32_t command;
 };
 
-cudaError_t pfd_launch_vertex(const PFSegment *segs, int nSegs, const PFDrawState *states, PFVertexOut *out,
-                              uint32_t nVerts, const PFDevCounters *cnt, cudaStream_t st);
+/* k_vertex also zeroes the tile bin counters and the batch counters. */
+cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st);
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
-cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);
+/* clearMode: 0 start from the framebuffer, 1 from a fused pfClear (pixels
+ * 0..7 kept; only when the pixel count is a multiple of 8), 2 from a fused
+ * pfClearFramebuffer. */
+cudaError_t pfd_launch_raster(const PFBatchLaunch &L, int clearMode, uint32_t clearColor, float clearDepth,
+                              cudaStream_t st);
 cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
                              const PFDevCounters *cnt, uint32_t command, cudaStream_t st);
 cudaError_t pfd_launch_hook(uint32_t *color, const float *depth, size_t n, int hook, const PFHookParams &hp,

@@ -267,7 +267,7 @@ struct Ctx {
     // device
     bool devInit = false, devOk = false;
     cudaStream_t stream = nullptr;
-    DevBuf arena, vout, prims, primsPh, pool, poolPh, clipQueue, binCount, bins, counters, misc;
+    DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters, misc;
     uint32_t cap = 256, poolCap = 4096;
     std::unordered_map<const void *, FBMirror> mirrors;     // keyed by framebuffer texture
     PFDevCounters *hostCounters = nullptr;
@@ -651,6 +651,19 @@ bool flush(Ctx *c)
     }
 
     PFDevCounters *dcnt = (PFDevCounters *)c->counters.p;
+    // A clear immediately followed by a DRAW on the same framebuffer is
+    // folded into that DRAW's raster kernel (every tile is written once).
+    // pfClear keeps pixels 0..7 and copies pixel 0 into the tail of a
+    // framebuffer whose size is not a multiple of 8; only the first is
+    // handled in the fused form.
+    std::vector<char> fusedClear(c->cmds.size(), 0);
+    for (size_t ci = 0; ci + 1 < c->cmds.size(); ci++) {
+        const Cmd &a = c->cmds[ci], &b = c->cmds[ci + 1];
+        if ((a.kind == CMD_CLEAR || a.kind == CMD_FILL) && b.kind == CMD_DRAW && a.fb == b.fb) {
+            const Tex *t = (const Tex *)a.fb->texture;
+            if (a.kind == CMD_FILL || ((size_t)t->w * t->h) % 8 == 0) fusedClear[ci] = 1;
+        }
+    }
     uint32_t startCmd = 0;
     for (int attempt = 0;; attempt++) {
         if (!c->vout.ensure((size_t)maxVerts * sizeof(PFVertexOut) + 64) ||
@@ -658,7 +671,6 @@ bool flush(Ctx *c)
             !c->primsPh.ensure(anyPhong ? (size_t)maxItems * sizeof(PFPrimPhong) + 128 : 128) ||
             !c->pool.ensure((size_t)c->poolCap * sizeof(PFPrim)) ||
             !c->poolPh.ensure(anyPhong ? (size_t)c->poolCap * sizeof(PFPrimPhong) : 128) ||
-            !c->clipQueue.ensure((size_t)maxItems * 4 + 64) ||
             !c->binCount.ensure((size_t)maxTiles * 4 + 64) ||
             !c->bins.ensure((size_t)maxTiles * c->cap * 4 + 64) ||
             !c->misc.ensure(64)) {
@@ -681,10 +693,12 @@ bool flush(Ctx *c)
             const Cmd &cmd = c->cmds[ci];
             FBMirror *m = &c->mirrors[(Tex *)cmd.fb->texture];
             const size_t n = m->w * m->h;
-            c->stats.kernel_launches += (cmd.kind == CMD_DRAW) ? 4 : 1;
             if (cmd.kind == CMD_CLEAR || cmd.kind == CMD_FILL) {
+                if (fusedClear[ci]) continue;              // applied by the next DRAW's raster kernel
+                c->stats.kernel_launches += 1;
                 e = pfd_launch_clear(m->dColor, m->dDepth, n, cmd.color, cmd.depth, cmd.kind == CMD_FILL, dcnt, (uint32_t)ci, st);
             } else if (cmd.kind == CMD_HOOK) {
+                c->stats.kernel_launches += 1;
                 e = pfd_launch_hook(m->dColor, m->dDepth, n, cmd.hook, cmd.hp, dcnt, (uint32_t)ci, st);
             } else {
                 const PFSegment *dsegs = (const PFSegment *)(dbase + segsOff) + cmd.segBegin;
@@ -696,26 +710,27 @@ bool flush(Ctx *c)
                 L.vout = (PFVertexOut *)c->vout.p; L.nVerts = nV; L.nItems = nI;
                 L.prims = (PFPrim *)c->prims.p; L.primsPh = (PFPrimPhong *)c->primsPh.p;
                 L.pool = (PFPrim *)c->pool.p; L.poolPh = (PFPrimPhong *)c->poolPh.p; L.poolCap = c->poolCap;
-                L.clipQueue = (uint32_t *)c->clipQueue.p; L.clipQueueCount = (uint32_t *)c->misc.p;
                 L.binCount = (uint32_t *)c->binCount.p; L.bins = (uint32_t *)c->bins.p; L.cap = c->cap;
                 L.color = m->dColor; L.depth = m->dDepth;
                 L.W = (uint32_t)m->w; L.H = (uint32_t)m->h;
                 L.tilesX = (L.W + PF_TILE - 1) / PF_TILE; L.tilesY = (L.H + PF_TILE - 1) / PF_TILE;
                 L.cnt = dcnt; L.command = (uint32_t)ci;
-                e = pfd_launch_vertex(L.segs, ns, dStates, L.vout, nV, dcnt, st);
-                if (e == cudaSuccess) e = cudaMemsetAsync(L.binCount, 0, (size_t)L.tilesX * L.tilesY * 4, st);
-                if (e == cudaSuccess) e = cudaMemsetAsync(L.clipQueueCount, 0, 4, st);
-                if (e == cudaSuccess) e = cudaMemsetAsync(&dcnt->clipCount, 0, 4, st);
-                if (e == cudaSuccess) e = cudaMemsetAsync(&dcnt->batchRasterized, 0, 8, st);
+                int clearMode = 0; uint32_t cc = 0; float cd = 0.0f;
+                if (ci > 0 && fusedClear[ci - 1]) {
+                    const Cmd &cl = c->cmds[ci - 1];
+                    clearMode = (cl.kind == CMD_FILL) ? 2 : 1; cc = cl.color; cd = cl.depth;
+                }
+                c->stats.kernel_launches += 3;
+                e = pfd_launch_vertex(L, st);
                 if (e == cudaSuccess) e = pfd_launch_items(L, st);
                 if (c->timing) {
                     if (c->rasterEv.size() <= nRaster) {
-                        cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b);
-                        c->rasterEv.push_back({ a, b });
+                        cudaEvent_t ev0, ev1; cudaEventCreate(&ev0); cudaEventCreate(&ev1);
+                        c->rasterEv.push_back({ ev0, ev1 });
                     }
                     cudaEventRecord(c->rasterEv[nRaster].first, st);
                 }
-                if (e == cudaSuccess) e = pfd_launch_raster(L, st);
+                if (e == cudaSuccess) e = pfd_launch_raster(L, clearMode, cc, cd, st);
                 if (c->timing) cudaEventRecord(c->rasterEv[nRaster].second, st);
                 nRaster++;
             }
@@ -723,6 +738,16 @@ bool flush(Ctx *c)
         }
         if (c->timing) cudaEventRecord(c->evEnd, st);
         e = cudaMemcpyAsync(c->hostCounters, dcnt, sizeof(PFDevCounters), cudaMemcpyDeviceToHost, st);
+        // write back colour (and user-visible depth); if a bin overflowed the
+        // replay below writes back again
+        for (PFframebuffer *fb : used) {
+            if (e != cudaSuccess) break;
+            FBMirror *m = &c->mirrors[(Tex *)fb->texture];
+            const size_t n = m->w * m->h;
+            e = cudaMemcpyAsync(m->tex->pixels, m->dColor, n * 4, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess && m->depthUserVisible)
+                e = cudaMemcpyAsync(m->hostDepth, m->dDepth, n * 4, cudaMemcpyDeviceToHost, st);
+        }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail("pipeline", e);
         if (c->timing) {
@@ -759,19 +784,9 @@ bool flush(Ctx *c)
         if (hc.status & PFD_CLIP_OVERFLOW) c->poolCap = std::max(c->poolCap * 4, hc.clipCount * 2);
         if (attempt > 8) return fail("overflow retries", cudaErrorUnknown);
         startCmd = hc.abortCommand;
+        if (startCmd > 0 && fusedClear[startCmd - 1]) startCmd -= 1;   // the fused clear did not run either
     }
 
-    // --- write back -------------------------------------------------------------
-    for (PFframebuffer *fb : used) {
-        FBMirror *m = &c->mirrors[(Tex *)fb->texture];
-        const size_t n = m->w * m->h;
-        e = cudaMemcpyAsync(m->tex->pixels, m->dColor, n * 4, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess && m->depthUserVisible)
-            e = cudaMemcpyAsync(m->hostDepth, m->dDepth, n * 4, cudaMemcpyDeviceToHost, st);
-        if (e != cudaSuccess) return fail("cudaMemcpyAsync(write-back)", e);
-    }
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return fail("write-back", e);
     c->stats.flushes += 1;
     discard_recording(c);
     return true;
@@ -830,7 +845,7 @@ void pfDeleteContext(PFcontext ctx)
     release_mirrors(c);
     if (c->devOk) {
         c->arena.release(); c->vout.release(); c->prims.release(); c->primsPh.release(); c->pool.release();
-        c->poolPh.release(); c->clipQueue.release(); c->binCount.release(); c->bins.release();
+        c->poolPh.release(); c->binCount.release(); c->bins.release();
         c->counters.release(); c->misc.release();
         if (c->hostCounters) cudaFreeHost(c->hostCounters);
         if (c->evStart) { cudaEventDestroy(c->evStart); cudaEventDestroy(c->evEnd); }

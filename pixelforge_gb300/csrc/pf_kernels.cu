@@ -3,14 +3,15 @@
 //   k_vertex   one thread per vertex: transform, Gouraud lighting
 //              (src/internal/primitives/triangles.c:72-104, lighting.c:24-134)
 //   k_items    one thread per triangle-face item, in submission order:
-//              2D/3D decision, unclipped projection, setup, cull and
-//              order-keyed binning into 16x16 tiles (triangles.c:246-339);
-//              items that cross a clip plane are queued for k_clip
-//   k_clip     polygon clipping of queued items (triangles.c:157-244)
-//   k_raster   one CTA per tile: sorts the tile's bin keys (submission
-//              order), then evaluates every sub-triangle for the tile's 256
-//              pixels with the reference's integer edge functions, depth
-//              test, texturing, Phong, blending (triangles.c:398-557)
+//              2D/3D decision, projection, polygon clipping of the rare items
+//              that cross a plane (triangles.c:157-280), setup, cull and
+//              order-keyed binning into 16x16 tiles (triangles.c:287-339)
+//   k_raster   one CTA per tile: restores submission order of the tile's
+//              bin, then per chunk of sub-triangles computes coverage with
+//              the reference's integer edge functions, shades fragments
+//              densely and resolves each pixel's fragments in order (depth
+//              test, blend) (triangles.c:398-557); optionally starts from
+//              a fused clear
 //   k_clear, k_fill, k_hook  framebuffer-wide passes (pfClear,
 //              pfClearFramebuffer, device post-process hooks)
 //
@@ -83,6 +84,22 @@ __device__ __forceinline__ float v3_dot(const float *a, const float *b) { return
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t min255(int32_t n) { return (uint32_t)(n | ((255 - n) >> 31)) & 255u; }
 
+// powf(x, y) for the Gouraud specular term (lighting.c:114), correctly
+// rounded through double precision.  Whole exponents up to 256 (shininess is
+// usually one) use binary powering in double -- at most 16 roundings of 2^-53
+// each, far below the float rounding step -- instead of the FP64 pow routine,
+// which is slow on this part.
+__device__ __forceinline__ float pow_gouraud(float x, float y)
+{
+    if (y >= 1.0f && y <= 256.0f && y == truncf(y)) {
+        uint32_t n = (uint32_t)y;
+        double b = (double)x, r = 1.0;
+        while (n) { if (n & 1u) r *= b; b *= b; n >>= 1; }
+        return (float)r;
+    }
+    return (float)pow((double)x, (double)y);
+}
+
 __device__ uint32_t light_gouraud(const PFDrawState &S, const PFDevMaterial &m, uint32_t diffuse,
                                   const float *P, const float *N)
 {
@@ -134,7 +151,7 @@ __device__ uint32_t light_gouraud(const PFDrawState &S, const PFDevMaterial &m, 
                 float H[3] = { L[0] + V[0], L[1] + V[1], L[2] + V[2] };
                 v3_normalize(H);
                 float nh = fmaxf(v3_dot(N, H), 0.0f);
-                float pw = (float)pow((double)nh, (double)shin);
+                float pw = pow_gouraud(nh, shin);
                 uint32_t spec = x86_ftoub(255.0f * pw);
                 lR = min255((int32_t)(lR + (chn(m.spec, 0) * chn(l.spec, 0) * spec) / (255 * 255)));
                 lG = min255((int32_t)(lG + (chn(m.spec, 1) * chn(l.spec, 1) * spec) / (255 * 255)));
@@ -417,11 +434,17 @@ __device__ __forceinline__ int seg_of_item(const PFSegment *segs, int nSegs, uin
     return lo;
 }
 
+// One thread per vertex of the batch.  The grid also clears the tile bin
+// counters and the per-batch counters for k_items (so no memset launches).
 __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
-                         PFVertexOut *__restrict__ out, uint32_t nVerts, const PFDevCounters *cnt)
+                         PFVertexOut *__restrict__ out, uint32_t nVerts, PFDevCounters *cnt,
+                         uint32_t *__restrict__ binCount, uint32_t nTiles)
 {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nVerts || cnt->abortCommand != 0xffffffffu) return;
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cnt->abortCommand != 0xffffffffu) return;
+    for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
+    if (g == 0) { cnt->clipCount = 0; cnt->batchRasterized = 0; }
+    if (g >= nVerts) return;
     const PFSegment &sg = segs[seg_of_vertex(segs, nSegs, g)];
     const PFDrawState &S = states[sg.state];
     const uint32_t j = g - sg.vtxBase;
@@ -473,7 +496,7 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
 }
 
 // ---------------------------------------------------------------------------
-// setup + binning (shared by k_items and k_clip)
+// setup + binning
 // ---------------------------------------------------------------------------
 struct SVert {                 // a vertex after projection to the screen
     float sx, sy, z, u, v;
@@ -566,9 +589,6 @@ __device__ __forceinline__ void store_phong(PFPrimPhong *dst, const SVert &a, co
     *dst = q;
 }
 
-// ---------------------------------------------------------------------------
-// k_items
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ void item_vertices(const PFSegment &sg, uint32_t k, uint32_t v[3], int &face)
 {
     uint32_t s[3];
@@ -577,70 +597,19 @@ __device__ __forceinline__ void item_vertices(const PFSegment &sg, uint32_t k, u
         face = (sg.nFaces == 2) ? (int)(k & 1) : sg.face0;
         s[0] = 3 * tri; s[1] = 3 * tri + 1; s[2] = 3 * tri + 2;
     } else {
-        const int32_t *e = sg.explicitItems + 4 * (size_t)k;
-        s[0] = (uint32_t)e[0]; s[1] = (uint32_t)e[1]; s[2] = (uint32_t)e[2]; face = e[3];
+        const int4 e = reinterpret_cast<const int4 *>(sg.explicitItems)[k];
+        s[0] = (uint32_t)e.x; s[1] = (uint32_t)e.y; s[2] = (uint32_t)e.z; face = e.w;
     }
     for (int m = 0; m < 3; m++) {
-        uint32_t j = sg.idx ? sg.idx[s[m]] : s[m];
+        uint32_t j = sg.idx ? __ldg(sg.idx + s[m]) : s[m];
         if (j >= sg.nVerts) j = sg.nVerts - 1;        // memory guard; the host sizes nVerts from the indices
         v[m] = sg.vtxBase + j;
     }
 }
 
-__global__ void k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
-                        const PFVertexOut *__restrict__ vout, uint32_t nItems,
-                        PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
-                        uint32_t *__restrict__ clipQueue, uint32_t *__restrict__ clipQueueCount, BinArgs B)
-{
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nItems || B.cnt->abortCommand != 0xffffffffu) return;
-    const PFSegment &sg = segs[seg_of_item(segs, nSegs, g)];
-    const PFDrawState &S = states[sg.state];
-    uint32_t vi[3]; int face;
-    item_vertices(sg, g - sg.itemBase, vi, face);
-    const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
-    float ws = 0.0f;
-    for (int m = 0; m < 3; m++) ws += V[m]->h[3];
-    const bool is2D = fabsf(ws - 3.0f) < 1e-5f;
-    if (!is2D) {
-        bool inside = true;
-        for (int m = 0; m < 3; m++) {
-            const float *h = V[m]->h;
-            inside = inside && !(h[3] < 1e-5f);
-            for (int ax = 0; ax < 3; ax++) inside = inside && (h[ax] <= h[3]) && (-h[ax] <= h[3]);
-        }
-        if (!inside) {                                   // clip plane crossed: k_clip handles it
-            uint32_t q = atomicAdd(clipQueueCount, 1u);
-            clipQueue[q] = g;
-            return;
-        }
-    }
-    SVert s[3];
-    for (int m = 0; m < 3; m++) {
-        const PFVertexOut &o = *V[m];
-        if (is2D) {
-            to_screen(S, o.h[0], o.h[1], s[m].sx, s[m].sy);
-            s[m].z = o.h[2]; s[m].u = o.uv[0]; s[m].v = o.uv[1];
-        } else {
-            float hz = 1.0f / o.h[2];
-            s[m].u = o.uv[0] * hz; s[m].v = o.uv[1] * hz;
-            float invW = 1.0f / o.h[3];
-            to_screen(S, o.h[0] * invW, o.h[1] * invW, s[m].sx, s[m].sy);
-            s[m].z = hz;
-        }
-        s[m].c = o.col[face];
-        for (int i = 0; i < 3; i++) { s[m].n[i] = o.n[i]; s[m].p[i] = o.p[i]; }
-    }
-    PFPrim P;
-    if (!setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P)) return;
-    atomicAdd(&B.cnt->batchRasterized, 1ull);
-    prims[g] = P;
-    if (S.flags & PFS_PHONG) store_phong(&primsPh[g], s[0], s[1], s[2]);
-    bin_prim(B, P, g << PF_SUB_BITS);
-}
-
 // ---------------------------------------------------------------------------
-// k_clip (triangles.c:157-280)
+// polygon clipping (triangles.c:157-280), for the rare items that cross a
+// clip plane; called out of line from k_items
 // ---------------------------------------------------------------------------
 struct CVert { float h[4]; float pos[4]; float n[3]; float uv[2]; uint32_t c; };
 
@@ -688,41 +657,23 @@ __device__ int clip_plane(CVert *poly, int n, CVert *tmp, int ax, int sign)
     return m;
 }
 
-__device__ __noinline__ void clip_one(const PFSegment *__restrict__ segs, int nSegs,
-                                      const PFDrawState *__restrict__ states, const PFVertexOut *__restrict__ vout,
-                                      uint32_t g, PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
-                                      PFPrim *__restrict__ pool, PFPrimPhong *__restrict__ poolPh, uint32_t poolCap,
-                                      const BinArgs &B);
+struct ItemOut {
+    PFPrim *prims;
+    PFPrimPhong *primsPh;
+    PFPrim *pool;
+    PFPrimPhong *poolPh;
+    uint32_t poolCap;
+};
 
-__global__ void k_clip(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
-                       const PFVertexOut *__restrict__ vout, const uint32_t *__restrict__ clipQueue,
-                       const uint32_t *__restrict__ clipQueueCount,
-                       PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
-                       PFPrim *__restrict__ pool, PFPrimPhong *__restrict__ poolPh, uint32_t poolCap,
-                       BinArgs B)
+__device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const PFVertexOut *const *V, int face,
+                                       uint32_t g, const ItemOut &O, const BinArgs &B)
 {
-    if (B.cnt->abortCommand != 0xffffffffu) return;
-    const uint32_t nq = *clipQueueCount;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
-        clip_one(segs, nSegs, states, vout, clipQueue[q], prims, primsPh, pool, poolPh, poolCap, B);
-}
-
-__device__ __noinline__ void clip_one(const PFSegment *__restrict__ segs, int nSegs,
-                                      const PFDrawState *__restrict__ states, const PFVertexOut *__restrict__ vout,
-                                      uint32_t g, PFPrim *__restrict__ prims, PFPrimPhong *__restrict__ primsPh,
-                                      PFPrim *__restrict__ pool, PFPrimPhong *__restrict__ poolPh, uint32_t poolCap,
-                                      const BinArgs &B)
-{
-    const PFSegment &sg = segs[seg_of_item(segs, nSegs, g)];
-    const PFDrawState &S = states[sg.state];
-    uint32_t vi[3]; int face;
-    item_vertices(sg, g - sg.itemBase, vi, face);
     CVert poly[PF_CLIP_MAXV], tmp[PF_CLIP_MAXV];
     for (int m = 0; m < 3; m++) {
-        const PFVertexOut &o = vout[vi[m]];
+        const PFVertexOut &o = *V[m];
         for (int i = 0; i < 4; i++) poly[m].h[i] = o.h[i];
         poly[m].pos[0] = o.p[0]; poly[m].pos[1] = o.p[1]; poly[m].pos[2] = o.p[2];
-        poly[m].pos[3] = 1.0f;
+        poly[m].pos[3] = 1.0f;     // object-space w is not read after clipping
         for (int i = 0; i < 3; i++) poly[m].n[i] = o.n[i];
         poly[m].uv[0] = o.uv[0]; poly[m].uv[1] = o.uv[1];
         poly[m].c = o.col[face];
@@ -748,7 +699,7 @@ __device__ __noinline__ void clip_one(const PFSegment *__restrict__ segs, int nS
     uint32_t base = 0;
     if (nsub > 1) {
         base = atomicAdd(&B.cnt->clipCount, (unsigned)(nsub - 1));
-        if (base + (uint32_t)(nsub - 1) > poolCap) {
+        if (base + (uint32_t)(nsub - 1) > O.poolCap) {
             atomicOr(&B.cnt->status, (unsigned)PFD_CLIP_OVERFLOW);
             atomicMin(&B.cnt->abortCommand, B.command);
             return;
@@ -758,28 +709,97 @@ __device__ __noinline__ void clip_one(const PFSegment *__restrict__ segs, int nS
     bool firstSet = false;
     for (int i = 0; i < nsub; i++) {
         PFPrim P;
-        if (!setup_prim(S, face, true, s[0], s[i + 1], s[i + 2], sg.state, P)) continue;
+        if (!setup_prim(S, face, true, s[0], s[i + 1], s[i + 2], stateIdx, P)) continue;
         atomicAdd(&B.cnt->batchRasterized, 1ull);
         if (i == 0) { first = P; firstSet = true; }
         else {
-            pool[base + i - 1] = P;
-            if (S.flags & PFS_PHONG) store_phong(&poolPh[base + i - 1], s[0], s[i + 1], s[i + 2]);
+            O.pool[base + i - 1] = P;
+            if (S.flags & PFS_PHONG) store_phong(&O.poolPh[base + i - 1], s[0], s[i + 1], s[i + 2]);
         }
         bin_prim(B, P, (g << PF_SUB_BITS) | (uint32_t)i);
     }
-    // prims[g] carries the pool base for sub-triangles >= 1 even when
+    // prims[g] carries the pool base of sub-triangles >= 1 even when
     // sub-triangle 0 was culled.
     if (!firstSet) { first.flags = 0; first.xMin = 1; first.xMax = 0; }
     first.poolBase = (int32_t)base;
-    prims[g] = first;
-    if (firstSet && (S.flags & PFS_PHONG)) store_phong(&primsPh[g], s[0], s[1], s[2]);
+    O.prims[g] = first;
+    if (firstSet && (S.flags & PFS_PHONG)) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
 }
 
 // ---------------------------------------------------------------------------
-// k_raster
+// k_items: one thread per triangle-face item, in submission order
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
+                        const PFVertexOut *__restrict__ vout, uint32_t nItems, ItemOut O, BinArgs B)
+{
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nItems || B.cnt->abortCommand != 0xffffffffu) return;
+    const PFSegment &sg = segs[seg_of_item(segs, nSegs, g)];
+    const PFDrawState &S = states[sg.state];
+    uint32_t vi[3]; int face;
+    item_vertices(sg, g - sg.itemBase, vi, face);
+    const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
+    float4 hv[3];
+    for (int m = 0; m < 3; m++) hv[m] = *reinterpret_cast<const float4 *>(V[m]->h);
+    float ws = 0.0f;
+    for (int m = 0; m < 3; m++) ws += hv[m].w;
+    const bool is2D = fabsf(ws - 3.0f) < 1e-5f;
+    if (!is2D) {
+        bool inside = true;
+        for (int m = 0; m < 3; m++) {
+            const float4 h = hv[m];
+            inside = inside && !(h.w < 1e-5f) && (h.x <= h.w) && (-h.x <= h.w) && (h.y <= h.w) && (-h.y <= h.w) &&
+                     (h.z <= h.w) && (-h.z <= h.w);
+        }
+        if (!inside) { clip_item(S, sg.state, V, face, g, O, B); return; }
+    }
+    SVert s[3];
+    for (int m = 0; m < 3; m++) {
+        const PFVertexOut &o = *V[m];
+        const float4 h = hv[m];
+        const float2 uv = *reinterpret_cast<const float2 *>(o.uv);
+        if (is2D) {
+            to_screen(S, h.x, h.y, s[m].sx, s[m].sy);
+            s[m].z = h.z; s[m].u = uv.x; s[m].v = uv.y;
+        } else {
+            float hz = 1.0f / h.z;
+            s[m].u = uv.x * hz; s[m].v = uv.y * hz;
+            float invW = 1.0f / h.w;
+            to_screen(S, h.x * invW, h.y * invW, s[m].sx, s[m].sy);
+            s[m].z = hz;
+        }
+        s[m].c = o.col[face];
+        if (S.flags & PFS_PHONG)
+            for (int i = 0; i < 3; i++) { s[m].n[i] = o.n[i]; s[m].p[i] = o.p[i]; }
+    }
+    PFPrim P;
+    if (!setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P)) return;
+    atomicAdd(&B.cnt->batchRasterized, 1ull);
+    O.prims[g] = P;
+    if (S.flags & PFS_PHONG) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
+    bin_prim(B, P, g << PF_SUB_BITS);
+}
+
+// ---------------------------------------------------------------------------
+// k_raster: one CTA per 16x16 tile
+//
+// For each chunk of CH sub-triangles (in submission order):
+//   1. stage the records in shared memory, with each one's bounding box
+//      clipped to the tile and its edge functions at the tile origin;
+//   2. coverage, prim-parallel: the (sub-triangle, pixel) pairs of all
+//      clipped boxes are spread over the CTA's threads; a covered pair sets
+//      bit k of the pixel's 32-bit mask, so a pixel's fragments are ordered
+//      by bit position = submission order;
+//   3. shading, fragment-parallel: each warp compacts the fragments of its 32
+//      pixels and shades them densely (texture, Gouraud / Phong colour) --
+//      the source colour does not depend on the destination;
+//   4. resolve: every pixel applies its fragments in order (depth test,
+//      blend, depth write) on its colour and depth held in registers.
 // ---------------------------------------------------------------------------
 #define RASTER_THREADS PF_TILE_PIXELS
-#define PRIM_CHUNK 32
+#define CH 32
+#define FWIN 256
+#define RANK_SORT_MAX 1024
 
 struct RasterArgs {
     const uint32_t *binCount;
@@ -795,13 +815,70 @@ struct RasterArgs {
     uint32_t W, H, tilesX;
     PFDevCounters *cnt;
     uint32_t command;
+    int clearMode;            // 0 none, 1 pfClear (pixels 0..7 kept), 2 every pixel
+    uint32_t clearColor;
+    float clearDepth;
 };
 
-__global__ void __launch_bounds__(RASTER_THREADS) k_raster(RasterArgs a)
+struct ChunkPrim {             // per-sub-triangle data derived for this tile
+    int32_t e0[3];             // edge functions at the tile origin
+    int32_t ex[3], ey[3];      // their x and y steps
+    uint32_t bx0, by0, bw, bh; // bounding box clipped to the tile (tile-relative)
+    float invBw;
+    uint32_t flags;            // face | is3D | state << 8
+};
+
+// Source colour of one fragment (triangles.c:500-521): colour interpolation,
+// texturing, per-fragment lighting.  Independent of the destination pixel.
+__device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrimPhong *Q, const PFDrawState &S,
+                                                   float wn1, float wn2, float wn3, float z)
 {
-    extern __shared__ uint32_t skeys[];
-    __shared__ PFPrim sprim[PRIM_CHUNK];
-    __shared__ PFPrimPhong sph[PRIM_CHUNK];
+    const uint32_t fl = S.flags;
+    uint32_t frag;
+    if (fl & PFS_SMOOTH) {
+        const uint32_t u1 = (uint32_t)x86_cvt_rne(wn1 * 255.0f), u2 = (uint32_t)x86_cvt_rne(wn2 * 255.0f);
+        const uint32_t u3 = (uint32_t)x86_cvt_rne(wn3 * 255.0f);
+        int32_t o[4];
+        for (int i = 0; i < 4; i++) {
+            uint32_t s = u1 * chn(P.c1, i) + u2 * chn(P.c2, i);
+            s = s + u3 * chn(P.c3, i);
+            o[i] = (int32_t)((s * 257u) >> 16);
+        }
+        frag = pack4(o);
+    } else {
+        const float mx = x86_max(wn1, x86_max(wn2, wn3));
+        frag = ((mx == wn1) ? P.c1 : 0u) | (((mx == wn2) ? P.c2 : 0u) | ((mx == wn3) ? P.c3 : 0u));
+    }
+    if (fl & PFS_TEXTURE) {
+        float tu = P.u1 * wn1 + P.u2 * wn2;
+        tu = tu + P.u3 * wn3;
+        float tv = P.v1 * wn1 + P.v2 * wn2;
+        tv = tv + P.v3 * wn3;
+        if (P.flags & 2) { tu = tu * z; tv = tv * z; }
+        frag = blend_simd(4, tex_sample(S, tu, tv), frag);
+    }
+    if (fl & PFS_PHONG) {
+        float N[3], Pp[3];
+        for (int i = 0; i < 3; i++) {
+            float t0 = Q->n1[i] * wn1 + Q->n2[i] * wn2; N[i] = t0 + Q->n3[i] * wn3;
+            float t1 = Q->p1[i] * wn1 + Q->p2[i] * wn2; Pp[i] = t1 + Q->p3[i] * wn3;
+        }
+        frag = light_phong(S, frag, S.mat[P.flags & 1], Pp, N);
+    }
+    return frag;
+}
+
+__global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
+{
+    extern __shared__ uint32_t skeys[];               // [N] keys (+ [n] sorted copy when rank-sorting)
+    __shared__ PFPrim sprim[CH];
+    __shared__ PFPrimPhong sph[CH];
+    __shared__ ChunkPrim scp[CH];
+    __shared__ uint32_t sarea[CH + 1];
+    __shared__ uint32_t pmask[RASTER_THREADS];
+    __shared__ uint32_t fcol[RASTER_THREADS / 32][FWIN];
+    __shared__ float fz[RASTER_THREADS / 32][FWIN];
+    __shared__ uint32_t woff[RASTER_THREADS / 32][33];
     __shared__ int sHasPhong;
 
     if (a.cnt->abortCommand <= a.command) return;
@@ -809,132 +886,199 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(RasterArgs a)
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.cnt->rasterized, a.cnt->batchRasterized);
     const uint32_t tile = blockIdx.x;
     const uint32_t n = min(a.binCount[tile], a.cap);
-    if (n == 0) return;
-    const int tid = threadIdx.x;
-    const uint32_t *bin = a.bins + (size_t)tile * a.cap;
-    for (uint32_t i = tid; i < n; i += RASTER_THREADS) skeys[i] = bin[i];
-    __syncthreads();
-    // keys arrive in atomic order; restore submission order
-    int unsorted = 0;
-    for (uint32_t i = tid; i + 1 < n; i += RASTER_THREADS) unsorted |= (skeys[i] > skeys[i + 1]);
-    if (__syncthreads_or(unsorted)) {
-        uint32_t N = 1; while (N < n) N <<= 1;
-        for (uint32_t i = n + tid; i < N; i += RASTER_THREADS) skeys[i] = 0xffffffffu;
-        __syncthreads();
-        for (uint32_t k = 2; k <= N; k <<= 1)
-            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                for (uint32_t i = tid; i < N; i += RASTER_THREADS) {
-                    uint32_t ixj = i ^ j;
-                    if (ixj > i) {
-                        uint32_t x = skeys[i], y = skeys[ixj];
-                        bool up = (i & k) == 0;
-                        if ((x > y) == up) { skeys[i] = y; skeys[ixj] = x; }
-                    }
-                }
-                __syncthreads();
-            }
-    }
+    if (n == 0 && a.clearMode == 0) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t tx = tile % a.tilesX, ty = tile / a.tilesX;
-    const uint32_t px = tx * PF_TILE + (tid % PF_TILE), py = ty * PF_TILE + (tid / PF_TILE);
+    const uint32_t ox = tx * PF_TILE, oy = ty * PF_TILE;
+    const uint32_t lx = tid % PF_TILE, ly = tid / PF_TILE;
+    const uint32_t px = ox + lx, py = oy + ly;
     const bool inside = px < a.W && py < a.H;
     const size_t pidx = (size_t)py * a.W + px;
-    uint32_t col = 0; float dep = 0.0f;
-    if (inside) { col = a.color[pidx]; dep = a.depth[pidx]; }
-    unsigned long long frags = 0;
 
-    for (uint32_t c0 = 0; c0 < n; c0 += PRIM_CHUNK) {
-        const uint32_t cn = min((uint32_t)PRIM_CHUNK, n - c0);
+    // pixel state in registers
+    uint32_t col = 0; float dep = 0.0f;
+    if (inside) {
+        if (a.clearMode == 2 || (a.clearMode == 1 && pidx >= 8)) { col = a.clearColor; dep = a.clearDepth; }
+        else { col = a.color[pidx]; dep = a.depth[pidx]; }
+    }
+
+    unsigned long long frags = 0;
+    if (n > 0) {
+        const uint32_t *bin = a.bins + (size_t)tile * a.cap;
+        for (uint32_t i = tid; i < n; i += RASTER_THREADS) skeys[i] = bin[i];
         __syncthreads();
-        if (tid == 0) sHasPhong = 0;
-        __syncthreads();
-        // stage the chunk's records: 8 int4 per PFPrim, 5 int4 per PFPrimPhong
-        for (uint32_t w = tid; w < cn * 8; w += RASTER_THREADS) {
-            uint32_t pi = w >> 3, part = w & 7;
-            uint32_t key = skeys[c0 + pi];
-            uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
-            const PFPrim *src = &a.prims[item];
-            if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-            reinterpret_cast<int4 *>(&sprim[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
+        // keys arrive in atomic order; restore submission order
+        int unsorted = 0;
+        for (uint32_t i = tid; i + 1 < n; i += RASTER_THREADS) unsorted |= (skeys[i] > skeys[i + 1]);
+        const uint32_t *keys = skeys;
+        if (__syncthreads_or(unsorted)) {
+            if (n <= RANK_SORT_MAX) {
+                // rank sort: keys are unique; rank = number of smaller keys
+                uint32_t *dst = skeys + RANK_SORT_MAX;
+                for (uint32_t i = tid; i < n; i += RASTER_THREADS) {
+                    const uint32_t k = skeys[i];
+                    uint32_t r = 0;
+                    for (uint32_t j = 0; j < n; j++) r += (skeys[j] < k);
+                    dst[r] = k;
+                }
+                __syncthreads();
+                keys = dst;
+            } else {
+                uint32_t N = 1; while (N < n) N <<= 1;
+                for (uint32_t i = n + tid; i < N; i += RASTER_THREADS) skeys[i] = 0xffffffffu;
+                __syncthreads();
+                for (uint32_t k = 2; k <= N; k <<= 1)
+                    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                        for (uint32_t i = tid; i < N; i += RASTER_THREADS) {
+                            uint32_t ixj = i ^ j;
+                            if (ixj > i) {
+                                uint32_t x = skeys[i], y = skeys[ixj];
+                                bool up = (i & k) == 0;
+                                if ((x > y) == up) { skeys[i] = y; skeys[ixj] = x; }
+                            }
+                        }
+                        __syncthreads();
+                    }
+            }
         }
-        __syncthreads();
-        for (uint32_t w = tid; w < cn; w += RASTER_THREADS) {
-            uint32_t st = sprim[w].flags >> 8;
-            if (a.states[st].flags & PFS_PHONG) sHasPhong = 1;
-        }
-        __syncthreads();
-        if (sHasPhong) {
-            for (uint32_t w = tid; w < cn * 5; w += RASTER_THREADS) {
-                uint32_t pi = w / 5, part = w % 5;
-                uint32_t key = skeys[c0 + pi];
-                uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
-                const PFPrimPhong *src = &a.primsPh[item];
-                if (sub != 0) src = &a.poolPh[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-                reinterpret_cast<int4 *>(&sph[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
+
+        for (uint32_t c0 = 0; c0 < n; c0 += CH) {
+            const uint32_t cn = min((uint32_t)CH, n - c0);
+            __syncthreads();
+            if (tid == 0) sHasPhong = 0;
+            // 1. stage records: 8 int4 per PFPrim
+            for (uint32_t w = tid; w < cn * 8; w += RASTER_THREADS) {
+                const uint32_t pi = w >> 3, part = w & 7;
+                const uint32_t key = keys[c0 + pi];
+                const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+                const PFPrim *src = &a.prims[item];
+                if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
+                reinterpret_cast<int4 *>(&sprim[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
+            }
+            pmask[tid] = 0;
+            __syncthreads();
+            // derived per-sub-triangle data (one thread each)
+            if (tid < cn) {
+                const PFPrim &P = sprim[tid];
+                ChunkPrim cp;
+                cp.flags = P.flags;
+                const int face = P.flags & 1;
+                int32_t sx[3] = { P.y3 - P.y2, P.y1 - P.y3, P.y2 - P.y1 };
+                int32_t sy[3] = { P.x2 - P.x3, P.x3 - P.x1, P.x1 - P.x2 };
+                const int32_t rx[3] = { P.x2, P.x3, P.x1 }, ry[3] = { P.y2, P.y3, P.y1 };
+                for (int e = 0; e < 3; e++) {
+                    if (face) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
+                    cp.ex[e] = sx[e]; cp.ey[e] = sy[e];
+                    cp.e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
+                }
+                // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside tile and framebuffer
+                uint32_t x0 = max((uint32_t)P.xMin, ox), x1 = min(min((uint32_t)P.xMax, ox + PF_TILE), a.W);
+                uint32_t y0 = max((uint32_t)P.yMin, oy), y1e = min(min((uint32_t)P.yMax + 1u, oy + PF_TILE), a.H);
+                if ((uint32_t)P.yMax == 0xffffffffu) y1e = 0;    // yMax + 1 wrapped
+                const bool empty = (x0 >= x1) || (y0 >= y1e) || ((uint32_t)P.xMin >= (uint32_t)P.xMax) ||
+                                   ((uint32_t)P.yMin > (uint32_t)P.yMax);
+                cp.bx0 = empty ? 0 : x0 - ox; cp.by0 = empty ? 0 : y0 - oy;
+                cp.bw = empty ? 0 : x1 - x0; cp.bh = empty ? 0 : y1e - y0;
+                cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
+                scp[tid] = cp;
+                if (a.states[P.flags >> 8].flags & PFS_PHONG) sHasPhong = 1;
             }
             __syncthreads();
-        }
-        if (!inside) continue;
-        for (uint32_t k = 0; k < cn; k++) {
-            const PFPrim &P = sprim[k];
-            if (!(px >= (uint32_t)P.xMin && px < (uint32_t)P.xMax && py >= (uint32_t)P.yMin && py <= (uint32_t)P.yMax))
-                continue;
-            const int face = P.flags & 1;
-            int32_t w1X = P.y3 - P.y2, w1Y = P.x2 - P.x3, w2X = P.y1 - P.y3, w2Y = P.x3 - P.x1;
-            int32_t w3X = P.y2 - P.y1, w3Y = P.x1 - P.x2;
-            if (face) { w1X = -w1X; w1Y = -w1Y; w2X = -w2X; w2Y = -w2Y; w3X = -w3X; w3Y = -w3Y; }
-            const int32_t w1 = (int32_t)((px - (uint32_t)P.x2) * (uint32_t)w1X + (py - (uint32_t)P.y2) * (uint32_t)w1Y);
-            const int32_t w2 = (int32_t)((px - (uint32_t)P.x3) * (uint32_t)w2X + (py - (uint32_t)P.y3) * (uint32_t)w2Y);
-            const int32_t w3 = (int32_t)((px - (uint32_t)P.x1) * (uint32_t)w3X + (py - (uint32_t)P.y1) * (uint32_t)w3Y);
-            if ((w1 | w2 | w3) <= 0) continue;
-            frags++;
-            const PFDrawState &S = a.states[P.flags >> 8];
-            const float wn1 = (float)w1 * P.wInvSum, wn2 = (float)w2 * P.wInvSum, wn3 = (float)w3 * P.wInvSum;
-            float zs = P.z1 * wn1 + P.z2 * wn2;
-            zs = zs + P.z3 * wn3;
-            const float z = 1.0f / zs;
-            const uint32_t fl = S.flags;
-            if ((fl & PFS_DEPTH_TEST) && !depth_simd(S.depthFunc, z, dep)) continue;
-            uint32_t frag;
-            if (fl & PFS_SMOOTH) {
-                const uint32_t u1 = (uint32_t)x86_cvt_rne(wn1 * 255.0f), u2 = (uint32_t)x86_cvt_rne(wn2 * 255.0f);
-                const uint32_t u3 = (uint32_t)x86_cvt_rne(wn3 * 255.0f);
-                int32_t o[4];
-                for (int i = 0; i < 4; i++) {
-                    uint32_t s = u1 * chn(P.c1, i) + u2 * chn(P.c2, i);
-                    s = s + u3 * chn(P.c3, i);
-                    o[i] = (int32_t)((s * 257u) >> 16);
+            if (tid < 32) {                                   // prefix of clipped areas
+                uint32_t v = (tid < cn) ? scp[tid].bw * scp[tid].bh : 0;
+                uint32_t s = v;
+                for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
+                sarea[tid + 1] = s;
+                if (tid == 0) sarea[0] = 0;
+            }
+            if (sHasPhong) {
+                for (uint32_t w = tid; w < cn * 5; w += RASTER_THREADS) {
+                    const uint32_t pi = w / 5, part = w % 5;
+                    const uint32_t key = keys[c0 + pi];
+                    const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+                    const PFPrimPhong *src = &a.primsPh[item];
+                    if (sub != 0) src = &a.poolPh[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
+                    reinterpret_cast<int4 *>(&sph[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
                 }
-                frag = pack4(o);
-            } else {
-                const float mx = x86_max(wn1, x86_max(wn2, wn3));
-                frag = ((mx == wn1) ? P.c1 : 0u) | (((mx == wn2) ? P.c2 : 0u) | ((mx == wn3) ? P.c3 : 0u));
             }
-            if (fl & PFS_TEXTURE) {
-                float tu = P.u1 * wn1 + P.u2 * wn2;
-                tu = tu + P.u3 * wn3;
-                float tv = P.v1 * wn1 + P.v2 * wn2;
-                tv = tv + P.v3 * wn3;
-                if (P.flags & 2) { tu = tu * z; tv = tv * z; }
-                frag = blend_simd(4, tex_sample(S, tu, tv), frag);
+            __syncthreads();
+            // 2. coverage over all (sub-triangle, pixel) pairs of the clipped boxes
+            const uint32_t total = sarea[CH];
+            for (uint32_t t = tid; t < total; t += RASTER_THREADS) {
+                int lo = 0, hi = CH - 1;                          // largest k with sarea[k] <= t
+                while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
+                const ChunkPrim &cp = scp[lo];
+                const uint32_t i = t - sarea[lo];
+                const uint32_t dy = (uint32_t)(((float)i + 0.5f) * cp.invBw);
+                const uint32_t dx = i - dy * cp.bw;
+                const uint32_t X = cp.bx0 + dx, Y = cp.by0 + dy;
+                const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + X * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0]);
+                const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + X * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1]);
+                const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + X * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2]);
+                if ((w1 | w2 | w3) > 0) atomicOr(&pmask[Y * PF_TILE + X], 1u << lo);
             }
-            if (fl & PFS_PHONG) {
-                const PFPrimPhong &Q = sph[k];
-                float N[3], Pp[3];
-                for (int i = 0; i < 3; i++) {
-                    float t0 = Q.n1[i] * wn1 + Q.n2[i] * wn2; N[i] = t0 + Q.n3[i] * wn3;
-                    float t1 = Q.p1[i] * wn1 + Q.p2[i] * wn2; Pp[i] = t1 + Q.p3[i] * wn3;
+            __syncthreads();
+            // 3+4. per warp: compact, shade densely, resolve in order
+            const uint32_t m = pmask[tid];
+            const uint32_t cntp = __popc(m);
+            frags += cntp;
+            uint32_t s = cntp;
+            for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
+            const uint32_t myOff = s - cntp;
+            woff[warp][lane] = myOff;
+            if (lane == 31) woff[warp][32] = s;
+            __syncwarp();
+            const uint32_t wtotal = woff[warp][32];
+            for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
+                const uint32_t bEnd = min(wtotal, b0 + FWIN);
+                for (uint32_t f = b0 + lane; f < bEnd; f += 32) {
+                    int lo = 0, hi = 31;                      // owner lane: largest L with woff[L] <= f
+                    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (woff[warp][mid] <= f) lo = mid; else hi = mid - 1; }
+                    const uint32_t om = pmask[warp * 32 + lo];
+                    const uint32_t k = __fns(om, 0, (int)(f - woff[warp][lo]) + 1) & (CH - 1);
+                    const PFPrim &P = sprim[k];
+                    const ChunkPrim &cp = scp[k];
+                    const uint32_t X = (uint32_t)((warp * 32 + lo) % PF_TILE), Y = (uint32_t)((warp * 32 + lo) / PF_TILE);
+                    const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + X * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0]);
+                    const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + X * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1]);
+                    const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + X * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2]);
+                    const float wn1 = (float)w1 * P.wInvSum, wn2 = (float)w2 * P.wInvSum, wn3 = (float)w3 * P.wInvSum;
+                    float zs = P.z1 * wn1 + P.z2 * wn2;
+                    zs = zs + P.z3 * wn3;
+                    const float z = 1.0f / zs;
+                    const PFDrawState &S = a.states[P.flags >> 8];
+                    fcol[warp][f - b0] = shade_fragment(P, &sph[k], S, wn1, wn2, wn3, z);
+                    fz[warp][f - b0] = z;
                 }
-                frag = light_phong(S, frag, S.mat[face], Pp, N);
+                __syncwarp();
+                // resolve this window's fragments of my pixel, in submission order
+                if (cntp) {
+                    uint32_t f = myOff, mm = m;
+                    while (mm) {
+                        const uint32_t k = __ffs(mm) - 1;
+                        mm &= mm - 1;
+                        if (f >= b0 && f < bEnd) {
+                            const PFDrawState &S = a.states[scp[k].flags >> 8];
+                            const uint32_t fl = S.flags;
+                            const float z = fz[warp][f - b0];
+                            if (!(fl & PFS_DEPTH_TEST) || depth_simd(S.depthFunc, z, dep)) {
+                                uint32_t frag = fcol[warp][f - b0];
+                                if (fl & PFS_BLEND) frag = blend_simd(S.blendMode, frag, col);
+                                col = frag;
+                                if (fl & PFS_DEPTH_MASK) dep = z;
+                            }
+                        }
+                        f++;
+                    }
+                }
+                __syncwarp();
             }
-            if (fl & PFS_BLEND) frag = blend_simd(S.blendMode, frag, col);
-            col = frag;
-            if (fl & PFS_DEPTH_MASK) dep = z;
         }
     }
     if (inside) { a.color[pidx] = col; a.depth[pidx] = dep; }
     // fragment counter: warp reduce, one atomic per warp
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
-    if ((tid & 31) == 0 && frags) atomicAdd(&a.cnt->fragments, frags);
+    if (lane == 0 && frags) atomicAdd(&a.cnt->fragments, frags);
 }
 
 // ---------------------------------------------------------------------------
@@ -993,11 +1137,12 @@ __global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, 
 // ---------------------------------------------------------------------------
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
-cudaError_t pfd_launch_vertex(const PFSegment *segs, int nSegs, const PFDrawState *states, PFVertexOut *out,
-                              uint32_t nVerts, const PFDevCounters *cnt, cudaStream_t st)
+cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 {
-    if (nVerts == 0) return cudaSuccess;
-    k_vertex<<<grid_for(nVerts, 128), 128, 0, st>>>(segs, nSegs, states, out, nVerts, cnt);
+    const uint32_t nTiles = L.tilesX * L.tilesY;
+    const size_t work = L.nVerts > nTiles ? L.nVerts : nTiles;
+    k_vertex<<<grid_for(work, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nVerts, L.cnt,
+                                                  L.binCount, nTiles);
     return cudaGetLastError();
 }
 
@@ -1005,25 +1150,27 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
     BinArgs B{ L.binCount, L.bins, L.cap, L.W, L.H, L.tilesX, L.cnt, L.command };
-    k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, L.prims,
-                                                    L.primsPh, L.clipQueue, L.clipQueueCount, B);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_clip<<<152 * 4, 64, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.clipQueue, L.clipQueueCount,
-                                                  L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, B);
+    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap };
+    k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, O, B);
     return cudaGetLastError();
 }
 
-cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
+static size_t raster_smem(uint32_t cap)
+{
+    uint32_t N = 1; while (N < cap) N <<= 1;
+    size_t words = N > (uint32_t)RANK_SORT_MAX ? N : (size_t)2 * RANK_SORT_MAX;
+    if (cap <= RANK_SORT_MAX) words = (size_t)RANK_SORT_MAX + cap;
+    return words * sizeof(uint32_t);
+}
+
+cudaError_t pfd_launch_raster(const PFBatchLaunch &L, int clearMode, uint32_t clearColor, float clearDepth,
+                              cudaStream_t st)
 {
     RasterArgs a{ L.binCount, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.color, L.depth,
-                  L.W, L.H, L.tilesX, L.cnt, L.command };
-    uint32_t N = 1; while (N < L.cap) N <<= 1;
-    size_t smem = (size_t)N * sizeof(uint32_t);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+                  L.W, L.H, L.tilesX, L.cnt, L.command, clearMode, clearColor, clearDepth };
+    const size_t smem = raster_smem(L.cap);
+    cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
     k_raster<<<L.tilesX * L.tilesY, RASTER_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
