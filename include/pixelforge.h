@@ -393,6 +393,50 @@ enum {
 };
 PF_API PFuint pfGetDeviceStatus(void);
 
+/* ---- allocation-free entry point (no counterpart in the reference) --------
+ *
+ * pfgbDrawTrianglesStatic renders `ntris` triangles straight into device
+ * colour (RGBA8, width*height words) and depth (float) buffers that the
+ * caller owns, and allocates nothing: for callers that cannot call
+ * cudaMalloc -- inside someone else's stream capture, on a real-time frame
+ * path where an allocation may block and synchronise the device, or in a
+ * host that only lends out pre-allocated buffers.  It runs the same kernels
+ * as the pf* API and gives the same pixels as
+ *     pfMatrixMode(PF_PROJECTION); pfLoadIdentity(); pfMultMatrixf(mvp);
+ *     pfMatrixMode(PF_MODELVIEW);  pfLoadIdentity();
+ *     depthFunc < 0 ? pfDisable(PF_DEPTH_TEST) : pfEnable + pfDepthFunc(depthFunc);
+ *     cullMode 0: pfDisable(PF_CULL_FACE); 1: cull PF_BACK; 2: cull PF_FRONT;
+ *     pfBegin(PF_TRIANGLES); per vertex pfColor(colors[i]); pfVertex3fv(&positions[3*i]); pfEnd();
+ * on a framebuffer already holding `color` and `depth` (no clear), smooth
+ * shading, no lighting, texture or blending.
+ *
+ * positions: device, 9 floats per triangle (object-space x, y, z of its 3
+ * vertices); colors: device, one packed RGBA8 word per vertex; mvp: host,
+ * 16 floats in the reference's layout; stream: a cudaStream_t or NULL.
+ *
+ * Its intermediates live in one file-scope __device__ array of
+ * PFGB_STATIC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits.  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress) with the device current; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (other streams, other threads) race and corrupt
+ * each other, so issue them one after another.  Returns 0, or a negative
+ * PFGB_STATIC_E_* code; sizes beyond the limits below are rejected. */
+#define PFGB_STATIC_MAX_TRIANGLES   8192
+#define PFGB_STATIC_MAX_WIDTH       512
+#define PFGB_STATIC_MAX_HEIGHT      512
+#define PFGB_STATIC_BIN_CAPACITY    2048      /* sub-triangles per 16x16 tile */
+#define PFGB_STATIC_SCRATCH_BYTES   15209984  /* 14.5 MiB */
+#define PFGB_STATIC_E_TOO_LARGE     (-1)      /* more triangles or pixels than the limits */
+#define PFGB_STATIC_E_INVALID       (-2)      /* null pointer or invalid mode */
+#define PFGB_STATIC_E_CUDA          (-3)      /* a CUDA call failed */
+#define PFGB_STATIC_E_CAPACITY      (-4)      /* a tile needed more than PFGB_STATIC_BIN_CAPACITY entries;
+                                                 the buffers were not modified */
+PF_API int pfgbDrawTrianglesStatic(const float* positions, const uint32_t* colors, uint32_t ntris,
+                                   const float* mvp, uint32_t* color, float* depth,
+                                   uint32_t width, uint32_t height, int depthFunc, int cullMode,
+                                   void* stream);
+
 #if defined(__cplusplus)
 }
 #endif

@@ -37,8 +37,8 @@ def _cuda_home() -> Path:
 
 
 def _sources():
-    return [CSRC / "pf_kernels.cu", CSRC / "pf_host.cpp", CSRC / "pf_layout.h", CSRC / "pf_device.h",
-            INCLUDE / "pixelforge.h", Path(__file__)]
+    return [CSRC / "pf_kernels.cu", CSRC / "pf_noalloc.cu", CSRC / "pf_host.cpp", CSRC / "pf_layout.h",
+            CSRC / "pf_device.h", INCLUDE / "pixelforge.h", Path(__file__)]
 
 
 def up_to_date() -> bool:
@@ -55,15 +55,17 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     nvcc = str(cuda / "bin" / "nvcc")
     BUILD.mkdir(exist_ok=True)
     inc = [f"-I{INCLUDE}", f"-I{CSRC}"]
-    kobj, hobj = BUILD / "pf_kernels.o", BUILD / "pf_host.o"
+    kobj, nobj, hobj = BUILD / "pf_kernels.o", BUILD / "pf_noalloc.o", BUILD / "pf_host.o"
     kcmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-fmad=false", "-std=c++17", "-Xptxas", "-v",
             "-Xcompiler", "-fPIC,-fvisibility=hidden", *inc, "-c", str(CSRC / "pf_kernels.cu"), "-o", str(kobj)]
+    ncmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-fmad=false", "-std=c++17",
+            "-Xcompiler", "-fPIC,-fvisibility=hidden", *inc, "-c", str(CSRC / "pf_noalloc.cu"), "-o", str(nobj)]
     cxx = os.environ.get("CXX", "g++")
     hcmd = [cxx, "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fvisibility=hidden",
             "-Wall", "-Wno-unused-function", *inc, f"-I{cuda / 'include'}", "-c", str(CSRC / "pf_host.cpp"),
             "-o", str(hobj)]
-    procs = [(kcmd, subprocess.Popen(kcmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)),
-             (hcmd, subprocess.Popen(hcmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))]
+    procs = [(cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+             for cmd in (kcmd, hcmd, ncmd)]
     logs = []
     for cmd, p in procs:
         out, _ = p.communicate()
@@ -76,7 +78,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         alt = cuda / "targets" / ("sbsa-linux" if os.uname().machine == "aarch64" else "x86_64-linux") / "lib"
         libdir = alt if (alt / "libcudart_static.a").exists() else libdir
     tmp = LIB.with_suffix(".so.tmp")
-    lcmd = [cxx, "-shared", "-o", str(tmp), str(hobj), str(kobj), f"-L{libdir}", "-lcudart_static",
+    lcmd = [cxx, "-shared", "-o", str(tmp), str(hobj), str(kobj), str(nobj), f"-L{libdir}", "-lcudart_static",
             "-lrt", "-ldl", "-lpthread", "-Wl,-Bsymbolic"]
     r = subprocess.run(lcmd, capture_output=True, text=True)
     if r.returncode != 0:
