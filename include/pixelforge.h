@@ -393,6 +393,34 @@ enum {
 };
 PF_API PFuint pfGetDeviceStatus(void);
 
+/* ---- batches (no counterpart in the reference) -----------------------------
+ *
+ * Between pfgbBatchBegin and pfgbBatchEnd every context made current on the
+ * calling thread records into the batch instead of rendering at its own
+ * observation points; pfgbBatchEnd renders all of it -- hundreds of contexts
+ * of uneven sizes -- with one launch of each pipeline kernel (the tile
+ * rasterizer is a persistent kernel over a work list of (framebuffer, tile)
+ * items) and writes every colour buffer back.  Observation points inside the
+ * batch (pfFinish, pfReadPixels, ...) render the whole batch so far. */
+typedef void* PFgbbatch;
+PF_API PFgbbatch pfgbBatchCreate(void);
+PF_API void      pfgbBatchDelete(PFgbbatch batch);
+PF_API void      pfgbBatchBegin(PFgbbatch batch);
+PF_API void      pfgbBatchEnd(PFgbbatch batch);
+/* Re-run the device work of the batch's last render `n` times from a CUDA
+ * graph (inputs already on the device; framebuffers are rewritten, so a
+ * batch that starts each framebuffer with a clear gives the same pixels
+ * every time).  Returns the mean GPU milliseconds per run, or < 0. */
+PF_API PFfloat   pfgbBatchReplay(PFgbbatch batch, PFuint n);
+PF_API void      pfgbBatchGetStats(PFgbbatch batch, PFstats* stats);
+PF_API void      pfgbBatchEnableTiming(PFgbbatch batch, PFboolean enable);
+/* Tuning knobs (set by the project's autotuner): tile-bin capacity (a power
+ * of two, 32..16384; bins still grow on overflow) and persistent raster CTAs
+ * per SM (1..8).  batch == NULL tunes the current context. */
+PF_API void      pfgbBatchTune(PFgbbatch batch, PFuint binCapacity, PFuint rasterCtasPerSM);
+/* The same graph replay for the current context's last render. */
+PF_API PFfloat   pfgbReplay(PFuint n);
+
 /* ---- allocation-free entry point (no counterpart in the reference) --------
  *
  * pfgbDrawTrianglesStatic renders `ntris` triangles straight into device
@@ -426,7 +454,7 @@ PF_API PFuint pfGetDeviceStatus(void);
 #define PFGB_STATIC_MAX_WIDTH       512
 #define PFGB_STATIC_MAX_HEIGHT      512
 #define PFGB_STATIC_BIN_CAPACITY    2048      /* sub-triangles per 16x16 tile */
-#define PFGB_STATIC_SCRATCH_BYTES   15209984  /* 14.5 MiB */
+#define PFGB_STATIC_SCRATCH_BYTES   15210240  /* 14.5 MiB */
 #define PFGB_STATIC_E_TOO_LARGE     (-1)      /* more triangles or pixels than the limits */
 #define PFGB_STATIC_E_INVALID       (-2)      /* null pointer or invalid mode */
 #define PFGB_STATIC_E_CUDA          (-3)      /* a CUDA call failed */

@@ -160,6 +160,15 @@ PROTOTYPES = {
     "pfGetDeviceStatus": (PFuint, []),
     "pfEnableTiming": (_V, [PFbool]),
     "pfGetTexturePixels": (PFptr, [PFptr, PFptr, PFptr, PFptr, PFptr]),
+    "pfgbBatchCreate": (PFptr, []),
+    "pfgbBatchDelete": (_V, [PFptr]),
+    "pfgbBatchBegin": (_V, [PFptr]),
+    "pfgbBatchEnd": (_V, [PFptr]),
+    "pfgbBatchReplay": (PFfloat, [PFptr, PFuint]),
+    "pfgbBatchGetStats": (_V, [PFptr, C.POINTER(PFstats)]),
+    "pfgbBatchEnableTiming": (_V, [PFptr, PFbool]),
+    "pfgbBatchTune": (_V, [PFptr, PFuint, PFuint]),
+    "pfgbReplay": (PFfloat, [PFuint]),
 }
 
 

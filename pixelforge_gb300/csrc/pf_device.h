@@ -28,12 +28,13 @@ struct PFBatchLaunch {
     PFPrim *pool;             /* clipped sub-triangles >= 1 */
     PFPrimPhong *poolPh;
     uint32_t poolCap;
-    uint32_t *binCount;       /* tilesX * tilesY */
-    uint32_t *bins;           /* tilesX * tilesY * cap */
+    uint32_t *binCount;       /* totalTiles */
+    uint32_t *bins;           /* totalTiles * cap */
     uint32_t cap;
-    uint32_t *color;
-    float *depth;
-    uint32_t W, H, tilesX, tilesY;
+    const PFTarget *targets;  /* device */
+    int nTargets;
+    uint32_t totalTiles;
+    int rasterCtasPerSM;      /* persistent raster grid: SMs x this */
     PFDevCounters *cnt;
     uint32_t command;
 };
@@ -41,11 +42,11 @@ struct PFBatchLaunch {
 /* k_vertex also zeroes the tile bin counters and the batch counters. */
 cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st);
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
-/* clearMode: 0 start from the framebuffer, 1 from a fused pfClear (pixels
- * 0..7 kept; only when the pixel count is a multiple of 8), 2 from a fused
- * pfClearFramebuffer. */
-cudaError_t pfd_launch_raster(const PFBatchLaunch &L, int clearMode, uint32_t clearColor, float clearDepth,
-                              cudaStream_t st);
+/* Persistent tile raster over every tile of every target; each target's
+ * clearMode says how its tiles start (see PFTarget). */
+cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);
+/* Number of SMs of the current device (cached). */
+int pfd_sm_count(void);
 cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
                              const PFDevCounters *cnt, uint32_t command, cudaStream_t st);
 cudaError_t pfd_launch_hook(uint32_t *color, const float *depth, size_t n, int hook, const PFHookParams &hp,

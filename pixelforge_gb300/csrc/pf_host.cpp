@@ -24,6 +24,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -118,6 +123,7 @@ struct Tex {
     float tx, ty;
     int wrap, filter;
     bool ownsPinned;     // colour of a pfGenFramebuffer framebuffer (pinned host memory)
+    bool isMain;         // a context's main framebuffer (its depth is internal)
 };
 
 struct Light {
@@ -162,6 +168,7 @@ struct Cmd {
 // Segment as recorded on the host: staging offsets instead of pointers.
 struct SegRec {
     PFSegment seg;                     // pointer fields left null until the flush
+    PFframebuffer *fb = nullptr;       // framebuffer the segment draws into
     int64_t recordsOff = -1, posOff = -1, nrmOff = -1, uvOff = -1, colOff = -1, idxOff = -1, itemsOff = -1;
     std::vector<int32_t> explicitItems;   // immediate / non-triangle modes, grown while recording
     std::vector<PFVertexIn> records;       // immediate mode vertices
@@ -219,6 +226,40 @@ struct DevBuf {
     void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
 };
 
+// Recording and device state of one renderer.  Every context owns one; a
+// batch (pfgbBatchBegin .. pfgbBatchEnd) owns one that all contexts made
+// current during the batch record into, so that the whole batch renders with
+// one launch of each pipeline kernel.
+struct Renderer {
+    // recording
+    Staging staging;
+    std::vector<StateRec> states;
+    std::vector<SegRec> segs;
+    std::vector<Cmd> cmds;
+    struct SnapKey { const void *p; size_t bytes; int64_t off; };
+    std::vector<SnapKey> snaps;          // dedup of texture / array snapshots in this recording
+
+    // device
+    bool devInit = false, devOk = false;
+    cudaStream_t stream = nullptr;
+    DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters;
+    uint32_t cap = 256, poolCap = 4096;
+    int rasterCtasPerSM = 4;
+    PFDevCounters *hostCounters = nullptr;
+    PFstats stats{};
+    PFuint devStatus = 0;
+    bool timing = false;
+    cudaEvent_t evStart = nullptr, evEnd = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rasterEv;   // per raster launch, reused
+
+    // the device work of the last successful flush, for graph replay
+    struct Op { int kind; int cmd; PFBatchLaunch L; size_t n; uint32_t *color; float *depth;
+                uint32_t cc; float cd; bool all; int hook; PFHookParams hp; };
+    std::vector<Op> lastOps;
+    cudaGraphExec_t graph = nullptr;
+    bool graphValid = false;
+};
+
 struct Ctx {
     PFframebuffer mainFB{ nullptr, nullptr };
     PFframebuffer *current = nullptr;
@@ -254,31 +295,25 @@ struct Ctx {
     bool depthMask = true;
     PFfloat pointSize = 1.0f, lineWidth = 1.0f;
 
-    // recording
-    Staging staging;
-    std::vector<StateRec> states;
-    std::vector<SegRec> segs;
-    std::vector<Cmd> cmds;
     bool stateDirty = true;
-    int openImmSeg = -1;                 // immediate-mode segment accepting primitives
-    struct SnapKey { const void *p; size_t bytes; int64_t off; };
-    std::vector<SnapKey> snaps;          // dedup of texture / array snapshots in this recording
+    int openImmSeg = -1;                 // immediate-mode segment accepting primitives (index in rend->segs)
+    Renderer own;
+    Renderer *rend = &own;
+};
 
-    // device
-    bool devInit = false, devOk = false;
-    cudaStream_t stream = nullptr;
-    DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters, misc;
-    uint32_t cap = 256, poolCap = 4096;
-    std::unordered_map<const void *, FBMirror> mirrors;     // keyed by framebuffer texture
-    PFDevCounters *hostCounters = nullptr;
-    PFstats stats{};
-    PFuint devStatus = 0;
-    bool timing = false;
-    cudaEvent_t evStart = nullptr, evEnd = nullptr;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rasterEv;   // per raster launch, reused
+struct Batch {
+    Renderer r;
+    std::vector<Ctx *> members;
+    bool open = false;
 };
 
 thread_local Ctx *G = nullptr;
+thread_local Batch *gBatch = nullptr;     // batch being recorded on this thread
+
+// Device copies of every framebuffer, shared by all renderers (a framebuffer
+// has one device copy whichever renderer draws into it).
+std::mutex gMirrorMutex;
+std::unordered_map<const void *, FBMirror> gMirrors;
 
 void set_err(PFerrcode e) { if (G) G->err = e; }
 
@@ -298,8 +333,118 @@ Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
     Tex *x = new Tex();
     x->pixels = pixels; x->w = w; x->h = h; x->format = f; x->type = t;
     x->tx = 1.0f / (float)w; x->ty = 1.0f / (float)h;
-    x->wrap = PF_REPEAT; x->filter = PF_NEAREST; x->ownsPinned = false;
+    x->wrap = PF_REPEAT; x->filter = PF_NEAREST; x->ownsPinned = false; x->isMain = false;
     return x;
+}
+
+// ---------------------------------------------------------------------------
+// host worker pool: large snapshots (vertex arrays, indices, textures) are
+// copied and compared by several threads, the caller taking a share
+// ---------------------------------------------------------------------------
+class Pool {
+public:
+    static Pool &get() { static Pool p; return p; }
+    int workers() const { return (int)threads_.size() + 1; }
+    // run fn(i) for i in [0, n); returns when all are done
+    void run(int n, const std::function<void(int)> &fn)
+    {
+        if (n <= 1 || threads_.empty()) { for (int i = 0; i < n; i++) fn(i); return; }
+        std::lock_guard<std::mutex> one(runMutex_);      // one parallel loop at a time
+        std::unique_lock<std::mutex> lk(m_);
+        fn_.store(&fn); n_ = n; next_.store(0); done_ = 0; gen_++;
+        lk.unlock();
+        cv_.notify_all();
+        work();
+        lk.lock();
+        doneCv_.wait(lk, [&] { return done_ == n_; });
+        fn_.store(nullptr);
+    }
+    ~Pool()
+    {
+        { std::lock_guard<std::mutex> lk(m_); stop_ = true; gen_++; }
+        cv_.notify_all();
+        for (auto &t : threads_) t.join();
+    }
+private:
+    Pool()
+    {
+        unsigned hw = std::thread::hardware_concurrency();
+        int n = (int)std::min(7u, hw > 1 ? hw / 2 : 0u);
+        for (int i = 0; i < n; i++) threads_.emplace_back([this] { loop(); });
+    }
+    void work()
+    {
+        for (;;) {
+            int i = next_.fetch_add(1);
+            const std::function<void(int)> *f = fn_.load();
+            if (i >= n_ || !f) break;
+            (*f)(i);
+            std::lock_guard<std::mutex> lk(m_);
+            if (++done_ == n_) doneCv_.notify_all();
+        }
+    }
+    void loop()
+    {
+        uint64_t seen = 0;
+        for (;;) {
+            std::unique_lock<std::mutex> lk(m_);
+            cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+            lk.unlock();
+            work();
+        }
+    }
+    std::vector<std::thread> threads_;
+    std::mutex m_, runMutex_;
+    std::condition_variable cv_, doneCv_;
+    std::atomic<const std::function<void(int)> *> fn_{ nullptr };
+    std::atomic<int> next_{ 0 };
+    int n_ = 0, done_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
+constexpr size_t kParallelChunk = (size_t)1 << 19;     // 512 KiB
+
+void par_memcpy(void *dst, const void *src, size_t bytes)
+{
+    if (bytes < 2 * kParallelChunk) { std::memcpy(dst, src, bytes); return; }
+    const int n = (int)((bytes + kParallelChunk - 1) / kParallelChunk);
+    Pool::get().run(n, [&](int i) {
+        size_t o = (size_t)i * kParallelChunk, len = std::min(kParallelChunk, bytes - o);
+        std::memcpy((uint8_t *)dst + o, (const uint8_t *)src + o, len);
+    });
+}
+
+bool par_equal(const void *a, const void *b, size_t bytes)
+{
+    if (bytes < 2 * kParallelChunk) return std::memcmp(a, b, bytes) == 0;
+    const int n = (int)((bytes + kParallelChunk - 1) / kParallelChunk);
+    std::atomic<bool> diff{ false };
+    Pool::get().run(n, [&](int i) {
+        if (diff.load(std::memory_order_relaxed)) return;
+        size_t o = (size_t)i * kParallelChunk, len = std::min(kParallelChunk, bytes - o);
+        if (std::memcmp((const uint8_t *)a + o, (const uint8_t *)b + o, len) != 0) diff.store(true);
+    });
+    return !diff.load();
+}
+
+// u32 indices: copy and return the largest
+uint32_t par_copy_max_u32(uint32_t *dst, const uint32_t *src, size_t count)
+{
+    const size_t chunk = kParallelChunk / 4;
+    const int n = (int)((count + chunk - 1) / chunk);
+    std::vector<uint32_t> mx((size_t)std::max(n, 1), 0u);
+    Pool::get().run(n, [&](int i) {
+        size_t o = (size_t)i * chunk, len = std::min(chunk, count - o);
+        uint32_t m = 0;
+        for (size_t k = 0; k < len; k++) { uint32_t v = src[o + k]; dst[o + k] = v; m = v > m ? v : m; }
+        mx[(size_t)i] = m;
+    });
+    uint32_t m = 0;
+    for (uint32_t v : mx) m = std::max(m, v);
+    return m;
 }
 
 // ---------------------------------------------------------------------------
@@ -307,15 +452,16 @@ Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
 // ---------------------------------------------------------------------------
 // Copy `bytes` of caller memory into staging, reusing an identical snapshot
 // taken earlier in the same recording.
-int64_t snapshot(Ctx *c, const void *p, size_t bytes)
+int64_t snapshot(Renderer *r, const void *p, size_t bytes)
 {
-    for (auto &s : c->snaps)
-        if (s.p == p && s.bytes == bytes && std::memcmp(c->staging.base + s.off, p, bytes) == 0) return s.off;
-    int64_t off = c->staging.alloc(bytes);
-    std::memcpy(c->staging.base + off, p, bytes);
-    c->snaps.push_back({ p, bytes, off });
+    for (auto &s : r->snaps)
+        if (s.p == p && s.bytes == bytes && par_equal(r->staging.base + s.off, p, bytes)) return s.off;
+    int64_t off = r->staging.alloc(bytes);
+    par_memcpy(r->staging.base + off, p, bytes);
+    r->snaps.push_back({ p, bytes, off });
     return off;
 }
+int64_t snapshot(Ctx *c, const void *p, size_t bytes) { return snapshot(c->rend, p, bytes); }
 
 void update_matrices(Ctx *c, bool withNormal)                      // context.c:96-111
 {
@@ -374,36 +520,8 @@ int snapshot_state(Ctx *c)
         s.mat[f].spec = pack(c->mat[f].specular); s.mat[f].emis = pack(c->mat[f].emission);
         s.mat[f].shininess = c->mat[f].shininess;
     }
-    c->states.push_back(r);
-    return (int)c->states.size() - 1;
-}
-
-// Append a DRAW of segment `si` to the command list, merging with the
-// previous DRAW when it targets the same framebuffer.
-void push_draw(Ctx *c, int si)
-{
-    if (!c->cmds.empty() && c->cmds.back().kind == CMD_DRAW && c->cmds.back().fb == c->current &&
-        c->cmds.back().segEnd == si) {
-        c->cmds.back().segEnd = si + 1;
-        return;
-    }
-    Cmd cmd{};
-    cmd.kind = CMD_DRAW; cmd.fb = c->current; cmd.segBegin = si; cmd.segEnd = si + 1;
-    c->cmds.push_back(cmd);
-}
-
-int new_segment(Ctx *c, int srcKind, int itemKind)
-{
-    SegRec r;
-    std::memset(&r.seg, 0, sizeof r.seg);
-    r.seg.state = snapshot_state(c);
-    r.seg.srcKind = srcKind;
-    r.seg.itemKind = itemKind;
-    c->segs.push_back(std::move(r));
-    int si = (int)c->segs.size() - 1;
-    push_draw(c, si);
-    c->stateDirty = false;
-    return si;
+    c->rend->states.push_back(r);
+    return (int)c->rend->states.size() - 1;
 }
 
 // Face passes of one primitive (internal/context/context.c:95-244): returns
@@ -467,6 +585,41 @@ template <typename T> PFsizei reset_for_next(PFdrawmode mode, T *slot)
     }
 }
 
+// Append a DRAW of segment `si` to the command list, merging with the
+// previous DRAW when it targets the same framebuffer.
+void push_draw(Renderer *r, PFframebuffer *fb, int si)
+{
+    if (!r->cmds.empty() && r->cmds.back().kind == CMD_DRAW && r->cmds.back().fb == fb && r->cmds.back().segEnd == si) {
+        r->cmds.back().segEnd = si + 1;
+        return;
+    }
+    Cmd cmd{};
+    cmd.kind = CMD_DRAW; cmd.fb = fb; cmd.segBegin = si; cmd.segEnd = si + 1;
+    r->cmds.push_back(cmd);
+}
+
+int new_segment(Ctx *c, int srcKind, int itemKind)
+{
+    Renderer *r = c->rend;
+    SegRec rec;
+    std::memset(&rec.seg, 0, sizeof rec.seg);
+    rec.seg.state = snapshot_state(c);
+    rec.seg.srcKind = srcKind;
+    rec.seg.itemKind = itemKind;
+    rec.fb = c->current;
+    r->segs.push_back(std::move(rec));
+    int si = (int)r->segs.size() - 1;
+    push_draw(r, c->current, si);
+    c->stateDirty = false;
+    return si;
+}
+
+void push_cmd(Ctx *c, const Cmd &cmd)
+{
+    c->rend->cmds.push_back(cmd);
+    c->openImmSeg = -1;
+}
+
 // pfVertex4fv path: a primitive completed in immediate mode.
 void immediate_primitive(Ctx *c)
 {
@@ -476,54 +629,74 @@ void immediate_primitive(Ctx *c)
     int faces[2];
     const int nf = faces_for(c, mode, faces);
     if (nf == 0) return;
-    if (c->openImmSeg < 0 || c->stateDirty) c->openImmSeg = new_segment(c, PF_SRC_RECORDS, PF_ITEMS_EXPLICIT);
-    SegRec &r = c->segs[c->openImmSeg];
+    Renderer *r = c->rend;
+    // a segment stays open only while it is the renderer's last one (another
+    // context of a batch may have appended since)
+    if (c->openImmSeg < 0 || c->stateDirty || c->openImmSeg != (int)r->segs.size() - 1)
+        c->openImmSeg = new_segment(c, PF_SRC_RECORDS, PF_ITEMS_EXPLICIT);
+    SegRec &rec = r->segs[c->openImmSeg];
     uint32_t s[6];
-    for (PFsizei i = 0; i < n; i++) { s[i] = (uint32_t)r.records.size(); r.records.push_back(c->slots[i]); }
-    emit_items(r.explicitItems, mode, s, faces, nf);
+    for (PFsizei i = 0; i < n; i++) { s[i] = (uint32_t)rec.records.size(); rec.records.push_back(c->slots[i]); }
+    emit_items(rec.explicitItems, mode, s, faces, nf);
 }
 
 // ---------------------------------------------------------------------------
 // device side
 // ---------------------------------------------------------------------------
-bool device_init(Ctx *c)
+bool device_init(Renderer *r)
 {
-    if (c->devInit) return c->devOk;
-    c->devInit = true;
+    if (r->devInit) return r->devOk;
+    r->devInit = true;
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess || n == 0) {
         report_device_failure("cudaGetDeviceCount", e == cudaSuccess ? cudaErrorNoDevice : e);
         cudaGetLastError();
-        c->devStatus |= PF_DEVICE_NO_GPU;
+        r->devStatus |= PF_DEVICE_NO_GPU;
         return false;
     }
-    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); c->devStatus |= PF_DEVICE_NO_GPU; return false; }
-    if (!c->counters.ensure(sizeof(PFDevCounters))) { c->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
-    if (cudaMallocHost((void **)&c->hostCounters, sizeof(PFDevCounters)) != cudaSuccess) {
-        cudaGetLastError(); c->devStatus |= PF_DEVICE_ALLOC_FAIL; return false;
+    e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); r->devStatus |= PF_DEVICE_NO_GPU; return false; }
+    if (!r->counters.ensure(sizeof(PFDevCounters))) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
+    if (cudaMallocHost((void **)&r->hostCounters, sizeof(PFDevCounters)) != cudaSuccess) {
+        cudaGetLastError(); r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false;
     }
-    c->devOk = true;
+    r->devOk = true;
     return true;
 }
 
-FBMirror *mirror_for(Ctx *c, PFframebuffer *fb)
+void release_renderer(Renderer *r)
 {
+    if (r->graph) { cudaGraphExecDestroy(r->graph); r->graph = nullptr; }
+    if (r->devOk) {
+        r->arena.release(); r->vout.release(); r->prims.release(); r->primsPh.release(); r->pool.release();
+        r->poolPh.release(); r->binCount.release(); r->bins.release(); r->counters.release();
+        if (r->hostCounters) cudaFreeHost(r->hostCounters);
+        if (r->evStart) { cudaEventDestroy(r->evStart); cudaEventDestroy(r->evEnd); }
+        for (auto &pr : r->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        if (r->stream) cudaStreamDestroy(r->stream);
+    }
+    r->staging.release();
+    r->devOk = r->devInit = false;
+}
+
+FBMirror *mirror_for(Renderer *r, PFframebuffer *fb)
+{
+    std::lock_guard<std::mutex> lk(gMirrorMutex);
     Tex *t = (Tex *)fb->texture;
-    FBMirror &m = c->mirrors[t];
+    FBMirror &m = gMirrors[t];
     const size_t w = t->w, h = t->h;
     if (m.dColor && (m.w != w || m.h != h)) { cudaFree(m.dColor); cudaFree(m.dDepth); m.dColor = nullptr; m.dDepth = nullptr; }
     if (!m.dColor) {
         if (cudaMalloc((void **)&m.dColor, w * h * 4) != cudaSuccess ||
             cudaMalloc((void **)&m.dDepth, w * h * 4) != cudaSuccess) {
-            cudaGetLastError(); c->devStatus |= PF_DEVICE_ALLOC_FAIL; return nullptr;
+            cudaGetLastError(); r->devStatus |= PF_DEVICE_ALLOC_FAIL; return nullptr;
         }
         m.w = w; m.h = h; m.depthOnDevice = false;
     }
     m.tex = t;
     m.hostDepth = fb->zbuffer;
-    m.depthUserVisible = (fb != &c->mainFB);
+    m.depthUserVisible = !t->isMain;
     if (m.registered != t->pixels && !t->ownsPinned) {
         if (m.registered) cudaHostUnregister(m.registered);
         m.registered = nullptr;
@@ -533,113 +706,214 @@ FBMirror *mirror_for(Ctx *c, PFframebuffer *fb)
     return &m;
 }
 
-void release_mirrors(Ctx *c)
+FBMirror *find_mirror(const void *tex)
 {
-    for (auto &kv : c->mirrors) {
-        if (kv.second.registered) cudaHostUnregister(kv.second.registered);
-        if (kv.second.dColor) cudaFree(kv.second.dColor);
-        if (kv.second.dDepth) cudaFree(kv.second.dDepth);
-    }
-    c->mirrors.clear();
+    std::lock_guard<std::mutex> lk(gMirrorMutex);
+    auto it = gMirrors.find(tex);
+    return it == gMirrors.end() ? nullptr : &it->second;
 }
 
-void discard_recording(Ctx *c)
+void drop_mirror(const void *tex)
 {
-    c->states.clear(); c->segs.clear(); c->cmds.clear(); c->snaps.clear();
-    c->staging.used = 0; c->openImmSeg = -1; c->stateDirty = true;
+    std::lock_guard<std::mutex> lk(gMirrorMutex);
+    auto it = gMirrors.find(tex);
+    if (it == gMirrors.end()) return;
+    if (it->second.registered) cudaHostUnregister(it->second.registered);
+    if (it->second.dColor) cudaFree(it->second.dColor);
+    if (it->second.dDepth) cudaFree(it->second.dDepth);
+    gMirrors.erase(it);
 }
+
+void discard_recording(Renderer *r)
+{
+    r->states.clear(); r->segs.clear(); r->cmds.clear(); r->snaps.clear();
+    r->staging.used = 0;
+}
+
+// One unit of device work of a flush: a multi-target raster batch (a run of
+// DRAW commands, each framebuffer's leading clear folded in), a standalone
+// clear / fill, or a post-process hook.
+struct FlushOp {
+    int kind;                  // 0 batch, 1 clear/fill, 2 hook
+    int cmd;                   // first command index (abort bookkeeping)
+    int cmdEnd;                // one past the last command covered
+    int segBegin, segEnd;
+    std::vector<PFframebuffer *> targets;
+    std::vector<int> clearCmd; // per target: fused clear command or -1
+};
 
 // Render everything recorded, then write colour (and user-visible depth) back
 // to host memory.  Returns false if the device could not be used.
-bool flush(Ctx *c)
+bool flush(Renderer *r)
 {
-    if (c->cmds.empty()) { discard_recording(c); return true; }
-    if (!device_init(c)) { set_err(PF_INVALID_OPERATION); discard_recording(c); return false; }
-    cudaStream_t st = c->stream;
+    if (r->cmds.empty()) { discard_recording(r); return true; }
+    if (!device_init(r)) { set_err(PF_INVALID_OPERATION); discard_recording(r); return false; }
+    cudaStream_t st = r->stream;
     auto fail = [&](const char *what, cudaError_t e) {
         report_device_failure(what, e);
-        c->devStatus |= PF_DEVICE_LAUNCH_FAIL;
+        r->devStatus |= PF_DEVICE_LAUNCH_FAIL;
         set_err(PF_INVALID_OPERATION);
         cudaGetLastError();
         cudaStreamSynchronize(st);
-        discard_recording(c);
+        discard_recording(r);
+        r->graphValid = false;
         return false;
     };
+    const std::vector<Cmd> &cmds = r->cmds;
 
-    // --- staging: states, segments and explicit items join the block -------
-    const size_t nStates = c->states.size(), nSegs = c->segs.size();
-    int64_t statesOff = c->staging.alloc(nStates * sizeof(PFDrawState));
-    int64_t segsOff = c->staging.alloc(nSegs * sizeof(PFSegment));
-    for (auto &r : c->segs) {
-        if (!r.records.empty()) {
-            r.recordsOff = c->staging.alloc(r.records.size() * sizeof(PFVertexIn));
-            std::memcpy(c->staging.base + r.recordsOff, r.records.data(), r.records.size() * sizeof(PFVertexIn));
-            r.seg.nVerts = (uint32_t)r.records.size();
+    // --- group commands into device operations ---------------------------------
+    std::vector<FlushOp> ops;
+    {
+        FlushOp cur; cur.kind = -1;
+        auto close = [&]() { if (cur.kind == 0) ops.push_back(cur); cur = FlushOp(); cur.kind = -1; };
+        auto targetIndex = [&](PFframebuffer *fb) {
+            for (size_t i = 0; i < cur.targets.size(); i++) if (cur.targets[i] == fb) return (int)i;
+            return -1;
+        };
+        for (size_t ci = 0; ci < cmds.size(); ci++) {
+            const Cmd &cmd = cmds[ci];
+            if (cmd.kind == CMD_DRAW) {
+                if (cur.kind != 0) { close(); cur.kind = 0; cur.cmd = (int)ci; cur.segBegin = cmd.segBegin; }
+                if (targetIndex(cmd.fb) < 0) { cur.targets.push_back(cmd.fb); cur.clearCmd.push_back(-1); }
+                cur.segEnd = cmd.segEnd; cur.cmdEnd = (int)ci + 1;
+                continue;
+            }
+            if (cmd.kind == CMD_CLEAR || cmd.kind == CMD_FILL) {
+                // fold into the next DRAW of the same framebuffer when that
+                // framebuffer has not been drawn yet in the current batch
+                const bool nextDraw = ci + 1 < cmds.size() && cmds[ci + 1].kind == CMD_DRAW && cmds[ci + 1].fb == cmd.fb;
+                const Tex *t = (const Tex *)cmd.fb->texture;
+                const bool fusable = nextDraw && (cmd.kind == CMD_FILL || ((size_t)t->w * t->h) % 8 == 0);
+                if (fusable && (cur.kind != 0 || targetIndex(cmd.fb) < 0)) {
+                    if (cur.kind != 0) { close(); cur.kind = 0; cur.cmd = (int)ci; cur.segBegin = cmds[ci + 1].segBegin; cur.segEnd = cur.segBegin; }
+                    cur.targets.push_back(cmd.fb); cur.clearCmd.push_back((int)ci);
+                    cur.cmdEnd = (int)ci + 1;
+                    continue;
+                }
+            }
+            close();
+            FlushOp o; o.kind = (cmd.kind == CMD_HOOK) ? 2 : 1; o.cmd = (int)ci; o.cmdEnd = (int)ci + 1;
+            o.segBegin = o.segEnd = 0;
+            o.targets.push_back(cmd.fb); o.clearCmd.push_back(-1);
+            ops.push_back(o);
         }
-        if (r.seg.itemKind == PF_ITEMS_EXPLICIT) {
-            r.itemsOff = c->staging.alloc(r.explicitItems.size() * 4 + 16);
-            if (!r.explicitItems.empty())
-                std::memcpy(c->staging.base + r.itemsOff, r.explicitItems.data(), r.explicitItems.size() * 4);
-            r.seg.nItems = (uint32_t)(r.explicitItems.size() / 4);
+        close();
+    }
+
+    // --- framebuffers used: device copies ------------------------------------------
+    std::vector<PFframebuffer *> used;
+    for (auto &cmd : cmds)
+        if (std::find(used.begin(), used.end(), cmd.fb) == used.end()) used.push_back(cmd.fb);
+    std::vector<FBMirror *> mirrors;
+    for (PFframebuffer *fb : used) {
+        FBMirror *m = mirror_for(r, fb);
+        if (!m) return fail("cudaMalloc(framebuffer)", cudaErrorMemoryAllocation);
+        mirrors.push_back(m);
+    }
+    auto mirrorOf = [&](PFframebuffer *fb) { return mirrors[std::find(used.begin(), used.end(), fb) - used.begin()]; };
+
+    // --- staging: states, segments, explicit items, targets join the block --------
+    const size_t nStates = r->states.size(), nSegs = r->segs.size();
+    int64_t statesOff = r->staging.alloc(nStates * sizeof(PFDrawState));
+    int64_t segsOff = r->staging.alloc(nSegs * sizeof(PFSegment));
+    size_t nTargetsTotal = 0;
+    for (auto &o : ops) if (o.kind == 0) nTargetsTotal += o.targets.size();
+    int64_t targetsOff = r->staging.alloc(std::max<size_t>(nTargetsTotal, 1) * sizeof(PFTarget));
+    for (auto &rec : r->segs) {
+        if (!rec.records.empty()) {
+            rec.recordsOff = r->staging.alloc(rec.records.size() * sizeof(PFVertexIn));
+            std::memcpy(r->staging.base + rec.recordsOff, rec.records.data(), rec.records.size() * sizeof(PFVertexIn));
+            rec.seg.nVerts = (uint32_t)rec.records.size();
+        }
+        if (rec.seg.itemKind == PF_ITEMS_EXPLICIT) {
+            rec.itemsOff = r->staging.alloc(rec.explicitItems.size() * 4 + 16);
+            if (!rec.explicitItems.empty())
+                std::memcpy(r->staging.base + rec.itemsOff, rec.explicitItems.data(), rec.explicitItems.size() * 4);
+            rec.seg.nItems = (uint32_t)(rec.explicitItems.size() / 4);
         }
     }
-    const size_t total = c->staging.used;
-    if (!c->arena.ensure(total)) { c->devStatus |= PF_DEVICE_ALLOC_FAIL; return fail("cudaMalloc(arena)", cudaErrorMemoryAllocation); }
-    uint8_t *dbase = (uint8_t *)c->arena.p;
+    const size_t total = r->staging.used;
+    if (!r->arena.ensure(total)) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return fail("cudaMalloc(arena)", cudaErrorMemoryAllocation); }
+    uint8_t *dbase = (uint8_t *)r->arena.p;
     auto dptr = [&](int64_t off) -> const void * { return off < 0 ? nullptr : (const void *)(dbase + off); };
-    PFDrawState *hs = (PFDrawState *)(c->staging.base + statesOff);
+    PFDrawState *hs = (PFDrawState *)(r->staging.base + statesOff);
     for (size_t i = 0; i < nStates; i++) {
-        hs[i] = c->states[i].st;
-        hs[i].tex = (const uint32_t *)dptr(c->states[i].texOff);
+        hs[i] = r->states[i].st;
+        hs[i].tex = (const uint32_t *)dptr(r->states[i].texOff);
     }
-    PFSegment *hseg = (PFSegment *)(c->staging.base + segsOff);
+    PFSegment *hseg = (PFSegment *)(r->staging.base + segsOff);
+    PFTarget *htg = (PFTarget *)(r->staging.base + targetsOff);
     for (size_t i = 0; i < nSegs; i++) {
-        SegRec &r = c->segs[i];
-        PFSegment s = r.seg;
-        s.records = (const PFVertexIn *)dptr(r.recordsOff);
-        s.pos = (const float *)dptr(r.posOff);
-        s.nrm = (const float *)dptr(r.nrmOff);
-        s.uv = (const float *)dptr(r.uvOff);
-        s.col = (const uint8_t *)dptr(r.colOff);
-        s.idx = (const uint32_t *)dptr(r.idxOff);
-        s.explicitItems = (const int32_t *)dptr(r.itemsOff);
+        SegRec &rec = r->segs[i];
+        PFSegment s = rec.seg;
+        s.records = (const PFVertexIn *)dptr(rec.recordsOff);
+        s.pos = (const float *)dptr(rec.posOff);
+        s.nrm = (const float *)dptr(rec.nrmOff);
+        s.uv = (const float *)dptr(rec.uvOff);
+        s.col = (const uint8_t *)dptr(rec.colOff);
+        s.idx = (const uint32_t *)dptr(rec.idxOff);
+        s.explicitItems = (const int32_t *)dptr(rec.itemsOff);
         hseg[i] = s;
     }
-    // --- scratch sizing -------------------------------------------------------
+    // per batch: vertex / item bases, targets, tile numbering
     uint32_t maxVerts = 0, maxItems = 0, maxTiles = 0;
     bool anyPhong = false;
-    for (auto &cmd : c->cmds) {
-        if (cmd.kind != CMD_DRAW) continue;
-        uint32_t v = 0, it = 0;
-        for (int si = cmd.segBegin; si < cmd.segEnd; si++) {
+    std::vector<PFBatchLaunch> launches(ops.size());
+    size_t tgCursor = 0;
+    for (size_t oi = 0; oi < ops.size(); oi++) {
+        FlushOp &o = ops[oi];
+        if (o.kind != 0) continue;
+        PFBatchLaunch &L = launches[oi];
+        L = PFBatchLaunch{};
+        uint32_t v = 0, it = 0, tiles = 0;
+        for (int si = o.segBegin; si < o.segEnd; si++) {
             hseg[si].vtxBase = v; hseg[si].itemBase = it;
             v += hseg[si].nVerts; it += hseg[si].nItems;
+            PFframebuffer *fb = r->segs[si].fb;
+            hseg[si].target = (int32_t)(std::find(o.targets.begin(), o.targets.end(), fb) - o.targets.begin());
             if (hs[hseg[si].state].flags & PFS_PHONG) anyPhong = true;
         }
-        Tex *t = (Tex *)cmd.fb->texture;
-        uint32_t tiles = ((t->w + PF_TILE - 1) / PF_TILE) * ((t->h + PF_TILE - 1) / PF_TILE);
+        for (size_t k = 0; k < o.targets.size(); k++) {
+            FBMirror *m = mirrorOf(o.targets[k]);
+            PFTarget &T = htg[tgCursor + k];
+            std::memset(&T, 0, sizeof T);
+            T.color = m->dColor; T.depth = m->dDepth;
+            T.W = (uint32_t)m->w; T.H = (uint32_t)m->h;
+            T.tilesX = (T.W + PF_TILE - 1) / PF_TILE; T.tilesY = (T.H + PF_TILE - 1) / PF_TILE;
+            T.tileBase = tiles;
+            tiles += T.tilesX * T.tilesY;
+            if (o.clearCmd[k] >= 0) {
+                const Cmd &cl = cmds[o.clearCmd[k]];
+                T.clearMode = (cl.kind == CMD_FILL) ? 2 : 1; T.clearColor = cl.color; T.clearDepth = cl.depth;
+            }
+        }
+        L.segs = (const PFSegment *)(dbase + segsOff) + o.segBegin;
+        L.nSegs = o.segEnd - o.segBegin;
+        L.states = (const PFDrawState *)(dbase + statesOff);
+        L.targets = (const PFTarget *)(dbase + targetsOff) + tgCursor;
+        L.nTargets = (int)o.targets.size();
+        L.totalTiles = tiles;
+        L.nVerts = v; L.nItems = it;
+        L.command = (uint32_t)oi;
+        tgCursor += o.targets.size();
         maxVerts = std::max(maxVerts, v); maxItems = std::max(maxItems, it); maxTiles = std::max(maxTiles, tiles);
     }
-
-    cudaError_t e = cudaMemcpyAsync(dbase, c->staging.base, total, cudaMemcpyHostToDevice, st);
+    cudaError_t e = cudaMemcpyAsync(dbase, r->staging.base, total, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail("cudaMemcpyAsync(staging)", e);
-    const PFDrawState *dStates = (const PFDrawState *)(dbase + statesOff);
 
-    // --- framebuffers used: bring host content to the device ----------------
-    std::vector<PFframebuffer *> used;
-    for (auto &cmd : c->cmds)
-        if (std::find(used.begin(), used.end(), cmd.fb) == used.end()) used.push_back(cmd.fb);
-    for (PFframebuffer *fb : used) {
-        FBMirror *m = mirror_for(c, fb);
-        if (!m) return fail("cudaMalloc(framebuffer)", cudaErrorMemoryAllocation);
+    // --- framebuffers: bring host content to the device unless the first
+    //     operation touching a framebuffer overwrites it --------------------------
+    for (size_t u = 0; u < used.size(); u++) {
+        PFframebuffer *fb = used[u];
+        FBMirror *m = mirrors[u];
         const size_t n = m->w * m->h;
         const Cmd *first = nullptr;
-        for (auto &cmd : c->cmds) if (cmd.fb == fb) { first = &cmd; break; }
+        for (auto &cmd : cmds) if (cmd.fb == fb) { first = &cmd; break; }
         const bool uploadDepth = m->depthUserVisible || !m->depthOnDevice;
         if (first->kind == CMD_FILL) {
             // every pixel is overwritten first
         } else if (first->kind == CMD_CLEAR) {
-            // the clear leaves pixels 0..7 and reads pixel 0 for the tail
+            // the clear leaves pixels 0..7 (and reads pixel 0 for the tail)
             const size_t k = std::min<size_t>(8, n);
             cudaMemcpyAsync(m->dColor, m->tex->pixels, k * 4, cudaMemcpyHostToDevice, st);
             if (uploadDepth) cudaMemcpyAsync(m->dDepth, m->hostDepth, k * 4, cudaMemcpyHostToDevice, st);
@@ -650,99 +924,75 @@ bool flush(Ctx *c)
         m->depthOnDevice = true;
     }
 
-    PFDevCounters *dcnt = (PFDevCounters *)c->counters.p;
-    // A clear immediately followed by a DRAW on the same framebuffer is
-    // folded into that DRAW's raster kernel (every tile is written once).
-    // pfClear keeps pixels 0..7 and copies pixel 0 into the tail of a
-    // framebuffer whose size is not a multiple of 8; only the first is
-    // handled in the fused form.
-    std::vector<char> fusedClear(c->cmds.size(), 0);
-    for (size_t ci = 0; ci + 1 < c->cmds.size(); ci++) {
-        const Cmd &a = c->cmds[ci], &b = c->cmds[ci + 1];
-        if ((a.kind == CMD_CLEAR || a.kind == CMD_FILL) && b.kind == CMD_DRAW && a.fb == b.fb) {
-            const Tex *t = (const Tex *)a.fb->texture;
-            if (a.kind == CMD_FILL || ((size_t)t->w * t->h) % 8 == 0) fusedClear[ci] = 1;
-        }
-    }
-    uint32_t startCmd = 0;
+    PFDevCounters *dcnt = (PFDevCounters *)r->counters.p;
+    uint32_t startOp = 0;
+    r->lastOps.clear();
     for (int attempt = 0;; attempt++) {
-        if (!c->vout.ensure((size_t)maxVerts * sizeof(PFVertexOut) + 64) ||
-            !c->prims.ensure((size_t)maxItems * sizeof(PFPrim) + 128) ||
-            !c->primsPh.ensure(anyPhong ? (size_t)maxItems * sizeof(PFPrimPhong) + 128 : 128) ||
-            !c->pool.ensure((size_t)c->poolCap * sizeof(PFPrim)) ||
-            !c->poolPh.ensure(anyPhong ? (size_t)c->poolCap * sizeof(PFPrimPhong) : 128) ||
-            !c->binCount.ensure((size_t)maxTiles * 4 + 64) ||
-            !c->bins.ensure((size_t)maxTiles * c->cap * 4 + 64) ||
-            !c->misc.ensure(64)) {
-            c->devStatus |= PF_DEVICE_ALLOC_FAIL;
+        if (!r->vout.ensure((size_t)maxVerts * sizeof(PFVertexOut) + 64) ||
+            !r->prims.ensure((size_t)maxItems * sizeof(PFPrim) + 128) ||
+            !r->primsPh.ensure(anyPhong ? (size_t)maxItems * sizeof(PFPrimPhong) + 128 : 128) ||
+            !r->pool.ensure((size_t)r->poolCap * sizeof(PFPrim)) ||
+            !r->poolPh.ensure(anyPhong ? (size_t)r->poolCap * sizeof(PFPrimPhong) : 128) ||
+            !r->binCount.ensure((size_t)maxTiles * 4 + 64) ||
+            !r->bins.ensure((size_t)maxTiles * r->cap * 4 + 64)) {
+            r->devStatus |= PF_DEVICE_ALLOC_FAIL;
             return fail("cudaMalloc(scratch)", cudaErrorMemoryAllocation);
         }
-        // counters: abortCommand = none
         PFDevCounters init{};
         init.abortCommand = 0xffffffffu;
-        *c->hostCounters = init;
-        e = cudaMemcpyAsync(dcnt, c->hostCounters, sizeof(PFDevCounters), cudaMemcpyHostToDevice, st);
+        *r->hostCounters = init;
+        e = cudaMemcpyAsync(dcnt, r->hostCounters, sizeof(PFDevCounters), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return fail("cudaMemcpyAsync(counters)", e);
-
         size_t nRaster = 0;
-        if (c->timing) {
-            if (!c->evStart) { cudaEventCreate(&c->evStart); cudaEventCreate(&c->evEnd); }
-            cudaEventRecord(c->evStart, st);
+        if (r->timing) {
+            if (!r->evStart) { cudaEventCreate(&r->evStart); cudaEventCreate(&r->evEnd); }
+            cudaEventRecord(r->evStart, st);
         }
-        for (size_t ci = startCmd; ci < c->cmds.size(); ci++) {
-            const Cmd &cmd = c->cmds[ci];
-            FBMirror *m = &c->mirrors[(Tex *)cmd.fb->texture];
-            const size_t n = m->w * m->h;
-            if (cmd.kind == CMD_CLEAR || cmd.kind == CMD_FILL) {
-                if (fusedClear[ci]) continue;              // applied by the next DRAW's raster kernel
-                c->stats.kernel_launches += 1;
-                e = pfd_launch_clear(m->dColor, m->dDepth, n, cmd.color, cmd.depth, cmd.kind == CMD_FILL, dcnt, (uint32_t)ci, st);
-            } else if (cmd.kind == CMD_HOOK) {
-                c->stats.kernel_launches += 1;
-                e = pfd_launch_hook(m->dColor, m->dDepth, n, cmd.hook, cmd.hp, dcnt, (uint32_t)ci, st);
+        std::vector<Renderer::Op> doneOps;
+        for (size_t oi = startOp; oi < ops.size(); oi++) {
+            const FlushOp &o = ops[oi];
+            Renderer::Op rop{};
+            rop.kind = o.kind; rop.cmd = (int)oi;
+            if (o.kind == 1 || o.kind == 2) {
+                const Cmd &cmd = cmds[o.cmd];
+                FBMirror *m = mirrorOf(cmd.fb);
+                rop.n = m->w * m->h; rop.color = m->dColor; rop.depth = m->dDepth;
+                rop.cc = cmd.color; rop.cd = cmd.depth; rop.all = cmd.kind == CMD_FILL; rop.hook = cmd.hook; rop.hp = cmd.hp;
+                r->stats.kernel_launches += 1;
+                e = (o.kind == 1) ? pfd_launch_clear(rop.color, rop.depth, rop.n, rop.cc, rop.cd, rop.all, dcnt, (uint32_t)oi, st)
+                                  : pfd_launch_hook(rop.color, rop.depth, rop.n, rop.hook, rop.hp, dcnt, (uint32_t)oi, st);
             } else {
-                const PFSegment *dsegs = (const PFSegment *)(dbase + segsOff) + cmd.segBegin;
-                const int ns = cmd.segEnd - cmd.segBegin;
-                const PFSegment &lastSeg = hseg[cmd.segEnd - 1];
-                const uint32_t nV = lastSeg.vtxBase + lastSeg.nVerts, nI = lastSeg.itemBase + lastSeg.nItems;
-                PFBatchLaunch L{};
-                L.segs = dsegs; L.nSegs = ns; L.states = dStates;
-                L.vout = (PFVertexOut *)c->vout.p; L.nVerts = nV; L.nItems = nI;
-                L.prims = (PFPrim *)c->prims.p; L.primsPh = (PFPrimPhong *)c->primsPh.p;
-                L.pool = (PFPrim *)c->pool.p; L.poolPh = (PFPrimPhong *)c->poolPh.p; L.poolCap = c->poolCap;
-                L.binCount = (uint32_t *)c->binCount.p; L.bins = (uint32_t *)c->bins.p; L.cap = c->cap;
-                L.color = m->dColor; L.depth = m->dDepth;
-                L.W = (uint32_t)m->w; L.H = (uint32_t)m->h;
-                L.tilesX = (L.W + PF_TILE - 1) / PF_TILE; L.tilesY = (L.H + PF_TILE - 1) / PF_TILE;
-                L.cnt = dcnt; L.command = (uint32_t)ci;
-                int clearMode = 0; uint32_t cc = 0; float cd = 0.0f;
-                if (ci > 0 && fusedClear[ci - 1]) {
-                    const Cmd &cl = c->cmds[ci - 1];
-                    clearMode = (cl.kind == CMD_FILL) ? 2 : 1; cc = cl.color; cd = cl.depth;
-                }
-                c->stats.kernel_launches += 3;
+                PFBatchLaunch L = launches[oi];
+                L.vout = (PFVertexOut *)r->vout.p;
+                L.prims = (PFPrim *)r->prims.p; L.primsPh = (PFPrimPhong *)r->primsPh.p;
+                L.pool = (PFPrim *)r->pool.p; L.poolPh = (PFPrimPhong *)r->poolPh.p; L.poolCap = r->poolCap;
+                L.binCount = (uint32_t *)r->binCount.p; L.bins = (uint32_t *)r->bins.p; L.cap = r->cap;
+                L.rasterCtasPerSM = r->rasterCtasPerSM;
+                L.cnt = dcnt;
+                rop.L = L;
+                r->stats.kernel_launches += 3;
                 e = pfd_launch_vertex(L, st);
                 if (e == cudaSuccess) e = pfd_launch_items(L, st);
-                if (c->timing) {
-                    if (c->rasterEv.size() <= nRaster) {
+                if (r->timing) {
+                    if (r->rasterEv.size() <= nRaster) {
                         cudaEvent_t ev0, ev1; cudaEventCreate(&ev0); cudaEventCreate(&ev1);
-                        c->rasterEv.push_back({ ev0, ev1 });
+                        r->rasterEv.push_back({ ev0, ev1 });
                     }
-                    cudaEventRecord(c->rasterEv[nRaster].first, st);
+                    cudaEventRecord(r->rasterEv[nRaster].first, st);
                 }
-                if (e == cudaSuccess) e = pfd_launch_raster(L, clearMode, cc, cd, st);
-                if (c->timing) cudaEventRecord(c->rasterEv[nRaster].second, st);
+                if (e == cudaSuccess) e = pfd_launch_raster(L, st);
+                if (r->timing) cudaEventRecord(r->rasterEv[nRaster].second, st);
                 nRaster++;
             }
             if (e != cudaSuccess) return fail("kernel launch", e);
+            doneOps.push_back(rop);
         }
-        if (c->timing) cudaEventRecord(c->evEnd, st);
-        e = cudaMemcpyAsync(c->hostCounters, dcnt, sizeof(PFDevCounters), cudaMemcpyDeviceToHost, st);
+        if (r->timing) cudaEventRecord(r->evEnd, st);
+        e = cudaMemcpyAsync(r->hostCounters, dcnt, sizeof(PFDevCounters), cudaMemcpyDeviceToHost, st);
         // write back colour (and user-visible depth); if a bin overflowed the
         // replay below writes back again
-        for (PFframebuffer *fb : used) {
+        for (FBMirror *m : mirrors) {
             if (e != cudaSuccess) break;
-            FBMirror *m = &c->mirrors[(Tex *)fb->texture];
             const size_t n = m->w * m->h;
             e = cudaMemcpyAsync(m->tex->pixels, m->dColor, n * 4, cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess && m->depthUserVisible)
@@ -750,60 +1000,106 @@ bool flush(Ctx *c)
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail("pipeline", e);
-        if (c->timing) {
+        if (r->timing) {
             float ms = 0.0f;
-            cudaEventElapsedTime(&ms, c->evStart, c->evEnd);
-            c->stats.device_ms += ms;
+            cudaEventElapsedTime(&ms, r->evStart, r->evEnd);
+            r->stats.device_ms += ms;
             for (size_t k = 0; k < nRaster; k++) {
-                cudaEventElapsedTime(&ms, c->rasterEv[k].first, c->rasterEv[k].second);
-                c->stats.raster_ms += ms;
+                cudaEventElapsedTime(&ms, r->rasterEv[k].first, r->rasterEv[k].second);
+                r->stats.raster_ms += ms;
             }
         }
-        c->stats.raster_launches += nRaster;
-        const PFDevCounters hc = *c->hostCounters;
+        r->stats.raster_launches += nRaster;
+        const PFDevCounters hc = *r->hostCounters;
+        r->stats.fragments += hc.fragments;
+        r->stats.rasterized += hc.rasterized;
         if (hc.abortCommand == 0xffffffffu) {
-            c->stats.fragments += hc.fragments;
-            c->stats.rasterized += hc.rasterized;
+            r->lastOps.insert(r->lastOps.end(), doneOps.begin(), doneOps.end());
             break;
         }
-        // A bin or the clip pool overflowed in command hc.abortCommand.  The
-        // commands before it completed; it and every later one wrote nothing
+        // A bin or the clip pool overflowed in operation hc.abortCommand.  The
+        // operations before it completed; it and every later one wrote nothing
         // to any framebuffer.  Grow the capacity and resume from it.
-        c->stats.fragments += hc.fragments;
-        c->stats.rasterized += hc.rasterized;
-        c->stats.bin_overflows += 1;
+        for (auto &d : doneOps) if ((uint32_t)d.cmd < hc.abortCommand) r->lastOps.push_back(d);
+        r->stats.bin_overflows += 1;
         if (hc.status & PFD_BIN_OVERFLOW) {
-            uint32_t need = std::max(hc.maxBin, c->cap * 2);
+            uint32_t need = std::max(hc.maxBin, r->cap * 2);
             uint32_t nc = 1; while (nc < need) nc <<= 1;
             if (nc > kCapMax) {
-                c->devStatus |= PF_DEVICE_BIN_LIMIT;
+                r->devStatus |= PF_DEVICE_BIN_LIMIT;
                 return fail("tile bin capacity", cudaErrorMemoryAllocation);
             }
-            c->cap = nc;
+            r->cap = nc;
         }
-        if (hc.status & PFD_CLIP_OVERFLOW) c->poolCap = std::max(c->poolCap * 4, hc.clipCount * 2);
+        if (hc.status & PFD_CLIP_OVERFLOW) r->poolCap = std::max(r->poolCap * 4, hc.clipCount * 2);
         if (attempt > 8) return fail("overflow retries", cudaErrorUnknown);
-        startCmd = hc.abortCommand;
-        if (startCmd > 0 && fusedClear[startCmd - 1]) startCmd -= 1;   // the fused clear did not run either
+        startOp = hc.abortCommand;
     }
-
-    c->stats.flushes += 1;
-    discard_recording(c);
+    r->stats.flushes += 1;
+    r->graphValid = false;      // a new flush: a replay graph must be captured again
+    discard_recording(r);
     return true;
 }
 
-// Bring the main framebuffer's internal depth back to the host (it stays on
+bool flush(Ctx *c) { return flush(c->rend); }
+
+// Bring a main framebuffer's internal depth back to the host (it stays on
 // the device otherwise: the reference exposes it only to pfPostProcess).
 void pull_main_depth(Ctx *c)
 {
-    auto it = c->mirrors.find(c->mainFB.texture);
-    if (it == c->mirrors.end() || !it->second.depthOnDevice) return;
-    FBMirror &m = it->second;
-    cudaMemcpy(m.hostDepth, m.dDepth, m.w * m.h * 4, cudaMemcpyDeviceToHost);
-    m.depthOnDevice = false;    // host copy authoritative again
+    FBMirror *m = find_mirror(c->mainFB.texture);
+    if (!m || !m->depthOnDevice) return;
+    cudaMemcpy(m->hostDepth, m->dDepth, m->w * m->h * 4, cudaMemcpyDeviceToHost);
+    m->depthOnDevice = false;    // host copy authoritative again
 }
 
 void sync_host(Ctx *c) { flush(c); }
+
+// Re-run the device work of the renderer's last flush (inputs already on the
+// device) `n` times from a CUDA graph; returns the mean GPU ms per run.
+float replay(Renderer *r, uint32_t n)
+{
+    if (!r->devOk || r->lastOps.empty() || n == 0) return -1.0f;
+    cudaStream_t st = r->stream;
+    PFDevCounters *dcnt = (PFDevCounters *)r->counters.p;
+    if (!r->graphValid) {
+        if (r->graph) { cudaGraphExecDestroy(r->graph); r->graph = nullptr; }
+        PFDevCounters init{};
+        init.abortCommand = 0xffffffffu;
+        *r->hostCounters = init;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return -1.0f; }
+        cudaMemcpyAsync(dcnt, r->hostCounters, sizeof(PFDevCounters), cudaMemcpyHostToDevice, st);
+        for (const auto &op : r->lastOps) {
+            if (op.kind == 1) pfd_launch_clear(op.color, op.depth, op.n, op.cc, op.cd, op.all, dcnt, (uint32_t)op.cmd, st);
+            else if (op.kind == 2) pfd_launch_hook(op.color, op.depth, op.n, op.hook, op.hp, dcnt, (uint32_t)op.cmd, st);
+            else {
+                pfd_launch_vertex(op.L, st);
+                pfd_launch_items(op.L, st);
+                pfd_launch_raster(op.L, st);
+            }
+        }
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (e != cudaSuccess || !g) { cudaGetLastError(); return -1.0f; }
+        e = cudaGraphInstantiate(&r->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { cudaGetLastError(); r->graph = nullptr; return -1.0f; }
+        r->graphValid = true;
+        cudaGraphLaunch(r->graph, st);                     // warm
+        cudaStreamSynchronize(st);
+    }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a); cudaEventCreate(&b);
+    cudaEventRecord(a, st);
+    for (uint32_t i = 0; i < n; i++) cudaGraphLaunch(r->graph, st);
+    cudaEventRecord(b, st);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a); cudaEventDestroy(b);
+    if (e != cudaSuccess) { cudaGetLastError(); return -1.0f; }
+    return ms / (float)n;
+}
 
 }  // namespace
 
@@ -819,8 +1115,10 @@ PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFda
     c->mainFB.texture = tex_new(buf, w, h, f, t);
     G = prev;
     if (!c->mainFB.texture) { delete c; return nullptr; }
+    ((Tex *)c->mainFB.texture)->isMain = true;
     c->mainFB.zbuffer = (float *)std::malloc((size_t)w * h * sizeof(float));
     if (!c->mainFB.zbuffer) { delete (Tex *)c->mainFB.texture; delete c; return nullptr; }
+    if (gBatch) { c->rend = &gBatch->r; gBatch->members.push_back(c); }
     for (size_t i = 0; i < (size_t)w * h; i++) c->mainFB.zbuffer[i] = FLT_MAX;
     c->current = &c->mainFB;
     c->vpDim[0] = w - 1; c->vpMax[0] = (PFint)w - 1;
@@ -842,17 +1140,12 @@ void pfDeleteContext(PFcontext ctx)
     Ctx *prev = G; G = c;
     flush(c);
     G = (prev == c) ? nullptr : prev;
-    release_mirrors(c);
-    if (c->devOk) {
-        c->arena.release(); c->vout.release(); c->prims.release(); c->primsPh.release(); c->pool.release();
-        c->poolPh.release(); c->binCount.release(); c->bins.release();
-        c->counters.release(); c->misc.release();
-        if (c->hostCounters) cudaFreeHost(c->hostCounters);
-        if (c->evStart) { cudaEventDestroy(c->evStart); cudaEventDestroy(c->evEnd); }
-        for (auto &pr : c->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
-        if (c->stream) cudaStreamDestroy(c->stream);
+    if (gBatch) {
+        auto &mm = gBatch->members;
+        mm.erase(std::remove(mm.begin(), mm.end(), c), mm.end());
     }
-    c->staging.release();
+    drop_mirror(c->mainFB.texture);
+    release_renderer(&c->own);
     std::free(c->mainFB.zbuffer);
     delete (Tex *)c->mainFB.texture;
     delete c;
@@ -869,15 +1162,10 @@ void pfSetMainBuffer(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatyp
         G->mainFB.zbuffer = (float *)std::malloc((size_t)w * h * sizeof(float));
         for (size_t i = 0; i < (size_t)w * h; i++) G->mainFB.zbuffer[i] = G->clearDepth;
     }
-    auto it = G->mirrors.find(old);
-    if (it != G->mirrors.end()) {
-        if (it->second.registered) cudaHostUnregister(it->second.registered);
-        if (it->second.dColor) cudaFree(it->second.dColor);
-        if (it->second.dDepth) cudaFree(it->second.dDepth);
-        G->mirrors.erase(it);
-    }
+    drop_mirror(old);
     delete old;
     G->mainFB.texture = tex_new(buf, w, h, f, t);
+    if (G->mainFB.texture) ((Tex *)G->mainFB.texture)->isMain = true;
     G->aux = nullptr;
 }
 
@@ -895,8 +1183,16 @@ PFcontext pfGetCurrentContext(void) { return G; }
 
 void pfMakeCurrent(PFcontext ctx)
 {
-    if (G && G != (Ctx *)ctx) flush(G);
-    G = (Ctx *)ctx;
+    Ctx *c = (Ctx *)ctx;
+    // outside a batch, switching away is an observation point of the context
+    if (G && G != c && !gBatch) flush(G);
+    G = c;
+    if (c && gBatch && c->rend != &gBatch->r) {
+        flush(c);                                   // what it recorded alone renders first
+        c->rend = &gBatch->r;
+        c->openImmSeg = -1;
+        gBatch->members.push_back(c);
+    }
 }
 
 PFboolean pfIsEnabled(PFstate s) { return (G->state & s) != 0; }
@@ -1125,8 +1421,7 @@ void pfClear(PFclearflag flag)
     if (!flag) return;
     Cmd cmd{};
     cmd.kind = CMD_CLEAR; cmd.fb = G->current; cmd.color = pack(G->clearColor); cmd.depth = G->clearDepth;
-    G->cmds.push_back(cmd);
-    G->openImmSeg = -1;
+    push_cmd(G, cmd);
 }
 void pfClearDepth(PFfloat d) { G->clearDepth = d; }
 void pfClearColor(PFubyte r, PFubyte g, PFubyte b, PFubyte a) { G->clearColor = PFcolor{ r, g, b, a }; }
@@ -1254,8 +1549,8 @@ static float attr_f(const Attrib &a, size_t i)
 static int64_t stage_float_attr(Ctx *c, const Attrib &a, int comps, size_t first, size_t count)
 {
     if (a.type == PF_FLOAT) return snapshot(c, (const float *)a.buf + first * comps, count * comps * 4);
-    int64_t off = c->staging.alloc(count * comps * 4);
-    float *dst = (float *)(c->staging.base + off);
+    int64_t off = c->rend->staging.alloc(count * comps * 4);
+    float *dst = (float *)(c->rend->staging.base + off);
     for (size_t i = 0; i < count * comps; i++) dst[i] = attr_f(a, first * comps + i);
     return off;
 }
@@ -1264,8 +1559,8 @@ static int64_t stage_color_attr(Ctx *c, const Attrib &a, size_t first, size_t co
 {
     const size_t k = (size_t)a.size;
     if (a.type == PF_UNSIGNED_BYTE) return snapshot(c, (const uint8_t *)a.buf + first * k, count * k);
-    int64_t off = c->staging.alloc(count * k);
-    uint8_t *dst = c->staging.base + off;
+    int64_t off = c->rend->staging.alloc(count * k);
+    uint8_t *dst = c->rend->staging.base + off;
     for (size_t i = 0; i < count * k; i++) {
         const size_t o = first * k + i;
         switch (a.type) {
@@ -1300,13 +1595,11 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     int64_t idxOff = -1;
     size_t nverts;
     if (indices) {
-        idxOff = c->staging.alloc((size_t)count * 4);
-        uint32_t *dst = (uint32_t *)(c->staging.base + idxOff);
+        idxOff = c->rend->staging.alloc((size_t)count * 4);
+        uint32_t *dst = (uint32_t *)(c->rend->staging.base + idxOff);
         uint32_t mx = 0;
         if (itype == PF_UNSIGNED_INT) {
-            const uint32_t *s = (const uint32_t *)indices;
-            std::memcpy(dst, s, (size_t)count * 4);
-            for (PFsizei i = 0; i < count; i++) mx = std::max(mx, s[i]);
+            mx = par_copy_max_u32(dst, (const uint32_t *)indices, count);
         } else if (itype == PF_UNSIGNED_SHORT) {
             const uint16_t *s = (const uint16_t *)indices;
             for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
@@ -1324,7 +1617,7 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     const bool useC = (c->state & PF_COLOR_ARRAY) && c->colors.buf;
 
     const int si = new_segment(c, PF_SRC_ARRAYS, mode == PF_TRIANGLES ? PF_ITEMS_TRIS : PF_ITEMS_EXPLICIT);
-    SegRec &r = c->segs[si];
+    SegRec &r = c->rend->segs[si];
     r.posOff = stage_float_attr(c, c->positions, c->positions.size, (size_t)first, nverts);
     if (useN) r.nrmOff = stage_float_attr(c, c->normals, 3, (size_t)first, nverts);
     if (useT) r.uvOff = stage_float_attr(c, c->texcoords, 2, (size_t)first, nverts);
@@ -1514,14 +1807,70 @@ void pfPostProcessDevice(PFuint hookId, const void *params, PFsizei size)
     } break;
     default: G->err = PF_INVALID_ENUM; return;
     }
-    G->cmds.push_back(cmd);
-    G->openImmSeg = -1;
+    push_cmd(G, cmd);
 }
 
-void pfGetStats(PFstats *s) { *s = G->stats; }
-void pfResetStats(void) { G->stats = PFstats{}; }
-void pfEnableTiming(PFboolean enable) { G->timing = enable; }
-PFuint pfGetDeviceStatus(void) { return G ? G->devStatus : 0; }
+// --- batches: many contexts, one launch of each pipeline kernel --------------
+PFgbbatch pfgbBatchCreate(void) { return new Batch(); }
+
+void pfgbBatchDelete(PFgbbatch batch)
+{
+    Batch *b = (Batch *)batch;
+    if (!b) return;
+    if (gBatch == b) pfgbBatchEnd(batch);
+    release_renderer(&b->r);
+    delete b;
+}
+
+void pfgbBatchBegin(PFgbbatch batch)
+{
+    Batch *b = (Batch *)batch;
+    if (!b || gBatch) { set_err(PF_INVALID_OPERATION); return; }
+    gBatch = b;
+    b->open = true;
+    if (G) {
+        flush(G);                         // the current context's own work renders first
+        G->rend = &b->r;
+        G->openImmSeg = -1;
+        b->members.push_back(G);
+    }
+}
+
+void pfgbBatchEnd(PFgbbatch batch)
+{
+    Batch *b = (Batch *)batch;
+    if (!b || gBatch != b) { set_err(PF_INVALID_OPERATION); return; }
+    flush(&b->r);
+    for (Ctx *c : b->members) { c->rend = &c->own; c->openImmSeg = -1; }
+    b->members.clear();
+    b->open = false;
+    gBatch = nullptr;
+}
+
+PFfloat pfgbBatchReplay(PFgbbatch batch, PFuint n)
+{
+    Batch *b = (Batch *)batch;
+    if (!b || b->open) return -1.0f;
+    return replay(&b->r, n);
+}
+
+void pfgbBatchGetStats(PFgbbatch batch, PFstats *s) { *s = ((Batch *)batch)->r.stats; }
+void pfgbBatchEnableTiming(PFgbbatch batch, PFboolean enable) { ((Batch *)batch)->r.timing = enable; }
+
+void pfgbBatchTune(PFgbbatch batch, PFuint binCapacity, PFuint rasterCtasPerSM)
+{
+    Renderer *r = batch ? &((Batch *)batch)->r : (G ? &G->own : nullptr);
+    if (!r) return;
+    if (binCapacity >= 32 && binCapacity <= kCapMax && (binCapacity & (binCapacity - 1)) == 0) r->cap = binCapacity;
+    if (rasterCtasPerSM >= 1 && rasterCtasPerSM <= 8) r->rasterCtasPerSM = (int)rasterCtasPerSM;
+}
+
+PFfloat pfgbReplay(PFuint n) { return G ? replay(&G->own, n) : -1.0f; }
+
+void pfGetStats(PFstats *s) { *s = G->own.stats; }
+void pfResetStats(void) { G->own.stats = PFstats{}; }
+void pfEnableTiming(PFboolean enable) { G->own.timing = enable; }
+PFuint pfGetDeviceStatus(void) { return G ? G->own.devStatus : 0; }
 
 // --- framebuffers (framebuffer.c) ----------------------------------------------
 PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
@@ -1550,14 +1899,7 @@ void pfDeleteFramebuffer(PFframebuffer *fb)
     if (G) flush(G);
     Tex *t = (Tex *)fb->texture;
     if (t) {
-        if (G) {
-            auto it = G->mirrors.find(t);
-            if (it != G->mirrors.end()) {
-                if (it->second.registered) cudaHostUnregister(it->second.registered);
-                cudaFree(it->second.dColor); cudaFree(it->second.dDepth);
-                G->mirrors.erase(it);
-            }
-        }
+        drop_mirror(t);
         if (t->ownsPinned) cudaFreeHost(t->pixels); else std::free(t->pixels);
         if (fb->zbuffer) { if (cudaFreeHost(fb->zbuffer) != cudaSuccess) { cudaGetLastError(); std::free(fb->zbuffer); } }
         delete t;
@@ -1575,7 +1917,7 @@ void pfClearFramebuffer(PFframebuffer *fb, PFcolor color, PFfloat depth)
 {
     Cmd cmd{};
     cmd.kind = CMD_FILL; cmd.fb = fb; cmd.color = pack(color); cmd.depth = depth;
-    if (G) { G->cmds.push_back(cmd); G->openImmSeg = -1; }
+    if (G) push_cmd(G, cmd);
 }
 
 PFcolor pfGetFramebufferPixel(const PFframebuffer *fb, PFsizei x, PFsizei y)

@@ -260,7 +260,7 @@ __device__ __forceinline__ uint32_t lerp_color(uint32_t a, uint32_t b, float t)
         float af = (float)chn(a, i) * inv255;
         float bf = (float)chn(b, i) * inv255;
         float r = af + t * (bf - af);
-        o[i] = x86_cvt_rne(x86_min(x86_max(r, 0.0f), 1.0f) * 255.0f);
+        o[i] = __float2int_rn(x86_min(x86_max(r, 0.0f), 1.0f) * 255.0f);   // clamped: in range
     }
     return pack4(o);
 }
@@ -414,7 +414,7 @@ __device__ uint32_t light_phong(const PFDrawState &S, uint32_t frag, const PFDev
         for (int i = 0; i < 3; i++) { acc[i] = acc[i] + amb[i]; acc[i] = acc[i] + dif[i]; acc[i] = acc[i] + spe[i]; }
     }
     int32_t o[4] = { 0, 0, 0, 0 };
-    for (int i = 0; i < 3; i++) o[i] = x86_cvt_rne(x86_min(x86_max(acc[i], 0.0f), 1.0f) * 255.0f);
+    for (int i = 0; i < 3; i++) o[i] = __float2int_rn(x86_min(x86_max(acc[i], 0.0f), 1.0f) * 255.0f);
     return pack4(o);
 }
 
@@ -440,13 +440,36 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
                          PFVertexOut *__restrict__ out, uint32_t nVerts, PFDevCounters *cnt,
                          uint32_t *__restrict__ binCount, uint32_t nTiles)
 {
+    __shared__ __align__(16) PFSegment sSeg;
+    __shared__ __align__(16) PFDrawState sState;
+    __shared__ int sUniform;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (cnt->abortCommand != 0xffffffffu) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
-    if (g == 0) { cnt->clipCount = 0; cnt->batchRasterized = 0; }
+    if (g == 0) { cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0; }
+    const uint32_t g0 = blockIdx.x * blockDim.x;
+    if (g0 >= nVerts) return;
+    // the block's vertices usually belong to one segment: stage it and its
+    // draw state in shared memory instead of reading both field by field
+    if (threadIdx.x == 0) {
+        const int a = seg_of_vertex(segs, nSegs, g0), b = seg_of_vertex(segs, nSegs, min(g0 + blockDim.x, nVerts) - 1);
+        sUniform = (a == b) ? a : -1;
+    }
+    __syncthreads();
+    const int su = sUniform;
+    if (su >= 0) {
+        const int4 *src0 = reinterpret_cast<const int4 *>(&segs[su]);
+        const int4 *src1 = reinterpret_cast<const int4 *>(&states[segs[su].state]);
+        constexpr int n0 = sizeof(PFSegment) / 16, n1 = sizeof(PFDrawState) / 16;
+        for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
+            if (i < n0) reinterpret_cast<int4 *>(&sSeg)[i] = __ldg(src0 + i);
+            else reinterpret_cast<int4 *>(&sState)[i - n0] = __ldg(src1 + (i - n0));
+        }
+        __syncthreads();
+    }
     if (g >= nVerts) return;
-    const PFSegment &sg = segs[seg_of_vertex(segs, nSegs, g)];
-    const PFDrawState &S = states[sg.state];
+    const PFSegment &sg = (su >= 0) ? sSeg : segs[seg_of_vertex(segs, nSegs, g)];
+    const PFDrawState &S = (su >= 0) ? sState : states[sg.state];
     const uint32_t j = g - sg.vtxBase;
     float pos[4], nrm[3], uv[2];
     uint32_t col;
@@ -515,10 +538,21 @@ struct BinArgs {
     uint32_t *binCount;
     uint32_t *bins;
     uint32_t cap;
-    uint32_t W, H, tilesX;
+    const PFTarget *targets;
     PFDevCounters *cnt;
     uint32_t command;
 };
+
+// Framebuffer geometry a sub-triangle is binned against.
+struct TileSpace {
+    uint32_t W, H, tilesX, tileBase;
+};
+
+__device__ __forceinline__ TileSpace tile_space(const BinArgs &B, int target)
+{
+    const PFTarget &t = B.targets[target];
+    return TileSpace{ t.W, t.H, t.tilesX, t.tileBase };
+}
 
 // Rasterize_Triangle set-up (triangles.c:287-349).  Returns false if culled.
 __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVert &a, const SVert &b,
@@ -554,28 +588,70 @@ __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVer
     return true;
 }
 
-__device__ void bin_prim(const BinArgs &B, const PFPrim &P, uint32_t key)
+// Tile range of a set-up sub-triangle: pixels x in [xMin, xMax) and y in
+// [yMin, yMax], compared as unsigned (the reference's PFsizei loop bounds),
+// clipped to the framebuffer.  Returns false when no pixel remains.
+__device__ __forceinline__ bool tile_range(const TileSpace &T, const PFPrim &P, uint32_t &tx0, uint32_t &ty0,
+                                           uint32_t &ntx, uint32_t &nty)
 {
-    // pixels: x in [xMin, xMax) and y in [yMin, yMax], compared as unsigned
-    // (the reference's PFsizei loop bounds), then clipped to the framebuffer.
     uint32_t x0 = (uint32_t)P.xMin, x1 = (uint32_t)P.xMax, y0 = (uint32_t)P.yMin, y1 = (uint32_t)P.yMax;
-    if (x1 > B.W) x1 = B.W;
-    if (y1 >= B.H) y1 = B.H - 1;
-    if (x0 >= x1 || y0 > y1) return;
-    uint32_t tx0 = x0 / PF_TILE, tx1 = (x1 - 1) / PF_TILE, ty0 = y0 / PF_TILE, ty1 = y1 / PF_TILE;
-    for (uint32_t ty = ty0; ty <= ty1; ty++)
-        for (uint32_t tx = tx0; tx <= tx1; tx++) {
-            uint32_t t = ty * B.tilesX + tx;
-            uint32_t slot = atomicAdd(&B.binCount[t], 1u);
-            if (slot < B.cap) B.bins[(size_t)t * B.cap + slot] = key;
-            else {
-                atomicMax(&B.cnt->maxBin, slot + 1);
-                if (slot == B.cap) {
-                    atomicOr(&B.cnt->status, (unsigned)PFD_BIN_OVERFLOW);
-                    atomicMin(&B.cnt->abortCommand, B.command);
-                }
-            }
+    if (x1 > T.W) x1 = T.W;
+    if (y1 >= T.H) y1 = T.H - 1;
+    if (x0 >= x1 || y0 > y1) return false;
+    tx0 = x0 / PF_TILE; ty0 = y0 / PF_TILE;
+    ntx = (x1 - 1) / PF_TILE - tx0 + 1; nty = y1 / PF_TILE - ty0 + 1;
+    return true;
+}
+
+__device__ __forceinline__ void bin_slot(const BinArgs &B, uint32_t t, uint32_t slot, uint32_t key)
+{
+    if (slot < B.cap) B.bins[(size_t)t * B.cap + slot] = key;
+    else {
+        atomicMax(&B.cnt->maxBin, slot + 1);
+        if (slot == B.cap) {
+            atomicOr(&B.cnt->status, (unsigned)PFD_BIN_OVERFLOW);
+            atomicMin(&B.cnt->abortCommand, B.command);
         }
+    }
+}
+
+// Append `key` to the bin of every tile the sub-triangle touches (one
+// thread; used by the clipping path).
+__device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, uint32_t key)
+{
+    uint32_t tx0, ty0, ntx, nty;
+    if (!tile_range(T, P, tx0, ty0, ntx, nty)) return;
+    for (uint32_t ty = ty0; ty < ty0 + nty; ty++)
+        for (uint32_t tx = tx0; tx < tx0 + ntx; tx++) {
+            const uint32_t t = T.tileBase + ty * T.tilesX + tx;
+            bin_slot(B, t, atomicAdd(&B.binCount[t], 1u), key);
+        }
+}
+
+// Warp-cooperative binning: lanes whose sub-triangles touch the same tile
+// share one atomic on its counter (neighbouring triangles of a mesh usually
+// do); slots within a group follow lane order.  Every lane of the warp must
+// call it (lanes with nothing to bin pass n = 0).
+__device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, const PFPrim &P, uint32_t key)
+{
+    uint32_t tx0 = 0, ty0 = 0, ntx = 0, nty = 0;
+    if (has && !tile_range(T, P, tx0, ty0, ntx, nty)) has = false;
+    const uint32_t n = has ? ntx * nty : 0;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1;
+    uint32_t most = n;
+    for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+    for (uint32_t i = 0; i < most; i++) {
+        const bool act = i < n;
+        const uint32_t t = act ? T.tileBase + (ty0 + i / ntx) * T.tilesX + (tx0 + i % ntx) : 0xffffffffu;
+        const uint32_t grp = __match_any_sync(0xffffffffu, t);
+        if (!act) continue;
+        const uint32_t leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&B.binCount[t], (unsigned)__popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        bin_slot(B, t, base + __popc(grp & lt), key);
+    }
 }
 
 __device__ __forceinline__ void store_phong(PFPrimPhong *dst, const SVert &a, const SVert &b, const SVert &c)
@@ -666,7 +742,7 @@ struct ItemOut {
 };
 
 __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const PFVertexOut *const *V, int face,
-                                       uint32_t g, const ItemOut &O, const BinArgs &B)
+                                       uint32_t g, const ItemOut &O, const BinArgs &B, const TileSpace &T)
 {
     CVert poly[PF_CLIP_MAXV], tmp[PF_CLIP_MAXV];
     for (int m = 0; m < 3; m++) {
@@ -716,7 +792,7 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
             O.pool[base + i - 1] = P;
             if (S.flags & PFS_PHONG) store_phong(&O.poolPh[base + i - 1], s[0], s[i + 1], s[i + 2]);
         }
-        bin_prim(B, P, (g << PF_SUB_BITS) | (uint32_t)i);
+        bin_prim(B, T, P, (g << PF_SUB_BITS) | (uint32_t)i);
     }
     // prims[g] carries the pool base of sub-triangles >= 1 even when
     // sub-triangle 0 was culled.
@@ -729,13 +805,15 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
 // ---------------------------------------------------------------------------
 // k_items: one thread per triangle-face item, in submission order
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
-                        const PFVertexOut *__restrict__ vout, uint32_t nItems, ItemOut O, BinArgs B)
+// Project, clip if needed and set up item g.  Returns true when its
+// unclipped sub-triangle survived culling and must be binned by the caller
+// (clipped items bin their sub-triangles themselves).
+__device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawState *sState,
+                                           const PFDrawState *__restrict__ states,
+                                           const PFVertexOut *__restrict__ vout, uint32_t g, const ItemOut &O,
+                                           const BinArgs &B, const TileSpace &T, PFPrim &P)
 {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nItems || B.cnt->abortCommand != 0xffffffffu) return;
-    const PFSegment &sg = segs[seg_of_item(segs, nSegs, g)];
-    const PFDrawState &S = states[sg.state];
+    const PFDrawState &S = sState ? *sState : states[sg.state];
     uint32_t vi[3]; int face;
     item_vertices(sg, g - sg.itemBase, vi, face);
     const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
@@ -751,7 +829,7 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
             inside = inside && !(h.w < 1e-5f) && (h.x <= h.w) && (-h.x <= h.w) && (h.y <= h.w) && (-h.y <= h.w) &&
                      (h.z <= h.w) && (-h.z <= h.w);
         }
-        if (!inside) { clip_item(S, sg.state, V, face, g, O, B); return; }
+        if (!inside) { clip_item(S, sg.state, V, face, g, O, B, T); return false; }
     }
     SVert s[3];
     for (int m = 0; m < 3; m++) {
@@ -772,12 +850,54 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
         if (S.flags & PFS_PHONG)
             for (int i = 0; i < 3; i++) { s[m].n[i] = o.n[i]; s[m].p[i] = o.p[i]; }
     }
-    PFPrim P;
-    if (!setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P)) return;
-    atomicAdd(&B.cnt->batchRasterized, 1ull);
+    if (!setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P)) return false;
     O.prims[g] = P;
     if (S.flags & PFS_PHONG) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
-    bin_prim(B, P, g << PF_SUB_BITS);
+    return true;
+}
+__global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
+                        const PFVertexOut *__restrict__ vout, uint32_t nItems, ItemOut O, BinArgs B)
+{
+    __shared__ __align__(16) PFSegment sSeg;
+    __shared__ __align__(16) PFDrawState sState;
+    __shared__ int sUniform;
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (B.cnt->abortCommand != 0xffffffffu) return;
+    const uint32_t g0 = blockIdx.x * blockDim.x;
+    if (threadIdx.x == 0) {
+        const int a = seg_of_item(segs, nSegs, g0), b = seg_of_item(segs, nSegs, min(g0 + blockDim.x, nItems) - 1);
+        sUniform = (a == b) ? a : -1;
+    }
+    __syncthreads();
+    const int su = sUniform;
+    if (su >= 0) {
+        const int4 *src0 = reinterpret_cast<const int4 *>(&segs[su]);
+        const int4 *src1 = reinterpret_cast<const int4 *>(&states[segs[su].state]);
+        constexpr int n0 = sizeof(PFSegment) / 16, n1 = sizeof(PFDrawState) / 16;
+        for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
+            if (i < n0) reinterpret_cast<int4 *>(&sSeg)[i] = __ldg(src0 + i);
+            else reinterpret_cast<int4 *>(&sState)[i - n0] = __ldg(src1 + (i - n0));
+        }
+        __syncthreads();
+    }
+    // every lane stays to the end: binning below is warp-cooperative
+    PFPrim P;
+    bool kept = false;
+    TileSpace T{ 0, 0, 0, 0 };
+    if (g < nItems) {
+        const PFSegment &sg = su >= 0 ? sSeg : segs[seg_of_item(segs, nSegs, g)];
+        T = tile_space(B, sg.target);
+        kept = item_setup(sg, su >= 0 ? &sState : nullptr, states, vout, g, O, B, T, P);
+    }
+    // one counter update per block: same-address atomics serialise in L2
+    __shared__ unsigned sKept;
+    if (threadIdx.x == 0) sKept = 0;
+    __syncthreads();
+    const unsigned wk = __popc(__ballot_sync(0xffffffffu, kept));
+    if ((threadIdx.x & 31) == 0 && wk) atomicAdd(&sKept, wk);
+    bin_prim_warp(B, T, kept, P, g << PF_SUB_BITS);
+    __syncthreads();
+    if (threadIdx.x == 0 && sKept) atomicAdd(&B.cnt->batchRasterized, (unsigned long long)sKept);
 }
 
 // ---------------------------------------------------------------------------
@@ -810,14 +930,11 @@ struct RasterArgs {
     const PFPrim *pool;
     const PFPrimPhong *poolPh;
     const PFDrawState *states;
-    uint32_t *color;
-    float *depth;
-    uint32_t W, H, tilesX;
+    const PFTarget *targets;
+    int nTargets;
+    uint32_t totalTiles;
     PFDevCounters *cnt;
     uint32_t command;
-    int clearMode;            // 0 none, 1 pfClear (pixels 0..7 kept), 2 every pixel
-    uint32_t clearColor;
-    float clearDepth;
 };
 
 struct ChunkPrim {             // per-sub-triangle data derived for this tile
@@ -836,8 +953,9 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
     const uint32_t fl = S.flags;
     uint32_t frag;
     if (fl & PFS_SMOOTH) {
-        const uint32_t u1 = (uint32_t)x86_cvt_rne(wn1 * 255.0f), u2 = (uint32_t)x86_cvt_rne(wn2 * 255.0f);
-        const uint32_t u3 = (uint32_t)x86_cvt_rne(wn3 * 255.0f);
+        // covered pixels have weights in [0, 1]: the conversions are in range
+        const uint32_t u1 = (uint32_t)__float2int_rn(wn1 * 255.0f), u2 = (uint32_t)__float2int_rn(wn2 * 255.0f);
+        const uint32_t u3 = (uint32_t)__float2int_rn(wn3 * 255.0f);
         int32_t o[4];
         for (int i = 0; i < 4; i++) {
             uint32_t s = u1 * chn(P.c1, i) + u2 * chn(P.c2, i);
@@ -884,27 +1002,39 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     if (a.cnt->abortCommand <= a.command) return;
     // the batch completed set-up without overflow: its sub-triangles count
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.cnt->rasterized, a.cnt->batchRasterized);
-    const uint32_t tile = blockIdx.x;
-    const uint32_t n = min(a.binCount[tile], a.cap);
-    if (n == 0 && a.clearMode == 0) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t tx = tile % a.tilesX, ty = tile / a.tilesX;
-    const uint32_t ox = tx * PF_TILE, oy = ty * PF_TILE;
     const uint32_t lx = tid % PF_TILE, ly = tid / PF_TILE;
+    unsigned long long frags = 0;
+
+    // persistent: CTAs take tiles of all targets from a shared work queue
+    __shared__ uint32_t sNext;
+    for (;;) {
+    __syncthreads();                                   // sNext and the previous tile's shared data are free
+    if (tid == 0) sNext = atomicAdd(&a.cnt->tileQueue, 1u);
+    __syncthreads();
+    const uint32_t gt = sNext;
+    if (gt >= a.totalTiles) break;
+    int tlo = 0, thi = a.nTargets - 1;
+    while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gt) tlo = mid; else thi = mid - 1; }
+    const PFTarget &T = a.targets[tlo];
+    const uint32_t tile = gt - T.tileBase;
+    const uint32_t n = min(a.binCount[gt], a.cap);
+    if (n == 0 && T.clearMode == 0) continue;
+    const uint32_t tx = tile % T.tilesX, ty = tile / T.tilesX;
+    const uint32_t ox = tx * PF_TILE, oy = ty * PF_TILE;
     const uint32_t px = ox + lx, py = oy + ly;
-    const bool inside = px < a.W && py < a.H;
-    const size_t pidx = (size_t)py * a.W + px;
+    const bool inside = px < T.W && py < T.H;
+    const size_t pidx = (size_t)py * T.W + px;
 
     // pixel state in registers
     uint32_t col = 0; float dep = 0.0f;
     if (inside) {
-        if (a.clearMode == 2 || (a.clearMode == 1 && pidx >= 8)) { col = a.clearColor; dep = a.clearDepth; }
-        else { col = a.color[pidx]; dep = a.depth[pidx]; }
+        if (T.clearMode == 2 || (T.clearMode == 1 && pidx >= 8)) { col = T.clearColor; dep = T.clearDepth; }
+        else { col = T.color[pidx]; dep = T.depth[pidx]; }
     }
 
-    unsigned long long frags = 0;
     if (n > 0) {
-        const uint32_t *bin = a.bins + (size_t)tile * a.cap;
+        const uint32_t *bin = a.bins + (size_t)gt * a.cap;
         for (uint32_t i = tid; i < n; i += RASTER_THREADS) skeys[i] = bin[i];
         __syncthreads();
         // keys arrive in atomic order; restore submission order
@@ -972,8 +1102,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     cp.e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
                 }
                 // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside tile and framebuffer
-                uint32_t x0 = max((uint32_t)P.xMin, ox), x1 = min(min((uint32_t)P.xMax, ox + PF_TILE), a.W);
-                uint32_t y0 = max((uint32_t)P.yMin, oy), y1e = min(min((uint32_t)P.yMax + 1u, oy + PF_TILE), a.H);
+                uint32_t x0 = max((uint32_t)P.xMin, ox), x1 = min(min((uint32_t)P.xMax, ox + PF_TILE), T.W);
+                uint32_t y0 = max((uint32_t)P.yMin, oy), y1e = min(min((uint32_t)P.yMax + 1u, oy + PF_TILE), T.H);
                 if ((uint32_t)P.yMax == 0xffffffffu) y1e = 0;    // yMax + 1 wrapped
                 const bool empty = (x0 >= x1) || (y0 >= y1e) || ((uint32_t)P.xMin >= (uint32_t)P.xMax) ||
                                    ((uint32_t)P.yMin > (uint32_t)P.yMax);
@@ -984,8 +1114,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 if (a.states[P.flags >> 8].flags & PFS_PHONG) sHasPhong = 1;
             }
             __syncthreads();
-            if (tid < 32) {                                   // prefix of clipped areas
-                uint32_t v = (tid < cn) ? scp[tid].bw * scp[tid].bh : 0;
+            if (tid < 32) {                                   // prefix of clipped box rows
+                uint32_t v = (tid < cn && scp[tid].bw) ? scp[tid].bh : 0;
                 uint32_t s = v;
                 for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
                 sarea[tid + 1] = s;
@@ -1002,20 +1132,23 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 }
             }
             __syncthreads();
-            // 2. coverage over all (sub-triangle, pixel) pairs of the clipped boxes
+            // 2. coverage: one work item per (sub-triangle, row of its clipped
+            //    box); edge functions stepped along the row
             const uint32_t total = sarea[CH];
             for (uint32_t t = tid; t < total; t += RASTER_THREADS) {
                 int lo = 0, hi = CH - 1;                          // largest k with sarea[k] <= t
                 while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
                 const ChunkPrim &cp = scp[lo];
-                const uint32_t i = t - sarea[lo];
-                const uint32_t dy = (uint32_t)(((float)i + 0.5f) * cp.invBw);
-                const uint32_t dx = i - dy * cp.bw;
-                const uint32_t X = cp.bx0 + dx, Y = cp.by0 + dy;
-                const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + X * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0]);
-                const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + X * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1]);
-                const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + X * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2]);
-                if ((w1 | w2 | w3) > 0) atomicOr(&pmask[Y * PF_TILE + X], 1u << lo);
+                const uint32_t Y = cp.by0 + (t - sarea[lo]);
+                const uint32_t bit = 1u << lo;
+                uint32_t w1 = (uint32_t)cp.e0[0] + cp.bx0 * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0];
+                uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
+                uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
+                uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
+                for (uint32_t dx = 0; dx < cp.bw; dx++) {
+                    if ((int32_t)(w1 | w2 | w3) > 0) atomicOr(row + dx, bit);
+                    w1 += (uint32_t)cp.ex[0]; w2 += (uint32_t)cp.ex[1]; w3 += (uint32_t)cp.ex[2];
+                }
             }
             __syncthreads();
             // 3+4. per warp: compact, shade densely, resolve in order
@@ -1075,10 +1208,16 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             }
         }
     }
-    if (inside) { a.color[pidx] = col; a.depth[pidx] = dep; }
-    // fragment counter: warp reduce, one atomic per warp
+    if (inside) { T.color[pidx] = col; T.depth[pidx] = dep; }
+    }   // tile loop
+    // fragment counter: one atomic per CTA (same-address atomics serialise)
+    __shared__ unsigned long long sFrags;
+    if (tid == 0) sFrags = 0;
+    __syncthreads();
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
-    if (lane == 0 && frags) atomicAdd(&a.cnt->fragments, frags);
+    if (lane == 0 && frags) atomicAdd(&sFrags, frags);
+    __syncthreads();
+    if (tid == 0 && sFrags) atomicAdd(&a.cnt->fragments, sFrags);
 }
 
 // ---------------------------------------------------------------------------
@@ -1137,9 +1276,22 @@ __global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, 
 // ---------------------------------------------------------------------------
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
+int pfd_sm_count(void)
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 152;
+        }
+    }
+    return sms;
+}
+
 cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 {
-    const uint32_t nTiles = L.tilesX * L.tilesY;
+    const uint32_t nTiles = L.totalTiles;
     const size_t work = L.nVerts > nTiles ? L.nVerts : nTiles;
     k_vertex<<<grid_for(work, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nVerts, L.cnt,
                                                   L.binCount, nTiles);
@@ -1149,7 +1301,7 @@ cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
-    BinArgs B{ L.binCount, L.bins, L.cap, L.W, L.H, L.tilesX, L.cnt, L.command };
+    BinArgs B{ L.binCount, L.bins, L.cap, L.targets, L.cnt, L.command };
     ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap };
     k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, O, B);
     return cudaGetLastError();
@@ -1163,15 +1315,17 @@ static size_t raster_smem(uint32_t cap)
     return words * sizeof(uint32_t);
 }
 
-cudaError_t pfd_launch_raster(const PFBatchLaunch &L, int clearMode, uint32_t clearColor, float clearDepth,
-                              cudaStream_t st)
+cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
-    RasterArgs a{ L.binCount, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.color, L.depth,
-                  L.W, L.H, L.tilesX, L.cnt, L.command, clearMode, clearColor, clearDepth };
+    if (L.totalTiles == 0) return cudaSuccess;
+    RasterArgs a{ L.binCount, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
+                  L.totalTiles, L.cnt, L.command };
     const size_t smem = raster_smem(L.cap);
     cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_raster<<<L.tilesX * L.tilesY, RASTER_THREADS, smem, st>>>(a);
+    const uint32_t per = (uint32_t)(L.rasterCtasPerSM > 0 ? L.rasterCtasPerSM : 4);
+    const uint32_t grid = min(L.totalTiles, (uint32_t)pfd_sm_count() * per);
+    k_raster<<<grid, RASTER_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 

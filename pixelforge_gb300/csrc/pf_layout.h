@@ -101,7 +101,23 @@ typedef struct {
     const int32_t *explicitItems; /* PF_ITEMS_EXPLICIT: int4 {s0, s1, s2, face} */
     int32_t nFaces;               /* PF_ITEMS_TRIS: 1 or 2 */
     int32_t face0;                /* PF_ITEMS_TRIS with nFaces == 1 */
-} PFSegment;
+    int32_t target;               /* framebuffer of this segment (index into the batch's targets) */
+    int32_t pad_[3];
+} PFSegment;                      /* 144 bytes */
+
+/* A framebuffer rendered by a batch.  Its tiles are numbered
+ * tileBase .. tileBase + tilesX*tilesY - 1 in the batch's bin arrays. */
+typedef struct {
+    uint32_t *color;
+    float *depth;
+    uint32_t W, H;
+    uint32_t tilesX, tilesY;
+    uint32_t tileBase;
+    int32_t clearMode;            /* 0 keep, 1 fused pfClear (pixels 0..7 kept), 2 fused full fill */
+    uint32_t clearColor;
+    float clearDepth;
+    uint32_t pad_[4];
+} PFTarget;                       /* 64 bytes */
 
 /* Transformed vertex. */
 typedef struct {
@@ -149,6 +165,8 @@ typedef struct {
     unsigned int maxBin;          /* largest tile bin count seen */
     unsigned int clipCount;       /* clipped sub-triangles allocated */
     unsigned long long batchRasterized;   /* sub-triangles set up by the current batch */
+    unsigned int tileQueue;       /* next tile of the current batch's raster work list */
+    unsigned int pad_;
 } PFDevCounters;
 
 #endif /* PF_LAYOUT_H */

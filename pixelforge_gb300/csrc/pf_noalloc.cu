@@ -38,7 +38,8 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffState = 0;
 constexpr size_t kOffSeg = align256(kOffState + sizeof(PFDrawState));
 constexpr size_t kOffCnt = align256(kOffSeg + sizeof(PFSegment));
-constexpr size_t kOffVout = align256(kOffCnt + sizeof(PFDevCounters));
+constexpr size_t kOffTarget = align256(kOffCnt + sizeof(PFDevCounters));
+constexpr size_t kOffVout = align256(kOffTarget + sizeof(PFTarget));
 constexpr size_t kOffPrims = align256(kOffVout + sizeof(PFVertexOut) * 3 * (size_t)kMaxTris);
 constexpr size_t kOffPool = align256(kOffPrims + sizeof(PFPrim) * (size_t)kMaxTris);
 constexpr size_t kOffPh = align256(kOffPool + sizeof(PFPrim) * (size_t)kPoolCap);
@@ -121,11 +122,17 @@ extern "C" int pfgbDrawTrianglesStatic(const float *positions, const uint32_t *c
     PFDevCounters C;
     std::memset(&C, 0, sizeof C);
     C.abortCommand = 0xffffffffu;
+    PFTarget T;
+    std::memset(&T, 0, sizeof T);
+    T.color = color; T.depth = depth; T.W = width; T.H = height;
+    T.tilesX = (width + PF_TILE - 1) / PF_TILE; T.tilesY = (height + PF_TILE - 1) / PF_TILE;
+    T.tileBase = 0; T.clearMode = 0;
 
     // pageable sources: these copies return once the data left the stack
     cudaError_t e = cudaMemcpyAsync(s + kOffState, &S, sizeof S, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s + kOffSeg, &G, sizeof G, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s + kOffCnt, &C, sizeof C, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s + kOffTarget, &T, sizeof T, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { cudaGetLastError(); return PFGB_STATIC_E_CUDA; }
 
     PFBatchLaunch L{};
@@ -135,12 +142,12 @@ extern "C" int pfgbDrawTrianglesStatic(const float *positions, const uint32_t *c
     L.prims = (PFPrim *)(s + kOffPrims); L.primsPh = (PFPrimPhong *)(s + kOffPh);
     L.pool = (PFPrim *)(s + kOffPool); L.poolPh = (PFPrimPhong *)(s + kOffPh); L.poolCap = kPoolCap;
     L.binCount = (uint32_t *)(s + kOffBinCount); L.bins = (uint32_t *)(s + kOffBins); L.cap = kBinCap;
-    L.color = color; L.depth = depth; L.W = width; L.H = height;
-    L.tilesX = (width + PF_TILE - 1) / PF_TILE; L.tilesY = (height + PF_TILE - 1) / PF_TILE;
+    L.targets = (const PFTarget *)(s + kOffTarget); L.nTargets = 1; L.totalTiles = T.tilesX * T.tilesY;
+    L.rasterCtasPerSM = 4;
     L.cnt = (PFDevCounters *)(s + kOffCnt); L.command = 0;
     e = pfd_launch_vertex(L, st);
     if (e == cudaSuccess) e = pfd_launch_items(L, st);
-    if (e == cudaSuccess) e = pfd_launch_raster(L, 0, 0u, 0.0f, st);
+    if (e == cudaSuccess) e = pfd_launch_raster(L, st);
     if (e != cudaSuccess) { cudaGetLastError(); return PFGB_STATIC_E_CUDA; }
     // the counters say whether a tile bin or the clip pool overflowed
     e = cudaMemcpyAsync(&C, s + kOffCnt, sizeof C, cudaMemcpyDeviceToHost, st);

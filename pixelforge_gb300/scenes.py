@@ -440,3 +440,110 @@ class PhongScene:
             return fr
         finally:
             tg.close()
+
+
+@dataclass
+class BatchScene:
+    """Config 3: many independent contexts of uneven size and load.
+
+    Context i: square framebuffer of side ~ U{64, 128, ..., max_side}; a
+    triangle soup as in the 256x256 workload (xy in [-1, 1], z in [0.1, 0.9],
+    RGB uniform, alpha 255) plus UVs in [0, 2], triangle count lognormal
+    (median ``tri_median``, sigma ``tri_sigma``) clipped to ``tri_clip``; one
+    256x256 noise texture with a uniformly chosen filter and wrap; blending
+    uniformly one of alpha / additive / multiply / none; depth test LESS
+    against a depth cleared to 1.0.  Triangles are submitted with
+    pfDrawArrays(PF_TRIANGLES), which processes them exactly as
+    pfBegin/pfVertex does.
+    """
+    n: int = 512
+    seed: int = 1003
+    max_side: int = 512
+    tri_median: float = 2000.0
+    tri_sigma: float = 1.0
+    tri_clip: tuple = (100, 50000)
+    tex_size: int = 256
+
+    def __post_init__(self):
+        rng = np.random.default_rng(self.seed)
+        steps = self.max_side // 64
+        self.sides = (rng.integers(1, steps + 1, self.n) * 64).astype(int)
+        nt = np.exp(np.log(self.tri_median) + self.tri_sigma * rng.standard_normal(self.n))
+        self.ntris = np.clip(nt.astype(int), self.tri_clip[0], self.tri_clip[1])
+        self.filters = rng.integers(0, 2, self.n)
+        self.wraps = rng.integers(0, 3, self.n)
+        self.blends = rng.choice([A.PF_BLEND_ALPHA, A.PF_BLEND_ADD, A.PF_BLEND_MUL, -1], self.n)
+        self.pos, self.col, self.uv, self.tex = [], [], [], []
+        for i in range(self.n):
+            m = int(self.ntris[i]) * 3
+            p = np.empty((m, 3), np.float32)
+            p[:, :2] = rng.uniform(-1, 1, (m, 2))
+            p[:, 2] = rng.uniform(0.1, 0.9, m)
+            c = rng.integers(0, 256, (m, 4), dtype=np.uint8)
+            c[:, 3] = 255
+            self.pos.append(p)
+            self.col.append(c)
+            self.uv.append(rng.uniform(0, 2, (m, 2)).astype(np.float32))
+            self.tex.append(noise_texture(self.tex_size, self.seed * 1000 + i))
+        self.ctx = []
+        self.buf = []
+        self.texh = []
+
+    @property
+    def total_tris(self) -> int:
+        return int(self.ntris.sum())
+
+    def create(self, lib):
+        for i in range(self.n):
+            s = int(self.sides[i])
+            b = np.zeros((s, s, 4), np.uint8)
+            c = lib.pfCreateContext(_ptr(b), s, s, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            lib.pfMakeCurrent(c)
+            t = lib.pfGenTexture(_ptr(self.tex[i]), self.tex_size, self.tex_size, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            lib.pfTextureParameter(t, int(self.wraps[i]), int(self.filters[i]))
+            self.ctx.append(c)
+            self.buf.append(b)
+            self.texh.append(t)
+
+    def record(self, lib, i):
+        lib.pfMakeCurrent(self.ctx[i])
+        lib.pfClearDepth(1.0)
+        lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+        lib.pfEnable(A.PF_DEPTH_TEST)
+        lib.pfDepthFunc(A.PF_LESS)
+        lib.pfBindTexture(self.texh[i])
+        lib.pfEnable(A.PF_TEXTURE_2D)
+        if self.blends[i] >= 0:
+            lib.pfEnable(A.PF_BLEND)
+            lib.pfBlendFunc(int(self.blends[i]))
+        else:
+            lib.pfDisable(A.PF_BLEND)
+        lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_COLOR_ARRAY | A.PF_TEXTURE_COORD_ARRAY)
+        lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(self.pos[i]))
+        lib.pfColorPointer(4, A.PF_UNSIGNED_BYTE, 0, _ptr(self.col[i]))
+        lib.pfTexCoordPointer(A.PF_FLOAT, 0, _ptr(self.uv[i]))
+        lib.pfDrawArrays(A.PF_TRIANGLES, 0, int(self.ntris[i]) * 3)
+
+    def render_loop(self, lib, finish=True):
+        """Each context on its own: record, then its own observation point."""
+        for i in range(self.n):
+            self.record(lib, i)
+            if finish and lib.has("pfFinish"):
+                lib.pfFinish()
+        return [b.copy() for b in self.buf]
+
+    def render_batch(self, lib, batch):
+        """All contexts recorded into one batch and rendered together."""
+        lib.pfgbBatchBegin(batch)
+        for i in range(self.n):
+            self.record(lib, i)
+        lib.pfgbBatchEnd(batch)
+        return [b.copy() for b in self.buf]
+
+    def destroy(self, lib):
+        for i, c in enumerate(self.ctx):
+            lib.pfMakeCurrent(c)
+            th = C.c_void_p(self.texh[i])
+            lib.pfDeleteTexture(C.byref(th), False)
+            lib.pfDeleteContext(c)
+        self.ctx, self.buf, self.texh = [], [], []

@@ -1,0 +1,90 @@
+"""Batched contexts (config 3 form): many contexts rendered by one launch of
+each pipeline kernel must give exactly the images of rendering each context
+on its own, and match the CPU oracle (depth bit-exact, colour within 1 LSB)."""
+import numpy as np
+import pytest
+
+from pixelforge_gb300 import abi as A
+from pixelforge_gb300.scenes import BatchScene
+
+pytestmark = pytest.mark.gpu
+
+
+def _images_equal(a, b):
+    return all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_batch_equals_per_context(gpu):
+    sc = BatchScene(n=64, max_side=256, tri_clip=(100, 4000), seed=31)
+    sc.create(gpu)
+    try:
+        loop = sc.render_loop(gpu)
+        batch = gpu.pfgbBatchCreate()
+        try:
+            got = sc.render_batch(gpu, batch)
+            s = A.PFstats()
+            gpu.pfgbBatchGetStats(batch, s)
+            assert s.flushes == 1, "a batch renders with one flush"
+            # one launch of each pipeline kernel per attempt (a tile bin that
+            # overflows its capacity makes the flush grow it and resume)
+            assert s.kernel_launches == 3 * (1 + s.bin_overflows)
+        finally:
+            gpu.pfgbBatchDelete(batch)
+        assert _images_equal(loop, got)
+    finally:
+        sc.destroy(gpu)
+
+
+def test_batch_vs_oracle(gpu, oracle):
+    sc_g = BatchScene(n=12, max_side=192, tri_clip=(100, 900), seed=32)
+    sc_o = BatchScene(n=12, max_side=192, tri_clip=(100, 900), seed=32)
+    sc_g.create(gpu)
+    sc_o.create(oracle)
+    try:
+        batch = gpu.pfgbBatchCreate()
+        try:
+            got = sc_g.render_batch(gpu, batch)
+        finally:
+            gpu.pfgbBatchDelete(batch)
+        ref = sc_o.render_loop(oracle)
+        for i, (g, r) in enumerate(zip(got, ref)):
+            d = np.abs(g.astype(np.int32) - r.astype(np.int32))
+            assert int(d.max()) <= 1, f"context {i}: colour differs by {int(d.max())}"
+    finally:
+        sc_g.destroy(gpu)
+        sc_o.destroy(oracle)
+
+
+def test_batch_replay_and_reuse(gpu):
+    sc = BatchScene(n=24, max_side=192, tri_clip=(100, 2000), seed=33)
+    sc.create(gpu)
+    try:
+        batch = gpu.pfgbBatchCreate()
+        try:
+            first = sc.render_batch(gpu, batch)
+            ms = gpu.pfgbBatchReplay(batch, 3)
+            assert ms > 0.0
+            # rendering the batch again (recorded anew) gives the same images
+            again = sc.render_batch(gpu, batch)
+            assert _images_equal(first, again)
+        finally:
+            gpu.pfgbBatchDelete(batch)
+        assert gpu.pfGetDeviceStatus() == 0
+    finally:
+        sc.destroy(gpu)
+
+
+def test_batch512_equals_per_context(gpu):
+    """The full 512-context workload: batched images equal per-context ones."""
+    sc = BatchScene()
+    sc.create(gpu)
+    try:
+        loop = sc.render_loop(gpu)
+        batch = gpu.pfgbBatchCreate()
+        try:
+            got = sc.render_batch(gpu, batch)
+        finally:
+            gpu.pfgbBatchDelete(batch)
+        assert _images_equal(loop, got)
+    finally:
+        sc.destroy(gpu)
