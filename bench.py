@@ -189,7 +189,63 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, samples=2)
     tg.close()
+    if not args.no_batched:
+        out["batched"] = run_batched(lib)
     return out
+
+
+def run_batched(lib) -> dict:
+    """512 independent contexts of uneven size: one batch versus looping the
+    plain path (one flush per context), on identical images."""
+    import numpy as np
+    from pixelforge_gb300 import abi as A
+    from pixelforge_gb300.autotune import tune_batch
+    from pixelforge_gb300.scenes import BatchScene
+
+    sc = BatchScene()
+    sc.create(lib)
+    for c in sc.ctx:
+        lib.pfMakeCurrent(c)
+        lib.pfEnableTiming(True)
+        lib.pfResetStats()
+    # plain path: each context recorded and flushed on its own
+    sc.render_loop(lib)                                  # warm-up (allocations)
+    for c in sc.ctx:
+        lib.pfMakeCurrent(c)
+        lib.pfResetStats()
+    t0 = time.perf_counter()
+    loop_imgs = sc.render_loop(lib)
+    loop_wall = time.perf_counter() - t0
+    loop_dev_ms = 0.0
+    frags = 0
+    for c in sc.ctx:
+        lib.pfMakeCurrent(c)
+        s = A.PFstats()
+        lib.pfGetStats(s)
+        loop_dev_ms += s.device_ms
+        frags += s.fragments
+    batch = lib.pfgbBatchCreate()
+    lib.pfgbBatchEnableTiming(batch, True)
+    tune = tune_batch(lib, batch, lambda b: sc.render_batch(lib, b), "batch512")
+    sc.render_batch(lib, batch)                          # warm-up at the tuned setting
+    t0 = time.perf_counter()
+    batch_imgs = sc.render_batch(lib, batch)
+    batch_wall = time.perf_counter() - t0
+    identical = all(np.array_equal(a, b) for a, b in zip(loop_imgs, batch_imgs))
+    replay_ms = lib.pfgbBatchReplay(batch, 10)
+    lib.pfgbBatchDelete(batch)
+    sc.destroy(lib)
+    n = sc.n
+    return {"workload": "batch512: 512 contexts, sides 64..512, lognormal triangle counts "
+                        f"({sc.total_tris} triangles), textured, per-context blend",
+            "views_per_s_graph": n / (replay_ms / 1e3), "replay_ms": replay_ms,
+            "views_per_s_batch_e2e": n / batch_wall, "batch_e2e_ms": batch_wall * 1e3,
+            "views_per_s_loop_e2e": n / loop_wall, "loop_e2e_ms": loop_wall * 1e3,
+            "views_per_s_loop_device": n / (loop_dev_ms / 1e3), "loop_device_ms": loop_dev_ms,
+            "speedup_graph_vs_loop_device": loop_dev_ms / replay_ms,
+            "speedup_batch_vs_loop_e2e": loop_wall / batch_wall,
+            "fragments": frags, "images_identical": identical,
+            "tuning": {k: v for k, v in tune.items() if k != "trials"}}
 
 
 def _reference_lib():
@@ -253,6 +309,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 512-context batch measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

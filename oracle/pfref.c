@@ -939,33 +939,87 @@ void pfDisable(PFstate s)
 }
 PFerrcode pfGetError(void) { PFerrcode e = G->err; G->err = PF_NO_ERROR; return e; }
 
-/* getters: a host-state subset (src/getter.c) */
+/* getters (src/getter.c:24-521): the reference's cases; other names set
+ * PF_INVALID_ENUM and leave the output untouched.  Point size, line width,
+ * raster position and pixel zoom are not modelled by this oracle (the
+ * triangle path does not read them) and read as their initial values
+ * (context.c:179-180). */
+void pfGetBooleanv(PFenum p, PFboolean *v)
+{
+    switch (p) {
+    case PF_TEXTURE_2D: case PF_FRAMEBUFFER: case PF_BLEND: case PF_DEPTH_TEST: case PF_CULL_FACE:
+    case PF_NORMALIZE: case PF_LIGHTING: case PF_COLOR_MATERIAL: case PF_VERTEX_ARRAY: case PF_NORMAL_ARRAY:
+    case PF_COLOR_ARRAY: case PF_TEXTURE_COORD_ARRAY:
+        *v = (G->state & p) != 0; break;
+    case PF_VERTEX_ARRAY_TYPE: *v = G->positions.type != 0; break;
+    case PF_NORMAL_ARRAY_STRIDE: *v = G->normals.stride != 0; break;
+    case PF_NORMAL_ARRAY_TYPE: *v = G->normals.type != 0; break;
+    case PF_TEXTURE_COORD_ARRAY_STRIDE: *v = G->texcoords.stride != 0; break;
+    case PF_TEXTURE_COORD_ARRAY_TYPE: *v = G->texcoords.type != 0; break;
+    case PF_COLOR_ARRAY_SIZE: *v = G->colors.size != 0; break;
+    case PF_COLOR_ARRAY_STRIDE: *v = G->colors.stride != 0; break;
+    case PF_COLOR_ARRAY_TYPE: *v = G->colors.type != 0; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
 void pfGetIntegerv(PFenum p, PFint *v)
 {
     switch (p) {
     case PF_VIEWPORT: v[0] = G->vpPos[0]; v[1] = G->vpPos[1]; v[2] = (PFint)G->vpDim[0] + 1; v[3] = (PFint)G->vpDim[1] + 1; break;
-    case PF_BLEND_FUNC: v[0] = G->blend; break;
-    case PF_DEPTH_FUNC: v[0] = G->depthFunc; break;
+    case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r; v[1] = G->clearColor.g; v[2] = G->clearColor.b; v[3] = G->clearColor.a; break;
     case PF_CULL_FACE_MODE: v[0] = G->cullFace; break;
-    case PF_SHADE_MODEL: v[0] = G->shade; break;
+    case PF_CURRENT_COLOR: v[0] = G->curColor.r; v[1] = G->curColor.g; v[2] = G->curColor.b; v[3] = G->curColor.a; break;
+    case PF_CURRENT_RASTER_POSITION: v[0] = 0; v[1] = 0; break;
+    case PF_POLYGON_MODE: v[0] = G->polygonMode[0]; v[1] = G->polygonMode[1]; break;
     case PF_MATRIX_MODE: v[0] = G->matMode; break;
+    case PF_MAX_PROJECTION_STACK_DEPTH: v[0] = 2; break;
+    case PF_MAX_MODELVIEW_STACK_DEPTH: v[0] = 8; break;
+    case PF_MAX_TEXTURE_STACK_DEPTH: v[0] = 4; break;
+    case PF_SHADE_MODEL: v[0] = G->shade; break;
     case PF_MAX_LIGHTS: v[0] = MAX_LIGHTS; break;
+    case PF_VERTEX_ARRAY_SIZE: v[0] = G->positions.size; break;
+    case PF_VERTEX_ARRAY_STRIDE: v[0] = (PFint)G->positions.stride; break;
+    case PF_VERTEX_ARRAY_TYPE: v[0] = (PFint)G->positions.type; break;
+    case PF_NORMAL_ARRAY_STRIDE: v[0] = (PFint)G->normals.stride; break;
+    case PF_NORMAL_ARRAY_TYPE: v[0] = (PFint)G->normals.type; break;
+    case PF_TEXTURE_COORD_ARRAY_STRIDE: v[0] = (PFint)G->texcoords.stride; break;
+    case PF_TEXTURE_COORD_ARRAY_TYPE: v[0] = (PFint)G->texcoords.type; break;
+    case PF_COLOR_ARRAY_SIZE: v[0] = G->colors.size; break;
+    case PF_COLOR_ARRAY_STRIDE: v[0] = (PFint)G->colors.stride; break;
+    case PF_COLOR_ARRAY_TYPE: v[0] = (PFint)G->colors.type; break;
     default: G->err = PF_INVALID_ENUM; break;
     }
 }
-void pfGetFloatv(PFenum p, PFfloat *v)
+#define GET_REAL(T, INV)                                                                      \
+    switch (p) {                                                                              \
+    case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r*(INV); v[1] = G->clearColor.g*(INV);    \
+        v[2] = G->clearColor.b*(INV); v[3] = G->clearColor.a*(INV); break;                    \
+    case PF_DEPTH_CLEAR_VALUE: v[0] = G->clearDepth; break;                                   \
+    case PF_CURRENT_COLOR: v[0] = G->curColor.r*(INV); v[1] = G->curColor.g*(INV);            \
+        v[2] = G->curColor.b*(INV); v[3] = G->curColor.a*(INV); break;                        \
+    case PF_CURRENT_NORMAL: for (int i = 0; i < 3; i++) v[i] = G->curNormal[i]; break;        \
+    case PF_CURRENT_TEXTURE_COORDS: for (int i = 0; i < 2; i++) v[i] = G->curTex[i]; break;   \
+    case PF_CURRENT_RASTER_POSITION: v[0] = 0; v[1] = 0; break;                               \
+    case PF_POINT_SIZE: case PF_LINE_WIDTH: case PF_ZOOM_X: case PF_ZOOM_Y: v[0] = 1; break;  \
+    case PF_PROJECTION_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->proj[i]; break;        \
+    case PF_MODELVIEW_MATRIX: { mat4 mv; m_mul(mv, G->model, G->view);                       \
+        for (int i = 0; i < 16; i++) { v[i] = mv[i]; } break; }                               \
+    case PF_TEXTURE_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->tex[i]; break;            \
+    default: G->err = PF_INVALID_ENUM; break;                                                 \
+    }
+void pfGetFloatv(PFenum p, PFfloat *v) { GET_REAL(PFfloat, (PFfloat)(1.0 / 255)) }
+void pfGetDoublev(PFenum p, PFdouble *v) { GET_REAL(PFdouble, (1.0 / 255)) }
+#undef GET_REAL
+void pfGetPointerv(PFenum p, const void **v)
 {
     switch (p) {
-    case PF_DEPTH_CLEAR_VALUE: v[0] = G->clearDepth; break;
-    case PF_PROJECTION_MATRIX: memcpy(v, G->proj, 64); break;
-    case PF_MODELVIEW_MATRIX: memcpy(v, G->modelUsed ? G->model : G->view, 64); break;
-    case PF_TEXTURE_MATRIX: memcpy(v, G->tex, 64); break;
+    case PF_TEXTURE_2D: *v = G->texture; break;
+    case PF_FRAMEBUFFER: *v = G->bound; break;
+    case PF_BLEND_FUNC: *v = &G->blend; break;
+    case PF_DEPTH_FUNC: *v = &G->depthFunc; break;
     default: G->err = PF_INVALID_ENUM; break;
     }
 }
-void pfGetBooleanv(PFenum p, PFboolean *v) { (void)p; (void)v; G->err = PF_INVALID_ENUM; }
-void pfGetDoublev(PFenum p, PFdouble *v) { (void)p; (void)v; G->err = PF_INVALID_ENUM; }
-void pfGetPointerv(PFenum p, const void **v) { (void)p; (void)v; G->err = PF_INVALID_ENUM; }
 
 /* ------------------------------------------------------------------------ */
 /* API: matrices (context.c:392-548)                                         */

@@ -72,7 +72,11 @@ PF_POSITION, PF_SPOT_DIRECTION = 7, 8
 PF_SPOT_INNER_CUTOFF, PF_SPOT_OUTER_CUTOFF = 10, 11
 PF_CONSTANT_ATTENUATION, PF_LINEAR_ATTENUATION, PF_QUADRATIC_ATTENUATION = 12, 13, 14
 PF_RGBA = 7
-PF_VIEWPORT, PF_BLEND_FUNC, PF_DEPTH_FUNC = 10000, 10008, 10009
+(PF_VIEWPORT, PF_COLOR_CLEAR_VALUE, PF_DEPTH_CLEAR_VALUE, PF_CULL_FACE_MODE, PF_CURRENT_COLOR,
+ PF_CURRENT_NORMAL, PF_CURRENT_TEXTURE_COORDS, PF_CURRENT_RASTER_POSITION, PF_BLEND_FUNC, PF_DEPTH_FUNC,
+ PF_POLYGON_MODE, PF_POINT_SIZE, PF_LINE_WIDTH, PF_MATRIX_MODE, PF_PROJECTION_MATRIX, PF_MODELVIEW_MATRIX,
+ PF_TEXTURE_MATRIX, PF_MAX_PROJECTION_STACK_DEPTH, PF_MAX_MODELVIEW_STACK_DEPTH, PF_MAX_TEXTURE_STACK_DEPTH,
+ PF_SHADE_MODEL) = range(10000, 10021)
 PF_HOOK_IDENTITY, PF_HOOK_FOG_LINEAR, PF_HOOK_GRAYSCALE = 0, 1, 2
 
 _V = None
@@ -151,6 +155,65 @@ PROTOTYPES = {
     "pfGenTexture": (PFptr, [PFptr, PFsizei, PFsizei, PFenum_i, PFenum_i]),
     "pfDeleteTexture": (_V, [C.POINTER(C.c_void_p), PFbool]),
     "pfTextureParameter": (_V, [PFptr, PFenum_i, PFenum_i]),
+    "pfGetBooleanv": (_V, [PFenum, C.POINTER(PFbool)]),
+    "pfGetDoublev": (_V, [PFenum, C.POINTER(C.c_double)]),
+    "pfGetPointerv": (_V, [PFenum, C.POINTER(C.c_void_p)]),
+    "pfLineWidth": (_V, [PFfloat]),
+    "pfPointSize": (_V, [PFfloat]),
+    "pfVertex2i": (_V, [PFint] * 2),
+    "pfVertex2fv": (_V, [_FP]),
+    "pfVertex3i": (_V, [PFint] * 3),
+    "pfVertex4i": (_V, [PFint] * 4),
+    "pfVertex4fv": (_V, [_FP]),
+    "pfColor": (_V, [PFcolor]),
+    "pfColor1ui": (_V, [PFuint]),
+    "pfColor3ubv": (_V, [C.POINTER(PFubyte)]),
+    "pfColor3us": (_V, [PFushort] * 3),
+    "pfColor3usv": (_V, [C.POINTER(PFushort)]),
+    "pfColor3ui": (_V, [PFuint] * 3),
+    "pfColor3uiv": (_V, [C.POINTER(PFuint)]),
+    "pfColor3fv": (_V, [_FP]),
+    "pfColor4ubv": (_V, [C.POINTER(PFubyte)]),
+    "pfColor4us": (_V, [PFushort] * 4),
+    "pfColor4usv": (_V, [C.POINTER(PFushort)]),
+    "pfColor4ui": (_V, [PFuint] * 4),
+    "pfColor4uiv": (_V, [C.POINTER(PFuint)]),
+    "pfColor4fv": (_V, [_FP]),
+    "pfTexCoordfv": (_V, [_FP]),
+    "pfNormal3fv": (_V, [_FP]),
+    "pfRects": (_V, [PFshort] * 4),
+    "pfRectsv": (_V, [C.POINTER(PFshort)] * 2),
+    "pfRectf": (_V, [PFfloat] * 4),
+    "pfRectfv": (_V, [_FP] * 2),
+    "pfDrawPixels": (_V, [PFsizei, PFsizei, PFenum_i, PFenum_i, PFptr]),
+    "pfPixelZoom": (_V, [PFfloat] * 2),
+    "pfRasterPos2i": (_V, [PFint] * 2),
+    "pfRasterPos2f": (_V, [PFfloat] * 2),
+    "pfRasterPos2fv": (_V, [_FP]),
+    "pfRasterPos3i": (_V, [PFint] * 3),
+    "pfRasterPos3f": (_V, [PFfloat] * 3),
+    "pfRasterPos3fv": (_V, [_FP]),
+    "pfRasterPos4i": (_V, [PFint] * 4),
+    "pfRasterPos4f": (_V, [PFfloat] * 4),
+    "pfRasterPos4fv": (_V, [_FP]),
+    "pfFogi": (_V, [PFenum_i, PFint]),
+    "pfFogf": (_V, [PFenum_i, PFfloat]),
+    "pfFogiv": (_V, [PFenum_i, C.POINTER(PFint)]),
+    "pfFogfv": (_V, [PFenum_i, _FP]),
+    "pfFogProcess": (_V, []),
+    "pfGenList": (PFptr, []),
+    "pfDeleteList": (_V, [C.POINTER(C.c_void_p)]),
+    "pfNewList": (_V, [PFptr]),
+    "pfEndList": (_V, []),
+    "pfCallList": (_V, [PFptr]),
+    "pfIsValidFramebuffer": (PFbool, [C.POINTER(PFframebuffer)]),
+    "pfSetFramebufferPixelDepthTest": (_V, [C.POINTER(PFframebuffer), PFsizei, PFsizei, PFfloat, PFcolor,
+                                            PFenum_i]),
+    "pfSetFramebufferPixelDepth": (_V, [C.POINTER(PFframebuffer), PFsizei, PFsizei, PFfloat, PFcolor]),
+    "pfSetFramebufferPixel": (_V, [C.POINTER(PFframebuffer), PFsizei, PFsizei, PFcolor]),
+    "pfIsValidTexture": (PFbool, [PFptr]),
+    "pfgbDrawTrianglesStatic": (C.c_int, [PFptr, PFptr, C.c_uint32, PFptr, PFptr, PFptr, C.c_uint32, C.c_uint32,
+                                          C.c_int, C.c_int, PFptr]),
     # extensions (absent from the reference build)
     "pfFinish": (_V, []),
     "pfDepthMask": (_V, [PFbool]),

@@ -1106,6 +1106,43 @@ float replay(Renderer *r, uint32_t n)
 // ===========================================================================
 // C API
 // ===========================================================================
+// Getters (getter.c:24-521): the same cases as the reference; any other
+// name sets PF_INVALID_ENUM and leaves the output untouched.  The raster
+// position and pixel zoom keep their initial values (pfRasterPos* and
+// pfPixelZoom are not supported), context.c:179-180.
+static const float kRasterPos[4] = { 0.0f, 0.0f, 0.0f, 1.0f };
+static const float kPixelZoom[2] = { 1.0f, 1.0f };
+static const double kInv255 = 1.0 / 255;
+
+template <typename T>
+static bool get_real(PFenum p, T *v, T inv255)                           // getter.c:235-491
+{
+    switch (p) {
+    case PF_COLOR_CLEAR_VALUE:
+        v[0] = G->clearColor.r * inv255; v[1] = G->clearColor.g * inv255;
+        v[2] = G->clearColor.b * inv255; v[3] = G->clearColor.a * inv255; return true;
+    case PF_DEPTH_CLEAR_VALUE: v[0] = G->clearDepth; return true;
+    case PF_CURRENT_COLOR:
+        v[0] = G->curColor.r * inv255; v[1] = G->curColor.g * inv255;
+        v[2] = G->curColor.b * inv255; v[3] = G->curColor.a * inv255; return true;
+    case PF_CURRENT_NORMAL: for (int i = 0; i < 3; i++) v[i] = G->curNormal[i]; return true;
+    case PF_CURRENT_TEXTURE_COORDS: for (int i = 0; i < 2; i++) v[i] = G->curTex[i]; return true;
+    case PF_CURRENT_RASTER_POSITION: v[0] = kRasterPos[0]; v[1] = kRasterPos[1]; return true;
+    case PF_POINT_SIZE: v[0] = G->pointSize; return true;
+    case PF_LINE_WIDTH: v[0] = G->lineWidth; return true;
+    case PF_PROJECTION_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->proj[i]; return true;
+    case PF_MODELVIEW_MATRIX: {
+        Mat mv; m_mul(mv, G->model, G->view);
+        for (int i = 0; i < 16; i++) v[i] = mv[i];
+        return true;
+    }
+    case PF_TEXTURE_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->tex[i]; return true;
+    case PF_ZOOM_X: v[0] = kPixelZoom[0]; return true;
+    case PF_ZOOM_Y: v[0] = kPixelZoom[1]; return true;
+    default: G->err = PF_INVALID_ENUM; return false;
+    }
+}
+
 extern "C" {
 
 PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
@@ -1216,25 +1253,32 @@ void pfGetBooleanv(PFenum p, PFboolean *v)                            // getter.
     case PF_NORMALIZE: case PF_LIGHTING: case PF_COLOR_MATERIAL: case PF_VERTEX_ARRAY: case PF_NORMAL_ARRAY:
     case PF_COLOR_ARRAY: case PF_TEXTURE_COORD_ARRAY:
         *v = (G->state & p) != 0; break;
+    case PF_VERTEX_ARRAY_TYPE: *v = G->positions.type != 0; break;
+    case PF_NORMAL_ARRAY_STRIDE: *v = G->normals.stride != 0; break;
+    case PF_NORMAL_ARRAY_TYPE: *v = G->normals.type != 0; break;
+    case PF_TEXTURE_COORD_ARRAY_STRIDE: *v = G->texcoords.stride != 0; break;
+    case PF_TEXTURE_COORD_ARRAY_TYPE: *v = G->texcoords.type != 0; break;
+    case PF_COLOR_ARRAY_SIZE: *v = G->colors.size != 0; break;
+    case PF_COLOR_ARRAY_STRIDE: *v = G->colors.stride != 0; break;
+    case PF_COLOR_ARRAY_TYPE: *v = G->colors.type != 0; break;
     default: G->err = PF_INVALID_ENUM; break;
     }
 }
-void pfGetIntegerv(PFenum p, PFint *v)
+void pfGetIntegerv(PFenum p, PFint *v)                                // getter.c:115-233
 {
     switch (p) {
     case PF_VIEWPORT: v[0] = G->vpPos[0]; v[1] = G->vpPos[1]; v[2] = (PFint)G->vpDim[0] + 1; v[3] = (PFint)G->vpDim[1] + 1; break;
-    case PF_BLEND_FUNC: v[0] = G->blend; break;
-    case PF_DEPTH_FUNC: v[0] = G->depthFunc; break;
+    case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r; v[1] = G->clearColor.g; v[2] = G->clearColor.b; v[3] = G->clearColor.a; break;
     case PF_CULL_FACE_MODE: v[0] = G->cullFace; break;
-    case PF_SHADE_MODEL: v[0] = G->shade; break;
-    case PF_MATRIX_MODE: v[0] = G->matMode; break;
+    case PF_CURRENT_COLOR: v[0] = G->curColor.r; v[1] = G->curColor.g; v[2] = G->curColor.b; v[3] = G->curColor.a; break;
+    case PF_CURRENT_RASTER_POSITION: v[0] = (PFint)kRasterPos[0]; v[1] = (PFint)kRasterPos[1]; break;
     case PF_POLYGON_MODE: v[0] = G->polygonMode[0]; v[1] = G->polygonMode[1]; break;
-    case PF_MAX_LIGHTS: v[0] = PF_MAX_LIGHTS; break;
+    case PF_MATRIX_MODE: v[0] = G->matMode; break;
     case PF_MAX_PROJECTION_STACK_DEPTH: v[0] = 2; break;
     case PF_MAX_MODELVIEW_STACK_DEPTH: v[0] = 8; break;
     case PF_MAX_TEXTURE_STACK_DEPTH: v[0] = 4; break;
-    case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r; v[1] = G->clearColor.g; v[2] = G->clearColor.b; v[3] = G->clearColor.a; break;
-    case PF_CURRENT_COLOR: v[0] = G->curColor.r; v[1] = G->curColor.g; v[2] = G->curColor.b; v[3] = G->curColor.a; break;
+    case PF_SHADE_MODEL: v[0] = G->shade; break;
+    case PF_MAX_LIGHTS: v[0] = PF_MAX_LIGHTS; break;
     case PF_VERTEX_ARRAY_SIZE: v[0] = G->positions.size; break;
     case PF_VERTEX_ARRAY_STRIDE: v[0] = (PFint)G->positions.stride; break;
     case PF_VERTEX_ARRAY_TYPE: v[0] = (PFint)G->positions.type; break;
@@ -1248,36 +1292,16 @@ void pfGetIntegerv(PFenum p, PFint *v)
     default: G->err = PF_INVALID_ENUM; break;
     }
 }
-void pfGetFloatv(PFenum p, PFfloat *v)
-{
-    switch (p) {
-    case PF_DEPTH_CLEAR_VALUE: v[0] = G->clearDepth; break;
-    case PF_POINT_SIZE: v[0] = G->pointSize; break;
-    case PF_LINE_WIDTH: v[0] = G->lineWidth; break;
-    case PF_CURRENT_NORMAL: std::memcpy(v, G->curNormal, 12); break;
-    case PF_CURRENT_TEXTURE_COORDS: std::memcpy(v, G->curTex, 8); break;
-    case PF_PROJECTION_MATRIX: std::memcpy(v, G->proj, 64); break;
-    case PF_MODELVIEW_MATRIX: std::memcpy(v, G->modelUsed ? G->model : G->view, 64); break;
-    case PF_TEXTURE_MATRIX: std::memcpy(v, G->tex, 64); break;
-    default: G->err = PF_INVALID_ENUM; break;
-    }
-}
-void pfGetDoublev(PFenum p, PFdouble *v)
-{
-    float f[16];
-    int n = (p == PF_PROJECTION_MATRIX || p == PF_MODELVIEW_MATRIX || p == PF_TEXTURE_MATRIX) ? 16 :
-            (p == PF_CURRENT_NORMAL) ? 3 : (p == PF_CURRENT_TEXTURE_COORDS) ? 2 : 1;
-    PFerrcode before = G->err; G->err = PF_NO_ERROR;
-    pfGetFloatv(p, f);
-    if (G->err != PF_NO_ERROR) return;
-    G->err = before;
-    for (int i = 0; i < n; i++) v[i] = f[i];
-}
+void pfGetFloatv(PFenum p, PFfloat *v) { get_real<PFfloat>(p, v, (PFfloat)kInv255); }
+void pfGetDoublev(PFenum p, PFdouble *v) { get_real<PFdouble>(p, v, kInv255); }
 void pfGetPointerv(PFenum p, const void **v)                          // getter.c:493-521
 {
     switch (p) {
     case PF_TEXTURE_2D: *v = G->texture; break;
     case PF_FRAMEBUFFER: *v = G->bound; break;
+    // the reference returns the address of its internal function pointer
+    case PF_BLEND_FUNC: *v = &G->blend; break;
+    case PF_DEPTH_FUNC: *v = &G->depthFunc; break;
     default: G->err = PF_INVALID_ENUM; break;
     }
 }

@@ -9,6 +9,7 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
+sys.path.insert(0, str(ROOT / "oracle"))
 
 ORACLE_SO = ROOT / "oracle" / "_build" / "libpfref.so"
 REF_SHIM_SO = ROOT / "oracle" / "_ref" / "libpf_shim.so"

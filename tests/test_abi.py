@@ -1,0 +1,159 @@
+"""The drop-in boundary, without a GPU.
+
+libpixelforge_gb300.so must load on a host without a GPU, export every
+function that include/pixelforge.h and include/pixelforge_grad.h declare,
+and keep the reference's host-side state semantics (errors, matrix stacks,
+getters) -- those run on the host and are compared here with the CPU oracle
+and, where it can be built, the reference.  Rendering calls on a host
+without a device must fail loudly (a device status bit and
+PF_INVALID_OPERATION), never fall back to the CPU.
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from pixelforge_gb300 import LIB_PATH, abi as A, load_library
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared(header: str, macro: str):
+    text = (ROOT / "include" / header).read_text()
+    return sorted(set(re.findall(macro + r"\s+[\w\s\*]+?\b(pf\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return load_library()
+
+
+def test_exports_every_declared_function(lib):
+    names = declared("pixelforge.h", "PF_API") + declared("pixelforge_grad.h", "PFGRAD_API")
+    assert len(names) > 140
+    dll = C.CDLL(str(LIB_PATH))
+    missing = [n for n in names if not hasattr(dll, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_reference_api_is_complete():
+    """Every pf* function of the reference header (as re-declared, with its
+    line citation, in include/pixelforge.h) is bound by the ctypes layer."""
+    text = (ROOT / "include" / "pixelforge.h").read_text()
+    cited = re.findall(r"PF_API[^;]*?\b(pf\w+)\s*\([^;]*;\s*/\* pixelforge\.h:\d+", text, re.S)
+    assert len(cited) >= 120
+    assert not [n for n in cited if n not in A.PROTOTYPES]
+
+
+def _ctx(lib, w=16, h=16):
+    buf = np.zeros((h, w, 4), np.uint8)
+    c = lib.pfCreateContext(buf.ctypes.data_as(C.c_void_p), w, h, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+    assert c
+    lib.pfMakeCurrent(c)
+    return c, buf
+
+
+def state_script(lib):
+    """A sequence of host-side state calls; returns every observable result."""
+    out = []
+    c, buf = _ctx(lib)
+    try:
+        out.append(("err0", lib.pfGetError()))
+        lib.pfMatrixMode(A.PF_PROJECTION)
+        for _ in range(3):
+            lib.pfPushMatrix()
+            out.append(("push", lib.pfGetError()))
+        for _ in range(4):
+            lib.pfPopMatrix()
+            out.append(("pop", lib.pfGetError()))
+        lib.pfMatrixMode(A.PF_MODELVIEW)
+        for _ in range(9):
+            lib.pfPushMatrix()
+        out.append(("mv overflow", lib.pfGetError()))
+        for _ in range(9):
+            lib.pfPopMatrix()
+        out.append(("mv pops", lib.pfGetError()))
+        lib.pfLoadIdentity()
+        lib.pfTranslatef(0.25, -1.5, 3.0)
+        lib.pfRotatef(33.0, 0.3, 0.9, -0.2)
+        lib.pfScalef(1.5, 0.75, 2.0)
+        m = (C.c_float * 16)()
+        lib.pfGetFloatv(A.PF_MODELVIEW_MATRIX, m)
+        out.append(("modelview", [np.float32(x).view(np.uint32).item() for x in m]))
+        lib.pfMatrixMode(A.PF_PROJECTION)
+        lib.pfLoadIdentity()
+        lib.pfFrustum(-0.1, 0.1, -0.075, 0.075, 0.1, 100.0)
+        lib.pfGetFloatv(A.PF_PROJECTION_MATRIX, m)
+        out.append(("frustum", [np.float32(x).view(np.uint32).item() for x in m]))
+        lib.pfLoadIdentity()
+        lib.pfOrtho(-2.0, 3.0, -1.0, 1.5, 0.5, 20.0)
+        lib.pfGetFloatv(A.PF_PROJECTION_MATRIX, m)
+        out.append(("ortho", [np.float32(x).view(np.uint32).item() for x in m]))
+        lib.pfViewport(2, 3, 10, 9)
+        v = (C.c_int32 * 4)()
+        lib.pfGetIntegerv(A.PF_VIEWPORT, v)
+        out.append(("viewport", list(v)))
+        lib.pfEnable(A.PF_BLEND | A.PF_DEPTH_TEST)
+        lib.pfDisable(A.PF_CULL_FACE)
+        out.append(("enabled", [bool(lib.pfIsEnabled(s)) for s in
+                                (A.PF_BLEND, A.PF_DEPTH_TEST, A.PF_CULL_FACE, A.PF_TEXTURE_2D, A.PF_LIGHTING)]))
+        lib.pfBlendFunc(A.PF_BLEND_ADD)
+        lib.pfDepthFunc(A.PF_GREATER)
+        lib.pfClearDepth(0.5)
+        f = (C.c_float * 4)()
+        lib.pfGetFloatv(A.PF_DEPTH_CLEAR_VALUE, f)
+        out.append(("clear depth", f[0]))
+        lib.pfGetIntegerv(A.PF_DEPTH_FUNC, v)
+        out.append(("depth func", v[0]))
+        lib.pfGetIntegerv(A.PF_BLEND_FUNC, v)
+        out.append(("blend func", v[0]))
+        out.append(("err end", lib.pfGetError()))
+        lib.pfMatrixMode(12345)
+        out.append(("bad matrix mode", lib.pfGetError()))
+        out.append(("error reset", lib.pfGetError()))
+    finally:
+        lib.pfDeleteContext(c)
+    return out
+
+
+def test_host_state_matches_oracle(lib, oracle):
+    got, ref = state_script(lib), state_script(oracle)
+    for g, r in zip(got, ref):
+        assert g == r, f"{g[0]}: {g[1]} vs oracle {r[1]}"
+
+
+def test_host_state_matches_reference(lib, ref_shim):
+    got, ref = state_script(lib), state_script(ref_shim)
+    for g, r in zip(got, ref):
+        assert g == r, f"{g[0]}: {g[1]} vs reference {r[1]}"
+
+
+def test_no_device_fails_loudly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    c, buf = _ctx(lib)
+    try:
+        lib.pfBegin(A.PF_TRIANGLES)
+        lib.pfVertex2f(0.0, 0.0)
+        lib.pfVertex2f(1.0, 0.0)
+        lib.pfVertex2f(0.0, 1.0)
+        lib.pfEnd()
+        lib.pfFinish()
+        assert lib.pfGetDeviceStatus() != 0
+        assert lib.pfGetError() == A.PF_INVALID_OPERATION
+    finally:
+        lib.pfDeleteContext(c)
+
+
+def test_static_entry_rejects_oversize_without_device(lib):
+    f = lib.raw("pfgbDrawTrianglesStatic")
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                  C.c_uint32, C.c_int, C.c_int, C.c_void_p]
+    dummy = C.c_void_p(16)
+    assert f(dummy, dummy, 8193, dummy, dummy, dummy, 64, 64, 0, 0, None) == -1    # too many triangles
+    assert f(dummy, dummy, 1, dummy, dummy, dummy, 513, 64, 0, 0, None) == -1      # too wide
+    assert f(None, dummy, 1, dummy, dummy, dummy, 64, 64, 0, 0, None) == -2        # no positions
