@@ -191,7 +191,69 @@ def run_gpu(args):
     tg.close()
     if not args.no_batched:
         out["batched"] = run_batched(lib)
+    if not args.no_adjoint:
+        out["adjoint"] = run_adjoint(args)
     return out
+
+
+def run_adjoint(args) -> dict:
+    """One fitting iteration of the fit64 workload: forward (render 64 views
+    + loss) and forward + adjoint, timed with CUDA events on torch's stream,
+    on which the pfgrad calls run."""
+    import torch
+    from pixelforge_gb300.fit import FitScene, to_device
+
+    fs = FitScene()
+    sc = fs.build()
+    with torch.no_grad():
+        target = sc.render(*to_device(fs.truth(), requires_grad=False))
+    params = to_device(fs.initial())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def fwd():
+        img = sc.render(*params)
+        return ((img - target) ** 2).mean()
+
+    for _ in range(3):
+        for p in params:
+            p.grad = None
+        fwd().backward()
+    torch.cuda.synchronize()
+    n = max(args.steps, 5)
+    f_ms = b_ms = k_fwd = k_bwd = 0.0
+    for _ in range(n):
+        for p in params:
+            p.grad = None
+        ev[0].record()
+        loss = fwd()
+        ev[1].record()
+        loss.backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        f_ms += ev[0].elapsed_time(ev[1])
+        b_ms += ev[0].elapsed_time(ev[2])
+    # the two pfgrad kernels sequences alone
+    img = torch.empty(sc.image_shape(), device="cuda")
+    grads = [torch.empty_like(p) for p in params]
+    ts = [p.detach() for p in params]
+    dimg = torch.empty_like(img).fill_(1e-6)
+    for _ in range(n):
+        ev[0].record()
+        sc.forward_raw(ts, img)
+        ev[1].record()
+        sc.backward_raw(ts, dimg, grads)
+        ev[2].record()
+        torch.cuda.synchronize()
+        k_fwd += ev[0].elapsed_time(ev[1])
+        k_bwd += ev[1].elapsed_time(ev[2])
+    info = sc.info()
+    sc.close()
+    return {"workload": "fit64: icosphere subdiv 5 (20,480 triangles), 64 views of 512x512, 512^2 RGBA float "
+                        "texture, bilinear repeat, Gouraud Blinn-Phong, alpha-over, MSE loss",
+            "forward_ms": f_ms / n, "forward_adjoint_ms": b_ms / n, "ratio": b_ms / f_ms,
+            "pfgrad_forward_ms": k_fwd / n, "pfgrad_backward_ms": k_bwd / n,
+            "views_per_s_forward": fs.n_views / (f_ms / n / 1e3),
+            "tile_entries": info["tileEntries"], "primitives": info["primitives"], "iterations": n}
 
 
 def run_batched(lib) -> dict:
@@ -310,6 +372,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-context batch measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the fitting-iteration measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -16,10 +16,11 @@
 //                     reference, then float shading and alpha-over in item order
 //   k_gadjoint        one CTA per tile: replays the tile to find, per pixel, its
 //                     visible fragments and the colour under each, then walks
-//                     them back to front, scattering texel gradients (warp-
-//                     aggregated vector atomics) and vertex-colour gradients
-//                     (shared-memory accumulation per tile)
-//   k_glight_adjoint  one thread per vertex, over all views: back through the
+//                     them back to front, scattering texel gradients (vector
+//                     atomics, pairs of adjacent lanes on one texel combined
+//                     first) and vertex-colour gradients (shared-memory
+//                     accumulation per tile)
+//   k_glight_adjoint  one thread per (vertex, 8 views): back through the
 //                     Gouraud Blinn-Phong formula; scalar gradients reduced per CTA
 //   k_gfinish         light-direction normalisation adjoint
 //
@@ -41,7 +42,7 @@ namespace {
 
 constexpr int GTILE = 16;
 constexpr int GTHREADS = GTILE * GTILE;
-constexpr int GCH = 32;            // triangles staged per chunk
+constexpr int GCH = 32;            // triangles staged per chunk (adjoint)
 constexpr int RING = 4;            // visible fragments walked back per pixel per replay
 constexpr int NACC = 256;          // tile lists up to this length accumulate vertex gradients in shared memory
 constexpr uint32_t GP_VALID = 1u << 31;
@@ -426,6 +427,55 @@ struct RasterArgsG {
     float4 *dLit;                  // nViews x nv
 };
 
+__device__ __forceinline__ GPrim load_prim(const RasterArgsG &a, uint32_t i)
+{
+    GPrim P;
+    const int4 *src = reinterpret_cast<const int4 *>(a.prims + __ldg(a.list + i));
+    int4 *dst = reinterpret_cast<int4 *>(&P);
+    for (int w = 0; w < 6; w++) dst[w] = __ldg(src + w);
+    return P;
+}
+
+// A warp covers two pixel rows of its tile (y0, y0 + 1); triangles whose
+// rows [yMin, yMax] miss both are skipped by the whole warp.
+__device__ __forceinline__ bool misses_rows(const GPrim &P, uint32_t y0)
+{
+    return (uint32_t)P.yMin > y0 + 1 || (uint32_t)P.yMax < y0;
+}
+
+// Each warp walks the tile's list on its own (the list is read through L1,
+// the same addresses for all lanes): no block-wide barriers.
+__global__ void __launch_bounds__(GTHREADS) k_gforward(RasterArgsG a)
+{
+    const uint32_t gt = blockIdx.x;
+    const uint32_t view = gt / a.V.tilesPerView, tile = gt % a.V.tilesPerView;
+    const uint32_t px = (tile % a.V.tilesX) * GTILE + threadIdx.x % GTILE;
+    const uint32_t py = (tile / a.V.tilesX) * GTILE + threadIdx.x / GTILE;
+    const uint32_t y0 = py & ~1u;
+    const bool inside = px < a.V.W && py < a.V.H;
+    const float4 *lit = a.lit + (size_t)view * a.V.nv;
+    float C[3] = { a.V.bg[0], a.V.bg[1], a.V.bg[2] };
+    float D = a.V.clearDepth;
+    const uint32_t beg = a.off[gt], n = a.off[gt + 1] - beg;
+    for (uint32_t k = 0; k < n; k++) {
+        const GPrim P = load_prim(a, beg + k);
+        if (misses_rows(P, y0) || !inside) continue;
+        FragIn f;
+        if (!cover(P, px, py, f)) continue;
+        if (!(f.z < D)) continue;                  // PF_LESS, depth written
+        D = f.z;
+        Shade s;
+        shade(P, f, lit, a.T, s);
+        for (int c = 0; c < 3; c++) C[c] = s.a * s.src[c] + (1.0f - s.a) * C[c];
+    }
+    if (inside) {
+        float *o = a.image + (((size_t)view * a.V.H + py) * a.V.W + px) * 3;
+        o[0] = C[0]; o[1] = C[1]; o[2] = C[2];
+    }
+}
+
+__device__ __forceinline__ void add4(float4 *p, float4 v) { atomicAdd(p, v); }
+
 __device__ __forceinline__ void stage_chunk(const RasterArgsG &a, uint32_t beg, uint32_t c0, uint32_t cn, GPrim *sp)
 {
     for (uint32_t w = threadIdx.x; w < cn * 6; w += GTHREADS) {
@@ -434,58 +484,6 @@ __device__ __forceinline__ void stage_chunk(const RasterArgsG &a, uint32_t beg, 
         reinterpret_cast<int4 *>(&sp[k])[part] = __ldg(reinterpret_cast<const int4 *>(a.prims + pi) + part);
     }
 }
-
-__global__ void __launch_bounds__(GTHREADS) k_gforward(RasterArgsG a)
-{
-    __shared__ GPrim sp[GCH];
-    const uint32_t gt = blockIdx.x;
-    const uint32_t view = gt / a.V.tilesPerView, tile = gt % a.V.tilesPerView;
-    const uint32_t px = (tile % a.V.tilesX) * GTILE + threadIdx.x % GTILE;
-    const uint32_t py = (tile / a.V.tilesX) * GTILE + threadIdx.x / GTILE;
-    const bool inside = px < a.V.W && py < a.V.H;
-    const float4 *lit = a.lit + (size_t)view * a.V.nv;
-    float C[3] = { a.V.bg[0], a.V.bg[1], a.V.bg[2] };
-    float D = a.V.clearDepth;
-    const uint32_t beg = a.off[gt], n = a.off[gt + 1] - beg;
-    for (uint32_t c0 = 0; c0 < n; c0 += GCH) {
-        const uint32_t cn = min((uint32_t)GCH, n - c0);
-        __syncthreads();
-        stage_chunk(a, beg, c0, cn, sp);
-        __syncthreads();
-        if (!inside) continue;
-        for (uint32_t k = 0; k < cn; k++) {
-            FragIn f;
-            if (!cover(sp[k], px, py, f)) continue;
-            if (!(f.z < D)) continue;                  // PF_LESS, depth written
-            D = f.z;
-            Shade s;
-            shade(sp[k], f, lit, a.T, s);
-            for (int c = 0; c < 3; c++) C[c] = s.a * s.src[c] + (1.0f - s.a) * C[c];
-        }
-    }
-    if (inside) {
-        float *o = a.image + (((size_t)view * a.V.H + py) * a.V.W + px) * 3;
-        o[0] = C[0]; o[1] = C[1]; o[2] = C[2];
-    }
-}
-
-// Sum of v over the lanes of `peers` (which holds the calling lane), in the
-// lowest lane of the group; every lane of the warp calls it.
-__device__ __forceinline__ float4 peer_sum(uint32_t peers, float4 v)
-{
-    const int lane = threadIdx.x & 31;
-    float4 s = v;
-    uint32_t rest = (lane == __ffs(peers) - 1) ? (peers & ~(1u << lane)) : 0u;
-    while (__any_sync(0xffffffffu, rest != 0)) {
-        const int src = rest ? __ffs(rest) - 1 : lane;
-        const float x = __shfl_sync(0xffffffffu, v.x, src), y = __shfl_sync(0xffffffffu, v.y, src);
-        const float z = __shfl_sync(0xffffffffu, v.z, src), w = __shfl_sync(0xffffffffu, v.w, src);
-        if (rest) { s.x += x; s.y += y; s.z += z; s.w += w; rest &= rest - 1; }
-    }
-    return s;
-}
-
-__device__ __forceinline__ void add4(float4 *p, float4 v) { atomicAdd(p, v); }
 
 __global__ void __launch_bounds__(GTHREADS) k_gadjoint(RasterArgsG a)
 {
@@ -570,19 +568,35 @@ __global__ void __launch_bounds__(GTHREADS) k_gadjoint(RasterArgsG a)
             for (int k = 0; k < ntap; k++) {
                 const int32_t off = act ? s.tp.off[k] : -1;
                 const float w = act ? s.tp.w[k] : 0.0f;
-                const uint32_t peers = __match_any_sync(0xffffffffu, (uint32_t)off);
-                const float4 sum = peer_sum(peers, make_float4(dt.x * w, dt.y * w, dt.z * w, dt.w * w));
-                if (off >= 0 && lane == __ffs(peers) - 1) add4(a.dTex + off, sum);
+                const float4 v = make_float4(dt.x * w, dt.y * w, dt.z * w, dt.w * w);
+                // horizontally adjacent pixels (lanes 2i, 2i+1) that read the
+                // same texel send one atomic
+                const int32_t po = __shfl_xor_sync(0xffffffffu, off, 1);
+                const float4 pv = make_float4(__shfl_xor_sync(0xffffffffu, v.x, 1), __shfl_xor_sync(0xffffffffu, v.y, 1),
+                                              __shfl_xor_sync(0xffffffffu, v.z, 1), __shfl_xor_sync(0xffffffffu, v.w, 1));
+                if (off >= 0) {
+                    if (po != off) add4(a.dTex + off, v);
+                    else if ((lane & 1) == 0) add4(a.dTex + off, make_float4(v.x + pv.x, v.y + pv.y, v.z + pv.z, v.w + pv.w));
+                }
             }
             if (act) {
-                for (int m = 0; m < 3; m++) {
-                    const float w = f.wn[m];
-                    const float4 d = make_float4(dc[0] * w, dc[1] * w, dc[2] * w, dc[3] * w);
-                    if (useAcc) {
-                        float *acc = &sacc[q][4 * m];
-                        atomicAdd(acc, d.x); atomicAdd(acc + 1, d.y); atomicAdd(acc + 2, d.z); atomicAdd(acc + 3, d.w);
-                    } else {
-                        add4(dLit + P.v[m], d);
+                if (useAcc) {
+                    // the 12 accumulators of list position q in an order
+                    // rotated by lane, so that neighbouring lanes of the same
+                    // triangle add to different words in each step
+                    const uint32_t r = (uint32_t)lane % 12u;
+                    for (uint32_t i = 0; i < 12; i++) {
+                        uint32_t sl = i + r;
+                        sl = sl >= 12u ? sl - 12u : sl;
+                        const uint32_t m = sl >> 2, c = sl & 3u;
+                        const float w = m == 0 ? f.wn[0] : (m == 1 ? f.wn[1] : f.wn[2]);
+                        const float d = c == 0 ? dc[0] : (c == 1 ? dc[1] : (c == 2 ? dc[2] : dc[3]));
+                        atomicAdd(&sacc[q][sl], d * w);
+                    }
+                } else {
+                    for (int m = 0; m < 3; m++) {
+                        const float w = f.wn[m];
+                        add4(dLit + P.v[m], make_float4(dc[0] * w, dc[1] * w, dc[2] * w, dc[3] * w));
                     }
                 }
             }
@@ -606,19 +620,28 @@ __global__ void __launch_bounds__(GTHREADS) k_gadjoint(RasterArgsG a)
 // ---------------------------------------------------------------------------
 // vertex adjoint
 // ---------------------------------------------------------------------------
-// acc: [0] d diffuse, [1] d specular, [2] d shininess, [3..5] d L (unit light direction)
+// One thread per (vertex, group of GVIEWS views).  Per-vertex gradients are
+// added into dCol/dAlpha (zeroed first); acc: [0] d diffuse, [1] d specular,
+// [2] d shininess, [3..5] d L (unit light direction), reduced per CTA.
+constexpr uint32_t GVIEWS = 8;
+
 __global__ void __launch_bounds__(256) k_glight_adjoint(LightArgs a, const float4 *dLit, float *dCol, float *dAlpha,
                                                          float *acc)
 {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t groups = (a.nViews + GVIEWS - 1) / GVIEWS;
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = g < (uint64_t)a.nv * groups;
+    const uint32_t v = valid ? (uint32_t)(g % a.nv) : 0u;
+    const uint32_t v0 = valid ? (uint32_t)(g / a.nv) * GVIEWS : a.nViews;
     float L[3], llen;
     light_dir(a.light, L, llen);
     const float kd = a.material[0], ks = a.material[1], shin = a.material[2];
     float part[6] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
-    if (v < a.nv) {
+    if (valid) {
         const float C[3] = { a.col[3 * (size_t)v], a.col[3 * (size_t)v + 1], a.col[3 * (size_t)v + 2] };
         float dC[3] = { 0.f, 0.f, 0.f }, dA = 0.0f;
-        for (uint32_t view = 0; view < a.nViews; view++) {
+        const uint32_t vEnd = min(v0 + GVIEWS, a.nViews);
+        for (uint32_t view = v0; view < vEnd; view++) {
             const float4 g4 = dLit[(size_t)view * a.nv + v];
             dA += g4.w;
             if (g4.x == 0.0f && g4.y == 0.0f && g4.z == 0.0f) continue;
@@ -648,8 +671,13 @@ __global__ void __launch_bounds__(256) k_glight_adjoint(LightArgs a, const float
                 for (int i = 0; i < 3; i++) part[3 + i] += (gH[i] - t.H[i] * hg) / t.hlen;
             }
         }
-        for (int c = 0; c < 3; c++) dCol[3 * (size_t)v + c] = dC[c];
-        dAlpha[v] = dA;
+        if (groups == 1) {
+            for (int c = 0; c < 3; c++) dCol[3 * (size_t)v + c] = dC[c];
+            dAlpha[v] = dA;
+        } else {
+            for (int c = 0; c < 3; c++) if (dC[c] != 0.0f) atomicAdd(&dCol[3 * (size_t)v + c], dC[c]);
+            if (dA != 0.0f) atomicAdd(&dAlpha[v], dA);
+        }
     }
     __shared__ float red[8][6];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -863,7 +891,9 @@ extern "C" int pfgradBackward(PFgradScene s, const PFgradParams *p, const float 
     const size_t nv = s->desc.nVertices, nV = s->desc.nViews;
     if (cudaMemsetAsync(g->texture, 0, (size_t)s->desc.texWidth * s->desc.texHeight * sizeof(float4), st) != cudaSuccess ||
         cudaMemsetAsync(s->dLit, 0, nv * nV * sizeof(float4), st) != cudaSuccess ||
-        cudaMemsetAsync(s->acc, 0, 8 * sizeof(float), st) != cudaSuccess) {
+        cudaMemsetAsync(s->acc, 0, 8 * sizeof(float), st) != cudaSuccess ||
+        cudaMemsetAsync(g->colors, 0, nv * 3 * sizeof(float), st) != cudaSuccess ||
+        cudaMemsetAsync(g->alphas, 0, nv * sizeof(float), st) != cudaSuccess) {
         cudaGetLastError();
         return PFGRAD_ERR_CUDA;
     }
@@ -874,7 +904,8 @@ extern "C" int pfgradBackward(PFgradScene s, const PFgradParams *p, const float 
     ra.dTex = reinterpret_cast<float4 *>(g->texture);
     ra.dLit = s->dLit;
     k_gadjoint<<<s->nTiles, GTHREADS, 0, st>>>(ra);
-    k_glight_adjoint<<<blocks(nv, 256), 256, 0, st>>>(la, s->dLit, g->colors, g->alphas, s->acc);
+    const uint64_t groups = (nV + GVIEWS - 1) / GVIEWS;
+    k_glight_adjoint<<<blocks(nv * groups, 256), 256, 0, st>>>(la, s->dLit, g->colors, g->alphas, s->acc);
     k_gfinish<<<1, 1, 0, st>>>(p->light, s->acc, g->material, g->light);
     if (cudaGetLastError() != cudaSuccess) return PFGRAD_ERR_CUDA;
     return 0;

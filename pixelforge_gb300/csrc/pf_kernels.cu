@@ -824,7 +824,46 @@ struct ChunkPrim {             // per-sub-triangle data derived for this tile
     uint32_t bx0, by0, bw, bh; // bounding box clipped to the tile (tile-relative)
     float invBw;
     uint32_t flags;            // face | is3D | state << 8
+    uint32_t rstate;           // the state's PFS_* flags | depth function << 16 | blend mode << 24
 };
+
+// Exclusive offsets of each lane's count within the warp (wo[0..31]) and
+// the warp total (wo[32]).
+__device__ __forceinline__ void warp_offsets(uint32_t cnt, uint32_t *wo, uint32_t &myOff, uint32_t &total)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t s = cnt;
+    for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
+    __syncwarp();                                      // previous readers of wo are done
+    myOff = s - cnt;
+    wo[lane] = myOff;
+    if (lane == 31) wo[32] = s;
+    __syncwarp();
+    total = wo[32];
+}
+
+// Owner lane of the f-th fragment of a warp's compacted list and its chunk
+// sub-triangle (the owner's n-th set mask bit).
+__device__ __forceinline__ void frag_owner(const uint32_t *wo, const uint32_t *masks, uint32_t f, int &lo, uint32_t &k)
+{
+    int l = 0, h = 31;                                 // largest L with wo[L] <= f
+    while (l < h) { int mid = (l + h + 1) >> 1; if (wo[mid] <= f) l = mid; else h = mid - 1; }
+    lo = l;
+    k = __fns(masks[l], 0, (int)(f - wo[l]) + 1) & (CH - 1);
+}
+
+// Weights and depth of a covered fragment at tile pixel p (triangles.c:426-438).
+__device__ __forceinline__ float frag_depth(const PFPrim &P, const ChunkPrim &cp, uint32_t p, float *wn)
+{
+    const uint32_t X = p % PF_TILE, Y = p / PF_TILE;
+    const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + X * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0]);
+    const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + X * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1]);
+    const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + X * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2]);
+    wn[0] = (float)w1 * P.wInvSum; wn[1] = (float)w2 * P.wInvSum; wn[2] = (float)w3 * P.wInvSum;
+    float zs = P.z1 * wn[0] + P.z2 * wn[1];
+    zs = zs + P.z3 * wn[2];
+    return 1.0f / zs;
+}
 
 // Source colour of one fragment (triangles.c:500-521): colour interpolation,
 // texturing, per-fragment lighting.  Independent of the destination pixel.
@@ -879,6 +918,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ float fz[RASTER_THREADS / 32][FWIN];
     __shared__ uint32_t woff[RASTER_THREADS / 32][33];
     __shared__ int sHasPhong;
+    __shared__ int sDense;
 
     if (a.cnt->abortCommand <= a.command) return;
     // the batch completed set-up without overflow: its sub-triangles count
@@ -991,16 +1031,23 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 cp.bx0 = empty ? 0 : x0 - ox; cp.by0 = empty ? 0 : y0 - oy;
                 cp.bw = empty ? 0 : x1 - x0; cp.bh = empty ? 0 : y1e - y0;
                 cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
+                const PFDrawState &St = a.states[P.flags >> 8];
+                cp.rstate = (St.flags & 0xffffu) | ((uint32_t)St.depthFunc << 16) | ((uint32_t)St.blendMode << 24);
                 scp[tid] = cp;
-                if (a.states[P.flags >> 8].flags & PFS_PHONG) sHasPhong = 1;
+                if (St.flags & PFS_PHONG) sHasPhong = 1;
             }
             __syncthreads();
-            if (tid < 32) {                                   // prefix of clipped box rows
+            if (tid < 32) {                                   // prefix of clipped box rows; box area
                 uint32_t v = (tid < cn && scp[tid].bw) ? scp[tid].bh : 0;
                 uint32_t s = v;
                 for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
                 sarea[tid + 1] = s;
                 if (tid == 0) sarea[0] = 0;
+                uint32_t ar = (tid < cn) ? scp[tid].bw * scp[tid].bh : 0;
+                for (int o = 16; o > 0; o >>= 1) ar += __shfl_xor_sync(0xffffffffu, ar, o);
+                // boxes that cover half a tile on average: test every
+                // (pixel, sub-triangle) pair instead of stepping rows
+                if (tid == 0) sDense = ar > cn * (PF_TILE_PIXELS / 2);
             }
             if (sHasPhong) {
                 for (uint32_t w = tid; w < cn * 5; w += RASTER_THREADS) {
@@ -1013,74 +1060,117 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 }
             }
             __syncthreads();
-            // 2. coverage: one work item per (sub-triangle, row of its clipped
-            //    box); edge functions stepped along the row
-            const uint32_t total = sarea[CH];
-            for (uint32_t t = tid; t < total; t += RASTER_THREADS) {
-                int lo = 0, hi = CH - 1;                          // largest k with sarea[k] <= t
-                while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
-                const ChunkPrim &cp = scp[lo];
-                const uint32_t Y = cp.by0 + (t - sarea[lo]);
-                const uint32_t bit = 1u << lo;
-                uint32_t w1 = (uint32_t)cp.e0[0] + cp.bx0 * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0];
-                uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
-                uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
-                uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
-                for (uint32_t dx = 0; dx < cp.bw; dx++) {
-                    if ((int32_t)(w1 | w2 | w3) > 0) atomicOr(row + dx, bit);
-                    w1 += (uint32_t)cp.ex[0]; w2 += (uint32_t)cp.ex[1]; w3 += (uint32_t)cp.ex[2];
-                }
-            }
-            __syncthreads();
-            // 3+4. per warp: compact, shade densely, resolve in order
-            const uint32_t m = pmask[tid];
-            const uint32_t cntp = __popc(m);
-            frags += cntp;
-            uint32_t s = cntp;
-            for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
-            const uint32_t myOff = s - cntp;
-            woff[warp][lane] = myOff;
-            if (lane == 31) woff[warp][32] = s;
-            __syncwarp();
-            const uint32_t wtotal = woff[warp][32];
-            for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
-                const uint32_t bEnd = min(wtotal, b0 + FWIN);
-                for (uint32_t f = b0 + lane; f < bEnd; f += 32) {
-                    int lo = 0, hi = 31;                      // owner lane: largest L with woff[L] <= f
-                    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (woff[warp][mid] <= f) lo = mid; else hi = mid - 1; }
-                    const uint32_t om = pmask[warp * 32 + lo];
-                    const uint32_t k = __fns(om, 0, (int)(f - woff[warp][lo]) + 1) & (CH - 1);
-                    const PFPrim &P = sprim[k];
+            uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
+            if (sDense) {
+                // 2+3 (large sub-triangles). Each thread walks the chunk in
+                //    submission order at its own pixel: coverage, depth, test.
+                uint32_t cov = 0;
+                for (uint32_t k = 0; k < cn; k++) {
                     const ChunkPrim &cp = scp[k];
-                    const uint32_t X = (uint32_t)((warp * 32 + lo) % PF_TILE), Y = (uint32_t)((warp * 32 + lo) / PF_TILE);
-                    const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + X * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0]);
-                    const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + X * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1]);
-                    const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + X * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2]);
+                    if (lx - cp.bx0 >= cp.bw || ly - cp.by0 >= cp.bh) continue;
+                    const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + lx * (uint32_t)cp.ex[0] + ly * (uint32_t)cp.ey[0]);
+                    const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + lx * (uint32_t)cp.ex[1] + ly * (uint32_t)cp.ey[1]);
+                    const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + lx * (uint32_t)cp.ex[2] + ly * (uint32_t)cp.ey[2]);
+                    if (!((w1 | w2 | w3) > 0)) continue;
+                    cov++;
+                    const PFPrim &P = sprim[k];
                     const float wn1 = (float)w1 * P.wInvSum, wn2 = (float)w2 * P.wInvSum, wn3 = (float)w3 * P.wInvSum;
                     float zs = P.z1 * wn1 + P.z2 * wn2;
                     zs = zs + P.z3 * wn3;
                     const float z = 1.0f / zs;
-                    const PFDrawState &S = a.states[P.flags >> 8];
-                    fcol[warp][f - b0] = shade_fragment(P, &sph[k], S, wn1, wn2, wn3, z);
-                    fz[warp][f - b0] = z;
+                    const uint32_t rs = cp.rstate;
+                    if (!(rs & PFS_DEPTH_TEST) || depth_simd((int)((rs >> 16) & 255u), z, dep)) {
+                        vis |= 1u << k;
+                        if (rs & PFS_DEPTH_MASK) dep = z;
+                    }
+                }
+                frags += cov;
+            } else {
+                // 2. coverage: one work item per (sub-triangle, row of its clipped
+                //    box); edge functions stepped along the row
+                const uint32_t total = sarea[CH];
+                for (uint32_t t = tid; t < total; t += RASTER_THREADS) {
+                    int lo = 0, hi = CH - 1;                          // largest k with sarea[k] <= t
+                    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
+                    const ChunkPrim &cp = scp[lo];
+                    const uint32_t Y = cp.by0 + (t - sarea[lo]);
+                    const uint32_t bit = 1u << lo;
+                    uint32_t w1 = (uint32_t)cp.e0[0] + cp.bx0 * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0];
+                    uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
+                    uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
+                    uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
+                    for (uint32_t dx = 0; dx < cp.bw; dx++) {
+                        if ((int32_t)(w1 | w2 | w3) > 0) atomicOr(row + dx, bit);
+                        w1 += (uint32_t)cp.ex[0]; w2 += (uint32_t)cp.ex[1]; w3 += (uint32_t)cp.ex[2];
+                    }
+                }
+                __syncthreads();
+                // 3. per warp, depth first: the depth of every covered fragment
+                //    (dense over the warp), then each pixel's depth tests in
+                //    submission order, which leave the set of visible fragments
+                const uint32_t m = pmask[tid];
+                const uint32_t cntp = __popc(m);
+                frags += cntp;
+                uint32_t myOff, wtotal;
+                warp_offsets(cntp, woff[warp], myOff, wtotal);
+                for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
+                    const uint32_t bEnd = min(wtotal, b0 + FWIN);
+                    for (uint32_t f = b0 + lane; f < bEnd; f += 32) {
+                        int lo; uint32_t k;
+                        frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
+                        float wn[3];
+                        fz[warp][f - b0] = frag_depth(sprim[k], scp[k], (uint32_t)(warp * 32 + lo), wn);
+                    }
+                    __syncwarp();
+                    if (cntp) {
+                        uint32_t f = myOff, mm = m;
+                        while (mm) {
+                            const uint32_t k = __ffs(mm) - 1;
+                            mm &= mm - 1;
+                            if (f >= bEnd) break;
+                            if (f >= b0) {
+                                const uint32_t rs = scp[k].rstate;
+                                const float z = fz[warp][f - b0];
+                                if (!(rs & PFS_DEPTH_TEST) || depth_simd((int)((rs >> 16) & 255u), z, dep)) {
+                                    vis |= 1u << k;
+                                    if (rs & PFS_DEPTH_MASK) dep = z;
+                                }
+                            }
+                            f++;
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            // 4. shade the visible fragments (dense over the warp) and blend
+            //    them in submission order
+            __syncwarp();
+            pmask[tid] = vis;
+            const uint32_t cntv = __popc(vis);
+            uint32_t myOff, wtotal;
+            warp_offsets(cntv, woff[warp], myOff, wtotal);
+            for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
+                const uint32_t bEnd = min(wtotal, b0 + FWIN);
+                for (uint32_t f = b0 + lane; f < bEnd; f += 32) {
+                    int lo; uint32_t k;
+                    frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
+                    float wn[3];
+                    const PFPrim &P = sprim[k];
+                    const float z = frag_depth(P, scp[k], (uint32_t)(warp * 32 + lo), wn);
+                    fcol[warp][f - b0] = shade_fragment(P, &sph[k], a.states[P.flags >> 8], wn[0], wn[1], wn[2], z);
                 }
                 __syncwarp();
-                // resolve this window's fragments of my pixel, in submission order
-                if (cntp) {
-                    uint32_t f = myOff, mm = m;
+                if (cntv) {
+                    uint32_t f = myOff, mm = vis;
                     while (mm) {
                         const uint32_t k = __ffs(mm) - 1;
                         mm &= mm - 1;
-                        if (f >= b0 && f < bEnd) {
-                            const PFDrawState &S = a.states[scp[k].flags >> 8];
-                            const uint32_t fl = S.flags;
-                            const float z = fz[warp][f - b0];
-                            if (!(fl & PFS_DEPTH_TEST) || depth_simd(S.depthFunc, z, dep)) {
-                                uint32_t frag = fcol[warp][f - b0];
-                                if (fl & PFS_BLEND) frag = blend_simd(S.blendMode, frag, col);
-                                col = frag;
-                                if (fl & PFS_DEPTH_MASK) dep = z;
-                            }
+                        if (f >= bEnd) break;
+                        if (f >= b0) {
+                            const uint32_t rs = scp[k].rstate;
+                            uint32_t frag = fcol[warp][f - b0];
+                            if (rs & PFS_BLEND) frag = blend_simd((int)(rs >> 24), frag, col);
+                            col = frag;
                         }
                         f++;
                     }
