@@ -364,7 +364,10 @@ class PhongScene:
         self.nrm = v.astype(np.float32)
         u = 0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi)
         w = np.arccos(np.clip(v[:, 1], -1, 1)) / np.pi
-        self.uv = (np.stack([u, w], 1) * 2.0).astype(np.float32)
+        # scaled by 1.9 rather than 2 so that no vertex sits exactly on the
+        # mirrored edge (coordinate 1.0), where the reference's nearest map
+        # rounds to texel w and reads past its texture
+        self.uv = (np.stack([u, w], 1) * 1.9).astype(np.float32)
         add = rng.random(len(f)) < self.add_frac
         self.idx_opaque = f[~add].astype(np.uint32).ravel()
         self.idx_add = f[add].astype(np.uint32).ravel()

@@ -105,3 +105,32 @@ def test_bin_overflow_replay(gpu, oracle):
     sc = SoupScene(ntris=3000, xy_range=(-6.0, 6.0), cull=False, width=64, height=64)
     got, ref = sc.render(gpu), sc.render(oracle)
     assert_parity(got, ref, exact_color=True, label="overflow")
+
+
+# --- against the reference's own outputs (tests/golden) ----------------------
+def _golden():
+    import sys
+    from pathlib import Path
+    here = Path(__file__).resolve().parent / "golden"
+    sys.path.insert(0, str(here))
+    from cases import cases, uses_host_powf
+    return np.load(here / "golden.npz"), cases(), uses_host_powf
+
+
+GOLD, GOLD_CASES, GOLD_POWF = _golden()
+
+
+@pytest.mark.parametrize("name", sorted(GOLD_CASES))
+def test_gpu_matches_reference_golden(gpu, name):
+    """Colour and depth of the GPU library against the reference build's
+    (exact-reciprocal flavour) on every golden case: depth bit-exact, colour
+    bit-exact except the Gouraud specular powf cases (±1 LSB)."""
+    fr = GOLD_CASES[name](gpu)
+    assert gpu.pfGetDeviceStatus() == 0
+    gc, gd = GOLD[f"{name}.color"], GOLD[f"{name}.depth"]
+    if gd.size:
+        nd = int((fr.depth.view(np.uint32) != gd.view(np.uint32)).sum())
+        assert nd == 0, f"{name}: {nd} depth values differ from the reference"
+    diff = np.abs(fr.color.astype(np.int32) - gc.astype(np.int32))
+    tol = COLOR_TOL if GOLD_POWF(name) else 0
+    assert int(diff.max()) <= tol, f"{name}: colour differs by {int(diff.max())}"
