@@ -35,6 +35,7 @@ struct PFBatchLaunch {
     int nTargets;
     uint32_t totalTiles;
     int rasterCtasPerSM;      /* persistent raster grid: SMs x this */
+    int anyPhong;             /* some state of the launch lights per fragment */
     PFDevCounters *cnt;
     uint32_t command;
 };

@@ -865,6 +865,22 @@ bool flush(Renderer *r)
         if (o.kind != 0) continue;
         PFBatchLaunch &L = launches[oi];
         L = PFBatchLaunch{};
+        if (o.targets.size() > 1) {
+            // the raster's work queue hands out tiles in target order: put the
+            // targets with the most triangles first, so that their (longest)
+            // tiles do not start last
+            std::vector<uint64_t> load(o.targets.size(), 0);
+            for (int si = o.segBegin; si < o.segEnd; si++)
+                load[std::find(o.targets.begin(), o.targets.end(), r->segs[si].fb) - o.targets.begin()] += hseg[si].nItems;
+            std::vector<size_t> perm(o.targets.size());
+            for (size_t k = 0; k < perm.size(); k++) perm[k] = k;
+            std::stable_sort(perm.begin(), perm.end(), [&](size_t x, size_t y) { return load[x] > load[y]; });
+            std::vector<PFframebuffer *> tg(perm.size());
+            std::vector<int> cl(perm.size());
+            for (size_t k = 0; k < perm.size(); k++) { tg[k] = o.targets[perm[k]]; cl[k] = o.clearCmd[perm[k]]; }
+            o.targets.swap(tg);
+            o.clearCmd.swap(cl);
+        }
         uint32_t v = 0, it = 0, tiles = 0;
         for (int si = o.segBegin; si < o.segEnd; si++) {
             hseg[si].vtxBase = v; hseg[si].itemBase = it;
@@ -968,6 +984,7 @@ bool flush(Renderer *r)
                 L.pool = (PFPrim *)r->pool.p; L.poolPh = (PFPrimPhong *)r->poolPh.p; L.poolCap = r->poolCap;
                 L.binCount = (uint32_t *)r->binCount.p; L.bins = (uint32_t *)r->bins.p; L.cap = r->cap;
                 L.rasterCtasPerSM = r->rasterCtasPerSM;
+                L.anyPhong = anyPhong ? 1 : 0;
                 L.cnt = dcnt;
                 rop.L = L;
                 r->stats.kernel_launches += 3;

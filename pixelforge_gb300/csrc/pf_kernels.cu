@@ -816,6 +816,7 @@ struct RasterArgs {
     uint32_t totalTiles;
     PFDevCounters *cnt;
     uint32_t command;
+    int anyPhong;
 };
 
 struct ChunkPrim {             // per-sub-triangle data derived for this tile
@@ -826,6 +827,76 @@ struct ChunkPrim {             // per-sub-triangle data derived for this tile
     uint32_t flags;            // face | is3D | state << 8
     uint32_t rstate;           // the state's PFS_* flags | depth function << 16 | blend mode << 24
 };
+
+// The per-pixel pass's view of a chunk sub-triangle, four 16-byte words:
+// edge functions at the tile origin and their steps, the clipped box
+// (x0 | width << 8 | y0 << 16 | height << 24), the state bits, wInvSum, the
+// three depth terms and a depth-test rejection bound.
+struct __align__(16) DenseP {
+    int32_t e0[3], ex0;
+    int32_t ex1, ex2, ey0, ey1;
+    int32_t ey2;
+    uint32_t box, rstate;
+    float wInvSum;
+    float z1, z2, z3;
+    float zReject;             // every covered fragment fails the depth test when zReject >= depth (NaN: never)
+};
+
+// A bound below which no fragment depth of the sub-triangle can fall, for
+// PF_LESS (and, one step lower, PF_LEQUAL).  The depth of a covered pixel is
+// 1 / ((z1 wN1 + z2 wN2) + z3 wN3) with wN >= 0 summing to 1 within a few
+// ulps, so the interpolated term lies in [min z, max z] widened by a
+// relative 1e-5; its reciprocal is bounded by the reciprocals of the ends
+// when they have one sign.  NaN (never rejects) otherwise.
+__device__ __forceinline__ float depth_reject_bound(const PFPrim &P, uint32_t rstate)
+{
+    const float qnan = __int_as_float(0x7fffffff);
+    const int func = (int)((rstate >> 16) & 255u);
+    if (!(rstate & PFS_DEPTH_TEST) || (func != 2 && func != 3)) return qnan;
+    const float lo = fminf(P.z1, fminf(P.z2, P.z3)), hi = fmaxf(P.z1, fmaxf(P.z2, P.z3));
+    if (!(fabsf(lo) < 1e30f && fabsf(hi) < 1e30f)) return qnan;
+    float b;
+    if (lo > 0.0f) b = __fdiv_rn(1.0f, hi * 1.00001f) * 0.99999f;         // interpolated term <= hi (1 + 1e-5)
+    else if (hi < 0.0f) b = __fdiv_rn(1.0f, hi * 0.99999f) * 1.00001f;    // term <= hi (1 - 1e-5) < 0
+    else return qnan;
+    if (!(fabsf(b) < 1e30f)) return qnan;
+    return func == 2 ? b : nextafterf(b, -INFINITY);
+}
+
+// Tile-relative set-up of sub-triangle P for the tile at (ox, oy).
+__device__ __forceinline__ void derive_chunk_prim(const PFPrim &P, uint32_t ox, uint32_t oy, uint32_t W, uint32_t H,
+                                                  const PFDrawState *states, ChunkPrim &cp, DenseP &dp)
+{
+    cp.flags = P.flags;
+    const int face = P.flags & 1;
+    int32_t sx[3] = { P.y3 - P.y2, P.y1 - P.y3, P.y2 - P.y1 };
+    int32_t sy[3] = { P.x2 - P.x3, P.x3 - P.x1, P.x1 - P.x2 };
+    const int32_t rx[3] = { P.x2, P.x3, P.x1 }, ry[3] = { P.y2, P.y3, P.y1 };
+    for (int e = 0; e < 3; e++) {
+        if (face) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
+        cp.ex[e] = sx[e]; cp.ey[e] = sy[e];
+        cp.e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
+    }
+    // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside tile and framebuffer
+    uint32_t x0 = max((uint32_t)P.xMin, ox), x1 = min(min((uint32_t)P.xMax, ox + PF_TILE), W);
+    uint32_t y0 = max((uint32_t)P.yMin, oy), y1e = min(min((uint32_t)P.yMax + 1u, oy + PF_TILE), H);
+    if ((uint32_t)P.yMax == 0xffffffffu) y1e = 0;    // yMax + 1 wrapped
+    const bool empty = (x0 >= x1) || (y0 >= y1e) || ((uint32_t)P.xMin >= (uint32_t)P.xMax) ||
+                       ((uint32_t)P.yMin > (uint32_t)P.yMax);
+    cp.bx0 = empty ? 0 : x0 - ox; cp.by0 = empty ? 0 : y0 - oy;
+    cp.bw = empty ? 0 : x1 - x0; cp.bh = empty ? 0 : y1e - y0;
+    cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
+    const PFDrawState &St = states[P.flags >> 8];
+    cp.rstate = (St.flags & 0xffffu) | ((uint32_t)St.depthFunc << 16) | ((uint32_t)St.blendMode << 24);
+    dp.e0[0] = cp.e0[0]; dp.e0[1] = cp.e0[1]; dp.e0[2] = cp.e0[2];
+    dp.ex0 = cp.ex[0]; dp.ex1 = cp.ex[1]; dp.ex2 = cp.ex[2];
+    dp.ey0 = cp.ey[0]; dp.ey1 = cp.ey[1]; dp.ey2 = cp.ey[2];
+    dp.box = cp.bx0 | (cp.bw << 8) | (cp.by0 << 16) | (cp.bh << 24);
+    dp.rstate = cp.rstate;
+    dp.wInvSum = P.wInvSum;
+    dp.z1 = P.z1; dp.z2 = P.z2; dp.z3 = P.z3;
+    dp.zReject = depth_reject_bound(P, cp.rstate);
+}
 
 // Exclusive offsets of each lane's count within the warp (wo[0..31]) and
 // the warp total (wo[32]).
@@ -906,18 +977,54 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
     return frag;
 }
 
+// 16-byte global-to-shared copies that complete asynchronously (cp.async):
+// the next chunk's records are fetched while the current one is rasterized.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Issue the copies of chunk records keys[c0 .. c0 + cn) into sp (and their
+// per-fragment lighting data into sq when the launch has any).
+__device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uint32_t *keys, uint32_t c0, uint32_t cn,
+                                                  PFPrim *sp, PFPrimPhong *sq)
+{
+    for (uint32_t w = threadIdx.x; w < cn * 8; w += RASTER_THREADS) {
+        const uint32_t pi = w >> 3, part = w & 7;
+        const uint32_t key = keys[c0 + pi];
+        const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+        const PFPrim *src = &a.prims[item];
+        if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
+        cp_async16(reinterpret_cast<int4 *>(&sp[pi]) + part, reinterpret_cast<const int4 *>(src) + part);
+    }
+    if (a.anyPhong) {
+        for (uint32_t w = threadIdx.x; w < cn * 5; w += RASTER_THREADS) {
+            const uint32_t pi = w / 5, part = w % 5;
+            const uint32_t key = keys[c0 + pi];
+            const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+            const PFPrimPhong *src = &a.primsPh[item];
+            if (sub != 0) src = &a.poolPh[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
+            cp_async16(reinterpret_cast<int4 *>(&sq[pi]) + part, reinterpret_cast<const int4 *>(src) + part);
+        }
+    }
+    cp_async_commit();
+}
+
 __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
 {
     extern __shared__ uint32_t skeys[];               // [N] keys (+ [n] sorted copy when rank-sorting)
-    __shared__ PFPrim sprim[CH];
-    __shared__ PFPrimPhong sph[CH];
+    __shared__ __align__(16) PFPrim sprimBuf[2][CH];         // double-buffered chunk records
+    __shared__ __align__(16) PFPrimPhong sphBuf[2][CH];
     __shared__ ChunkPrim scp[CH];
+    __shared__ DenseP sdp[CH];
     __shared__ uint32_t sarea[CH + 1];
     __shared__ uint32_t pmask[RASTER_THREADS];
     __shared__ uint32_t fcol[RASTER_THREADS / 32][FWIN];
     __shared__ float fz[RASTER_THREADS / 32][FWIN];
     __shared__ uint32_t woff[RASTER_THREADS / 32][33];
-    __shared__ int sHasPhong;
     __shared__ int sDense;
 
     if (a.cnt->abortCommand <= a.command) return;
@@ -993,71 +1100,41 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             }
         }
 
-        for (uint32_t c0 = 0; c0 < n; c0 += CH) {
+        stage_chunk_async(a, keys, 0, min((uint32_t)CH, n), sprimBuf[0], sphBuf[0]);
+        for (uint32_t c0 = 0, it = 0; c0 < n; c0 += CH, it++) {
             const uint32_t cn = min((uint32_t)CH, n - c0);
-            __syncthreads();
-            if (tid == 0) sHasPhong = 0;
-            // 1. stage records: 8 int4 per PFPrim
-            for (uint32_t w = tid; w < cn * 8; w += RASTER_THREADS) {
-                const uint32_t pi = w >> 3, part = w & 7;
-                const uint32_t key = keys[c0 + pi];
-                const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
-                const PFPrim *src = &a.prims[item];
-                if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-                reinterpret_cast<int4 *>(&sprim[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
-            }
+            PFPrim *const sprim = sprimBuf[it & 1];
+            PFPrimPhong *const sph = sphBuf[it & 1];
+            cp_async_wait_all();
+            __syncthreads();                                  // this chunk is staged; the previous one's data are free
+            if (c0 + CH < n)
+                stage_chunk_async(a, keys, c0 + CH, min((uint32_t)CH, n - c0 - CH), sprimBuf[(it + 1) & 1],
+                                  sphBuf[(it + 1) & 1]);
             pmask[tid] = 0;
-            __syncthreads();
-            // derived per-sub-triangle data (one thread each)
-            if (tid < cn) {
-                const PFPrim &P = sprim[tid];
-                ChunkPrim cp;
-                cp.flags = P.flags;
-                const int face = P.flags & 1;
-                int32_t sx[3] = { P.y3 - P.y2, P.y1 - P.y3, P.y2 - P.y1 };
-                int32_t sy[3] = { P.x2 - P.x3, P.x3 - P.x1, P.x1 - P.x2 };
-                const int32_t rx[3] = { P.x2, P.x3, P.x1 }, ry[3] = { P.y2, P.y3, P.y1 };
-                for (int e = 0; e < 3; e++) {
-                    if (face) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
-                    cp.ex[e] = sx[e]; cp.ey[e] = sy[e];
-                    cp.e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
+            // 1. warp 0 derives the chunk's tile-relative set-up (one
+            //    sub-triangle per lane)
+            if (warp == 0) {
+                const bool has = lane < cn;
+                uint32_t bh = 0, area = 0;
+                if (has) {
+                    const PFPrim &P = sprim[lane];
+                    ChunkPrim cp;
+                    DenseP dp;
+                    derive_chunk_prim(P, ox, oy, T.W, T.H, a.states, cp, dp);
+                    scp[lane] = cp;
+                    sdp[lane] = dp;
+                    bh = cp.bw ? cp.bh : 0;
+                    area = cp.bw * cp.bh;
                 }
-                // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside tile and framebuffer
-                uint32_t x0 = max((uint32_t)P.xMin, ox), x1 = min(min((uint32_t)P.xMax, ox + PF_TILE), T.W);
-                uint32_t y0 = max((uint32_t)P.yMin, oy), y1e = min(min((uint32_t)P.yMax + 1u, oy + PF_TILE), T.H);
-                if ((uint32_t)P.yMax == 0xffffffffu) y1e = 0;    // yMax + 1 wrapped
-                const bool empty = (x0 >= x1) || (y0 >= y1e) || ((uint32_t)P.xMin >= (uint32_t)P.xMax) ||
-                                   ((uint32_t)P.yMin > (uint32_t)P.yMax);
-                cp.bx0 = empty ? 0 : x0 - ox; cp.by0 = empty ? 0 : y0 - oy;
-                cp.bw = empty ? 0 : x1 - x0; cp.bh = empty ? 0 : y1e - y0;
-                cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
-                const PFDrawState &St = a.states[P.flags >> 8];
-                cp.rstate = (St.flags & 0xffffu) | ((uint32_t)St.depthFunc << 16) | ((uint32_t)St.blendMode << 24);
-                scp[tid] = cp;
-                if (St.flags & PFS_PHONG) sHasPhong = 1;
-            }
-            __syncthreads();
-            if (tid < 32) {                                   // prefix of clipped box rows; box area
-                uint32_t v = (tid < cn && scp[tid].bw) ? scp[tid].bh : 0;
-                uint32_t s = v;
+                // prefix of clipped box rows; box area
+                uint32_t s = bh;
                 for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
-                sarea[tid + 1] = s;
-                if (tid == 0) sarea[0] = 0;
-                uint32_t ar = (tid < cn) ? scp[tid].bw * scp[tid].bh : 0;
-                for (int o = 16; o > 0; o >>= 1) ar += __shfl_xor_sync(0xffffffffu, ar, o);
+                sarea[lane + 1] = s;
+                if (lane == 0) sarea[0] = 0;
+                for (int o = 16; o > 0; o >>= 1) area += __shfl_xor_sync(0xffffffffu, area, o);
                 // boxes that cover half a tile on average: test every
                 // (pixel, sub-triangle) pair instead of stepping rows
-                if (tid == 0) sDense = ar > cn * (PF_TILE_PIXELS / 2);
-            }
-            if (sHasPhong) {
-                for (uint32_t w = tid; w < cn * 5; w += RASTER_THREADS) {
-                    const uint32_t pi = w / 5, part = w % 5;
-                    const uint32_t key = keys[c0 + pi];
-                    const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
-                    const PFPrimPhong *src = &a.primsPh[item];
-                    if (sub != 0) src = &a.poolPh[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-                    reinterpret_cast<int4 *>(&sph[pi])[part] = __ldg(reinterpret_cast<const int4 *>(src) + part);
-                }
+                if (lane == 0) sDense = area > cn * (PF_TILE_PIXELS / 2);
             }
             __syncthreads();
             uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
@@ -1066,19 +1143,23 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 //    submission order at its own pixel: coverage, depth, test.
                 uint32_t cov = 0;
                 for (uint32_t k = 0; k < cn; k++) {
-                    const ChunkPrim &cp = scp[k];
-                    if (lx - cp.bx0 >= cp.bw || ly - cp.by0 >= cp.bh) continue;
-                    const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + lx * (uint32_t)cp.ex[0] + ly * (uint32_t)cp.ey[0]);
-                    const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + lx * (uint32_t)cp.ex[1] + ly * (uint32_t)cp.ey[1]);
-                    const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + lx * (uint32_t)cp.ex[2] + ly * (uint32_t)cp.ey[2]);
+                    const int4 *d4 = reinterpret_cast<const int4 *>(&sdp[k]);
+                    const int4 q0 = d4[0], q1 = d4[1], q2 = d4[2];
+                    const uint32_t box = (uint32_t)q2.y;
+                    if (lx - (box & 255u) >= ((box >> 8) & 255u) || ly - ((box >> 16) & 255u) >= (box >> 24)) continue;
+                    const int32_t w1 = (int32_t)((uint32_t)q0.x + lx * (uint32_t)q0.w + ly * (uint32_t)q1.z);
+                    const int32_t w2 = (int32_t)((uint32_t)q0.y + lx * (uint32_t)q1.x + ly * (uint32_t)q1.w);
+                    const int32_t w3 = (int32_t)((uint32_t)q0.z + lx * (uint32_t)q1.y + ly * (uint32_t)q2.x);
                     if (!((w1 | w2 | w3) > 0)) continue;
                     cov++;
-                    const PFPrim &P = sprim[k];
-                    const float wn1 = (float)w1 * P.wInvSum, wn2 = (float)w2 * P.wInvSum, wn3 = (float)w3 * P.wInvSum;
-                    float zs = P.z1 * wn1 + P.z2 * wn2;
-                    zs = zs + P.z3 * wn3;
+                    const float4 zq = reinterpret_cast<const float4 *>(&sdp[k])[3];
+                    if (zq.w >= dep) continue;                   // every fragment of it fails the depth test
+                    const float wInvSum = __int_as_float(q2.w);
+                    const float wn1 = (float)w1 * wInvSum, wn2 = (float)w2 * wInvSum, wn3 = (float)w3 * wInvSum;
+                    float zs = zq.x * wn1 + zq.y * wn2;
+                    zs = zs + zq.z * wn3;
                     const float z = 1.0f / zs;
-                    const uint32_t rs = cp.rstate;
+                    const uint32_t rs = (uint32_t)q2.z;
                     if (!(rs & PFS_DEPTH_TEST) || depth_simd((int)((rs >> 16) & 255u), z, dep)) {
                         vis |= 1u << k;
                         if (rs & PFS_DEPTH_MASK) dep = z;
@@ -1290,7 +1371,7 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
     RasterArgs a{ L.binCount, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
-                  L.totalTiles, L.cnt, L.command };
+                  L.totalTiles, L.cnt, L.command, L.anyPhong };
     const size_t smem = raster_smem(L.cap);
     cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
