@@ -35,7 +35,17 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+TRAFFIC_FILE = ROOT / "profiles" / "roofline_traffic.json"
 FALLBACK_HBM_GBS = 6800.0
+
+
+def _traffic(kernel: str):
+    """DRAM bytes per launch of a kernel from the committed ncu summary (one
+    capture of the same workload), or None."""
+    try:
+        return float(json.loads(TRAFFIC_FILE.read_text())[kernel]["bytes_per_launch"])
+    except Exception:
+        return None
 
 
 def _peaks():
@@ -180,7 +190,8 @@ def run_gpu(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": st["kernel_launches"],
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": _traffic("k_raster"),
+                     "launch_share_of_frame": (st["raster_ms"] / max(st["device_ms"], 1e-9)),
                      "algorithmic_bytes_per_launch": fb["raster"], "launch_ms": raster_ms,
                      "frame_algorithmic_bytes": fb["total"],
                      "frame_frac": fb["total"] / (ms_frame / 1e3) / 1e9 / peak},
