@@ -182,3 +182,72 @@ def run_mix(lib: A.PixelForgeLib, case: dict, target: str = "fbo") -> Frame:
         return fr
     finally:
         tg.close()
+
+
+TYPE_CASES = [
+    # (position type, normal/uv type, colour type, index type)
+    (A.PF_SHORT, A.PF_FLOAT, A.PF_UNSIGNED_SHORT, A.PF_UNSIGNED_BYTE),
+    (A.PF_INT, A.PF_DOUBLE, A.PF_UNSIGNED_INT, A.PF_UNSIGNED_SHORT),
+    (A.PF_DOUBLE, A.PF_DOUBLE, A.PF_FLOAT, A.PF_UNSIGNED_INT),
+    (A.PF_FLOAT, A.PF_FLOAT, A.PF_DOUBLE, A.PF_UNSIGNED_BYTE),
+]
+
+_NP = {A.PF_SHORT: np.int16, A.PF_INT: np.int32, A.PF_FLOAT: np.float32, A.PF_DOUBLE: np.float64,
+       A.PF_UNSIGNED_BYTE: np.uint8, A.PF_UNSIGNED_SHORT: np.uint16, A.PF_UNSIGNED_INT: np.uint32}
+
+
+def run_types(lib: A.PixelForgeLib, seed: int, types, target: str = "fbo") -> Frame:
+    """Vertex arrays of every accepted element type (context.c:1231-1575):
+    integer or floating positions, float or double normals and texture
+    coordinates, 8/16/32-bit or floating colours, 8/16/32-bit indices."""
+    ptype, ntype, ctype, itype = types
+    r = np.random.default_rng(seed)
+    W, H = 96, 72
+    tg = Target(lib, W, H, target)
+    texh = None
+    try:
+        n = 60
+        pos = r.integers(-100, 101, (n, 3)).astype(np.float64)
+        pos[:, 2] = r.integers(-90, 91, n)
+        nrm = r.normal(size=(n, 3))
+        uv = r.uniform(0.0, 0.95, (n, 2))
+        colf = r.uniform(0, 1, (n, 4))
+        colf[:, 3] = 1.0
+        if ctype in (A.PF_FLOAT, A.PF_DOUBLE):
+            col = colf.astype(_NP[ctype])
+        else:
+            scale = {A.PF_UNSIGNED_BYTE: 255, A.PF_UNSIGNED_SHORT: 65535, A.PF_UNSIGNED_INT: 4294967295}[ctype]
+            col = np.floor(colf * scale).astype(_NP[ctype])
+        idx = r.integers(0, n, 90).astype(_NP[itype])
+        pos_t = pos.astype(_NP[ptype])
+        nrm_t, uv_t = nrm.astype(_NP[ntype]), uv.astype(_NP[ntype])
+        texture = r.integers(0, 256, (8, 8, 4)).astype(np.uint8)
+        lib.pfClearDepth(1e30)
+        lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+        lib.pfMatrixMode(A.PF_PROJECTION)
+        lib.pfLoadIdentity()
+        lib.pfOrtho(-110.0, 110.0, -110.0, 110.0, -120.0, 120.0)
+        lib.pfMatrixMode(A.PF_MODELVIEW)
+        lib.pfLoadIdentity()
+        lib.pfDisable(A.PF_CULL_FACE)
+        lib.pfEnable(A.PF_DEPTH_TEST)
+        texh = lib.pfGenTexture(_ptr(texture), 8, 8, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+        lib.pfBindTexture(texh)
+        lib.pfEnable(A.PF_TEXTURE_2D)
+        lib.pfEnable(A.PF_LIGHTING)
+        lib.pfEnableLight(0)
+        lp = np.array([50.0, 80.0, 150.0], np.float32)
+        lib.pfLightfv(0, A.PF_POSITION, _ptr(lp))
+        lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_NORMAL_ARRAY | A.PF_TEXTURE_COORD_ARRAY | A.PF_COLOR_ARRAY)
+        lib.pfVertexPointer(3, ptype, 0, _ptr(pos_t))
+        lib.pfNormalPointer(ntype, 0, _ptr(nrm_t))
+        lib.pfTexCoordPointer(ntype, 0, _ptr(uv_t))
+        lib.pfColorPointer(4, ctype, 0, _ptr(col))
+        lib.pfDrawElements(A.PF_TRIANGLES, len(idx), itype, _ptr(idx))
+        fr = tg.finish()
+        if texh is not None:
+            th = C.c_void_p(texh)
+            lib.pfDeleteTexture(C.byref(th), False)
+        return fr
+    finally:
+        tg.close()

@@ -29,3 +29,11 @@ def test_oracle_equals_reference_mixed(oracle, ref_shim, seed):
 def test_oracle_equals_reference_soup(oracle, ref_shim, kw):
     sc = SoupScene(**kw)
     same(sc.render(oracle), sc.render(ref_shim), f"soup {kw}")
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_oracle_equals_reference_array_types(oracle, ref_shim, k):
+    from mixscenes import TYPE_CASES, run_types
+    a, b = run_types(oracle, 40 + k, TYPE_CASES[k]), run_types(ref_shim, 40 + k, TYPE_CASES[k])
+    assert (a.depth < 1e29).sum() > 500
+    same(a, b, f"types {TYPE_CASES[k]}")

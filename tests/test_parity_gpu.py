@@ -134,3 +134,10 @@ def test_gpu_matches_reference_golden(gpu, name):
     diff = np.abs(fr.color.astype(np.int32) - gc.astype(np.int32))
     tol = COLOR_TOL if GOLD_POWF(name) else 0
     assert int(diff.max()) <= tol, f"{name}: colour differs by {int(diff.max())}"
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_vertex_array_types(gpu, oracle, k):
+    from mixscenes import TYPE_CASES, run_types
+    assert_parity(run_types(gpu, 40 + k, TYPE_CASES[k]), run_types(oracle, 40 + k, TYPE_CASES[k]),
+                  label=f"types {TYPE_CASES[k]}")
