@@ -374,6 +374,8 @@ typedef struct {
     PFdouble raster_ms;        /* with pfEnableTiming: GPU time of the tile-raster kernel */
     PFuint64 raster_launches;  /* tile-raster kernel launches */
     PFuint64 kernel_launches;  /* all kernels launched by this library */
+    PFuint64 draw_splits;      /* draw groups rendered in two passes because a tile held more
+                                  sub-triangles than one bin can sort */
 } PFstats;
 
 PF_API void pfGetStats(PFstats* stats);

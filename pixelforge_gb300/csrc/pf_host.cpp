@@ -256,6 +256,7 @@ struct Renderer {
     struct Op { int kind; int cmd; PFBatchLaunch L; size_t n; uint32_t *color; float *depth;
                 uint32_t cc; float cd; bool all; int hook; PFHookParams hp; };
     std::vector<Op> lastOps;
+    std::vector<void *> splitMem;        // device segments/targets of draw groups split by the last flush
     cudaGraphExec_t graph = nullptr;
     bool graphValid = false;
 };
@@ -675,6 +676,8 @@ void release_renderer(Renderer *r)
         if (r->evStart) { cudaEventDestroy(r->evStart); cudaEventDestroy(r->evEnd); }
         for (auto &pr : r->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
         if (r->stream) cudaStreamDestroy(r->stream);
+        for (void *q : r->splitMem) cudaFree(q);
+        r->splitMem.clear();
     }
     r->staging.release();
     r->devOk = r->devInit = false;
@@ -943,6 +946,73 @@ bool flush(Renderer *r)
     PFDevCounters *dcnt = (PFDevCounters *)r->counters.p;
     uint32_t startOp = 0;
     r->lastOps.clear();
+    for (void *q : r->splitMem) cudaFree(q);
+    r->splitMem.clear();
+    // Host copies of the segments and targets of each draw group, for
+    // splitting a group whose tile bins exceed the largest capacity.
+    std::vector<std::vector<PFSegment>> opSegs(ops.size());
+    std::vector<std::vector<PFTarget>> opTargets(ops.size());
+    {
+        size_t tc = 0;
+        for (size_t oi = 0; oi < ops.size(); oi++) {
+            if (ops[oi].kind != 0) continue;
+            opSegs[oi].assign(hseg + ops[oi].segBegin, hseg + ops[oi].segEnd);
+            opTargets[oi].assign(htg + tc, htg + tc + ops[oi].targets.size());
+            tc += ops[oi].targets.size();
+        }
+    }
+    // Split draw group oi into two passes of half its items each; the second
+    // pass starts from the first one's framebuffers (no fused clear).
+    auto split_op = [&](size_t oi) -> bool {
+        const std::vector<PFSegment> S = opSegs[oi];
+        uint64_t N = 0;
+        for (auto &sg : S) N += sg.nItems;
+        if (ops[oi].kind != 0 || N < 2) return false;
+        const uint64_t half = N / 2;
+        std::vector<PFSegment> A, B;
+        uint64_t acc = 0;
+        for (const PFSegment &sg : S) {
+            if (acc + sg.nItems <= half) A.push_back(sg);
+            else if (acc >= half) B.push_back(sg);
+            else {
+                const uint32_t h = (uint32_t)(half - acc);
+                PFSegment a = sg, b = sg;
+                a.nItems = h;
+                b.itemSkip = sg.itemSkip + h; b.nItems = sg.nItems - h;
+                A.push_back(a); B.push_back(b);
+            }
+            acc += sg.nItems;
+        }
+        std::vector<PFTarget> TA = opTargets[oi], TB = opTargets[oi];
+        for (auto &t : TB) t.clearMode = 0;
+        PFBatchLaunch LA = launches[oi], LB = launches[oi];
+        auto place = [&](std::vector<PFSegment> &segs, std::vector<PFTarget> &tg, PFBatchLaunch &L) -> bool {
+            uint32_t v = 0, it = 0;
+            for (auto &sg : segs) { sg.vtxBase = v; sg.itemBase = it; v += sg.nVerts; it += sg.nItems; }
+            const size_t sb = segs.size() * sizeof(PFSegment), tb = tg.size() * sizeof(PFTarget);
+            void *mem = nullptr;
+            if (cudaMalloc(&mem, sb + tb) != cudaSuccess) { cudaGetLastError(); return false; }
+            r->splitMem.push_back(mem);
+            if (cudaMemcpyAsync(mem, segs.data(), sb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                cudaMemcpyAsync((uint8_t *)mem + sb, tg.data(), tb, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            L.segs = (const PFSegment *)mem; L.nSegs = (int)segs.size();
+            L.targets = (const PFTarget *)((uint8_t *)mem + sb);
+            L.nVerts = v; L.nItems = it;
+            return true;
+        };
+        if (!place(A, TA, LA) || !place(B, TB, LB)) return false;
+        ops.insert(ops.begin() + (long)oi + 1, ops[oi]);
+        launches[oi] = LA;
+        launches.insert(launches.begin() + (long)oi + 1, LB);
+        opSegs[oi] = A; opSegs.insert(opSegs.begin() + (long)oi + 1, B);
+        opTargets[oi] = TA; opTargets.insert(opTargets.begin() + (long)oi + 1, TB);
+        for (size_t j = oi; j < launches.size(); j++) launches[j].command = (uint32_t)j;
+        r->stats.draw_splits += 1;
+        return true;
+    };
     for (int attempt = 0;; attempt++) {
         if (!r->vout.ensure((size_t)maxVerts * sizeof(PFVertexOut) + 64) ||
             !r->prims.ensure((size_t)maxItems * sizeof(PFPrim) + 128) ||
@@ -1043,13 +1113,18 @@ bool flush(Renderer *r)
             uint32_t need = std::max(hc.maxBin, r->cap * 2);
             uint32_t nc = 1; while (nc < need) nc <<= 1;
             if (nc > kCapMax) {
-                r->devStatus |= PF_DEVICE_BIN_LIMIT;
-                return fail("tile bin capacity", cudaErrorMemoryAllocation);
+                // more sub-triangles in one tile than a bin can sort: render
+                // the draw group in two passes of half its items each
+                if (!split_op(hc.abortCommand)) {
+                    r->devStatus |= PF_DEVICE_BIN_LIMIT;
+                    return fail("tile bin capacity", cudaErrorMemoryAllocation);
+                }
+                nc = kCapMax;
             }
             r->cap = nc;
         }
         if (hc.status & PFD_CLIP_OVERFLOW) r->poolCap = std::max(r->poolCap * 4, hc.clipCount * 2);
-        if (attempt > 8) return fail("overflow retries", cudaErrorUnknown);
+        if (attempt > 64) return fail("overflow retries", cudaErrorUnknown);
         startOp = hc.abortCommand;
     }
     r->stats.flushes += 1;

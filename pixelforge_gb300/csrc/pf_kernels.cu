@@ -696,7 +696,7 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
 {
     const PFDrawState &S = sState ? *sState : states[sg.state];
     uint32_t vi[3]; int face;
-    item_vertices(sg, g - sg.itemBase, vi, face);
+    item_vertices(sg, g - sg.itemBase + sg.itemSkip, vi, face);
     const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
     float4 hv[3];
     for (int m = 0; m < 3; m++) hv[m] = *reinterpret_cast<const float4 *>(V[m]->h);

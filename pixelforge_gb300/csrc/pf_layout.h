@@ -102,7 +102,8 @@ typedef struct {
     int32_t nFaces;               /* PF_ITEMS_TRIS: 1 or 2 */
     int32_t face0;                /* PF_ITEMS_TRIS with nFaces == 1 */
     int32_t target;               /* framebuffer of this segment (index into the batch's targets) */
-    int32_t pad_[3];
+    uint32_t itemSkip;            /* items of the draw before this segment's first (a draw split into passes) */
+    int32_t pad_[2];
 } PFSegment;                      /* 144 bytes */
 
 /* A framebuffer rendered by a batch.  Its tiles are numbered

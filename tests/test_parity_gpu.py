@@ -141,3 +141,13 @@ def test_vertex_array_types(gpu, oracle, k):
     from mixscenes import TYPE_CASES, run_types
     assert_parity(run_types(gpu, 40 + k, TYPE_CASES[k]), run_types(oracle, 40 + k, TYPE_CASES[k]),
                   label=f"types {TYPE_CASES[k]}")
+
+
+def test_tile_overfull_draw_is_split(gpu, oracle):
+    """More sub-triangles in one tile than a bin can sort (16,384): the draw
+    group is rendered in passes, with the same result."""
+    sc = SoupScene(width=32, height=32, ntris=80000, seed=77, xy_range=(-3.0, 3.0), cull=False)
+    got, ref = sc.render(gpu), sc.render(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert got.stats["draw_splits"] >= 1
+    assert_parity(got, ref, exact_color=True, label="overfull tiles")
