@@ -339,13 +339,139 @@ static void tex_map(const RTex *t, float u, float v, int32_t *x, int32_t *y)
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* texel formats: the SIMD pixel getters (src/internal/pixel.h:2253-3045)     */
+/* ------------------------------------------------------------------------ */
+
+/* Bytes of one texel of a sampling format, 0 when the reference has no SIMD
+ * getter for the combination (src/internal/pixel.h:3046-3097). */
+static int texel_bytes(PFpixelformat f, PFdatatype t)
+{
+    int comps;
+    switch (f) {
+    case PF_RED: case PF_GREEN: case PF_BLUE: case PF_ALPHA: case PF_LUMINANCE: comps = 1; break;
+    case PF_LUMINANCE_ALPHA: comps = 2; break;
+    case PF_RGB: case PF_BGR: comps = 3; break;
+    case PF_RGBA: case PF_BGRA: comps = 4; break;
+    default: return 0;
+    }
+    switch (t) {
+    case PF_UNSIGNED_BYTE: return comps;
+    case PF_HALF_FLOAT: return 2 * comps;
+    case PF_FLOAT: return 4 * comps;
+    case PF_UNSIGNED_SHORT_5_6_5: return (f == PF_RGB || f == PF_BGR) ? 2 : 0;
+    case PF_UNSIGNED_SHORT_5_5_5_1: case PF_UNSIGNED_SHORT_4_4_4_4: return (f == PF_RGBA || f == PF_BGRA) ? 2 : 0;
+    default: return 0;
+    }
+}
+
+/* Byte b of the texture buffer; bytes past its end read 0 (the reference's
+ * 32-bit gathers read past the buffer). */
+static inline uint32_t tbyte(const RTex *t, int64_t b)
+{
+    const int64_t n = (int64_t)t->w * t->h * texel_bytes(t->format, t->type);
+    return (b >= 0 && b < n) ? ((const uint8_t *)t->pixels)[b] : 0u;
+}
+static inline uint32_t tword(const RTex *t, int64_t b)   /* little-endian 32-bit gather */
+{
+    return tbyte(t, b) | tbyte(t, b + 1) << 8 | tbyte(t, b + 2) << 16 | tbyte(t, b + 3) << 24;
+}
+/* pfmHalfToFloat (src/pfm.h:129-161): denormals flush to zero */
+static inline float half_to_float(uint32_t h)
+{
+    uint32_t s = (h & 0x8000u) << 16;
+    int32_t em = (int32_t)(h & 0x7fffu);
+    int32_t r = (int32_t)((uint32_t)(em + (112 << 10)) << 13);
+    r = (em < (1 << 10)) ? 0 : r;
+    r += (em >= (31 << 10)) ? (112 << 23) : 0;
+    return ox_bitsf(s | (uint32_t)r);
+}
+static inline uint32_t h8(const RTex *t, int64_t halfIndex)      /* cvt(half * 255) */
+{
+    return (uint32_t)ox_cvt_rne(half_to_float(tword(t, 2 * halfIndex) & 0xffffu) * 255.0f);
+}
+static inline uint32_t f8(const RTex *t, int64_t floatIndex)     /* cvt(float * 255) */
+{
+    return (uint32_t)ox_cvt_rne(ox_bitsf(tword(t, 4 * floatIndex)) * 255.0f);
+}
+
+/* RGBA8 value the reference's SIMD getter returns for texel o. */
+static uint32_t texel_rgba8(const RTex *t, int64_t o)
+{
+    const PFpixelformat f = t->format;
+    switch (t->type) {
+    case PF_UNSIGNED_BYTE:
+        switch (f) {
+        case PF_RED: return (tword(t, o) >> 24) | 0xff000000u;           /* the gather's top byte: texel o+3 */
+        case PF_GREEN: return ((tword(t, o) >> 24) << 8) | 0xff000000u;
+        case PF_BLUE: return ((tword(t, o) >> 24) << 16) | 0xff000000u;
+        case PF_ALPHA: return tword(t, o) << 24;
+        case PF_LUMINANCE: { uint32_t v = tword(t, o) >> 24; return v | v << 8 | v << 16 | 0xff000000u; }
+        case PF_LUMINANCE_ALPHA: {                                         /* bytes 2o+2, 2o+3: texel o+1 */
+            uint32_t w = tword(t, 2 * o), l = (w >> 16) & 255u, a = w >> 24;
+            return l | l << 8 | l << 16 | a << 24;
+        }
+        case PF_RGB: { uint32_t w = tword(t, 3 * o); return (w & 0xffffffu) | 0xff000000u; }
+        case PF_BGR: { uint32_t w = tword(t, 3 * o); return ((w >> 16) & 255u) | (w & 0xff00u) | (w & 255u) << 16 | 0xff000000u; }
+        case PF_RGBA: return tword(t, 4 * o);
+        case PF_BGRA: { uint32_t w = tword(t, 4 * o); return ((w >> 16) & 255u) | (w & 0xff00u) | (w & 255u) << 16 | (w & 0xff000000u); }
+        default: return 0;
+        }
+    case PF_HALF_FLOAT:
+        switch (f) {
+        case PF_RED: return h8(t, o) | 0xff000000u;
+        case PF_GREEN: return h8(t, o) << 8 | 0xff000000u;
+        case PF_BLUE: return h8(t, o) << 16 | 0xff000000u;
+        case PF_ALPHA: return h8(t, o) << 24;
+        case PF_LUMINANCE: { uint32_t v = h8(t, o); return 0xff000000u | v << 16 | v << 8 | v; }
+        case PF_LUMINANCE_ALPHA: { uint32_t v = h8(t, 2 * o), a = h8(t, 2 * o + 1); return a << 24 | v << 16 | v << 8 | v; }
+        case PF_RGB: return 0xff000000u | h8(t, 3 * o + 2) << 16 | h8(t, 3 * o + 1) << 8 | h8(t, 3 * o);
+        case PF_BGR: return 0xff000000u | h8(t, 3 * o + 2) << 16 | h8(t, 3 * o + 1) << 8 | h8(t, 3 * o);
+        case PF_RGBA: return h8(t, 4 * o + 3) << 24 | h8(t, 4 * o + 2) << 16 | h8(t, 4 * o + 1) << 8 | h8(t, 4 * o);
+        case PF_BGRA: return h8(t, 4 * o + 3) << 24 | h8(t, 4 * o) << 16 | h8(t, 4 * o + 1) << 8 | h8(t, 4 * o + 2);
+        default: return 0;
+        }
+    case PF_FLOAT:
+        switch (f) {
+        case PF_RED: return f8(t, o) | 0xff000000u;
+        case PF_GREEN: return f8(t, o) << 8 | 0xff000000u;
+        case PF_BLUE: return f8(t, o) << 16 | 0xff000000u;
+        case PF_ALPHA: return f8(t, o) << 24;
+        case PF_LUMINANCE: { uint32_t v = f8(t, o); return 0xff000000u | v << 16 | v << 8 | v; }
+        case PF_LUMINANCE_ALPHA: { uint32_t v = f8(t, 2 * o), a = f8(t, 2 * o + 1); return a << 24 | v << 16 | v << 8 | v; }
+        case PF_RGB: return 0xff000000u | f8(t, 3 * o + 2) << 16 | f8(t, 3 * o + 1) << 8 | f8(t, 3 * o);
+        case PF_BGR: return 0xff000000u | f8(t, 3 * o + 2) << 16 | f8(t, 3 * o + 1) << 8 | f8(t, 3 * o);
+        case PF_RGBA: return f8(t, 4 * o + 3) << 24 | f8(t, 4 * o + 2) << 16 | f8(t, 4 * o + 1) << 8 | f8(t, 4 * o);
+        case PF_BGRA: return f8(t, 4 * o + 3) << 24 | f8(t, 4 * o) << 16 | f8(t, 4 * o + 1) << 8 | f8(t, 4 * o + 2);
+        default: return 0;
+        }
+    case PF_UNSIGNED_SHORT_5_6_5: {
+        uint32_t w = tword(t, 2 * o);
+        uint32_t hi = ((w & 0xf800u) >> 11) << 3, g = ((w & 0x07e0u) >> 5) << 2, lo = (w & 0x1fu) << 3;
+        return (f == PF_RGB) ? (0xff000000u | lo << 16 | g << 8 | hi) : (0xff000000u | hi << 16 | g << 8 | lo);
+    }
+    case PF_UNSIGNED_SHORT_5_5_5_1: {
+        uint32_t w = tword(t, 2 * o);
+        uint32_t c0 = ((w >> 11) & 0x1fu) * 8u, c1 = ((w >> 6) & 0x1fu) * 8u, c2 = ((w >> 1) & 0x1fu) * 8u, a = (w & 1u) * 255u;
+        return (f == PF_RGBA) ? (a << 24 | c2 << 16 | c1 << 8 | c0) : (a << 24 | c0 << 16 | c1 << 8 | c2);
+    }
+    case PF_UNSIGNED_SHORT_4_4_4_4: {
+        uint32_t w = tword(t, 2 * o);
+        uint32_t c0 = ((w >> 12) & 0xfu) * 17u, c1 = ((w >> 8) & 0xfu) * 17u, c2 = ((w >> 4) & 0xfu) * 17u, a = (w & 0xfu) * 17u;
+        return (f == PF_RGBA) ? (a << 24 | c2 << 16 | c1 << 8 | c0) : (a << 24 | c0 << 16 | c1 << 8 | c2);
+    }
+    default: return 0;
+    }
+}
+
 static uint32_t tex_fetch(const RTex *t, int32_t x, int32_t y)
 {
     int64_t off = (int64_t)(int32_t)((uint32_t)y * t->w + (uint32_t)x);
     /* The reference reads past the texture buffer here (mirrored or clamped
      * coordinates of exactly 1.0 round to row h); pinned to 0. */
     if (off < 0 || off >= (int64_t)t->w * t->h) return 0;
-    return ((const uint32_t *)t->pixels)[off];
+    if (t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE) return ((const uint32_t *)t->pixels)[off];
+    return texel_rgba8(t, off);
 }
 
 /* Colour lerp with both endpoints defined (see header). */
@@ -848,9 +974,16 @@ static void update_matrices(RCtx *c, int withNormal)   /* context.c:96-111 */
 /* API: contexts                                                             */
 /* ------------------------------------------------------------------------ */
 
-static RTex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
+static int texel_bytes(PFpixelformat f, PFdatatype t);
+
+/* Framebuffers are RGBA / unsigned byte; textures may use any format the
+ * reference has a SIMD getter for. */
+static RTex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, int sampled)
 {
-    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { if (G) G->err = PF_INVALID_ENUM; return NULL; }
+    if (sampled ? !texel_bytes(f, t) : !(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) {
+        if (G) G->err = PF_INVALID_ENUM;
+        return NULL;
+    }
     RTex *x = (RTex *)calloc(1, sizeof(RTex));
     x->pixels = pixels; x->format = f; x->type = t; x->w = w; x->h = h;
     x->tx = 1.0f / (float)w; x->ty = 1.0f / (float)h;
@@ -862,7 +995,7 @@ PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFda
 {
     RCtx *c = (RCtx *)calloc(1, sizeof(RCtx));
     if (!c) return NULL;
-    c->main.texture = tex_new(buf, w, h, f, t);
+    c->main.texture = tex_new(buf, w, h, f, t, 0);
     if (!c->main.texture) { free(c); return NULL; }
     c->main.zbuffer = (float *)malloc((size_t)w * h * sizeof(float));
     for (size_t i = 0; i < (size_t)w * h; i++) c->main.zbuffer[i] = FLT_MAX;
@@ -913,7 +1046,7 @@ void pfSetMainBuffer(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatyp
         for (size_t i = 0; i < (size_t)w * h; i++) G->main.zbuffer[i] = G->clearDepth;
     }
     free(old);
-    G->main.texture = tex_new(buf, w, h, f, t);
+    G->main.texture = tex_new(buf, w, h, f, t, 0);
     G->aux = NULL;
 }
 
@@ -1539,7 +1672,7 @@ PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype
     PFframebuffer fb = { NULL, NULL };
     if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { if (G) G->err = PF_INVALID_ENUM; return fb; }
     void *px = calloc((size_t)w * h, 4);
-    fb.texture = tex_new(px, w, h, f, t);
+    fb.texture = tex_new(px, w, h, f, t, 0);
     fb.zbuffer = (float *)malloc((size_t)w * h * sizeof(float));
     for (size_t i = 0; i < (size_t)w * h; i++) fb.zbuffer[i] = FLT_MAX;
     return fb;
@@ -1597,7 +1730,7 @@ void pfSetFramebufferPixel(PFframebuffer *fb, PFsizei x, PFsizei y, PFcolor col)
     ((uint32_t *)t->pixels)[(size_t)y * t->w + x] = col_pack(col);
 }
 
-PFtexture pfGenTexture(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t) { return tex_new(pixels, w, h, f, t); }
+PFtexture pfGenTexture(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t) { return tex_new(pixels, w, h, f, t, 1); }
 void pfDeleteTexture(PFtexture *tex, PFboolean freeBuffer)
 {
     RTex *t = (RTex *)*tex;

@@ -237,7 +237,9 @@ struct Renderer {
     std::vector<SegRec> segs;
     std::vector<Cmd> cmds;
     struct SnapKey { const void *p; size_t bytes; int64_t off; };
-    std::vector<SnapKey> snaps;          // dedup of texture / array snapshots in this recording
+    std::vector<SnapKey> snaps;
+    struct Conversion { int64_t rawOff, off; PFpixelformat format; PFdatatype type; };
+    std::vector<Conversion> conversions;   // RGBA8 copies of textures of other formats in this recording          // dedup of texture / array snapshots in this recording
 
     // device
     bool devInit = false, devOk = false;
@@ -328,9 +330,124 @@ void report_device_failure(const char *what, cudaError_t e)
     }
 }
 
-Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
+// ---------------------------------------------------------------------------
+// texel formats.  The device samples RGBA8; a texture in another format is
+// converted when it is snapshotted, texel by texel, to the value the
+// reference's SIMD pixel getter returns for it (src/internal/pixel.h:
+// 2253-3097), including its reads: a single-channel unsigned-byte getter takes
+// the top byte of a 32-bit load (the texel three places further on), the
+// luminance-alpha one the next texel's pair, half and float channels scale by
+// 255 and round to nearest even without clamping, and the BGR half/float
+// getters return the channels in memory order.  Bytes past the end of the
+// caller's buffer read 0.  BGRA / unsigned byte uses the per-texel swizzle
+// (the reference's shuffle mask repeats the first texel of each half vector,
+// src/internal/simd.h:564-583).
+// ---------------------------------------------------------------------------
+int texel_bytes(PFpixelformat f, PFdatatype t)
 {
-    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { set_err(PF_INVALID_ENUM); return nullptr; }
+    int comps;
+    switch (f) {
+    case PF_RED: case PF_GREEN: case PF_BLUE: case PF_ALPHA: case PF_LUMINANCE: comps = 1; break;
+    case PF_LUMINANCE_ALPHA: comps = 2; break;
+    case PF_RGB: case PF_BGR: comps = 3; break;
+    case PF_RGBA: case PF_BGRA: comps = 4; break;
+    default: return 0;
+    }
+    switch (t) {
+    case PF_UNSIGNED_BYTE: return comps;
+    case PF_HALF_FLOAT: return 2 * comps;
+    case PF_FLOAT: return 4 * comps;
+    case PF_UNSIGNED_SHORT_5_6_5: return (f == PF_RGB || f == PF_BGR) ? 2 : 0;
+    case PF_UNSIGNED_SHORT_5_5_5_1: case PF_UNSIGNED_SHORT_4_4_4_4: return (f == PF_RGBA || f == PF_BGRA) ? 2 : 0;
+    default: return 0;
+    }
+}
+
+struct TexelSrc {
+    const uint8_t *p;
+    int64_t n;                  // bytes
+    uint32_t byte(int64_t b) const { return (b >= 0 && b < n) ? p[b] : 0u; }
+    uint32_t word(int64_t b) const { return byte(b) | byte(b + 1) << 8 | byte(b + 2) << 16 | byte(b + 3) << 24; }
+};
+
+// pfmHalfToFloat (src/pfm.h:129-161): denormals flush to zero
+inline float half_to_float(uint32_t h)
+{
+    const uint32_t sgn = (h & 0x8000u) << 16;
+    const int32_t em = (int32_t)(h & 0x7fffu);
+    int32_t r = (int32_t)((uint32_t)(em + (112 << 10)) << 13);
+    r = (em < (1 << 10)) ? 0 : r;
+    r += (em >= (31 << 10)) ? (112 << 23) : 0;
+    const uint32_t u = sgn | (uint32_t)r;
+    float f; std::memcpy(&f, &u, 4);
+    return f;
+}
+// CVTPS2DQ: round to nearest even, 0x80000000 for NaN or out of range
+inline uint32_t cvt_rne_u(float x)
+{
+    if (!(x > -2147483648.0f && x < 2147483648.0f)) return 0x80000000u;
+    return (uint32_t)(int32_t)std::nearbyint(x);
+}
+
+uint32_t texel_rgba8(PFpixelformat f, PFdatatype t, const TexelSrc &s, int64_t o)
+{
+    auto h8 = [&](int64_t i) { return cvt_rne_u(half_to_float(s.word(2 * i) & 0xffffu) * 255.0f); };
+    auto f8 = [&](int64_t i) { const uint32_t u = s.word(4 * i); float x; std::memcpy(&x, &u, 4); return cvt_rne_u(x * 255.0f); };
+    switch (t) {
+    case PF_UNSIGNED_BYTE:
+        switch (f) {
+        case PF_RED: return (s.word(o) >> 24) | 0xff000000u;
+        case PF_GREEN: return ((s.word(o) >> 24) << 8) | 0xff000000u;
+        case PF_BLUE: return ((s.word(o) >> 24) << 16) | 0xff000000u;
+        case PF_ALPHA: return s.word(o) << 24;
+        case PF_LUMINANCE: { const uint32_t v = s.word(o) >> 24; return v | v << 8 | v << 16 | 0xff000000u; }
+        case PF_LUMINANCE_ALPHA: { const uint32_t w = s.word(2 * o), l = (w >> 16) & 255u; return l | l << 8 | l << 16 | (w & 0xff000000u); }
+        case PF_RGB: return (s.word(3 * o) & 0xffffffu) | 0xff000000u;
+        case PF_BGR: { const uint32_t w = s.word(3 * o); return ((w >> 16) & 255u) | (w & 0xff00u) | (w & 255u) << 16 | 0xff000000u; }
+        case PF_RGBA: return s.word(4 * o);
+        case PF_BGRA: { const uint32_t w = s.word(4 * o); return ((w >> 16) & 255u) | (w & 0xff00u) | (w & 255u) << 16 | (w & 0xff000000u); }
+        default: return 0;
+        }
+    case PF_HALF_FLOAT:
+    case PF_FLOAT: {
+        auto c8 = [&](int64_t i) { return t == PF_HALF_FLOAT ? h8(i) : f8(i); };
+        switch (f) {
+        case PF_RED: return c8(o) | 0xff000000u;
+        case PF_GREEN: return c8(o) << 8 | 0xff000000u;
+        case PF_BLUE: return c8(o) << 16 | 0xff000000u;
+        case PF_ALPHA: return c8(o) << 24;
+        case PF_LUMINANCE: { const uint32_t v = c8(o); return 0xff000000u | v << 16 | v << 8 | v; }
+        case PF_LUMINANCE_ALPHA: { const uint32_t v = c8(2 * o), a = c8(2 * o + 1); return a << 24 | v << 16 | v << 8 | v; }
+        case PF_RGB: case PF_BGR: return 0xff000000u | c8(3 * o + 2) << 16 | c8(3 * o + 1) << 8 | c8(3 * o);
+        case PF_RGBA: return c8(4 * o + 3) << 24 | c8(4 * o + 2) << 16 | c8(4 * o + 1) << 8 | c8(4 * o);
+        case PF_BGRA: return c8(4 * o + 3) << 24 | c8(4 * o) << 16 | c8(4 * o + 1) << 8 | c8(4 * o + 2);
+        default: return 0;
+        }
+    }
+    case PF_UNSIGNED_SHORT_5_6_5: {
+        const uint32_t w = s.word(2 * o);
+        const uint32_t hi = ((w & 0xf800u) >> 11) << 3, g = ((w & 0x07e0u) >> 5) << 2, lo = (w & 0x1fu) << 3;
+        return (f == PF_RGB) ? (0xff000000u | lo << 16 | g << 8 | hi) : (0xff000000u | hi << 16 | g << 8 | lo);
+    }
+    case PF_UNSIGNED_SHORT_5_5_5_1: {
+        const uint32_t w = s.word(2 * o);
+        const uint32_t c0 = ((w >> 11) & 0x1fu) * 8u, c1 = ((w >> 6) & 0x1fu) * 8u, c2 = ((w >> 1) & 0x1fu) * 8u, a = (w & 1u) * 255u;
+        return (f == PF_RGBA) ? (a << 24 | c2 << 16 | c1 << 8 | c0) : (a << 24 | c0 << 16 | c1 << 8 | c2);
+    }
+    case PF_UNSIGNED_SHORT_4_4_4_4: {
+        const uint32_t w = s.word(2 * o);
+        const uint32_t c0 = ((w >> 12) & 0xfu) * 17u, c1 = ((w >> 8) & 0xfu) * 17u, c2 = ((w >> 4) & 0xfu) * 17u, a = (w & 0xfu) * 17u;
+        return (f == PF_RGBA) ? (a << 24 | c2 << 16 | c1 << 8 | c0) : (a << 24 | c0 << 16 | c1 << 8 | c2);
+    }
+    default: return 0;
+    }
+}
+
+// Framebuffers are RGBA / unsigned byte; textures may use any format the
+// reference has a SIMD getter for.
+Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, bool sampled)
+{
+    if (sampled ? !texel_bytes(f, t) : !(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { set_err(PF_INVALID_ENUM); return nullptr; }
     Tex *x = new Tex();
     x->pixels = pixels; x->w = w; x->h = h; x->format = f; x->type = t;
     x->tx = 1.0f / (float)w; x->ty = 1.0f / (float)h;
@@ -464,6 +581,29 @@ int64_t snapshot(Renderer *r, const void *p, size_t bytes)
 }
 int64_t snapshot(Ctx *c, const void *p, size_t bytes) { return snapshot(c->rend, p, bytes); }
 
+// RGBA8 snapshot of a texture: its own bytes, or the converted texels of
+// another format (from a snapshot of its bytes, converted once per recording).
+int64_t snapshot_texture(Renderer *r, const Tex *t)
+{
+    const size_t n = (size_t)t->w * t->h;
+    if (t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE) return snapshot(r, t->pixels, n * 4);
+    const int64_t raw = snapshot(r, t->pixels, n * (size_t)texel_bytes(t->format, t->type));
+    for (auto &cv : r->conversions)
+        if (cv.rawOff == raw && cv.format == t->format && cv.type == t->type) return cv.off;
+    const int64_t off = r->staging.alloc(n * 4);
+    const TexelSrc src{ r->staging.base + raw, (int64_t)(n * (size_t)texel_bytes(t->format, t->type)) };
+    uint32_t *dst = (uint32_t *)(r->staging.base + off);
+    const size_t chunk = 1 << 16;
+    const int parts = (int)((n + chunk - 1) / chunk);
+    auto work = [&](int i) {
+        const size_t b = (size_t)i * chunk, e = std::min(n, b + chunk);
+        for (size_t k = b; k < e; k++) dst[k] = texel_rgba8(t->format, t->type, src, (int64_t)k);
+    };
+    if (parts > 1) Pool::get().run(parts, work); else work(0);
+    r->conversions.push_back({ raw, off, t->format, t->type });
+    return off;
+}
+
 void update_matrices(Ctx *c, bool withNormal)                      // context.c:96-111
 {
     if (c->modelUsed) {
@@ -496,7 +636,7 @@ int snapshot_state(Ctx *c)
     Tex *t = ((c->state & PF_TEXTURE_2D) && c->texture) ? c->texture : nullptr;
     if (t) {
         fl |= PFS_TEXTURE;
-        r.texOff = snapshot(c, t->pixels, (size_t)t->w * t->h * 4);
+        r.texOff = snapshot_texture(c->rend, t);
         s.texW = t->w; s.texH = t->h; s.texWrap = t->wrap; s.texFilter = t->filter; s.texTx = t->tx; s.texTy = t->ty;
     }
     if (c->state & PF_BLEND) fl |= PFS_BLEND;
@@ -729,7 +869,7 @@ void drop_mirror(const void *tex)
 
 void discard_recording(Renderer *r)
 {
-    r->states.clear(); r->segs.clear(); r->cmds.clear(); r->snaps.clear();
+    r->states.clear(); r->segs.clear(); r->cmds.clear(); r->snaps.clear(); r->conversions.clear();
     r->staging.used = 0;
 }
 
@@ -1241,7 +1381,7 @@ PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFda
 {
     Ctx *c = new Ctx();
     Ctx *prev = G; G = c;
-    c->mainFB.texture = tex_new(buf, w, h, f, t);
+    c->mainFB.texture = tex_new(buf, w, h, f, t, false);
     G = prev;
     if (!c->mainFB.texture) { delete c; return nullptr; }
     ((Tex *)c->mainFB.texture)->isMain = true;
@@ -1293,7 +1433,7 @@ void pfSetMainBuffer(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatyp
     }
     drop_mirror(old);
     delete old;
-    G->mainFB.texture = tex_new(buf, w, h, f, t);
+    G->mainFB.texture = tex_new(buf, w, h, f, t, false);
     if (G->mainFB.texture) ((Tex *)G->mainFB.texture)->isMain = true;
     G->aux = nullptr;
 }
@@ -1999,7 +2139,7 @@ PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype
     if (!pinned) { cudaGetLastError(); px = std::malloc(n * 4); }
     if (!px) { set_err(PF_ERROR_OUT_OF_MEMORY); return fb; }
     std::memset(px, 0, n * 4);
-    Tex *tx = tex_new(px, w, h, f, t);
+    Tex *tx = tex_new(px, w, h, f, t, false);
     tx->ownsPinned = pinned;
     float *z = nullptr;
     bool zp = cudaMallocHost((void **)&z, n * 4) == cudaSuccess;
@@ -2080,7 +2220,7 @@ void pfSetFramebufferPixel(PFframebuffer *fb, PFsizei x, PFsizei y, PFcolor col)
 }
 
 // --- textures (texture.c) --------------------------------------------------------
-PFtexture pfGenTexture(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t) { return tex_new(pixels, w, h, f, t); }
+PFtexture pfGenTexture(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t) { return tex_new(pixels, w, h, f, t, true); }
 void pfDeleteTexture(PFtexture *tex, PFboolean freeBuffer)
 {
     Tex *t = (Tex *)*tex;

@@ -182,6 +182,60 @@ def kat_clear():
     return lambda lib: _frame(lib, 6, 5, body, init=init)
 
 
+TEX_FORMATS = [(f, t) for f in ("RED", "GREEN", "BLUE", "ALPHA", "LUMINANCE", "LUMINANCE_ALPHA", "RGB", "RGBA",
+                                 "BGR", "BGRA") for t in ("UBYTE", "HALF", "FLOAT")] + \
+              [("RGB", "S565"), ("BGR", "S565"), ("RGBA", "S5551"), ("BGRA", "S5551"), ("RGBA", "S4444"),
+               ("BGRA", "S4444")]
+_FMT = dict(RED=0, GREEN=1, BLUE=2, ALPHA=3, LUMINANCE=4, LUMINANCE_ALPHA=5, RGB=6, RGBA=7, BGR=8, BGRA=9)
+_TYP = dict(UBYTE=0, S565=2, S5551=3, S4444=4, HALF=9, FLOAT=10)
+_COMPS = dict(RED=1, GREEN=1, BLUE=1, ALPHA=1, LUMINANCE=1, LUMINANCE_ALPHA=2, RGB=3, RGBA=4, BGR=3, BGRA=4)
+
+
+def tex_format_data(f, t, w=8, h=8, seed=3):
+    """Texels of format f / type t (values slightly outside [0, 1] for the
+    floating types), padded so that the getters' wide loads stay inside."""
+    rng = np.random.default_rng(seed + 17 * _FMT[f] + _TYP[t])
+    n = w * h
+    if t == "UBYTE":
+        d = rng.integers(0, 256, n * _COMPS[f] + 8).astype(np.uint8)
+    elif t == "HALF":
+        d = rng.uniform(-0.2, 1.2, n * _COMPS[f] + 8).astype(np.float16)
+    elif t == "FLOAT":
+        d = rng.uniform(-0.2, 1.2, n * _COMPS[f] + 8).astype(np.float32)
+    else:
+        d = rng.integers(0, 65536, n + 8).astype(np.uint16)
+    d[-8:] = 0
+    return d
+
+
+def kat_texfmt(f, t, filt=A.PF_NEAREST):
+    """A textured quad sampling an 8x8 texture of format f / type t
+    (src/texture.c:30-70, src/internal/pixel.h:2253-3097)."""
+    data = tex_format_data(f, t)
+    handle = {}
+
+    def body(lib):
+        lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+        lib.pfDisable(A.PF_CULL_FACE)
+        tx = lib.pfGenTexture(_ptr(data), 8, 8, _FMT[f], _TYP[t])
+        handle["t"] = tx
+        lib.pfTextureParameter(tx, A.PF_REPEAT, filt)
+        lib.pfBindTexture(tx)
+        lib.pfEnable(A.PF_TEXTURE_2D)
+        quad = [(-1.0, -1.0, 0.0), (1.0, -1.0, 0.0), (1.0, 1.0, 0.0),
+                (-1.0, -1.0, 0.0), (1.0, 1.0, 0.0), (-1.0, 1.0, 0.0)]
+        uvs = [(0.0, 0.0), (0.97, 0.0), (0.97, 0.97), (0.0, 0.0), (0.97, 0.97), (0.0, 0.97)]
+        _tri(lib, quad, [(255, 255, 255, 255)], uvs)
+
+    def run(lib):
+        fr = _frame(lib, 16, 16, body)
+        if handle.get("t"):
+            th = C.c_void_p(handle["t"])
+            lib.pfDeleteTexture(C.byref(th), False)
+        return fr
+    return run
+
+
 def mix(seed):
     from mixscenes import mix_case, run_mix
     return lambda lib: run_mix(lib, mix_case(seed))
@@ -209,6 +263,10 @@ def cases() -> dict:
                     ("lequal", A.PF_LEQUAL), ("greater", A.PF_GREATER), ("gequal", A.PF_GEQUAL)):
         c[f"kat_depth_{name}"] = kat_depth(f)
     c["kat_clear"] = kat_clear()
+    for f, t in TEX_FORMATS:
+        if (f, t) == ("BGRA", "UBYTE"):
+            continue   # the reference repeats one texel per half vector here (simd.h:564-583); pinned to the per-texel swizzle
+        c[f"kat_texfmt_{f}_{t}"] = kat_texfmt(f, t)
     c["soup256"] = _scene(SoupScene())
     c["soup128_nocull_flat_lequal"] = _scene(SoupScene(width=128, height=128, ntris=600, seed=11, cull=False,
                                                        shade=A.PF_FLAT, depth_func=A.PF_LEQUAL))

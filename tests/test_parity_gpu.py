@@ -151,3 +151,14 @@ def test_tile_overfull_draw_is_split(gpu, oracle):
     assert gpu.pfGetDeviceStatus() == 0
     assert got.stats["draw_splits"] >= 1
     assert_parity(got, ref, exact_color=True, label="overfull tiles")
+
+
+@pytest.mark.parametrize("fmt", [("BGRA", "UBYTE"), ("LUMINANCE_ALPHA", "UBYTE"), ("RGB", "HALF"), ("RGBA", "FLOAT"),
+                                 ("BGRA", "S4444")])
+def test_texture_formats_bilinear(gpu, oracle, fmt):
+    """Non-RGBA8 textures (converted per the reference's getters when
+    snapshotted) under both filters, GPU against the oracle."""
+    from cases import kat_texfmt
+    for filt in (A.PF_NEAREST, A.PF_BILINEAR):
+        run = kat_texfmt(*fmt, filt=filt)
+        assert_parity(run(gpu), run(oracle), exact_color=True, label=f"{fmt} filter {filt}")
