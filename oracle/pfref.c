@@ -121,6 +121,7 @@ typedef struct {
     PFblendmode blend; PFdepthmode depthFunc;
     PFerrcode err; PFuint state;
     PFboolean depthMask;
+    float pointSize, lineWidth;
     PFstats stats;
 } RCtx;
 
@@ -906,15 +907,294 @@ static void tri_strip(RCtx *c, PFface face, int n)  /* triangles.c:137-152 */
     }
 }
 
-/* pfiProcessAndRasterize (src/internal/context/context.c:95-244), fill mode. */
+/* ------------------------------------------------------------------------ */
+/* points and lines (src/internal/primitives/points.c, lines.c)              */
+/* ------------------------------------------------------------------------ */
+
+/* SISD depth tests (src/internal/depth.h:27-74): NOTEQUAL is a real != here */
+static int depth_sisd(PFdepthmode f, float src, float dst)
+{
+    switch (f) {
+    case PF_EQUAL: return src == dst;
+    case PF_NOTEQUAL: return src != dst;
+    case PF_LESS: return src < dst;
+    case PF_LEQUAL: return src <= dst;
+    case PF_GREATER: return src > dst;
+    default: return src >= dst;
+    }
+}
+
+/* SISD blending (src/internal/blend.h:27-126) */
+static uint32_t blend_sisd(PFblendmode m, uint32_t src, uint32_t dst)
+{
+    int32_t o[4];
+    for (int i = 0; i < 4; i++) {
+        const int32_t s = (int32_t)ch(src, i), d = (int32_t)ch(dst, i);
+        int32_t v;
+        switch (m) {
+        case PF_BLEND_AVERAGE: v = (s + d) >> 1; break;
+        case PF_BLEND_ALPHA: {
+            const uint32_t a = ch(src, 3) + 1, ia = 256 - a;
+            v = (int32_t)((a * (uint32_t)(i == 3 ? 255 : s) + ia * (uint32_t)d) >> 8);
+            break;
+        }
+        case PF_BLEND_ADD: v = (d + s) < 255 ? (d + s) : 255; break;
+        case PF_BLEND_SUB: v = (d - s) > 0 ? (d - s) : 0; break;
+        case PF_BLEND_MUL: v = (s * d) / 255; break;
+        case PF_BLEND_SCREEN: { int32_t t = ((d * (255 - s)) >> 8) + s; v = t < 255 ? t : 255; break; }
+        case PF_BLEND_LIGHTEN: v = s > d ? s : d; break;
+        default: v = s < d ? s : d; break;
+        }
+        o[i] = v & 255;
+    }
+    return (uint32_t)o[0] | (uint32_t)o[1] << 8 | (uint32_t)o[2] << 16 | (uint32_t)o[3] << 24;
+}
+
+/* One pixel of a point or line.  Pixels outside the framebuffer are not
+ * drawn (the reference writes them at y*w + x, outside its buffers or
+ * wrapped into a neighbouring row). */
+static void lp_pixel(RCtx *c, int32_t x, int32_t y, float z, uint32_t col, int test)
+{
+    RTex *fbt = (RTex *)c->current->texture;
+    if (x < 0 || y < 0 || (uint32_t)x >= fbt->w || (uint32_t)y >= fbt->h) return;
+    const size_t p = (size_t)y * fbt->w + (size_t)x;
+    uint32_t *pb = (uint32_t *)fbt->pixels;
+    float *zb = c->current->zbuffer;
+    c->stats.fragments++;
+    if (test && !depth_sisd(c->depthFunc, z, zb[p])) return;
+    if (c->state & PF_BLEND) col = blend_sisd(c->blend, col, pb[p]);
+    pb[p] = col;
+    if (c->depthMask) zb[p] = z;
+}
+
+/* Process_ProjectPoint (points.c:44-81) */
+static int project_point(const RCtx *c, const RVert *v, float *sx, float *sy, float *z)
+{
+    float h[4];
+    v4_transform(h, v->position, c->mvp);
+    if (h[3] != 1.0f) {
+        for (int i = 0; i < 3; i++) if (h[i] < -h[3] || h[i] > h[3]) return 0;
+        const float invW = 1.0f / h[3];
+        h[0] = h[0] * invW; h[1] = h[1] * invW;
+    }
+    *sx = ((float)c->vpPos[0] + (h[0] + 1.0f) * 0.5f * (float)c->vpDim[0]) + 0.5f;
+    *sy = ((float)c->vpPos[1] + (1.0f - h[1]) * 0.5f * (float)c->vpDim[1]) + 0.5f;
+    *z = h[2];
+    return *sx >= (float)c->vpMin[0] && *sy >= (float)c->vpMin[1] && *sx <= (float)c->vpMax[0] && *sy <= (float)c->vpMax[1];
+}
+
+/* Rasterize_Point_{DEPTH,NODEPTH} (points.c:85-183) */
+static void raster_point(RCtx *c, const RVert *v)
+{
+    float sx, sy, z;
+    if (!project_point(c, v, &sx, &sy, &z)) return;
+    const int32_t cx = ox_ftoi(sx), cy = ox_ftoi(sy);
+    const uint32_t col = col_pack(v->color);
+    const int test = (c->state & PF_DEPTH_TEST) != 0;
+    if (c->pointSize <= 1.0f) { lp_pixel(c, cx, cy, z, col, test); return; }
+    const float r = c->pointSize * 0.5f, rSq = r * r;
+    const int32_t ir = ox_ftoi(r);
+    for (int32_t y = -ir; y <= ir; y++)
+        for (int32_t x = -ir; x <= ir; x++)
+            if ((float)(y * y + x * x) <= rSq) lp_pixel(c, cx + x, cy + y, z, col, test);
+}
+
+static void screen_map(const RCtx *c, RVert *v)
+{
+    v->screen[0] = ((float)c->vpPos[0] + (v->homogeneous[0] + 1.0f) * 0.5f * (float)c->vpDim[0]) + 0.5f;
+    v->screen[1] = ((float)c->vpPos[1] + (1.0f - v->homogeneous[1]) * 0.5f * (float)c->vpDim[1]) + 0.5f;
+}
+
+/* Helper_EncodeClip2D (lines.c:116-125): 1 left, 2 right, 4 below (y > yMax),
+ * 8 above (y < yMin) */
+static uint32_t clip_code(const float *sc, int32_t xMin, int32_t yMin, int32_t xMax, int32_t yMax)
+{
+    uint32_t code = 0;
+    if (sc[0] < (float)xMin) code |= 1;
+    if (sc[0] > (float)xMax) code |= 2;
+    if (sc[1] < (float)yMin) code |= 8;
+    if (sc[1] > (float)yMax) code |= 4;
+    return code;
+}
+
+/* Process_ClipLine2D (lines.c:158-223), Cohen-Sutherland in screen space
+ * with the reference's assignments (a point below the viewport moves to
+ * its top row and the reverse).  Bounded to 32 rounds (the reference loops
+ * until it accepts or rejects). */
+static int clip_line_2d(const RCtx *c, RVert *v1, RVert *v2)
+{
+    const int32_t xMin = c->vpMin[0], yMin = c->vpMin[1], xMax = c->vpMax[0], yMax = c->vpMax[1];
+    float m = 0.0f;
+    if (v1->screen[0] != v2->screen[0]) m = (v2->screen[1] - v1->screen[1]) / (v2->screen[0] - v1->screen[0]);
+    for (int round = 0; round < 32; round++) {
+        uint32_t code0 = clip_code(v1->screen, xMin, yMin, xMax, yMax), code1 = clip_code(v2->screen, xMin, yMin, xMax, yMax);
+        if ((code0 | code1) == 0) return 1;
+        if (code0 & code1) return 0;
+        if (code0 == 0) {
+            uint32_t t = code0; code0 = code1; code1 = t;
+            RVert tv = *v1; *v1 = *v2; *v2 = tv;
+        }
+        if (code0 & 1) {
+            v1->screen[1] = v1->screen[1] + ((float)xMin - v1->screen[0]) * m;
+            v1->screen[0] = (float)xMin;
+        } else if (code0 & 2) {
+            v1->screen[1] = v1->screen[1] + ((float)xMax - v1->screen[0]) * m;
+            v1->screen[0] = (float)xMax;
+        } else if (code0 & 4) {
+            if (m != 0.0f) v1->screen[0] = v1->screen[0] + ((float)yMin - v1->screen[1]) / m;
+            v1->screen[1] = (float)yMin;
+        } else if (code0 & 8) {
+            if (m != 0.0f) v1->screen[0] = v1->screen[0] + ((float)yMax - v1->screen[1]) / m;
+            v1->screen[1] = (float)yMax;
+        }
+    }
+    return 0;
+}
+
+/* Helper_ClipCoord3D (lines.c:127-150) */
+static int clip_coord_3d(float q, float p, float *t1, float *t2)
+{
+    if (fabsf(p) < CLIP_EPS) return !(q < -CLIP_EPS);
+    const float r = q / p;
+    if (p < 0) {
+        if (r > *t2) return 0;
+        if (r > *t1) *t1 = r;
+    } else {
+        if (r < *t1) return 0;
+        if (r < *t2) *t2 = r;
+    }
+    return 1;
+}
+
+/* Process_ClipLine3D (lines.c:225-262), Liang-Barsky in clip space */
+static int clip_line_3d(RVert *v1, RVert *v2)
+{
+    float t1 = 0.0f, t2 = 1.0f, d[4];
+    const float *a = v1->homogeneous;
+    for (int i = 0; i < 4; i++) d[i] = v2->homogeneous[i] - a[i];
+    if (!clip_coord_3d(a[3] - a[0], -d[3] + d[0], &t1, &t2)) return 0;
+    if (!clip_coord_3d(a[3] + a[0], -d[3] - d[0], &t1, &t2)) return 0;
+    if (!clip_coord_3d(a[3] - a[1], -d[3] + d[1], &t1, &t2)) return 0;
+    if (!clip_coord_3d(a[3] + a[1], -d[3] - d[1], &t1, &t2)) return 0;
+    if (!clip_coord_3d(a[3] - a[2], -d[3] + d[2], &t1, &t2)) return 0;
+    if (!clip_coord_3d(a[3] + a[2], -d[3] - d[2], &t1, &t2)) return 0;
+    if (t2 < 1.0f) for (int i = 0; i < 4; i++) v2->homogeneous[i] = v1->homogeneous[i] + d[i] * t2;
+    if (t1 > 0.0f) for (int i = 0; i < 4; i++) v1->homogeneous[i] = v1->homogeneous[i] + d[i] * t1;
+    return 1;
+}
+
+/* Process_ProjectAndClipLine (lines.c:264-300) */
+static int project_clip_line(const RCtx *c, RVert *l)
+{
+    for (int i = 0; i < 2; i++) v4_transform(l[i].homogeneous, l[i].position, c->mvp);
+    if (l[0].homogeneous[3] == 1.0f && l[1].homogeneous[3] == 1.0f) {
+        screen_map(c, &l[0]); screen_map(c, &l[1]);
+        return clip_line_2d(c, &l[0], &l[1]);
+    }
+    if (!clip_line_3d(&l[0], &l[1])) return 0;
+    for (int i = 0; i < 2; i++) {
+        const float invW = 1.0f / l[i].homogeneous[3];
+        l[i].homogeneous[0] = l[i].homogeneous[0] * invW;
+        l[i].homogeneous[1] = l[i].homogeneous[1] * invW;
+    }
+    screen_map(c, &l[0]); screen_map(c, &l[1]);
+    return 1;
+}
+
+/* Rasterize_Line_{DEPTH,NODEPTH} (lines.c:304-431): DDA in 16.16 fixed point */
+static void raster_line_thin(RCtx *c, const RVert *v1, const RVert *v2, int test)
+{
+    const int32_t x1 = ox_ftoi(v1->screen[0]), y1 = ox_ftoi(v1->screen[1]);
+    const int32_t x2 = ox_ftoi(v2->screen[0]), y2 = ox_ftoi(v2->screen[1]);
+    const float z1 = v1->homogeneous[2], z2 = v2->homogeneous[2];
+    const PFcolor c1 = v1->color, c2 = v2->color;
+    int32_t shortLen = y2 - y1, longLen = x2 - x1;
+    int yLonger = 0;
+    if (ox_iabs(shortLen) > ox_iabs(longLen)) { int32_t t = shortLen; shortLen = longLen; longLen = t; yLonger = 1; }
+    const float invEndVal = 1.0f / (float)longLen;
+    const int32_t endVal = longLen;
+    int32_t sgnInc = 1;
+    if (longLen < 0) { longLen = -longLen; sgnInc = -1; }
+    const int32_t decInc = (longLen == 0) ? 0 : (int32_t)((uint32_t)shortLen << 16) / longLen;
+    int32_t j = 0;
+    for (int32_t i = 0; i != endVal; i += sgnInc, j += decInc) {
+        const float t = (float)i * invEndVal;
+        const int32_t x = yLonger ? x1 + (j >> 16) : x1 + i;
+        const int32_t y = yLonger ? y1 + i : y1 + (j >> 16);
+        const float z = z1 + t * (z2 - z1);
+        const uint8_t o[4] = { ox_ftoub((float)c1.r + t * (float)(c2.r - c1.r)), ox_ftoub((float)c1.g + t * (float)(c2.g - c1.g)),
+                               ox_ftoub((float)c1.b + t * (float)(c2.b - c1.b)), ox_ftoub((float)c1.a + t * (float)(c2.a - c1.a)) };
+        lp_pixel(c, x, y, z, (uint32_t)o[0] | (uint32_t)o[1] << 8 | (uint32_t)o[2] << 16 | (uint32_t)o[3] << 24, test);
+    }
+}
+
+/* pfiProcessRasterize_LINE (lines.c:57-79) and the thick variants
+ * (lines.c:433-531): the centre line is always depth-tested */
+static void raster_line(RCtx *c, const RVert *a, const RVert *b, int *rejected)
+{
+    RVert l[2] = { *a, *b };
+    if (!project_clip_line(c, l)) { if (rejected) *rejected = 1; return; }
+    const int test = (c->state & PF_DEPTH_TEST) != 0;
+    if (!(c->lineWidth > 1.5f)) { raster_line_thin(c, &l[0], &l[1], test); return; }
+    const int32_t x1 = ox_ftoi(l[0].screen[0]), y1 = ox_ftoi(l[0].screen[1]);
+    const int32_t x2 = ox_ftoi(l[1].screen[0]), y2 = ox_ftoi(l[1].screen[1]);
+    const int32_t dx = x2 - x1, dy = y2 - y1;
+    raster_line_thin(c, &l[0], &l[1], 1);
+    const float rs = 1.0f / sqrtf((float)(dx * dx + dy * dy));
+    if (dx != 0 && ox_iabs(dy / dx) < 1) {
+        const int32_t wy = ox_ftoi((c->lineWidth - 1.0f) * rs * (float)ox_iabs(dx)) >> 1;
+        for (int32_t i = 1; i <= wy; i++) {
+            RVert t1 = l[0], t2 = l[1];
+            t1.screen[1] -= (float)i; t2.screen[1] -= (float)i;
+            raster_line_thin(c, &t1, &t2, test);
+            t1 = l[0]; t2 = l[1];
+            t1.screen[1] += (float)i; t2.screen[1] += (float)i;
+            raster_line_thin(c, &t1, &t2, test);
+        }
+    } else if (dy != 0) {
+        const int32_t wx = ox_ftoi((c->lineWidth - 1.0f) * rs * (float)ox_iabs(dy)) >> 1;
+        for (int32_t i = 1; i <= wx; i++) {
+            RVert t1 = l[0], t2 = l[1];
+            t1.screen[0] -= (float)i; t2.screen[0] -= (float)i;
+            raster_line_thin(c, &t1, &t2, test);
+            t1 = l[0]; t2 = l[1];
+            t1.screen[0] += (float)i; t2.screen[0] += (float)i;
+            raster_line_thin(c, &t1, &t2, test);
+        }
+    }
+}
+
+/* pfiProcessRasterize_POLY_POINTS / _POLY_LINES (points.c:33-41, lines.c:81-110):
+ * the edges stop at the first one clipped away */
+static void poly_points(RCtx *c, int n) { for (int i = 0; i < n; i++) raster_point(c, &c->vbuf[i]); }
+static void poly_lines(RCtx *c, int n)
+{
+    for (int i = 0; i < n; i++) {
+        int rejected = 0;
+        raster_line(c, &c->vbuf[i], &c->vbuf[(i + 1) % n], &rejected);
+        if (rejected) return;
+    }
+}
+
+static void poly_pass(RCtx *c, PFface face, int n)
+{
+    switch (c->polygonMode[face]) {
+    case PF_POINT: poly_points(c, n); break;
+    case PF_LINE: poly_lines(c, n); break;
+    default: if (n == 3) tri_from(c, face, 0, 1, 2); else tri_fan(c, face, 2); break;
+    }
+}
+
+/* pfiProcessAndRasterize (src/internal/context/context.c:95-244) */
 static void process_and_raster(RCtx *c)
 {
     PFface f = (c->state & PF_CULL_FACE) ? (PFface)!c->cullFace : PF_FRONT_AND_BACK;
     switch (c->drawMode) {
+    case PF_POINTS: raster_point(c, &c->vbuf[0]); break;
+    case PF_LINES: raster_line(c, &c->vbuf[0], &c->vbuf[1], NULL); break;
     case PF_TRIANGLES:
-        if (f == PF_FRONT_AND_BACK) {
-            for (int i = 0; i < 2; i++) if (c->polygonMode[i] == PF_FILL) tri_from(c, (PFface)i, 0, 1, 2);
-        } else if (c->polygonMode[f] == PF_FILL) tri_from(c, f, 0, 1, 2);
+        if (f == PF_FRONT_AND_BACK) { poly_pass(c, PF_FRONT, 3); poly_pass(c, PF_BACK, 3); }
+        else poly_pass(c, f, 3);
         break;
     case PF_TRIANGLE_FAN:
         if (f == PF_FRONT_AND_BACK) { tri_fan(c, PF_FRONT, 2); tri_fan(c, PF_BACK, 2); } else tri_fan(c, f, 2);
@@ -923,9 +1203,8 @@ static void process_and_raster(RCtx *c)
         if (f == PF_FRONT_AND_BACK) { tri_strip(c, PF_FRONT, 2); tri_strip(c, PF_BACK, 2); } else tri_strip(c, f, 2);
         break;
     case PF_QUADS:
-        if (f == PF_FRONT_AND_BACK) {
-            for (int i = 0; i < 2; i++) if (c->polygonMode[i] == PF_FILL) tri_fan(c, (PFface)i, 2);
-        } else if (c->polygonMode[f] == PF_FILL) tri_fan(c, f, 2);
+        if (f == PF_FRONT_AND_BACK) { poly_pass(c, PF_FRONT, 4); poly_pass(c, PF_BACK, 4); }
+        else poly_pass(c, f, 4);
         break;
     case PF_QUAD_FAN:
         if (f == PF_FRONT_AND_BACK) { tri_fan(c, PF_FRONT, 4); tri_fan(c, PF_BACK, 4); } else tri_fan(c, f, 4);
@@ -934,7 +1213,6 @@ static void process_and_raster(RCtx *c)
         if (f == PF_FRONT_AND_BACK) { tri_strip(c, PF_FRONT, 4); tri_strip(c, PF_BACK, 4); } else tri_strip(c, f, 4);
         break;
     default:
-        c->err = PF_INVALID_OPERATION;   /* points and lines are outside the pipeline */
         break;
     }
 }
@@ -1006,6 +1284,7 @@ PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFda
     c->blend = PF_BLEND_ALPHA; c->depthFunc = PF_LESS;
     PFcolor cc = { 0, 0, 0, 255 }; c->clearColor = cc; c->clearDepth = FLT_MAX;
     c->polygonMode[0] = c->polygonMode[1] = PF_FILL;
+    c->pointSize = 1.0f; c->lineWidth = 1.0f;
     PFcolor white = { 255, 255, 255, 255 }; c->curColor = white;
     for (int i = 0; i < MAX_LIGHTS; i++) {
         RLight *l = &c->lights[i]; memset(l, 0, sizeof *l);
@@ -1133,7 +1412,9 @@ void pfGetIntegerv(PFenum p, PFint *v)
     case PF_CURRENT_NORMAL: for (int i = 0; i < 3; i++) v[i] = G->curNormal[i]; break;        \
     case PF_CURRENT_TEXTURE_COORDS: for (int i = 0; i < 2; i++) v[i] = G->curTex[i]; break;   \
     case PF_CURRENT_RASTER_POSITION: v[0] = 0; v[1] = 0; break;                               \
-    case PF_POINT_SIZE: case PF_LINE_WIDTH: case PF_ZOOM_X: case PF_ZOOM_Y: v[0] = 1; break;  \
+    case PF_POINT_SIZE: v[0] = G->pointSize; break;                                          \
+    case PF_LINE_WIDTH: v[0] = G->lineWidth; break;                                          \
+    case PF_ZOOM_X: case PF_ZOOM_Y: v[0] = 1; break;                                         \
     case PF_PROJECTION_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->proj[i]; break;        \
     case PF_MODELVIEW_MATRIX: { mat4 mv; m_mul(mv, G->model, G->view);                       \
         for (int i = 0; i < 16; i++) { v[i] = mv[i]; } break; }                               \
@@ -1269,8 +1550,8 @@ void pfPolygonMode(PFface f, PFpolygonmode m)
 }
 void pfShadeModel(PFshademode m) { G->shade = m; }
 void pfLightModel(PFlightmode m) { G->lightMode = m; }
-void pfLineWidth(PFfloat w) { if (w <= 0.0f) G->err = PF_INVALID_VALUE; }
-void pfPointSize(PFfloat s) { if (s <= 0.0f) G->err = PF_INVALID_VALUE; }
+void pfLineWidth(PFfloat w) { if (w <= 0.0f) { G->err = PF_INVALID_VALUE; return; } G->lineWidth = w; }   /* context.c:610-626 */
+void pfPointSize(PFfloat s) { if (s <= 0.0f) { G->err = PF_INVALID_VALUE; return; } G->pointSize = s; }
 void pfCullFace(PFface f) { if (f < PF_FRONT || f > PF_BACK) { G->err = PF_INVALID_ENUM; return; } G->cullFace = f; }
 void pfBlendFunc(PFblendmode m) { if (m < PF_BLEND_AVERAGE || m > PF_BLEND_DARKEN) { G->err = PF_INVALID_ENUM; return; } G->blend = m; }
 void pfDepthFunc(PFdepthmode m) { if (m < PF_EQUAL || m > PF_GEQUAL) { G->err = PF_INVALID_ENUM; return; } G->depthFunc = m; }

@@ -241,6 +241,11 @@ def mix(seed):
     return lambda lib: run_mix(lib, mix_case(seed))
 
 
+def lp(seed):
+    from lpscenes import lp_case, run_lp
+    return lambda lib: run_lp(lib, lp_case(seed))
+
+
 def _scene(sc, **kw):
     return lambda lib: sc.render(lib, "fbo", **kw)
 
@@ -276,6 +281,8 @@ def cases() -> dict:
     c["phong_320"] = _scene(PhongScene(width=320, height=180, subdiv=4, tex_size=128, fog=False))
     for s in range(40):
         c[f"mix_{s}"] = mix(5000 + s)
+    for s in range(24):
+        c[f"lp_{s}"] = lp(7000 + s)
     return c
 
 

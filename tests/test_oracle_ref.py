@@ -37,3 +37,10 @@ def test_oracle_equals_reference_array_types(oracle, ref_shim, k):
     a, b = run_types(oracle, 40 + k, TYPE_CASES[k]), run_types(ref_shim, 40 + k, TYPE_CASES[k])
     assert (a.depth < 1e29).sum() > 500
     same(a, b, f"types {TYPE_CASES[k]}")
+
+
+@pytest.mark.parametrize("seed", range(0, 160))
+def test_oracle_equals_reference_points_lines(oracle, ref_shim, seed):
+    from lpscenes import lp_case, run_lp
+    case = lp_case(seed)
+    same(run_lp(oracle, case), run_lp(ref_shim, case), f"points/lines {seed} {case}")
