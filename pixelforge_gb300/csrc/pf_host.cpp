@@ -172,6 +172,8 @@ struct SegRec {
     int64_t recordsOff = -1, posOff = -1, nrmOff = -1, uvOff = -1, colOff = -1, idxOff = -1, itemsOff = -1;
     std::vector<int32_t> explicitItems;   // immediate / non-triangle modes, grown while recording
     std::vector<PFVertexIn> records;       // immediate mode vertices
+    std::vector<PFPrim> prebuilt;          // points and lines set up on the host
+    int64_t prebuiltOff = -1;
 };
 
 struct StateRec {
@@ -665,19 +667,28 @@ int snapshot_state(Ctx *c)
     return (int)c->rend->states.size() - 1;
 }
 
-// Face passes of one primitive (internal/context/context.c:95-244): returns
-// the faces to fill, in order.
-int faces_for(const Ctx *c, PFdrawmode mode, int faces[2])
+// Face passes of one primitive (internal/context/context.c:95-244): the
+// faces, in order, and the polygon mode of each (PF_FILL outside
+// PF_TRIANGLES / PF_QUADS, the only modes with a polygon-mode switch).
+int face_passes(const Ctx *c, PFdrawmode mode, int faces[2], PFpolygonmode pm[2])
 {
     const bool cull = (c->state & PF_CULL_FACE) != 0;
     const PFface f = cull ? (PFface)!c->cullFace : PF_FRONT_AND_BACK;
     const bool usesPolyMode = (mode == PF_TRIANGLES || mode == PF_QUADS);
     int n = 0;
-    if (f == PF_FRONT_AND_BACK) {
-        for (int i = 0; i < 2; i++)
-            if (!usesPolyMode || c->polygonMode[i] == PF_FILL) faces[n++] = i;
-    } else if (!usesPolyMode || c->polygonMode[f] == PF_FILL) faces[n++] = f;
-    if (usesPolyMode && n < (f == PF_FRONT_AND_BACK ? 2 : 1)) set_err(PF_INVALID_OPERATION);   // point/line modes
+    if (f == PF_FRONT_AND_BACK) { faces[n++] = PF_FRONT; faces[n++] = PF_BACK; }
+    else faces[n++] = f;
+    for (int k = 0; k < n; k++) pm[k] = usesPolyMode ? c->polygonMode[faces[k]] : PF_FILL;
+    return n;
+}
+
+// Filled faces of a primitive drawn by the device's vertex path alone.
+int fill_faces(const Ctx *c, PFdrawmode mode, int faces[2], bool &allFill)
+{
+    PFpolygonmode pm[2];
+    const int n = face_passes(c, mode, faces, pm);
+    allFill = mode != PF_POINTS && mode != PF_LINES;
+    for (int k = 0; k < n; k++) allFill = allFill && pm[k] == PF_FILL;
     return n;
 }
 
@@ -761,25 +772,292 @@ void push_cmd(Ctx *c, const Cmd &cmd)
     c->openImmSeg = -1;
 }
 
-// pfVertex4fv path: a primitive completed in immediate mode.
-void immediate_primitive(Ctx *c)
+// ---------------------------------------------------------------------------
+// points and lines (src/internal/primitives/points.c, lines.c)
+//
+// Their set-up runs here, on the host, when the primitive is recorded: the
+// projection, the reference's two line clippers and the 16.16 DDA
+// parameters, all in the reference's operation order (this file is built
+// without contraction of multiply-adds).  Each point, thin line and offset
+// line of a thick line becomes one PFPrim record (fields as k_raster's
+// lp_covers reads them) and one explicit item {record, 0, 0, -1} in
+// submission order; the tile rasterizer covers, depth-tests (scalar rules)
+// and blends (scalar rules) their pixels in order with the triangles'.
+// Pixels outside the framebuffer are not drawn (the reference writes them
+// at y*w + x, outside its buffers or wrapped into a neighbouring row).
+// ---------------------------------------------------------------------------
+struct LPVert { float pos[4]; float h[4]; float sx, sy; uint32_t col; };
+
+inline int32_t ftoi_x86(float x)                // cvttss2si: 0x80000000 out of range
 {
-    const PFdrawmode mode = c->drawMode;
+    if (!(x > -2147483649.0f && x < 2147483648.0f)) return INT32_MIN;
+    return (int32_t)x;
+}
+inline int32_t iabs32(int32_t v) { return v < 0 ? (int32_t)(0u - (uint32_t)v) : v; }
+inline int32_t isub32(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+
+void v4_transform(float *dst, const float *v, const float *m)      // pfm.h:1996-2006
+{
+    const float t[4] = {
+        m[0]*v[0] + m[4]*v[1] + m[8]*v[2] + m[12]*v[3],
+        m[1]*v[0] + m[5]*v[1] + m[9]*v[2] + m[13]*v[3],
+        m[2]*v[0] + m[6]*v[1] + m[10]*v[2] + m[14]*v[3],
+        m[3]*v[0] + m[7]*v[1] + m[11]*v[2] + m[15]*v[3] };
+    std::memcpy(dst, t, 16);
+}
+
+// Where set-up records of one recording go.
+struct LPOut {
+    std::vector<PFPrim> &prims;
+    std::vector<int32_t> &items;
+    int32_t W, H;                               // framebuffer the records draw into
+};
+
+// Append record P with pixels in the inclusive box [x0, x1] x [y0, y1]
+// (clipped to the framebuffer; nothing is appended when no pixel remains).
+void lp_emit(LPOut &o, PFPrim &P, int64_t x0, int64_t x1, int64_t y0, int64_t y1)
+{
+    x0 = std::max<int64_t>(x0, 0); y0 = std::max<int64_t>(y0, 0);
+    x1 = std::min<int64_t>(x1, (int64_t)o.W - 1); y1 = std::min<int64_t>(y1, (int64_t)o.H - 1);
+    if (x0 > x1 || y0 > y1) return;
+    P.xMin = (int32_t)x0; P.xMax = (int32_t)(x1 + 1); P.yMin = (int32_t)y0; P.yMax = (int32_t)y1;
+    P.poolBase = 0;
+    const int32_t item[4] = { (int32_t)o.prims.size(), 0, 0, -1 };
+    o.items.insert(o.items.end(), item, item + 4);
+    o.prims.push_back(P);
+}
+
+void screen_map(const Ctx *c, LPVert &v)                           // lines.c:272-298
+{
+    v.sx = ((float)c->vpPos[0] + (v.h[0] + 1.0f) * 0.5f * (float)c->vpDim[0]) + 0.5f;
+    v.sy = ((float)c->vpPos[1] + (1.0f - v.h[1]) * 0.5f * (float)c->vpDim[1]) + 0.5f;
+}
+
+// Rasterize_Point_{DEPTH,NODEPTH} after Process_ProjectPoint (points.c:44-183)
+void lp_point(const Ctx *c, LPOut &o, const LPVert &v)
+{
+    float h[4];
+    v4_transform(h, v.pos, c->mvp);
+    if (h[3] != 1.0f) {
+        for (int i = 0; i < 3; i++) if (h[i] < -h[3] || h[i] > h[3]) return;
+        const float invW = 1.0f / h[3];
+        h[0] = h[0] * invW; h[1] = h[1] * invW;
+    }
+    const float sx = ((float)c->vpPos[0] + (h[0] + 1.0f) * 0.5f * (float)c->vpDim[0]) + 0.5f;
+    const float sy = ((float)c->vpPos[1] + (1.0f - h[1]) * 0.5f * (float)c->vpDim[1]) + 0.5f;
+    if (!(sx >= (float)c->vpMin[0] && sy >= (float)c->vpMin[1] && sx <= (float)c->vpMax[0] && sy <= (float)c->vpMax[1]))
+        return;
+    PFPrim P;
+    std::memset(&P, 0, sizeof P);
+    P.x1 = ftoi_x86(sx); P.y1 = ftoi_x86(sy);
+    P.flags = PFP_POINT | ((c->state & PF_DEPTH_TEST) ? PFP_DEPTH_TEST : 0u);
+    P.z1 = h[2];
+    P.c1 = v.col;
+    int32_t ir = 0;
+    if (c->pointSize <= 1.0f) P.x2 = -1;
+    else {
+        const float rad = c->pointSize * 0.5f;
+        ir = ftoi_x86(rad);
+        if (ir < 0) return;                     // the reference's loop runs no step
+        P.x2 = ir;
+        P.wInvSum = rad * rad;
+    }
+    lp_emit(o, P, (int64_t)P.x1 - ir, (int64_t)P.x1 + ir, (int64_t)P.y1 - ir, (int64_t)P.y1 + ir);
+}
+
+// Helper_EncodeClip2D (lines.c:116-125): 1 left, 2 right, 4 y > yMax, 8 y < yMin
+uint32_t clip_code(float x, float y, const Ctx *c)
+{
+    uint32_t code = 0;
+    if (x < (float)c->vpMin[0]) code |= 1;
+    if (x > (float)c->vpMax[0]) code |= 2;
+    if (y < (float)c->vpMin[1]) code |= 8;
+    if (y > (float)c->vpMax[1]) code |= 4;
+    return code;
+}
+
+// Process_ClipLine2D (lines.c:158-223): Cohen-Sutherland in screen space with
+// the reference's assignments (an end beyond the bottom edge moves to the
+// top row, and the reverse).  Bounded to 32 rounds; the reference loops
+// until it accepts or rejects.
+bool clip_line_2d(const Ctx *c, LPVert &v1, LPVert &v2)
+{
+    const float xMin = (float)c->vpMin[0], yMin = (float)c->vpMin[1], xMax = (float)c->vpMax[0], yMax = (float)c->vpMax[1];
+    float m = 0.0f;
+    if (v1.sx != v2.sx) m = (v2.sy - v1.sy) / (v2.sx - v1.sx);
+    for (int round = 0; round < 32; round++) {
+        uint32_t code0 = clip_code(v1.sx, v1.sy, c), code1 = clip_code(v2.sx, v2.sy, c);
+        if ((code0 | code1) == 0) return true;
+        if (code0 & code1) return false;
+        if (code0 == 0) { std::swap(code0, code1); std::swap(v1, v2); }
+        if (code0 & 1) { v1.sy = v1.sy + (xMin - v1.sx) * m; v1.sx = xMin; }
+        else if (code0 & 2) { v1.sy = v1.sy + (xMax - v1.sx) * m; v1.sx = xMax; }
+        else if (code0 & 4) { if (m != 0.0f) v1.sx = v1.sx + (yMin - v1.sy) / m; v1.sy = yMin; }
+        else if (code0 & 8) { if (m != 0.0f) v1.sx = v1.sx + (yMax - v1.sy) / m; v1.sy = yMax; }
+    }
+    return false;
+}
+
+bool clip_coord_3d(float q, float p, float &t1, float &t2)           // lines.c:127-150
+{
+    if (std::fabs(p) < 1e-5f) return !(q < -1e-5f);
+    const float r = q / p;
+    if (p < 0) { if (r > t2) return false; if (r > t1) t1 = r; }
+    else { if (r < t1) return false; if (r < t2) t2 = r; }
+    return true;
+}
+
+// Process_ClipLine3D (lines.c:225-262): Liang-Barsky in clip space
+bool clip_line_3d(LPVert &v1, LPVert &v2)
+{
+    float t1 = 0.0f, t2 = 1.0f, d[4];
+    const float *a = v1.h;
+    for (int i = 0; i < 4; i++) d[i] = v2.h[i] - a[i];
+    if (!clip_coord_3d(a[3] - a[0], -d[3] + d[0], t1, t2)) return false;
+    if (!clip_coord_3d(a[3] + a[0], -d[3] - d[0], t1, t2)) return false;
+    if (!clip_coord_3d(a[3] - a[1], -d[3] + d[1], t1, t2)) return false;
+    if (!clip_coord_3d(a[3] + a[1], -d[3] - d[1], t1, t2)) return false;
+    if (!clip_coord_3d(a[3] - a[2], -d[3] + d[2], t1, t2)) return false;
+    if (!clip_coord_3d(a[3] + a[2], -d[3] - d[2], t1, t2)) return false;
+    if (t2 < 1.0f) for (int i = 0; i < 4; i++) v2.h[i] = v1.h[i] + d[i] * t2;
+    if (t1 > 0.0f) for (int i = 0; i < 4; i++) v1.h[i] = v1.h[i] + d[i] * t1;
+    return true;
+}
+
+// Process_ProjectAndClipLine (lines.c:264-300)
+bool project_clip_line(const Ctx *c, LPVert *l)
+{
+    for (int i = 0; i < 2; i++) v4_transform(l[i].h, l[i].pos, c->mvp);
+    if (l[0].h[3] == 1.0f && l[1].h[3] == 1.0f) {
+        screen_map(c, l[0]); screen_map(c, l[1]);
+        return clip_line_2d(c, l[0], l[1]);
+    }
+    if (!clip_line_3d(l[0], l[1])) return false;
+    for (int i = 0; i < 2; i++) {
+        const float invW = 1.0f / l[i].h[3];
+        l[i].h[0] = l[i].h[0] * invW; l[i].h[1] = l[i].h[1] * invW;
+    }
+    screen_map(c, l[0]); screen_map(c, l[1]);
+    return true;
+}
+
+// Rasterize_Line_{DEPTH,NODEPTH} (lines.c:304-431): one record holding the
+// DDA's start, step count, 16.16 short-axis step and direction.
+void lp_thin_line(LPOut &o, float sx1, float sy1, float sx2, float sy2, const LPVert &a, const LPVert &b, bool test)
+{
+    const int32_t x1 = ftoi_x86(sx1), y1 = ftoi_x86(sy1), x2 = ftoi_x86(sx2), y2 = ftoi_x86(sy2);
+    int32_t shortLen = isub32(y2, y1), longLen = isub32(x2, x1);
+    bool yLonger = false;
+    if (iabs32(shortLen) > iabs32(longLen)) { std::swap(shortLen, longLen); yLonger = true; }
+    if (longLen == 0) return;                   // the loop runs no step
+    const float invEndVal = 1.0f / (float)longLen;
+    const int32_t endVal = longLen;
+    int32_t sgnInc = 1;
+    if (longLen < 0) { longLen = iabs32(longLen); sgnInc = -1; }
+    if (longLen < 0 || longLen > (1 << 30)) return;   // only from unrepresentable coordinates
+    const int32_t decInc = (int32_t)((uint32_t)shortLen << 16) / longLen;
+    PFPrim P;
+    std::memset(&P, 0, sizeof P);
+    P.x1 = x1; P.y1 = y1; P.x2 = endVal; P.y2 = decInc; P.x3 = sgnInc;
+    P.flags = PFP_LINE | (test ? PFP_DEPTH_TEST : 0u) | (yLonger ? PFP_Y_LONGER : 0u);
+    P.wInvSum = invEndVal;
+    P.z1 = a.h[2]; P.z2 = b.h[2];
+    P.c1 = a.col; P.c2 = b.col;
+    // long axis: a1 + i for i = 0, sgnInc, ..., endVal - sgnInc; short axis:
+    // b1 + (k decInc >> 16), monotone in the step k unless k decInc wraps
+    const int64_t a1 = yLonger ? y1 : x1, b1 = yLonger ? x1 : y1;
+    const int64_t aEnd = a1 + (int64_t)endVal - sgnInc;
+    const int64_t jl = (int64_t)(longLen - 1) * decInc;
+    int64_t bLo, bHi;
+    if (jl >= INT32_MIN && jl <= INT32_MAX) {
+        const int64_t bEnd = b1 + ((int32_t)jl >> 16);
+        bLo = std::min(b1, bEnd); bHi = std::max(b1, bEnd);
+    } else { bLo = INT32_MIN; bHi = INT32_MAX; }
+    const int64_t aLo = std::min(a1, aEnd), aHi = std::max(a1, aEnd);
+    if (yLonger) lp_emit(o, P, bLo, bHi, aLo, aHi);
+    else lp_emit(o, P, aLo, aHi, bLo, bHi);
+}
+
+// pfiProcessRasterize_LINE (lines.c:57-79) and its thick variants
+// (lines.c:433-531): the centre line is always depth-tested, offset copies
+// follow it one pixel further out each side in turn.  Returns false when
+// the line was clipped away.
+bool lp_line(const Ctx *c, LPOut &o, const LPVert &va, const LPVert &vb)
+{
+    LPVert l[2] = { va, vb };
+    if (!project_clip_line(c, l)) return false;
+    const bool test = (c->state & PF_DEPTH_TEST) != 0;
+    if (!(c->lineWidth > 1.5f)) { lp_thin_line(o, l[0].sx, l[0].sy, l[1].sx, l[1].sy, l[0], l[1], test); return true; }
+    const int32_t x1 = ftoi_x86(l[0].sx), y1 = ftoi_x86(l[0].sy), x2 = ftoi_x86(l[1].sx), y2 = ftoi_x86(l[1].sy);
+    const int32_t dx = isub32(x2, x1), dy = isub32(y2, y1);
+    lp_thin_line(o, l[0].sx, l[0].sy, l[1].sx, l[1].sy, l[0], l[1], true);
+    const float rs = 1.0f / std::sqrt((float)(int32_t)((uint32_t)dx * (uint32_t)dx + (uint32_t)dy * (uint32_t)dy));
+    if (dx != 0 && iabs32((dx == -1 && dy == INT32_MIN) ? dy : dy / dx) < 1) {
+        const int32_t wy = ftoi_x86((c->lineWidth - 1.0f) * rs * (float)iabs32(dx)) >> 1;
+        for (int32_t i = 1; i <= wy; i++) {
+            lp_thin_line(o, l[0].sx, l[0].sy - (float)i, l[1].sx, l[1].sy - (float)i, l[0], l[1], test);
+            lp_thin_line(o, l[0].sx, l[0].sy + (float)i, l[1].sx, l[1].sy + (float)i, l[0], l[1], test);
+        }
+    } else if (dy != 0) {
+        const int32_t wx = ftoi_x86((c->lineWidth - 1.0f) * rs * (float)iabs32(dy)) >> 1;
+        for (int32_t i = 1; i <= wx; i++) {
+            lp_thin_line(o, l[0].sx - (float)i, l[0].sy, l[1].sx - (float)i, l[1].sy, l[0], l[1], test);
+            lp_thin_line(o, l[0].sx + (float)i, l[0].sy, l[1].sx + (float)i, l[1].sy, l[0], l[1], test);
+        }
+    }
+    return true;
+}
+
+LPVert lp_vert(const PFVertexIn &v)
+{
+    LPVert r;
+    std::memcpy(r.pos, v.pos, 16);
+    std::memset(r.h, 0, 16);
+    r.sx = r.sy = 0.0f;
+    r.col = v.color;
+    return r;
+}
+
+// A completed primitive of `mode` over the vertices `slots` (immediate mode,
+// or vertex arrays assembled on the host): triangle faces become items over
+// vertex records, points and lines (the modes and the PF_POINT / PF_LINE
+// polygon modes) become set-up records; all in the reference's order
+// (internal/context/context.c:95-244, points.c:33-41, lines.c:81-110).
+void record_primitive(Ctx *c, PFdrawmode mode, const PFVertexIn *slots)
+{
     const PFsizei n = mode_count(mode);
-    if (mode == PF_POINTS || mode == PF_LINES) { set_err(PF_INVALID_OPERATION); return; }
-    int faces[2];
-    const int nf = faces_for(c, mode, faces);
-    if (nf == 0) return;
+    int faces[2]; PFpolygonmode pm[2];
+    const int nf = (mode == PF_POINTS || mode == PF_LINES) ? 0 : face_passes(c, mode, faces, pm);
     Renderer *r = c->rend;
     // a segment stays open only while it is the renderer's last one (another
     // context of a batch may have appended since)
     if (c->openImmSeg < 0 || c->stateDirty || c->openImmSeg != (int)r->segs.size() - 1)
         c->openImmSeg = new_segment(c, PF_SRC_RECORDS, PF_ITEMS_EXPLICIT);
     SegRec &rec = r->segs[c->openImmSeg];
+    const Tex *fbt = (const Tex *)c->current->texture;
+    LPOut o{ rec.prebuilt, rec.explicitItems, (int32_t)fbt->w, (int32_t)fbt->h };
+    if (mode == PF_POINTS) { lp_point(c, o, lp_vert(slots[0])); return; }
+    if (mode == PF_LINES) { lp_line(c, o, lp_vert(slots[0]), lp_vert(slots[1])); return; }
     uint32_t s[6];
-    for (PFsizei i = 0; i < n; i++) { s[i] = (uint32_t)rec.records.size(); rec.records.push_back(c->slots[i]); }
-    emit_items(rec.explicitItems, mode, s, faces, nf);
+    bool stored = false;
+    for (int k = 0; k < nf; k++) {
+        if (pm[k] == PF_POINT) {
+            for (PFsizei i = 0; i < n; i++) lp_point(c, o, lp_vert(slots[i]));
+        } else if (pm[k] == PF_LINE) {
+            for (PFsizei i = 0; i < n; i++)
+                if (!lp_line(c, o, lp_vert(slots[i]), lp_vert(slots[(i + 1) % n]))) break;
+        } else {
+            if (!stored) {
+                for (PFsizei i = 0; i < n; i++) { s[i] = (uint32_t)rec.records.size(); rec.records.push_back(slots[i]); }
+                stored = true;
+            }
+            emit_items(rec.explicitItems, mode, s, &faces[k], 1);
+        }
+    }
 }
+
+// pfVertex4fv path: a primitive completed in immediate mode.
+void immediate_primitive(Ctx *c) { record_primitive(c, c->drawMode, c->slots); }
 
 // ---------------------------------------------------------------------------
 // device side
@@ -974,6 +1252,10 @@ bool flush(Renderer *r)
                 std::memcpy(r->staging.base + rec.itemsOff, rec.explicitItems.data(), rec.explicitItems.size() * 4);
             rec.seg.nItems = (uint32_t)(rec.explicitItems.size() / 4);
         }
+        if (!rec.prebuilt.empty()) {
+            rec.prebuiltOff = r->staging.alloc(rec.prebuilt.size() * sizeof(PFPrim));
+            std::memcpy(r->staging.base + rec.prebuiltOff, rec.prebuilt.data(), rec.prebuilt.size() * sizeof(PFPrim));
+        }
     }
     const size_t total = r->staging.used;
     if (!r->arena.ensure(total)) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return fail("cudaMalloc(arena)", cudaErrorMemoryAllocation); }
@@ -996,6 +1278,7 @@ bool flush(Renderer *r)
         s.col = (const uint8_t *)dptr(rec.colOff);
         s.idx = (const uint32_t *)dptr(rec.idxOff);
         s.explicitItems = (const int32_t *)dptr(rec.itemsOff);
+        s.prebuilt = dptr(rec.prebuiltOff);
         hseg[i] = s;
     }
     // per batch: vertex / item bases, targets, tile numbering
@@ -1829,6 +2112,57 @@ static int64_t stage_color_attr(Ctx *c, const Attrib &a, size_t first, size_t co
     return off;
 }
 
+// Colour component o of the colour array as the reference converts it.
+static uint8_t color_comp(const Attrib &a, size_t o)
+{
+    switch (a.type) {
+    case PF_UNSIGNED_BYTE: return ((const PFubyte *)a.buf)[o];
+    case PF_UNSIGNED_SHORT: return (uint8_t)(((const PFushort *)a.buf)[o] >> 8);
+    case PF_UNSIGNED_INT: return (uint8_t)(((const PFuint *)a.buf)[o] >> 24);
+    case PF_FLOAT: return ftoub(((const PFfloat *)a.buf)[o] * 255);
+    case PF_DOUBLE: return dtoub(((const PFdouble *)a.buf)[o] * 255);
+    }
+    return 0;
+}
+
+// A draw with points or lines (the modes, or a PF_POINT / PF_LINE polygon
+// mode): the reference's slot assembly (context.c:1231-1300, 1415-1460) on
+// the host, each element read into a vertex record; slots start zeroed with
+// the current colour, and attributes whose array is off keep what the slot
+// held.
+static void assemble_arrays(Ctx *c, PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first)
+{
+    const bool useT = (c->state & PF_TEXTURE_COORD_ARRAY) && c->texcoords.buf;
+    const bool useN = (c->state & PF_NORMAL_ARRAY) && c->normals.buf;
+    const bool useC = (c->state & PF_COLOR_ARRAY) && c->colors.buf;
+    const PFsizei nv = mode_count(mode);
+    PFVertexIn slots[6];
+    std::memset(slots, 0, sizeof slots);
+    for (PFVertexIn &v : slots) v.color = pack(c->curColor);
+    PFsizei vc = 0;
+    for (PFsizei i = 0; i < count; i++) {
+        size_t j = (size_t)first + (size_t)i;
+        if (indices) {
+            if (itype == PF_UNSIGNED_BYTE) j = ((const uint8_t *)indices)[i];
+            else if (itype == PF_UNSIGNED_SHORT) j = ((const uint16_t *)indices)[i];
+            else j = ((const uint32_t *)indices)[i];
+        }
+        PFVertexIn &v = slots[vc++];
+        v.pos[0] = v.pos[1] = v.pos[2] = 0.0f; v.pos[3] = 1.0f;
+        const size_t ps = (size_t)c->positions.size;
+        for (size_t k = 0; k < ps; k++) v.pos[k] = attr_f(c->positions, j * ps + k);
+        if (useN) for (size_t k = 0; k < 3; k++) v.normal[k] = attr_f(c->normals, j * 3 + k);
+        if (useT) for (size_t k = 0; k < 2; k++) v.uv[k] = attr_f(c->texcoords, j * 2 + k);
+        if (useC) {
+            uint8_t cb[4] = { 255, 255, 255, 255 };
+            const size_t cs = (size_t)c->colors.size;
+            for (size_t k = 0; k < cs; k++) cb[k] = color_comp(c->colors, j * cs + k);
+            std::memcpy(&v.color, cb, 4);
+        }
+        if (vc == nv) { record_primitive(c, mode, slots); vc = reset_for_next(mode, slots); }
+    }
+}
+
 // pfDrawElements / pfDrawArrays: one segment whose vertices are the arrays'
 // elements [first, first + nverts) and whose primitives follow `indices`
 // (or the sequence 0..count-1).
@@ -1840,12 +2174,18 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     c->stateDirty = true;
     c->openImmSeg = -1;
     if (mode > PF_QUAD_STRIP) { c->err = PF_INVALID_ENUM; return; }
-    if (mode == PF_POINTS || mode == PF_LINES) { c->err = PF_INVALID_OPERATION; return; }
     const PFsizei nv = mode_count(mode);
     const PFsizei nprim = count / nv;
     int faces[2];
-    const int nf = faces_for(c, mode, faces);
-    if (nprim == 0 || nf == 0) return;
+    bool allFill = false;
+    const int nf = fill_faces(c, mode, faces, allFill);
+    if (nprim == 0) return;
+    if (!allFill) {
+        assemble_arrays(c, mode, count, indices, itype, first);
+        c->stateDirty = true;
+        c->openImmSeg = -1;
+        return;
+    }
 
     // indices: stage as u32 and find the vertex range
     int64_t idxOff = -1;

@@ -31,6 +31,8 @@ namespace {
 
 #include "pf_common.cuh"
 
+static_assert((unsigned)PFP_DEPTH_TEST == (unsigned)PFS_DEPTH_TEST, "points and lines reuse the draw-state depth-test bit");
+
 
 // ---------------------------------------------------------------------------
 // Gouraud lighting, ubyte arithmetic (lighting.c:24-134), Blinn-Phong
@@ -695,8 +697,17 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
                                            const BinArgs &B, const TileSpace &T, PFPrim &P)
 {
     const PFDrawState &S = sState ? *sState : states[sg.state];
+    const uint32_t k = g - sg.itemBase + sg.itemSkip;
+    if (sg.itemKind == PF_ITEMS_EXPLICIT && reinterpret_cast<const int4 *>(sg.explicitItems)[k].w < 0) {
+        // a point or a line set up on the host: its record, under this draw state
+        const uint32_t r = (uint32_t)reinterpret_cast<const int4 *>(sg.explicitItems)[k].x;
+        P = static_cast<const PFPrim *>(sg.prebuilt)[r];
+        P.flags = (P.flags & 0xffu) | ((uint32_t)sg.state << 8);
+        O.prims[g] = P;
+        return true;
+    }
     uint32_t vi[3]; int face;
-    item_vertices(sg, g - sg.itemBase + sg.itemSkip, vi, face);
+    item_vertices(sg, k, vi, face);
     const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
     float4 hv[3];
     for (int m = 0; m < 3; m++) hv[m] = *reinterpret_cast<const float4 *>(V[m]->h);
@@ -888,6 +899,8 @@ __device__ __forceinline__ void derive_chunk_prim(const PFPrim &P, uint32_t ox, 
     cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
     const PFDrawState &St = states[P.flags >> 8];
     cp.rstate = (St.flags & 0xffffu) | ((uint32_t)St.depthFunc << 16) | ((uint32_t)St.blendMode << 24);
+    // points and lines carry their own depth-test bit (a thick line's centre is always tested)
+    if (P.flags & PFP_KIND) cp.rstate = (cp.rstate & ~(uint32_t)PFS_DEPTH_TEST) | (P.flags & PFP_DEPTH_TEST);
     dp.e0[0] = cp.e0[0]; dp.e0[1] = cp.e0[1]; dp.e0[2] = cp.e0[2];
     dp.ex0 = cp.ex[0]; dp.ex1 = cp.ex[1]; dp.ex2 = cp.ex[2];
     dp.ey0 = cp.ey[0]; dp.ey1 = cp.ey[1]; dp.ey2 = cp.ey[2];
@@ -975,6 +988,104 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
         frag = light_phong(S, frag, S.mat[P.flags & 1], Pp, N);
     }
     return frag;
+}
+
+// ---------------------------------------------------------------------------
+// points and lines (src/internal/primitives/points.c, lines.c), set up on
+// the host into PFPrim records:
+//   line   x1, y1 first pixel; x2 endVal (signed pixel count along the long
+//          axis); y2 decInc (16.16 step of the short axis); x3 sgnInc;
+//          wInvSum 1 / endVal; z1, z2 and c1, c2 at the ends
+//   point  x1, y1 centre; x2 radius in pixels (-1: the single centre
+//          pixel); wInvSum the squared radius; z1, c1
+// Pixels are absolute framebuffer coordinates.  These run out of line: the
+// triangle path stays free of their registers.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ bool lp_covers(const PFPrim &P, int32_t X, int32_t Y)
+{
+    if ((P.flags & PFP_KIND) == PFP_POINT) {                     // points.c:106-183
+        const int32_t dx = X - P.x1, dy = Y - P.y1;
+        if (P.x2 < 0) return dx == 0 && dy == 0;
+        if (dx < -P.x2 || dx > P.x2 || dy < -P.x2 || dy > P.x2) return false;
+        return (float)(dy * dy + dx * dx) <= P.wInvSum;
+    }
+    // lines.c:304-431: step i of the DDA lands on long-axis coordinate a1 + i
+    const bool yl = (P.flags & PFP_Y_LONGER) != 0;
+    const int32_t a = yl ? Y : X, b = yl ? X : Y, a1 = yl ? P.y1 : P.x1, b1 = yl ? P.x1 : P.y1;
+    const uint32_t k = ((uint32_t)a - (uint32_t)a1) * (uint32_t)P.x3;          // steps taken
+    const uint32_t steps = P.x2 < 0 ? 0u - (uint32_t)P.x2 : (uint32_t)P.x2;
+    if (k >= steps) return false;
+    const int32_t j = (int32_t)(k * (uint32_t)P.y2);
+    return (uint32_t)b == (uint32_t)b1 + (uint32_t)(j >> 16);
+}
+
+// Interpolation parameter of a line pixel: t = i / endVal (lines.c:366).
+__device__ __forceinline__ float lp_t(const PFPrim &P, int32_t X, int32_t Y)
+{
+    const bool yl = (P.flags & PFP_Y_LONGER) != 0;
+    const int32_t i = (int32_t)((uint32_t)(yl ? Y : X) - (uint32_t)(yl ? P.y1 : P.x1));
+    return (float)i * P.wInvSum;
+}
+
+__device__ __noinline__ float lp_depth(const PFPrim &P, int32_t X, int32_t Y)
+{
+    if ((P.flags & PFP_KIND) == PFP_POINT) return P.z1;
+    const float t = lp_t(P, X, Y);
+    return P.z1 + t * (P.z2 - P.z1);
+}
+
+// pfiColorLerpSmooth (src/internal/color.h): (PFubyte)(a + t (b - a)) per channel
+__device__ __noinline__ uint32_t lp_color(const PFPrim &P, int32_t X, int32_t Y)
+{
+    if ((P.flags & PFP_KIND) == PFP_POINT) return P.c1;
+    const float t = lp_t(P, X, Y);
+    int32_t o[4];
+    for (int i = 0; i < 4; i++) {
+        const int32_t a = (int32_t)chn(P.c1, i), b = (int32_t)chn(P.c2, i);
+        o[i] = x86_cvt_trunc((float)a + t * (float)(b - a)) & 255;
+    }
+    return pack4(o);
+}
+
+// Scalar depth test of points and lines (src/internal/depth.h:27-74):
+// NOTEQUAL is a real !=.
+__device__ __forceinline__ bool depth_sisd(int f, float src, float dst)
+{
+    switch (f) {
+    case 0: return src == dst;                                   // EQUAL
+    case 1: return src != dst;                                   // NOTEQUAL
+    case 2: return src < dst;                                    // LESS
+    case 3: return src <= dst;                                   // LEQUAL
+    case 4: return src > dst;                                    // GREATER
+    default: return src >= dst;                                  // GEQUAL
+    }
+}
+
+// Scalar blending of points and lines (src/internal/blend.h:27-126): SUB
+// subtracts, MUL divides by 255, ALPHA weighs with a + 1.
+__device__ __noinline__ uint32_t blend_sisd(int mode, uint32_t src, uint32_t dst)
+{
+    int32_t o[4];
+    for (int i = 0; i < 4; i++) {
+        const int32_t s = (int32_t)chn(src, i), d = (int32_t)chn(dst, i);
+        int32_t v;
+        switch (mode) {
+        case 0: v = (s + d) >> 1; break;                         // AVERAGE
+        case 1: {                                                // ALPHA
+            const uint32_t al = chn(src, 3) + 1u, ia = 256u - al;
+            v = (int32_t)((al * (uint32_t)(i == 3 ? 255 : s) + ia * (uint32_t)d) >> 8);
+            break;
+        }
+        case 2: v = min(d + s, 255); break;                      // ADD
+        case 3: v = max(d - s, 0); break;                        // SUB
+        case 4: v = (s * d) / 255; break;                        // MUL
+        case 5: v = min(((d * (255 - s)) >> 8) + s, 255); break; // SCREEN
+        case 6: v = max(s, d); break;                            // LIGHTEN
+        default: v = min(s, d); break;                           // DARKEN
+        }
+        o[i] = v & 255;
+    }
+    return pack4(o);
 }
 
 // 16-byte global-to-shared copies that complete asynchronously (cp.async):
@@ -1116,6 +1227,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             if (warp == 0) {
                 const bool has = lane < cn;
                 uint32_t bh = 0, area = 0;
+                const bool anyLP = __any_sync(0xffffffffu, has && (sprim[lane].flags & PFP_KIND));
                 if (has) {
                     const PFPrim &P = sprim[lane];
                     ChunkPrim cp;
@@ -1134,7 +1246,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 for (int o = 16; o > 0; o >>= 1) area += __shfl_xor_sync(0xffffffffu, area, o);
                 // boxes that cover half a tile on average: test every
                 // (pixel, sub-triangle) pair instead of stepping rows
-                if (lane == 0) sDense = area > cn * (PF_TILE_PIXELS / 2);
+                // (points and lines always take the row path)
+                if (lane == 0) sDense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP;
             }
             __syncthreads();
             uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
@@ -1180,6 +1293,11 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
                     uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
                     uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
+                    if (cp.flags & PFP_KIND) {
+                        for (uint32_t dx = 0; dx < cp.bw; dx++)
+                            if (lp_covers(sprim[lo], (int32_t)(ox + cp.bx0 + dx), (int32_t)(oy + Y))) atomicOr(row + dx, bit);
+                        continue;
+                    }
                     for (uint32_t dx = 0; dx < cp.bw; dx++) {
                         if ((int32_t)(w1 | w2 | w3) > 0) atomicOr(row + dx, bit);
                         w1 += (uint32_t)cp.ex[0]; w2 += (uint32_t)cp.ex[1]; w3 += (uint32_t)cp.ex[2];
@@ -1200,7 +1318,10 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         int lo; uint32_t k;
                         frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
                         float wn[3];
-                        fz[warp][f - b0] = frag_depth(sprim[k], scp[k], (uint32_t)(warp * 32 + lo), wn);
+                        const uint32_t p = (uint32_t)(warp * 32 + lo);
+                        fz[warp][f - b0] = (scp[k].flags & PFP_KIND)
+                            ? lp_depth(sprim[k], (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
+                            : frag_depth(sprim[k], scp[k], p, wn);
                     }
                     __syncwarp();
                     if (cntp) {
@@ -1212,7 +1333,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                             if (f >= b0) {
                                 const uint32_t rs = scp[k].rstate;
                                 const float z = fz[warp][f - b0];
-                                if (!(rs & PFS_DEPTH_TEST) || depth_simd((int)((rs >> 16) & 255u), z, dep)) {
+                                const int func = (int)((rs >> 16) & 255u);
+                                if (!(rs & PFS_DEPTH_TEST) ||
+                                    ((scp[k].flags & PFP_KIND) ? depth_sisd(func, z, dep) : depth_simd(func, z, dep))) {
                                     vis |= 1u << k;
                                     if (rs & PFS_DEPTH_MASK) dep = z;
                                 }
@@ -1237,7 +1360,12 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
                     float wn[3];
                     const PFPrim &P = sprim[k];
-                    const float z = frag_depth(P, scp[k], (uint32_t)(warp * 32 + lo), wn);
+                    const uint32_t p = (uint32_t)(warp * 32 + lo);
+                    if (scp[k].flags & PFP_KIND) {
+                        fcol[warp][f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
+                        continue;
+                    }
+                    const float z = frag_depth(P, scp[k], p, wn);
                     fcol[warp][f - b0] = shade_fragment(P, &sph[k], a.states[P.flags >> 8], wn[0], wn[1], wn[2], z);
                 }
                 __syncwarp();
@@ -1250,7 +1378,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         if (f >= b0) {
                             const uint32_t rs = scp[k].rstate;
                             uint32_t frag = fcol[warp][f - b0];
-                            if (rs & PFS_BLEND) frag = blend_simd((int)(rs >> 24), frag, col);
+                            if (rs & PFS_BLEND)
+                                frag = (scp[k].flags & PFP_KIND) ? blend_sisd((int)(rs >> 24), frag, col)
+                                                                  : blend_simd((int)(rs >> 24), frag, col);
                             col = frag;
                         }
                         f++;

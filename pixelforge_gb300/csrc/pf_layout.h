@@ -103,7 +103,8 @@ typedef struct {
     int32_t face0;                /* PF_ITEMS_TRIS with nFaces == 1 */
     int32_t target;               /* framebuffer of this segment (index into the batch's targets) */
     uint32_t itemSkip;            /* items of the draw before this segment's first (a draw split into passes) */
-    int32_t pad_[2];
+    const void *prebuilt;         /* PFPrim records of points and lines set up on the host: an explicit
+                                     item {i, 0, 0, -1} stands for record i */
 } PFSegment;                      /* 144 bytes */
 
 /* A framebuffer rendered by a batch.  Its tiles are numbered
@@ -129,6 +130,17 @@ typedef struct {
     float p[3];                   /* object-space position */
     uint32_t pad[2];
 } PFVertexOut;                    /* 64 bytes */
+
+/* PFPrim.flags bits: bit0 face (1 = BACK), bit1 3D path, bits 2-3 the kind
+ * of primitive, bits 8.. the draw state.  Points and lines (set up on the
+ * host) use the fields as noted in pf_host.cpp (lp_line_prim, lp_point_prim). */
+enum {
+    PFP_LINE = 1u << 2,           /* a thin line of the reference's 16.16 DDA */
+    PFP_POINT = 2u << 2,          /* a point: one pixel or a disc */
+    PFP_KIND = 3u << 2,
+    PFP_DEPTH_TEST = 1u << 4,     /* points and lines: depth-test this primitive */
+    PFP_Y_LONGER = 1u << 5        /* lines: y is the long axis */
+};
 
 /* Set-up sub-triangle, as read by the tile rasterizer. */
 typedef struct {

@@ -90,3 +90,51 @@ def run_lp(lib: A.PixelForgeLib, case: dict, target: str = "fbo") -> Frame:
         return tg.finish()
     finally:
         tg.close()
+
+
+def run_wire(lib: A.PixelForgeLib, W: int = 1920, H: int = 1080, target: str = "fbo", seed: int = 5) -> Frame:
+    """A full-HD wireframe: a warped grid drawn as triangles with front faces
+    in PF_LINE mode and back faces filled, a thick polyline and a cloud of
+    large points over it, depth-tested, through vertex arrays."""
+    r = np.random.default_rng(seed)
+    tg = Target(lib, W, H, target)
+    try:
+        lib.pfClearDepth(1.0)
+        lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+        lib.pfEnable(A.PF_DEPTH_TEST)
+        lib.pfDepthFunc(A.PF_LEQUAL)
+        lib.pfDisable(A.PF_CULL_FACE)
+        g = 60
+        u, v = np.meshgrid(np.linspace(-0.92, 0.92, g + 1), np.linspace(-0.9, 0.9, g + 1))
+        z = 0.5 * np.sin(3.0 * u) * np.cos(2.0 * v)
+        pos = np.stack([u + 0.02 * np.sin(9 * v), v, z], -1).reshape(-1, 3).astype(np.float32)
+        col = r.integers(0, 256, (pos.shape[0], 4)).astype(np.uint8)
+        q = np.arange(g * g)
+        a = (q // g) * (g + 1) + q % g
+        tri = np.stack([a, a + 1, a + g + 2, a, a + g + 2, a + g + 1], -1).reshape(-1).astype(np.uint32)
+        lib.pfPolygonMode(A.PF_FRONT, A.PF_LINE)
+        lib.pfPolygonMode(A.PF_BACK, A.PF_FILL)
+        lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_COLOR_ARRAY)
+        lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(pos))
+        lib.pfColorPointer(4, A.PF_UNSIGNED_BYTE, 0, _ptr(col))
+        lib.pfDrawElements(A.PF_TRIANGLES, tri.size, A.PF_UNSIGNED_INT, _ptr(tri))
+        lib.pfDisable(A.PF_VERTEX_ARRAY | A.PF_COLOR_ARRAY)
+        lib.pfLineWidth(4.0)
+        lib.pfBegin(A.PF_LINES)
+        t = np.linspace(0, 2 * np.pi, 201)
+        for i in range(200):
+            lib.pfColor4ub(255, (i * 7) % 256, 40, 255)
+            for k in (i, i + 1):
+                lib.pfVertex3f(float(0.7 * np.cos(t[k])), float(0.7 * np.sin(2 * t[k])), -0.2)
+        lib.pfEnd()
+        lib.pfEnable(A.PF_BLEND)
+        lib.pfBlendFunc(A.PF_BLEND_ALPHA)
+        lib.pfPointSize(7.0)
+        lib.pfBegin(A.PF_POINTS)
+        for p in r.uniform(-0.95, 0.95, (500, 3)):
+            lib.pfColor4ub(40, 200, 255, 160)
+            lib.pfVertex3f(float(p[0]), float(p[1]), float(p[2]))
+        lib.pfEnd()
+        return tg.finish()
+    finally:
+        tg.close()

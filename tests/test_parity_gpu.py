@@ -162,3 +162,24 @@ def test_texture_formats_bilinear(gpu, oracle, fmt):
     for filt in (A.PF_NEAREST, A.PF_BILINEAR):
         run = kat_texfmt(*fmt, filt=filt)
         assert_parity(run(gpu), run(oracle), exact_color=True, label=f"{fmt} filter {filt}")
+
+
+@pytest.mark.parametrize("seed", range(0, 160))
+def test_points_lines(gpu, oracle, seed):
+    """Points, thin and thick lines, PF_POINT / PF_LINE polygon modes
+    (immediate mode and vertex arrays): colour and depth bit-exact."""
+    from lpscenes import lp_case, run_lp
+    case = lp_case(seed)
+    got = run_lp(gpu, case)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert_parity(got, run_lp(oracle, case), exact_color=True, label=f"points/lines {seed} {case}")
+
+
+@pytest.mark.parametrize("target", ["fbo", "main"])
+def test_wireframe_1080(gpu, oracle, target):
+    from lpscenes import run_wire
+    got, ref = run_wire(gpu, target=target), run_wire(oracle, target=target)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert (ref.color.reshape(-1, 4)[:, :3].any(-1)).sum() > 100000       # drawn pixels
+    assert_parity(got, ref, exact_color=True, label=f"wireframe {target}")
+    assert got.stats["fragments"] == ref.stats["fragments"]
