@@ -1136,7 +1136,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ uint32_t fcol[RASTER_THREADS / 32][FWIN];
     __shared__ float fz[RASTER_THREADS / 32][FWIN];
     __shared__ uint32_t woff[RASTER_THREADS / 32][33];
-    __shared__ int sDense;
+    __shared__ int sDense, sAnyLP;
 
     if (a.cnt->abortCommand <= a.command) return;
     // the batch completed set-up without overflow: its sub-triangles count
@@ -1247,10 +1247,11 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 // boxes that cover half a tile on average: test every
                 // (pixel, sub-triangle) pair instead of stepping rows
                 // (points and lines always take the row path)
-                if (lane == 0) sDense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP;
+                if (lane == 0) { sDense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP; sAnyLP = anyLP; }
             }
             __syncthreads();
             uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
+            const bool lpChunk = sAnyLP != 0;                 // the chunk holds points or lines
             if (sDense) {
                 // 2+3 (large sub-triangles). Each thread walks the chunk in
                 //    submission order at its own pixel: coverage, depth, test.
@@ -1293,7 +1294,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
                     uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
                     uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
-                    if (cp.flags & PFP_KIND) {
+                    if (lpChunk && (cp.flags & PFP_KIND)) {
                         for (uint32_t dx = 0; dx < cp.bw; dx++)
                             if (lp_covers(sprim[lo], (int32_t)(ox + cp.bx0 + dx), (int32_t)(oy + Y))) atomicOr(row + dx, bit);
                         continue;
@@ -1319,7 +1320,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
                         float wn[3];
                         const uint32_t p = (uint32_t)(warp * 32 + lo);
-                        fz[warp][f - b0] = (scp[k].flags & PFP_KIND)
+                        fz[warp][f - b0] = (lpChunk && (scp[k].flags & PFP_KIND))
                             ? lp_depth(sprim[k], (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
                             : frag_depth(sprim[k], scp[k], p, wn);
                     }
@@ -1335,7 +1336,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                                 const float z = fz[warp][f - b0];
                                 const int func = (int)((rs >> 16) & 255u);
                                 if (!(rs & PFS_DEPTH_TEST) ||
-                                    ((scp[k].flags & PFP_KIND) ? depth_sisd(func, z, dep) : depth_simd(func, z, dep))) {
+                                    ((lpChunk && (scp[k].flags & PFP_KIND)) ? depth_sisd(func, z, dep)
+                                                                             : depth_simd(func, z, dep))) {
                                     vis |= 1u << k;
                                     if (rs & PFS_DEPTH_MASK) dep = z;
                                 }
@@ -1361,7 +1363,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     float wn[3];
                     const PFPrim &P = sprim[k];
                     const uint32_t p = (uint32_t)(warp * 32 + lo);
-                    if (scp[k].flags & PFP_KIND) {
+                    if (lpChunk && (scp[k].flags & PFP_KIND)) {
                         fcol[warp][f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
                         continue;
                     }
@@ -1379,7 +1381,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                             const uint32_t rs = scp[k].rstate;
                             uint32_t frag = fcol[warp][f - b0];
                             if (rs & PFS_BLEND)
-                                frag = (scp[k].flags & PFP_KIND) ? blend_sisd((int)(rs >> 24), frag, col)
+                                frag = (lpChunk && (scp[k].flags & PFP_KIND)) ? blend_sisd((int)(rs >> 24), frag, col)
                                                                   : blend_simd((int)(rs >> 24), frag, col);
                             col = frag;
                         }
