@@ -122,8 +122,24 @@ typedef struct {
     PFerrcode err; PFuint state;
     PFboolean depthMask;
     float pointSize, lineWidth;
+    float rasterPos[4]; float pixelZoom[2];
+    struct { uint32_t mode; float density, start, end; PFcolor color; } fog;
+    struct RList *curList;             /* render list being recorded, or NULL */
+    struct { RMat mat[2]; float tex[2]; float nrm[3]; PFcolor col; RTex *texture; PFuint state; } backup;
     PFstats stats;
 } RCtx;
+
+/* Render lists (src/renderlist.c): per pfBegin, the draw mode, both
+ * materials, the texture, and per vertex its position, texcoord, normal and
+ * colour as they were current. */
+typedef struct {
+    PFdrawmode mode;
+    RMat mat[2];
+    RTex *texture;
+    float (*pos)[4]; float (*uv)[2]; float (*nrm)[3]; PFcolor *col;
+    size_t n, cap;
+} RCall;
+typedef struct RList { RCall *calls; size_t n, cap; } RList;
 
 static RCtx *G = NULL;   /* current context (one per process, as in GCC+OpenMP builds) */
 
@@ -1304,6 +1320,8 @@ PFcontext pfCreateContext(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFda
     m_identity(c->tex); m_identity(c->normal); m_identity(c->model); m_identity(c->view);
     c->state = PF_CULL_FACE; c->shade = PF_SMOOTH; c->lightMode = PF_GOURAUD; c->cullFace = PF_BACK;
     c->depthMask = PF_TRUE;
+    c->rasterPos[3] = 1.0f; c->pixelZoom[0] = c->pixelZoom[1] = 1.0f;          /* context.c:179-180 */
+    c->fog.mode = PF_LINEAR; c->fog.density = 1.0f; c->fog.start = 0.0f; c->fog.end = 1.0f;   /* :203-209 */
     return c;
 }
 
@@ -1381,7 +1399,7 @@ void pfGetIntegerv(PFenum p, PFint *v)
     case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r; v[1] = G->clearColor.g; v[2] = G->clearColor.b; v[3] = G->clearColor.a; break;
     case PF_CULL_FACE_MODE: v[0] = G->cullFace; break;
     case PF_CURRENT_COLOR: v[0] = G->curColor.r; v[1] = G->curColor.g; v[2] = G->curColor.b; v[3] = G->curColor.a; break;
-    case PF_CURRENT_RASTER_POSITION: v[0] = 0; v[1] = 0; break;
+    case PF_CURRENT_RASTER_POSITION: v[0] = ox_ftoi(G->rasterPos[0]); v[1] = ox_ftoi(G->rasterPos[1]); break;
     case PF_POLYGON_MODE: v[0] = G->polygonMode[0]; v[1] = G->polygonMode[1]; break;
     case PF_MATRIX_MODE: v[0] = G->matMode; break;
     case PF_MAX_PROJECTION_STACK_DEPTH: v[0] = 2; break;
@@ -1411,10 +1429,11 @@ void pfGetIntegerv(PFenum p, PFint *v)
         v[2] = G->curColor.b*(INV); v[3] = G->curColor.a*(INV); break;                        \
     case PF_CURRENT_NORMAL: for (int i = 0; i < 3; i++) v[i] = G->curNormal[i]; break;        \
     case PF_CURRENT_TEXTURE_COORDS: for (int i = 0; i < 2; i++) v[i] = G->curTex[i]; break;   \
-    case PF_CURRENT_RASTER_POSITION: v[0] = 0; v[1] = 0; break;                               \
+    case PF_CURRENT_RASTER_POSITION: v[0] = G->rasterPos[0]; v[1] = G->rasterPos[1]; break;   \
     case PF_POINT_SIZE: v[0] = G->pointSize; break;                                          \
     case PF_LINE_WIDTH: v[0] = G->lineWidth; break;                                          \
-    case PF_ZOOM_X: case PF_ZOOM_Y: v[0] = 1; break;                                         \
+    case PF_ZOOM_X: v[0] = G->pixelZoom[0]; break;                                           \
+    case PF_ZOOM_Y: v[0] = G->pixelZoom[1]; break;                                           \
     case PF_PROJECTION_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->proj[i]; break;        \
     case PF_MODELVIEW_MATRIX: { mat4 mv; m_mul(mv, G->model, G->view);                       \
         for (int i = 0; i < 16; i++) { v[i] = mv[i]; } break; }                               \
@@ -1773,17 +1792,22 @@ void pfDrawArrays(PFdrawmode mode, PFint first, PFsizei count)
     draw_arrays_common(mode, count, NULL, PF_UNSIGNED_INT, first);
 }
 
-void pfBegin(PFdrawmode mode)
+static void list_begin(RCtx *c, PFdrawmode mode);
+static void list_vertex(RCtx *c, const PFfloat *v);
+
+void pfBegin(PFdrawmode mode)   /* context.c:1580-1603 */
 {
+    if (G->curList) { list_begin(G, mode); return; }
     if (mode > PF_QUAD_STRIP) { G->err = PF_INVALID_ENUM; return; }
     update_matrices(G, !(mode == PF_POINTS || mode == PF_LINES));
     G->drawMode = mode; G->vcount = 0;
 }
 void pfEnd(void) { G->vcount = 0; }
 
-void pfVertex4fv(const PFfloat *v)
+void pfVertex4fv(const PFfloat *v)   /* context.c:1655-1685 */
 {
     RCtx *c = G;
+    if (c->curList) { list_vertex(c, v); return; }
     RVert *x = &c->vbuf[c->vcount++];
     memcpy(x->position, v, 16);
     memcpy(x->normal, c->curNormal, 12);
@@ -1848,32 +1872,348 @@ void pfNormal3fv(const PFfloat *v) { pfNormal3f(v[0], v[1], v[2]); }
 /* ------------------------------------------------------------------------ */
 /* outside the triangle pipeline                                             */
 /* ------------------------------------------------------------------------ */
-#define UNSUPPORTED { if (G) G->err = PF_INVALID_OPERATION; }
-void pfRects(PFshort a, PFshort b, PFshort c, PFshort d) { (void)a; (void)b; (void)c; (void)d; UNSUPPORTED }
-void pfRectsv(const PFshort *a, const PFshort *b) { (void)a; (void)b; UNSUPPORTED }
-void pfRectf(PFfloat a, PFfloat b, PFfloat c, PFfloat d) { (void)a; (void)b; (void)c; (void)d; UNSUPPORTED }
-void pfRectfv(const PFfloat *a, const PFfloat *b) { (void)a; (void)b; UNSUPPORTED }
-void pfDrawPixels(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, const void *p) { (void)w; (void)h; (void)f; (void)t; (void)p; UNSUPPORTED }
-void pfPixelZoom(PFfloat x, PFfloat y) { (void)x; (void)y; UNSUPPORTED }
-void pfRasterPos2i(PFint x, PFint y) { (void)x; (void)y; UNSUPPORTED }
-void pfRasterPos2f(PFfloat x, PFfloat y) { (void)x; (void)y; UNSUPPORTED }
-void pfRasterPos2fv(const PFfloat *v) { (void)v; UNSUPPORTED }
-void pfRasterPos3i(PFint x, PFint y, PFint z) { (void)x; (void)y; (void)z; UNSUPPORTED }
-void pfRasterPos3f(PFfloat x, PFfloat y, PFfloat z) { (void)x; (void)y; (void)z; UNSUPPORTED }
-void pfRasterPos3fv(const PFfloat *v) { (void)v; UNSUPPORTED }
-void pfRasterPos4i(PFint x, PFint y, PFint z, PFint w) { (void)x; (void)y; (void)z; (void)w; UNSUPPORTED }
-void pfRasterPos4f(PFfloat x, PFfloat y, PFfloat z, PFfloat w) { (void)x; (void)y; (void)z; (void)w; UNSUPPORTED }
-void pfRasterPos4fv(const PFfloat *v) { (void)v; UNSUPPORTED }
-void pfFogi(PFfogparam p, PFint v) { (void)p; (void)v; UNSUPPORTED }
-void pfFogf(PFfogparam p, PFfloat v) { (void)p; (void)v; UNSUPPORTED }
-void pfFogiv(PFfogparam p, PFint *v) { (void)p; (void)v; UNSUPPORTED }
-void pfFogfv(PFfogparam p, PFfloat *v) { (void)p; (void)v; UNSUPPORTED }
-void pfFogProcess(void) UNSUPPORTED
-PFrenderlist pfGenList(void) { UNSUPPORTED return NULL; }
-void pfDeleteList(PFrenderlist *l) { (void)l; UNSUPPORTED }
-void pfNewList(PFrenderlist l) { (void)l; UNSUPPORTED }
-void pfEndList(void) UNSUPPORTED
-void pfCallList(const PFrenderlist l) { (void)l; UNSUPPORTED }
+/* (PFsizei)(float) as GCC emits it on x86-64: a 64-bit truncating convert
+ * (cvttss2si), low 32 bits kept; 0 for NaN and out of range. */
+static inline uint32_t ox_ftou32(float x)
+{
+    if (!(x > -9.2e18f && x < 9.2e18f)) return 0u;
+    return (uint32_t)(int64_t)x;
+}
+
+static void put_pixel(RCtx *c, int64_t x, int64_t y, uint32_t col)
+{
+    RTex *fbt = (RTex *)c->current->texture;
+    if (x < 0 || y < 0 || x >= (int64_t)fbt->w || y >= (int64_t)fbt->h) return;
+    ((uint32_t *)fbt->pixels)[(size_t)y * fbt->w + (size_t)x] = col;
+}
+
+/* pfRectf (context.c:1936-1981): the two corners through the MVP to screen
+ * (no +0.5), ordered, clamped to the viewport; every pixel of the inclusive
+ * rectangle takes the current colour, no depth test, blending or depth
+ * write.  Pixels outside the framebuffer are not drawn (the reference writes
+ * them at y*w + x). */
+void pfRectf(PFfloat x1, PFfloat y1, PFfloat x2, PFfloat y2)
+{
+    RCtx *c = G;
+    update_matrices(c, 0);
+    float v1[4] = { x1, y1, 0.0f, 1.0f }, v2[4] = { x2, y2, 0.0f, 1.0f };
+    v4_transform(v1, v1, c->mvp);
+    v4_transform(v2, v2, c->mvp);
+    int32_t iX1 = ox_ftoi((float)c->vpPos[0] + (v1[0] + 1.0f) * 0.5f * (float)c->vpDim[0]);
+    int32_t iY1 = ox_ftoi((float)c->vpPos[1] + (1.0f - v1[1]) * 0.5f * (float)c->vpDim[1]);
+    int32_t iX2 = ox_ftoi((float)c->vpPos[0] + (v2[0] + 1.0f) * 0.5f * (float)c->vpDim[0]);
+    int32_t iY2 = ox_ftoi((float)c->vpPos[1] + (1.0f - v2[1]) * 0.5f * (float)c->vpDim[1]);
+    if (iX2 < iX1) { int32_t t = iX1; iX1 = iX2; iX2 = t; }
+    if (iY2 < iY1) { int32_t t = iY1; iY1 = iY2; iY2 = t; }
+#define ICLAMP(v, lo, hi) ((v) < (lo) ? (lo) : ((v) > (hi) ? (hi) : (v)))
+    iX1 = ICLAMP(iX1, c->vpMin[0], c->vpMax[0]); iY1 = ICLAMP(iY1, c->vpMin[1], c->vpMax[1]);
+    iX2 = ICLAMP(iX2, c->vpMin[0], c->vpMax[0]); iY2 = ICLAMP(iY2, c->vpMin[1], c->vpMax[1]);
+    const uint32_t col = col_pack(c->curColor);
+    for (int64_t y = iY1; y <= iY2; y++)
+        for (int64_t x = iX1; x <= iX2; x++) put_pixel(c, x, y, col);
+}
+void pfRects(PFshort x1, PFshort y1, PFshort x2, PFshort y2) { pfRectf((PFfloat)x1, (PFfloat)y1, (PFfloat)x2, (PFfloat)y2); }
+void pfRectsv(const PFshort *a, const PFshort *b) { pfRectf((PFfloat)a[0], (PFfloat)a[1], (PFfloat)b[0], (PFfloat)b[1]); }
+void pfRectfv(const PFfloat *a, const PFfloat *b) { pfRectf(a[0], a[1], b[0], b[1]); }
+
+/* RGBA8 value of the reference's scalar pixel getter for element o of a
+ * buffer (src/internal/pixel.h:410-760), which pfDrawPixels reads with. */
+static uint32_t pixel_sisd(PFpixelformat f, PFdatatype t, const void *p, size_t o)
+{
+    const uint8_t *b = (const uint8_t *)p;
+    const uint16_t *h = (const uint16_t *)p;
+    const float *fl = (const float *)p;
+    uint32_t r = 0, g = 0, bl = 0, a = 255;
+    if (t == PF_UNSIGNED_BYTE || t == PF_HALF_FLOAT || t == PF_FLOAT) {
+        int n = 1;
+        switch (f) {
+        case PF_LUMINANCE_ALPHA: n = 2; break;
+        case PF_RGB: case PF_BGR: n = 3; break;
+        case PF_RGBA: case PF_BGRA: n = 4; break;
+        default: n = 1; break;
+        }
+        uint32_t v[4] = { 0, 0, 0, 0 };
+        for (int k = 0; k < n; k++) {
+            const size_t i = o * (size_t)n + (size_t)k;
+            if (t == PF_UNSIGNED_BYTE) v[k] = b[i];
+            else if (t == PF_HALF_FLOAT) v[k] = ox_ftoub(255.0f * half_to_float(h[i]));
+            else v[k] = ox_ftoub(255.0f * fl[i]);
+        }
+        switch (f) {
+        case PF_RED: r = v[0]; break;
+        case PF_GREEN: g = v[0]; break;
+        case PF_BLUE: bl = v[0]; break;
+        case PF_ALPHA: r = g = bl = 255; a = v[0]; break;
+        case PF_LUMINANCE: r = g = bl = v[0]; break;
+        case PF_LUMINANCE_ALPHA: r = g = bl = v[0]; a = v[1]; break;
+        case PF_RGB: r = v[0]; g = v[1]; bl = v[2]; break;
+        case PF_BGR: r = v[2]; g = v[1]; bl = v[0]; break;
+        case PF_RGBA: r = v[0]; g = v[1]; bl = v[2]; a = v[3]; break;
+        default: r = v[2]; g = v[1]; bl = v[0]; a = v[3]; break;      /* BGRA */
+        }
+    } else {
+        const uint32_t px = h[o];
+        const uint32_t hi5 = ox_ftoub((float)((px & 0xF800u) >> 11) * (255.0f / 31));
+        if (t == PF_UNSIGNED_SHORT_5_6_5) {
+            const uint32_t mid = ox_ftoub((float)((px & 0x7E0u) >> 5) * (255.0f / 63));
+            const uint32_t lo = ox_ftoub((float)(px & 0x1Fu) * (255.0f / 31));
+            r = (f == PF_RGB) ? hi5 : lo; g = mid; bl = (f == PF_RGB) ? lo : hi5;
+        } else if (t == PF_UNSIGNED_SHORT_5_5_5_1) {
+            const uint32_t mid = ox_ftoub((float)((px & 0x7C0u) >> 6) * (255.0f / 31));
+            const uint32_t lo = ox_ftoub((float)((px & 0x3Eu) >> 1) * (255.0f / 31));
+            r = (f == PF_RGBA) ? hi5 : lo; g = mid; bl = (f == PF_RGBA) ? lo : hi5;
+            a = (px & 1u) * 255u;
+        } else {                                                      /* 4-4-4-4 */
+            const uint32_t c3 = ox_ftoub((float)((px & 0xF000u) >> 12) * (255.0f / 15));
+            const uint32_t c2 = ox_ftoub((float)((px & 0xF00u) >> 8) * (255.0f / 15));
+            const uint32_t c1 = ox_ftoub((float)((px & 0xF0u) >> 4) * (255.0f / 15));
+            a = ox_ftoub((float)(px & 0xFu) * (255.0f / 15));
+            r = (f == PF_RGBA) ? c3 : c1; g = c2; bl = (f == PF_RGBA) ? c1 : c3;
+        }
+    }
+    return (r & 255u) | (g & 255u) << 8 | (bl & 255u) << 16 | (a & 255u) << 24;
+}
+
+/* pfDrawPixels (context.c:1990-2087): the raster position through the MVP
+ * to screen; the destination rectangle [xMin, xMax] x [yMin, yMax] clamped
+ * to the viewport; each pixel samples the source at
+ * (u (w - 1), v (h - 1)) with u, v the offset over the zoomed size, passes
+ * the scalar depth test (if enabled), writes the raster depth and stores the
+ * (scalar-)blended colour.  Pixels outside the framebuffer, and source
+ * elements outside the source buffer, are neither drawn nor read. */
+void pfDrawPixels(PFsizei width, PFsizei height, PFpixelformat format, PFdatatype type, const void *pixels)
+{
+    RCtx *c = G;
+    if (width == 0 || height == 0) { c->err = PF_INVALID_VALUE; return; }
+    if (!(format >= PF_RED && format <= PF_BGRA && type >= PF_UNSIGNED_BYTE && type <= PF_DOUBLE)) { c->err = PF_INVALID_ENUM; return; }
+    if (!texel_bytes(format, type)) { c->err = PF_INVALID_ENUM; return; }
+    update_matrices(c, 0);
+    float rp[4];
+    v4_transform(rp, c->rasterPos, c->mvp);
+    const int32_t xScreen = ox_ftoi((float)c->vpPos[0] + (rp[0] + 1.0f) * 0.5f * (float)c->vpDim[0]);
+    const int32_t yScreen = ox_ftoi((float)c->vpPos[1] + (1.0f - rp[1]) * 0.5f * (float)c->vpDim[1]);
+    const float zPos = rp[2];
+    const int32_t xMin = ICLAMP(xScreen, c->vpMin[0], c->vpMax[0]);
+    const int32_t yMin = ICLAMP(yScreen, c->vpMin[1], c->vpMax[1]);
+    /* PF_CLAMP of a float against int bounds: the result is a float */
+    const float xe = (float)xScreen + (float)width * c->pixelZoom[0];
+    const float ye = (float)yScreen + (float)height * c->pixelZoom[1];
+    const int32_t xMax = ox_ftoi(xe < (float)c->vpMin[0] ? (float)c->vpMin[0] : (xe > (float)c->vpMax[0] ? (float)c->vpMax[0] : xe));
+    const int32_t yMax = ox_ftoi(ye < (float)c->vpMin[1] ? (float)c->vpMin[1] : (ye > (float)c->vpMax[1] ? (float)c->vpMax[1] : ye));
+    const float invXLen = 1.0f / ((float)width * c->pixelZoom[0]);
+    const float invYLen = 1.0f / ((float)height * c->pixelZoom[1]);
+    const uint32_t widthM1 = width - 1, heightM1 = height - 1;
+    RTex *dst = (RTex *)c->current->texture;
+    float *zb = c->current->zbuffer;
+    uint32_t *pb = (uint32_t *)dst->pixels;
+    const int test = (c->state & PF_DEPTH_TEST) != 0;
+    const size_t nSrc = (size_t)width * height;
+    for (int64_t y = yMin; y <= yMax; y++) {
+        const float v = (float)(int32_t)((uint32_t)y - (uint32_t)yScreen) * invYLen;
+        const uint32_t ySrc = ox_ftou32(v * (float)heightM1) * width;
+        for (int64_t x = xMin; x <= xMax; x++) {
+            if (x < 0 || y < 0 || x >= (int64_t)dst->w || y >= (int64_t)dst->h) continue;
+            const size_t p = (size_t)y * dst->w + (size_t)x;
+            if (test && !depth_sisd(c->depthFunc, zPos, zb[p])) continue;
+            const float u = (float)(int32_t)((uint32_t)x - (uint32_t)xScreen) * invXLen;
+            const uint32_t src = ySrc + ox_ftou32(u * (float)widthM1);
+            if (c->depthMask) zb[p] = zPos;
+            uint32_t col = src < nSrc ? pixel_sisd(format, type, pixels, src) : 0u;
+            if (c->state & PF_BLEND) col = blend_sisd(c->blend, col, pb[p]);
+            pb[p] = col;
+        }
+    }
+}
+
+void pfPixelZoom(PFfloat x, PFfloat y) { G->pixelZoom[0] = x; G->pixelZoom[1] = y; }   /* context.c:2089-2093 */
+static void raster_pos(float x, float y, float z, float w) { G->rasterPos[0] = x; G->rasterPos[1] = y; G->rasterPos[2] = z; G->rasterPos[3] = w; }
+void pfRasterPos2i(PFint x, PFint y) { raster_pos((PFfloat)x, (PFfloat)y, 0.0f, 1.0f); }
+void pfRasterPos2f(PFfloat x, PFfloat y) { raster_pos(x, y, 0.0f, 1.0f); }
+void pfRasterPos2fv(const PFfloat *v) { raster_pos(v[0], v[1], 0.0f, 1.0f); }
+void pfRasterPos3i(PFint x, PFint y, PFint z) { raster_pos((PFfloat)x, (PFfloat)y, (PFfloat)z, 1.0f); }
+void pfRasterPos3f(PFfloat x, PFfloat y, PFfloat z) { raster_pos(x, y, z, 1.0f); }
+void pfRasterPos3fv(const PFfloat *v) { raster_pos(v[0], v[1], v[2], 1.0f); }
+void pfRasterPos4i(PFint x, PFint y, PFint z, PFint w) { raster_pos((PFfloat)x, (PFfloat)y, (PFfloat)z, (PFfloat)w); }
+void pfRasterPos4f(PFfloat x, PFfloat y, PFfloat z, PFfloat w) { raster_pos(x, y, z, w); }
+void pfRasterPos4fv(const PFfloat *v) { raster_pos(v[0], v[1], v[2], v[3]); }
+
+/* Fog parameters (context.c:2161-2286), with the reference's behaviour: a
+ * density sets the mode (truncated), and the vector forms accept any mode
+ * and density (their range tests are always true). */
+void pfFogi(PFfogparam p, PFint v)
+{
+    switch (p) {
+    case PF_FOG_MODE: if (v >= PF_LINEAR && v <= PF_EXP2) G->fog.mode = (uint32_t)v; else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_DENSITY: if (v == 0 || v == 1) G->fog.mode = (uint32_t)v; else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_START: G->fog.start = (PFfloat)v; break;
+    case PF_FOG_END: G->fog.end = (PFfloat)v; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfFogf(PFfogparam p, PFfloat v)
+{
+    switch (p) {
+    case PF_FOG_DENSITY: if (v >= 0 && v <= 1) G->fog.mode = ox_ftou32(v); else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_START: G->fog.start = v; break;
+    case PF_FOG_END: G->fog.end = v; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfFogiv(PFfogparam p, PFint *v)
+{
+    switch (p) {
+    case PF_FOG_MODE: case PF_FOG_DENSITY: G->fog.mode = (uint32_t)*v; break;
+    case PF_FOG_START: G->fog.start = (PFfloat)*v; break;
+    case PF_FOG_END: G->fog.end = (PFfloat)*v; break;
+    case PF_FOG_COLOR: {
+        PFcolor fc = { (PFubyte)v[0], (PFubyte)v[1], (PFubyte)v[2], (PFubyte)v[3] };
+        G->fog.color = fc;
+        break;
+    }
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfFogfv(PFfogparam p, PFfloat *v)
+{
+    switch (p) {
+    case PF_FOG_DENSITY: if (*v >= 0 || *v <= 1) G->fog.mode = ox_ftou32(*v); else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_START: G->fog.start = *v; break;
+    case PF_FOG_END: G->fog.end = *v; break;
+    case PF_FOG_COLOR: {
+        PFcolor fc = { ox_ftoub(255 * v[0]), ox_ftoub(255 * v[1]), ox_ftoub(255 * v[2]), ox_ftoub(255 * v[3]) };
+        G->fog.color = fc;
+        break;
+    }
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+
+/* pfiBlendAlpha, scalar (src/internal/blend.h:41-52) */
+static uint32_t blend_alpha_sisd(uint32_t src, uint32_t dst) { return blend_sisd(PF_BLEND_ALPHA, src, dst); }
+
+/* pfFogProcess (context.c:2288-2351): over the current framebuffer, pixels
+ * at or beyond the end take the fog colour (alpha-blended unless opaque),
+ * pixels between start and end blend it with alpha t * a, t linear, 1 - e^-d
+ * or 1 - 2^-d of the depth past the start. */
+void pfFogProcess(void)
+{
+    RCtx *c = G;
+    RTex *t = (RTex *)c->current->texture;
+    uint32_t *pb = (uint32_t *)t->pixels;
+    const float *zb = c->current->zbuffer;
+    const float density = c->fog.density, start = c->fog.start, end = c->fog.end;
+    const float invLen = 1 / (end - start);
+    const uint32_t fc = col_pack(c->fog.color) & 0x00ffffffu, alpha = c->fog.color.a;
+    for (size_t o = 0; o < (size_t)t->w * t->h; o++) {
+        const float depth = zb[o];
+        if (depth >= end) {
+            const uint32_t f = fc | alpha << 24;
+            pb[o] = alpha == 255 ? f : blend_alpha_sisd(f, pb[o]);
+        } else if (depth > start) {
+            float tt = 0;
+            switch (c->fog.mode) {
+            case PF_LINEAR: tt = (depth - start) * invLen; break;
+            case PF_EXP: tt = 1.0f - expf(-density * (depth - start)); break;
+            case PF_EXP2: tt = 1.0f - exp2f(-density * (depth - start)); break;
+            default: break;
+            }
+            const uint32_t a = ox_ftoub(tt * (float)alpha);
+            pb[o] = blend_alpha_sisd(fc | a << 24, pb[o]);
+        }
+    }
+}
+
+/* Render lists (src/renderlist.c:6-97, context.c:1580-1685) */
+static void call_free(RCall *k) { free(k->pos); free(k->uv); free(k->nrm); free(k->col); memset(k, 0, sizeof *k); }
+
+static void list_begin(RCtx *c, PFdrawmode mode)
+{
+    RList *l = c->curList;
+    if (l->n == l->cap) {
+        l->cap = l->cap ? l->cap * 2 : 4;
+        l->calls = (RCall *)realloc(l->calls, l->cap * sizeof(RCall));
+    }
+    RCall *k = &l->calls[l->n++];
+    memset(k, 0, sizeof *k);
+    k->mode = mode;
+    k->mat[0] = c->mat[0]; k->mat[1] = c->mat[1];
+    k->texture = c->texture;
+}
+
+static void list_vertex(RCtx *c, const PFfloat *v)
+{
+    RList *l = c->curList;
+    if (l->n == 0) return;                       /* the reference indexes call -1 */
+    RCall *k = &l->calls[l->n - 1];
+    if (k->n == k->cap) {
+        k->cap = k->cap ? k->cap * 2 : 8;
+        k->pos = realloc(k->pos, k->cap * sizeof *k->pos); k->uv = realloc(k->uv, k->cap * sizeof *k->uv);
+        k->nrm = realloc(k->nrm, k->cap * sizeof *k->nrm); k->col = realloc(k->col, k->cap * sizeof *k->col);
+    }
+    memcpy(k->pos[k->n], v, 16); memcpy(k->uv[k->n], c->curTex, 8); memcpy(k->nrm[k->n], c->curNormal, 12);
+    k->col[k->n] = c->curColor;
+    k->n++;
+}
+
+static void ctx_backup(RCtx *c)   /* pfiMakeContextBackup (internal/context/context.c:26-36) */
+{
+    c->backup.mat[0] = c->mat[0]; c->backup.mat[1] = c->mat[1];
+    memcpy(c->backup.tex, c->curTex, 8); memcpy(c->backup.nrm, c->curNormal, 12);
+    c->backup.col = c->curColor; c->backup.texture = c->texture; c->backup.state = c->state;
+}
+static void ctx_restore(RCtx *c)  /* pfiRestoreContext (:38-48) */
+{
+    c->mat[0] = c->backup.mat[0]; c->mat[1] = c->backup.mat[1];
+    memcpy(c->curTex, c->backup.tex, 8); memcpy(c->curNormal, c->backup.nrm, 12);
+    c->curColor = c->backup.col; c->texture = c->backup.texture; c->state = c->backup.state;
+}
+
+PFrenderlist pfGenList(void) { return calloc(1, sizeof(RList)); }
+void pfDeleteList(PFrenderlist *pl)
+{
+    if (!pl) return;
+    RList *l = (RList *)*pl;
+    if (l) {
+        for (size_t i = 0; i < l->n; i++) call_free(&l->calls[i]);
+        free(l->calls); free(l);
+    }
+    *pl = NULL;
+}
+void pfNewList(PFrenderlist pl)
+{
+    if (!pl) { G->err = PF_INVALID_VALUE; return; }
+    RList *l = (RList *)pl;
+    for (size_t i = 0; i < l->n; i++) call_free(&l->calls[i]);
+    l->n = 0;
+    G->curList = l;
+    ctx_backup(G);
+}
+void pfEndList(void)
+{
+    if (!G->curList) G->err = PF_INVALID_OPERATION;
+    G->curList = NULL;
+    ctx_restore(G);
+}
+void pfCallList(const PFrenderlist pl)
+{
+    const RList *l = (const RList *)pl;
+    if (!l) { G->err = PF_INVALID_VALUE; return; }
+    ctx_backup(G);
+    for (size_t i = 0; i < l->n; i++) {
+        const RCall *k = &l->calls[i];
+        G->mat[0] = k->mat[0]; G->mat[1] = k->mat[1];
+        pfBindTexture(k->texture);
+        pfBegin(k->mode);
+        for (size_t j = 0; j < k->n; j++) {
+            pfColor4ubv((const PFubyte *)&k->col[j]);
+            pfTexCoordfv(k->uv[j]);
+            pfNormal3fv(k->nrm[j]);
+            pfVertex4fv(k->pos[j]);
+        }
+        pfEnd();
+    }
+    ctx_restore(G);
+}
 
 /* ------------------------------------------------------------------------ */
 /* readback, post-process, framebuffers, textures                            */

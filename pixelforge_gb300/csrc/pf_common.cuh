@@ -135,6 +135,6 @@ __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVer
     P.c1 = a.c; P.c2 = b.c; P.c3 = c.c; P.pad0 = 0;
     P.u1 = a.u; P.v1 = a.v; P.u2 = b.u; P.v2 = b.v; P.u3 = c.u; P.v3 = c.v;
     P.pad1 = P.pad2 = 0.0f;
-    P.pad3[0] = P.pad3[1] = P.pad3[2] = P.pad3[3] = 0.0f;
+    P.src = 0; P.nSrc = 0; P.pad3 = 0.0f;
     return true;
 }

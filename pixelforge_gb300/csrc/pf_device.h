@@ -12,6 +12,8 @@
 struct PFHookParams {
     float znear, zfar, start, end;
     uint32_t color;
+    uint32_t mode;                /* pfFogProcess: PF_LINEAR, PF_EXP, PF_EXP2 (others: no fog term) */
+    float density;
 };
 
 /* Device pointers and sizes of one raster batch (a run of draw segments on

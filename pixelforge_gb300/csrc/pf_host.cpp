@@ -172,7 +172,8 @@ struct SegRec {
     int64_t recordsOff = -1, posOff = -1, nrmOff = -1, uvOff = -1, colOff = -1, idxOff = -1, itemsOff = -1;
     std::vector<int32_t> explicitItems;   // immediate / non-triangle modes, grown while recording
     std::vector<PFVertexIn> records;       // immediate mode vertices
-    std::vector<PFPrim> prebuilt;          // points and lines set up on the host
+    std::vector<PFPrim> prebuilt;          // points, lines and rectangles set up on the host
+    std::vector<std::pair<uint32_t, int64_t>> blitSrc;   // pfDrawPixels records: record, staged image
     int64_t prebuiltOff = -1;
 };
 
@@ -265,6 +266,18 @@ struct Renderer {
     bool graphValid = false;
 };
 
+// A render list (src/renderlist.c): per pfBegin while recording, the draw
+// mode, both materials and the texture, and per vertex its position,
+// texcoord, normal and colour as they were current.
+struct RenderCall {
+    PFdrawmode mode;
+    Material mat[2];
+    Tex *texture;
+    std::vector<float> pos, uv, nrm;
+    std::vector<PFcolor> col;
+};
+struct RenderList { std::vector<RenderCall> calls; };
+
 struct Ctx {
     PFframebuffer mainFB{ nullptr, nullptr };
     PFframebuffer *current = nullptr;
@@ -299,6 +312,10 @@ struct Ctx {
     PFerrcode err = PF_NO_ERROR; PFuint state = PF_CULL_FACE;
     bool depthMask = true;
     PFfloat pointSize = 1.0f, lineWidth = 1.0f;
+    float rasterPos[4]{ 0.0f, 0.0f, 0.0f, 1.0f }; float pixelZoom[2]{ 1.0f, 1.0f };   // context.c:179-180
+    struct { uint32_t mode = PF_LINEAR; float density = 1.0f, start = 0.0f, end = 1.0f; PFcolor color{ 0, 0, 0, 0 }; } fog;
+    RenderList *curList = nullptr;          // render list being recorded
+    struct { Material mat[2]; float tex[2]; float nrm[3]; PFcolor col; Tex *texture; PFuint state; } backup{};
 
     bool stateDirty = true;
     int openImmSeg = -1;                 // immediate-mode segment accepting primitives (index in rend->segs)
@@ -815,16 +832,25 @@ struct LPOut {
 
 // Append record P with pixels in the inclusive box [x0, x1] x [y0, y1]
 // (clipped to the framebuffer; nothing is appended when no pixel remains).
-void lp_emit(LPOut &o, PFPrim &P, int64_t x0, int64_t x1, int64_t y0, int64_t y1)
+int64_t lp_emit(LPOut &o, PFPrim &P, int64_t x0, int64_t x1, int64_t y0, int64_t y1)
 {
     x0 = std::max<int64_t>(x0, 0); y0 = std::max<int64_t>(y0, 0);
     x1 = std::min<int64_t>(x1, (int64_t)o.W - 1); y1 = std::min<int64_t>(y1, (int64_t)o.H - 1);
-    if (x0 > x1 || y0 > y1) return;
+    if (x0 > x1 || y0 > y1) return -1;
     P.xMin = (int32_t)x0; P.xMax = (int32_t)(x1 + 1); P.yMin = (int32_t)y0; P.yMax = (int32_t)y1;
     P.poolBase = 0;
     const int32_t item[4] = { (int32_t)o.prims.size(), 0, 0, -1 };
     o.items.insert(o.items.end(), item, item + 4);
     o.prims.push_back(P);
+    return (int64_t)o.prims.size() - 1;
+}
+
+// Per-fragment operations of a point or line record: its depth test, and
+// blending and depth write as the state has them.
+uint32_t lp_ops(const Ctx *c, bool test)
+{
+    return (test ? (uint32_t)PFP_DEPTH_TEST : 0u) | ((c->state & PF_BLEND) ? (uint32_t)PFP_BLEND : 0u) |
+           (c->depthMask ? (uint32_t)PFP_DEPTH_WRITE : 0u);
 }
 
 void screen_map(const Ctx *c, LPVert &v)                           // lines.c:272-298
@@ -850,7 +876,7 @@ void lp_point(const Ctx *c, LPOut &o, const LPVert &v)
     PFPrim P;
     std::memset(&P, 0, sizeof P);
     P.x1 = ftoi_x86(sx); P.y1 = ftoi_x86(sy);
-    P.flags = PFP_POINT | ((c->state & PF_DEPTH_TEST) ? PFP_DEPTH_TEST : 0u);
+    P.flags = PFP_POINT | lp_ops(c, (c->state & PF_DEPTH_TEST) != 0);
     P.z1 = h[2];
     P.c1 = v.col;
     int32_t ir = 0;
@@ -943,7 +969,7 @@ bool project_clip_line(const Ctx *c, LPVert *l)
 
 // Rasterize_Line_{DEPTH,NODEPTH} (lines.c:304-431): one record holding the
 // DDA's start, step count, 16.16 short-axis step and direction.
-void lp_thin_line(LPOut &o, float sx1, float sy1, float sx2, float sy2, const LPVert &a, const LPVert &b, bool test)
+void lp_thin_line(LPOut &o, float sx1, float sy1, float sx2, float sy2, const LPVert &a, const LPVert &b, uint32_t ops)
 {
     const int32_t x1 = ftoi_x86(sx1), y1 = ftoi_x86(sy1), x2 = ftoi_x86(sx2), y2 = ftoi_x86(sy2);
     int32_t shortLen = isub32(y2, y1), longLen = isub32(x2, x1);
@@ -959,7 +985,7 @@ void lp_thin_line(LPOut &o, float sx1, float sy1, float sx2, float sy2, const LP
     PFPrim P;
     std::memset(&P, 0, sizeof P);
     P.x1 = x1; P.y1 = y1; P.x2 = endVal; P.y2 = decInc; P.x3 = sgnInc;
-    P.flags = PFP_LINE | (test ? PFP_DEPTH_TEST : 0u) | (yLonger ? PFP_Y_LONGER : 0u);
+    P.flags = PFP_LINE | ops | (yLonger ? PFP_Y_LONGER : 0u);
     P.wInvSum = invEndVal;
     P.z1 = a.h[2]; P.z2 = b.h[2];
     P.c1 = a.col; P.c2 = b.col;
@@ -986,11 +1012,11 @@ bool lp_line(const Ctx *c, LPOut &o, const LPVert &va, const LPVert &vb)
 {
     LPVert l[2] = { va, vb };
     if (!project_clip_line(c, l)) return false;
-    const bool test = (c->state & PF_DEPTH_TEST) != 0;
+    const uint32_t test = lp_ops(c, (c->state & PF_DEPTH_TEST) != 0);
     if (!(c->lineWidth > 1.5f)) { lp_thin_line(o, l[0].sx, l[0].sy, l[1].sx, l[1].sy, l[0], l[1], test); return true; }
     const int32_t x1 = ftoi_x86(l[0].sx), y1 = ftoi_x86(l[0].sy), x2 = ftoi_x86(l[1].sx), y2 = ftoi_x86(l[1].sy);
     const int32_t dx = isub32(x2, x1), dy = isub32(y2, y1);
-    lp_thin_line(o, l[0].sx, l[0].sy, l[1].sx, l[1].sy, l[0], l[1], true);
+    lp_thin_line(o, l[0].sx, l[0].sy, l[1].sx, l[1].sy, l[0], l[1], lp_ops(c, true));
     const float rs = 1.0f / std::sqrt((float)(int32_t)((uint32_t)dx * (uint32_t)dx + (uint32_t)dy * (uint32_t)dy));
     if (dx != 0 && iabs32((dx == -1 && dy == INT32_MIN) ? dy : dy / dx) < 1) {
         const int32_t wy = ftoi_x86((c->lineWidth - 1.0f) * rs * (float)iabs32(dx)) >> 1;
@@ -1018,6 +1044,17 @@ LPVert lp_vert(const PFVertexIn &v)
     return r;
 }
 
+// The immediate-mode segment accepting records under the current state.  A
+// segment stays open only while it is the renderer's last one (another
+// context of a batch may have appended since).
+SegRec &open_segment(Ctx *c)
+{
+    Renderer *r = c->rend;
+    if (c->openImmSeg < 0 || c->stateDirty || c->openImmSeg != (int)r->segs.size() - 1)
+        c->openImmSeg = new_segment(c, PF_SRC_RECORDS, PF_ITEMS_EXPLICIT);
+    return r->segs[c->openImmSeg];
+}
+
 // A completed primitive of `mode` over the vertices `slots` (immediate mode,
 // or vertex arrays assembled on the host): triangle faces become items over
 // vertex records, points and lines (the modes and the PF_POINT / PF_LINE
@@ -1028,12 +1065,7 @@ void record_primitive(Ctx *c, PFdrawmode mode, const PFVertexIn *slots)
     const PFsizei n = mode_count(mode);
     int faces[2]; PFpolygonmode pm[2];
     const int nf = (mode == PF_POINTS || mode == PF_LINES) ? 0 : face_passes(c, mode, faces, pm);
-    Renderer *r = c->rend;
-    // a segment stays open only while it is the renderer's last one (another
-    // context of a batch may have appended since)
-    if (c->openImmSeg < 0 || c->stateDirty || c->openImmSeg != (int)r->segs.size() - 1)
-        c->openImmSeg = new_segment(c, PF_SRC_RECORDS, PF_ITEMS_EXPLICIT);
-    SegRec &rec = r->segs[c->openImmSeg];
+    SegRec &rec = open_segment(c);
     const Tex *fbt = (const Tex *)c->current->texture;
     LPOut o{ rec.prebuilt, rec.explicitItems, (int32_t)fbt->w, (int32_t)fbt->h };
     if (mode == PF_POINTS) { lp_point(c, o, lp_vert(slots[0])); return; }
@@ -1279,6 +1311,10 @@ bool flush(Renderer *r)
         s.idx = (const uint32_t *)dptr(rec.idxOff);
         s.explicitItems = (const int32_t *)dptr(rec.itemsOff);
         s.prebuilt = dptr(rec.prebuiltOff);
+        if (!rec.blitSrc.empty()) {
+            PFPrim *pp = (PFPrim *)(r->staging.base + rec.prebuiltOff);
+            for (auto &bs : rec.blitSrc) pp[bs.first].src = (uint64_t)(uintptr_t)dptr(bs.second);
+        }
         hseg[i] = s;
     }
     // per batch: vertex / item bases, targets, tile numbering
@@ -1622,11 +1658,7 @@ float replay(Renderer *r, uint32_t n)
 // C API
 // ===========================================================================
 // Getters (getter.c:24-521): the same cases as the reference; any other
-// name sets PF_INVALID_ENUM and leaves the output untouched.  The raster
-// position and pixel zoom keep their initial values (pfRasterPos* and
-// pfPixelZoom are not supported), context.c:179-180.
-static const float kRasterPos[4] = { 0.0f, 0.0f, 0.0f, 1.0f };
-static const float kPixelZoom[2] = { 1.0f, 1.0f };
+// name sets PF_INVALID_ENUM and leaves the output untouched.
 static const double kInv255 = 1.0 / 255;
 
 template <typename T>
@@ -1642,7 +1674,7 @@ static bool get_real(PFenum p, T *v, T inv255)                           // gett
         v[2] = G->curColor.b * inv255; v[3] = G->curColor.a * inv255; return true;
     case PF_CURRENT_NORMAL: for (int i = 0; i < 3; i++) v[i] = G->curNormal[i]; return true;
     case PF_CURRENT_TEXTURE_COORDS: for (int i = 0; i < 2; i++) v[i] = G->curTex[i]; return true;
-    case PF_CURRENT_RASTER_POSITION: v[0] = kRasterPos[0]; v[1] = kRasterPos[1]; return true;
+    case PF_CURRENT_RASTER_POSITION: v[0] = G->rasterPos[0]; v[1] = G->rasterPos[1]; return true;
     case PF_POINT_SIZE: v[0] = G->pointSize; return true;
     case PF_LINE_WIDTH: v[0] = G->lineWidth; return true;
     case PF_PROJECTION_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->proj[i]; return true;
@@ -1652,8 +1684,8 @@ static bool get_real(PFenum p, T *v, T inv255)                           // gett
         return true;
     }
     case PF_TEXTURE_MATRIX: for (int i = 0; i < 16; i++) v[i] = G->tex[i]; return true;
-    case PF_ZOOM_X: v[0] = kPixelZoom[0]; return true;
-    case PF_ZOOM_Y: v[0] = kPixelZoom[1]; return true;
+    case PF_ZOOM_X: v[0] = G->pixelZoom[0]; return true;
+    case PF_ZOOM_Y: v[0] = G->pixelZoom[1]; return true;
     default: G->err = PF_INVALID_ENUM; return false;
     }
 }
@@ -1786,7 +1818,7 @@ void pfGetIntegerv(PFenum p, PFint *v)                                // getter.
     case PF_COLOR_CLEAR_VALUE: v[0] = G->clearColor.r; v[1] = G->clearColor.g; v[2] = G->clearColor.b; v[3] = G->clearColor.a; break;
     case PF_CULL_FACE_MODE: v[0] = G->cullFace; break;
     case PF_CURRENT_COLOR: v[0] = G->curColor.r; v[1] = G->curColor.g; v[2] = G->curColor.b; v[3] = G->curColor.a; break;
-    case PF_CURRENT_RASTER_POSITION: v[0] = (PFint)kRasterPos[0]; v[1] = (PFint)kRasterPos[1]; break;
+    case PF_CURRENT_RASTER_POSITION: v[0] = ftoi_x86(G->rasterPos[0]); v[1] = ftoi_x86(G->rasterPos[1]); break;
     case PF_POLYGON_MODE: v[0] = G->polygonMode[0]; v[1] = G->polygonMode[1]; break;
     case PF_MATRIX_MODE: v[0] = G->matMode; break;
     case PF_MAX_PROJECTION_STACK_DEPTH: v[0] = 2; break;
@@ -2251,8 +2283,12 @@ void pfDrawArrays(PFdrawmode mode, PFint first, PFsizei count)
     draw_arrays(mode, count, nullptr, PF_UNSIGNED_INT, first);
 }
 
-void pfBegin(PFdrawmode mode)
+static void list_begin(Ctx *c, PFdrawmode mode);
+static void list_vertex(Ctx *c, const PFfloat *v);
+
+void pfBegin(PFdrawmode mode)                                        // context.c:1580-1603
 {
+    if (G->curList) { list_begin(G, mode); return; }
     if (mode > PF_QUAD_STRIP) { G->err = PF_INVALID_ENUM; return; }
     update_matrices(G, !(mode == PF_POINTS || mode == PF_LINES));
     G->drawMode = mode; G->vcount = 0;
@@ -2260,9 +2296,10 @@ void pfBegin(PFdrawmode mode)
 }
 void pfEnd(void) { G->vcount = 0; }
 
-void pfVertex4fv(const PFfloat *v)
+void pfVertex4fv(const PFfloat *v)                                   // context.c:1655-1685
 {
     Ctx *c = G;
+    if (c->curList) { list_vertex(c, v); return; }
     PFVertexIn &x = c->slots[c->vcount++];
     std::memcpy(x.pos, v, 16);
     std::memcpy(x.normal, c->curNormal, 12);
@@ -2330,32 +2367,288 @@ void pfNormal3f(PFfloat x, PFfloat y, PFfloat z)
 void pfNormal3fv(const PFfloat *v) { pfNormal3f(v[0], v[1], v[2]); }
 
 // --- outside the triangle pipeline -------------------------------------------
-#define PF_UNSUPPORTED { if (G) G->err = PF_INVALID_OPERATION; }
-void pfRects(PFshort, PFshort, PFshort, PFshort) PF_UNSUPPORTED
-void pfRectsv(const PFshort *, const PFshort *) PF_UNSUPPORTED
-void pfRectf(PFfloat, PFfloat, PFfloat, PFfloat) PF_UNSUPPORTED
-void pfRectfv(const PFfloat *, const PFfloat *) PF_UNSUPPORTED
-void pfDrawPixels(PFsizei, PFsizei, PFpixelformat, PFdatatype, const void *) PF_UNSUPPORTED
-void pfPixelZoom(PFfloat, PFfloat) PF_UNSUPPORTED
-void pfRasterPos2i(PFint, PFint) PF_UNSUPPORTED
-void pfRasterPos2f(PFfloat, PFfloat) PF_UNSUPPORTED
-void pfRasterPos2fv(const PFfloat *) PF_UNSUPPORTED
-void pfRasterPos3i(PFint, PFint, PFint) PF_UNSUPPORTED
-void pfRasterPos3f(PFfloat, PFfloat, PFfloat) PF_UNSUPPORTED
-void pfRasterPos3fv(const PFfloat *) PF_UNSUPPORTED
-void pfRasterPos4i(PFint, PFint, PFint, PFint) PF_UNSUPPORTED
-void pfRasterPos4f(PFfloat, PFfloat, PFfloat, PFfloat) PF_UNSUPPORTED
-void pfRasterPos4fv(const PFfloat *) PF_UNSUPPORTED
-void pfFogi(PFfogparam, PFint) PF_UNSUPPORTED
-void pfFogf(PFfogparam, PFfloat) PF_UNSUPPORTED
-void pfFogiv(PFfogparam, PFint *) PF_UNSUPPORTED
-void pfFogfv(PFfogparam, PFfloat *) PF_UNSUPPORTED
-void pfFogProcess(void) PF_UNSUPPORTED
-PFrenderlist pfGenList(void) { PF_UNSUPPORTED return nullptr; }
-void pfDeleteList(PFrenderlist *) PF_UNSUPPORTED
-void pfNewList(PFrenderlist) PF_UNSUPPORTED
-void pfEndList(void) PF_UNSUPPORTED
-void pfCallList(const PFrenderlist) PF_UNSUPPORTED
+// --- rectangles and images (context.c:1936-2159) ----------------------------
+// Both become PFP_BLIT records of the recording, in submission order with
+// the primitives: the tile rasterizer fills their pixels (image pixels with
+// the scalar depth test and blending of the state).  Pixels outside the
+// framebuffer are not drawn (the reference writes them at y*w + x).
+
+// (PFsizei)(float) as the reference's x86-64 build converts it: a 64-bit
+// truncating conversion, low 32 bits kept; 0 for NaN and out of range.
+static inline uint32_t ftou32_x86(float x)
+{
+    if (!(x > -9.2e18f && x < 9.2e18f)) return 0u;
+    return (uint32_t)(int64_t)x;
+}
+
+static int32_t screen_x(const Ctx *c, float hx) { return ftoi_x86((float)c->vpPos[0] + (hx + 1.0f) * 0.5f * (float)c->vpDim[0]); }
+static int32_t screen_y(const Ctx *c, float hy) { return ftoi_x86((float)c->vpPos[1] + (1.0f - hy) * 0.5f * (float)c->vpDim[1]); }
+static int32_t iclamp(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+void pfRectf(PFfloat x1, PFfloat y1, PFfloat x2, PFfloat y2)          // context.c:1936-1981
+{
+    Ctx *c = G;
+    update_matrices(c, false);
+    float v1[4] = { x1, y1, 0.0f, 1.0f }, v2[4] = { x2, y2, 0.0f, 1.0f };
+    v4_transform(v1, v1, c->mvp);
+    v4_transform(v2, v2, c->mvp);
+    int32_t iX1 = screen_x(c, v1[0]), iY1 = screen_y(c, v1[1]), iX2 = screen_x(c, v2[0]), iY2 = screen_y(c, v2[1]);
+    if (iX2 < iX1) std::swap(iX1, iX2);
+    if (iY2 < iY1) std::swap(iY1, iY2);
+    iX1 = iclamp(iX1, c->vpMin[0], c->vpMax[0]); iY1 = iclamp(iY1, c->vpMin[1], c->vpMax[1]);
+    iX2 = iclamp(iX2, c->vpMin[0], c->vpMax[0]); iY2 = iclamp(iY2, c->vpMin[1], c->vpMax[1]);
+    PFPrim P;
+    std::memset(&P, 0, sizeof P);
+    P.flags = PFP_BLIT;                                    // no depth test, blending or depth write
+    P.c1 = pack(c->curColor);
+    SegRec &rec = open_segment(c);
+    const Tex *fbt = (const Tex *)c->current->texture;
+    LPOut o{ rec.prebuilt, rec.explicitItems, (int32_t)fbt->w, (int32_t)fbt->h };
+    lp_emit(o, P, iX1, iX2, iY1, iY2);
+}
+void pfRects(PFshort x1, PFshort y1, PFshort x2, PFshort y2) { pfRectf((PFfloat)x1, (PFfloat)y1, (PFfloat)x2, (PFfloat)y2); }
+void pfRectsv(const PFshort *a, const PFshort *b) { pfRectf((PFfloat)a[0], (PFfloat)a[1], (PFfloat)b[0], (PFfloat)b[1]); }
+void pfRectfv(const PFfloat *a, const PFfloat *b) { pfRectf(a[0], a[1], b[0], b[1]); }
+
+// RGBA8 value of the reference's scalar pixel getter for element o
+// (src/internal/pixel.h:410-760): plain reads, (PFubyte)(255 x) for half
+// and float channels, (PFubyte)(field * 255/31 ...) for packed shorts.
+static uint32_t pixel_sisd(PFpixelformat f, PFdatatype t, const void *p, size_t o)
+{
+    const uint8_t *b = (const uint8_t *)p;
+    const uint16_t *h = (const uint16_t *)p;
+    const float *fl = (const float *)p;
+    uint32_t r = 0, g = 0, bl = 0, a = 255;
+    if (t == PF_UNSIGNED_BYTE || t == PF_HALF_FLOAT || t == PF_FLOAT) {
+        const int n = f == PF_LUMINANCE_ALPHA ? 2 : (f == PF_RGB || f == PF_BGR) ? 3 : (f == PF_RGBA || f == PF_BGRA) ? 4 : 1;
+        uint32_t v[4] = { 0, 0, 0, 0 };
+        for (int k = 0; k < n; k++) {
+            const size_t i = o * (size_t)n + (size_t)k;
+            if (t == PF_UNSIGNED_BYTE) v[k] = b[i];
+            else if (t == PF_HALF_FLOAT) v[k] = ftoub(255.0f * half_to_float(h[i]));
+            else v[k] = ftoub(255.0f * fl[i]);
+        }
+        switch (f) {
+        case PF_RED: r = v[0]; break;
+        case PF_GREEN: g = v[0]; break;
+        case PF_BLUE: bl = v[0]; break;
+        case PF_ALPHA: r = g = bl = 255; a = v[0]; break;
+        case PF_LUMINANCE: r = g = bl = v[0]; break;
+        case PF_LUMINANCE_ALPHA: r = g = bl = v[0]; a = v[1]; break;
+        case PF_RGB: r = v[0]; g = v[1]; bl = v[2]; break;
+        case PF_BGR: r = v[2]; g = v[1]; bl = v[0]; break;
+        case PF_RGBA: r = v[0]; g = v[1]; bl = v[2]; a = v[3]; break;
+        default: r = v[2]; g = v[1]; bl = v[0]; a = v[3]; break;              // BGRA
+        }
+    } else {
+        const uint32_t px = h[o];
+        const uint32_t hi5 = ftoub((float)((px & 0xF800u) >> 11) * (255.0f / 31));
+        if (t == PF_UNSIGNED_SHORT_5_6_5) {
+            const uint32_t mid = ftoub((float)((px & 0x7E0u) >> 5) * (255.0f / 63));
+            const uint32_t lo = ftoub((float)(px & 0x1Fu) * (255.0f / 31));
+            r = f == PF_RGB ? hi5 : lo; g = mid; bl = f == PF_RGB ? lo : hi5;
+        } else if (t == PF_UNSIGNED_SHORT_5_5_5_1) {
+            const uint32_t mid = ftoub((float)((px & 0x7C0u) >> 6) * (255.0f / 31));
+            const uint32_t lo = ftoub((float)((px & 0x3Eu) >> 1) * (255.0f / 31));
+            r = f == PF_RGBA ? hi5 : lo; g = mid; bl = f == PF_RGBA ? lo : hi5;
+            a = (px & 1u) * 255u;
+        } else {                                                              // 4-4-4-4
+            const uint32_t c3 = ftoub((float)((px & 0xF000u) >> 12) * (255.0f / 15));
+            const uint32_t c2 = ftoub((float)((px & 0xF00u) >> 8) * (255.0f / 15));
+            const uint32_t c1 = ftoub((float)((px & 0xF0u) >> 4) * (255.0f / 15));
+            a = ftoub((float)(px & 0xFu) * (255.0f / 15));
+            r = f == PF_RGBA ? c3 : c1; g = c2; bl = f == PF_RGBA ? c1 : c3;
+        }
+    }
+    return (r & 255u) | (g & 255u) << 8 | (bl & 255u) << 16 | (a & 255u) << 24;
+}
+
+void pfDrawPixels(PFsizei width, PFsizei height, PFpixelformat format, PFdatatype type, const void *pixels)
+{                                                                          // context.c:1990-2087
+    Ctx *c = G;
+    if (width == 0 || height == 0) { c->err = PF_INVALID_VALUE; return; }
+    if (!(format >= PF_RED && format <= PF_BGRA && type >= PF_UNSIGNED_BYTE && type <= PF_DOUBLE)) { c->err = PF_INVALID_ENUM; return; }
+    if (!texel_bytes(format, type)) { c->err = PF_INVALID_ENUM; return; }
+    const size_t n = (size_t)width * height;
+    if (n > 0xffffffffu) { c->err = PF_INVALID_VALUE; return; }
+    update_matrices(c, false);
+    float rp[4];
+    v4_transform(rp, c->rasterPos, c->mvp);
+    const int32_t xScreen = screen_x(c, rp[0]), yScreen = screen_y(c, rp[1]);
+    const int32_t xMin = iclamp(xScreen, c->vpMin[0], c->vpMax[0]), yMin = iclamp(yScreen, c->vpMin[1], c->vpMax[1]);
+    // PF_CLAMP of a float against int bounds evaluates to a float
+    auto fclamp = [](float v, int32_t lo, int32_t hi) { return v < (float)lo ? (float)lo : (v > (float)hi ? (float)hi : v); };
+    const int32_t xMax = ftoi_x86(fclamp((float)xScreen + (float)width * c->pixelZoom[0], c->vpMin[0], c->vpMax[0]));
+    const int32_t yMax = ftoi_x86(fclamp((float)yScreen + (float)height * c->pixelZoom[1], c->vpMin[1], c->vpMax[1]));
+    PFPrim P;
+    std::memset(&P, 0, sizeof P);
+    P.flags = PFP_BLIT | ((c->state & PF_DEPTH_TEST) ? (uint32_t)PFP_DEPTH_TEST : 0u) |
+              ((c->state & PF_BLEND) ? (uint32_t)PFP_BLEND : 0u) | (c->depthMask ? (uint32_t)PFP_DEPTH_WRITE : 0u);
+    P.x1 = xScreen; P.y1 = yScreen;
+    P.x2 = (int32_t)width; P.y2 = (int32_t)(width - 1); P.x3 = (int32_t)(height - 1);
+    P.wInvSum = 1.0f / ((float)width * c->pixelZoom[0]);
+    P.z2 = 1.0f / ((float)height * c->pixelZoom[1]);
+    P.z1 = rp[2];
+    P.nSrc = (uint32_t)n;
+    SegRec &rec = open_segment(c);
+    const Tex *fbt = (const Tex *)c->current->texture;
+    LPOut o{ rec.prebuilt, rec.explicitItems, (int32_t)fbt->w, (int32_t)fbt->h };
+    const int64_t ri = lp_emit(o, P, xMin, xMax, yMin, yMax);
+    if (ri < 0) return;
+    // the image, converted once with the scalar getter
+    const int64_t off = c->rend->staging.alloc(n * 4);
+    uint32_t *dst = (uint32_t *)(c->rend->staging.base + off);
+    for (size_t i = 0; i < n; i++) dst[i] = pixel_sisd(format, type, pixels, i);
+    rec.blitSrc.push_back({ (uint32_t)ri, off });
+}
+
+void pfPixelZoom(PFfloat x, PFfloat y) { G->pixelZoom[0] = x; G->pixelZoom[1] = y; }   // context.c:2089-2093
+static void raster_pos(float x, float y, float z, float w)
+{
+    G->rasterPos[0] = x; G->rasterPos[1] = y; G->rasterPos[2] = z; G->rasterPos[3] = w;
+}
+void pfRasterPos2i(PFint x, PFint y) { raster_pos((PFfloat)x, (PFfloat)y, 0.0f, 1.0f); }
+void pfRasterPos2f(PFfloat x, PFfloat y) { raster_pos(x, y, 0.0f, 1.0f); }
+void pfRasterPos2fv(const PFfloat *v) { raster_pos(v[0], v[1], 0.0f, 1.0f); }
+void pfRasterPos3i(PFint x, PFint y, PFint z) { raster_pos((PFfloat)x, (PFfloat)y, (PFfloat)z, 1.0f); }
+void pfRasterPos3f(PFfloat x, PFfloat y, PFfloat z) { raster_pos(x, y, z, 1.0f); }
+void pfRasterPos3fv(const PFfloat *v) { raster_pos(v[0], v[1], v[2], 1.0f); }
+void pfRasterPos4i(PFint x, PFint y, PFint z, PFint w) { raster_pos((PFfloat)x, (PFfloat)y, (PFfloat)z, (PFfloat)w); }
+void pfRasterPos4f(PFfloat x, PFfloat y, PFfloat z, PFfloat w) { raster_pos(x, y, z, w); }
+void pfRasterPos4fv(const PFfloat *v) { raster_pos(v[0], v[1], v[2], v[3]); }
+
+// --- fog (context.c:2161-2351) -------------------------------------------------
+// The parameter setters keep the reference's behaviour: a density sets the
+// mode (truncated), and the vector forms accept any mode or density (their
+// range tests are always true).
+void pfFogi(PFfogparam p, PFint v)
+{
+    switch (p) {
+    case PF_FOG_MODE: if (v >= PF_LINEAR && v <= PF_EXP2) G->fog.mode = (uint32_t)v; else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_DENSITY: if (v == 0 || v == 1) G->fog.mode = (uint32_t)v; else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_START: G->fog.start = (PFfloat)v; break;
+    case PF_FOG_END: G->fog.end = (PFfloat)v; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfFogf(PFfogparam p, PFfloat v)
+{
+    switch (p) {
+    case PF_FOG_DENSITY: if (v >= 0 && v <= 1) G->fog.mode = ftou32_x86(v); else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_START: G->fog.start = v; break;
+    case PF_FOG_END: G->fog.end = v; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfFogiv(PFfogparam p, PFint *v)
+{
+    switch (p) {
+    case PF_FOG_MODE: case PF_FOG_DENSITY: G->fog.mode = (uint32_t)*v; break;
+    case PF_FOG_START: G->fog.start = (PFfloat)*v; break;
+    case PF_FOG_END: G->fog.end = (PFfloat)*v; break;
+    case PF_FOG_COLOR: G->fog.color = PFcolor{ (PFubyte)v[0], (PFubyte)v[1], (PFubyte)v[2], (PFubyte)v[3] }; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+void pfFogfv(PFfogparam p, PFfloat *v)
+{
+    switch (p) {
+    case PF_FOG_DENSITY: if (*v >= 0 || *v <= 1) G->fog.mode = ftou32_x86(*v); else G->err = PF_INVALID_VALUE; break;
+    case PF_FOG_START: G->fog.start = *v; break;
+    case PF_FOG_END: G->fog.end = *v; break;
+    case PF_FOG_COLOR: G->fog.color = PFcolor{ ftoub(255 * v[0]), ftoub(255 * v[1]), ftoub(255 * v[2]), ftoub(255 * v[3]) }; break;
+    default: G->err = PF_INVALID_ENUM; break;
+    }
+}
+// A framebuffer-wide device pass over the current framebuffer, in order
+// with the recorded draws.
+void pfFogProcess(void)
+{
+    Cmd cmd{};
+    cmd.kind = CMD_HOOK; cmd.fb = G->current; cmd.hook = 3;
+    cmd.hp.start = G->fog.start; cmd.hp.end = G->fog.end; cmd.hp.density = G->fog.density;
+    cmd.hp.mode = G->fog.mode; cmd.hp.color = pack(G->fog.color);
+    push_cmd(G, cmd);
+}
+
+// --- render lists (src/renderlist.c:6-97, context.c:1580-1685) ---------------
+// Recorded on the host as the reference records them (RenderList) and
+// replayed through the immediate-mode calls, which record into the deferred
+// renderer like any other draw.
+
+static void ctx_backup(Ctx *c)                       // pfiMakeContextBackup (internal/context/context.c:26-36)
+{
+    c->backup.mat[0] = c->mat[0]; c->backup.mat[1] = c->mat[1];
+    std::memcpy(c->backup.tex, c->curTex, 8); std::memcpy(c->backup.nrm, c->curNormal, 12);
+    c->backup.col = c->curColor; c->backup.texture = c->texture; c->backup.state = c->state;
+}
+static void ctx_restore(Ctx *c)                      // pfiRestoreContext (:38-48)
+{
+    c->mat[0] = c->backup.mat[0]; c->mat[1] = c->backup.mat[1];
+    std::memcpy(c->curTex, c->backup.tex, 8); std::memcpy(c->curNormal, c->backup.nrm, 12);
+    c->curColor = c->backup.col; c->texture = c->backup.texture; c->state = c->backup.state;
+    c->stateDirty = true;
+}
+static void list_begin(Ctx *c, PFdrawmode mode)
+{
+    RenderCall k;
+    k.mode = mode; k.mat[0] = c->mat[0]; k.mat[1] = c->mat[1]; k.texture = c->texture;
+    c->curList->calls.push_back(std::move(k));
+}
+static void list_vertex(Ctx *c, const PFfloat *v)
+{
+    if (c->curList->calls.empty()) return;           // the reference indexes call -1
+    RenderCall &k = c->curList->calls.back();
+    k.pos.insert(k.pos.end(), v, v + 4);
+    k.uv.insert(k.uv.end(), c->curTex, c->curTex + 2);
+    k.nrm.insert(k.nrm.end(), c->curNormal, c->curNormal + 3);
+    k.col.push_back(c->curColor);
+}
+
+PFrenderlist pfGenList(void) { return new RenderList(); }
+void pfDeleteList(PFrenderlist *pl)
+{
+    if (!pl) return;
+    RenderList *l = (RenderList *)*pl;
+    if (G && G->curList == l) G->curList = nullptr;
+    delete l;
+    *pl = nullptr;
+}
+void pfNewList(PFrenderlist pl)
+{
+    if (!pl) { G->err = PF_INVALID_VALUE; return; }
+    RenderList *l = (RenderList *)pl;
+    l->calls.clear();
+    G->curList = l;
+    ctx_backup(G);
+}
+void pfEndList(void)
+{
+    if (!G->curList) G->err = PF_INVALID_OPERATION;
+    G->curList = nullptr;
+    ctx_restore(G);
+}
+void pfCallList(const PFrenderlist pl)
+{
+    const RenderList *l = (const RenderList *)pl;
+    if (!l) { G->err = PF_INVALID_VALUE; return; }
+    Ctx *c = G;
+    ctx_backup(c);
+    for (const RenderCall &k : l->calls) {
+        c->mat[0] = k.mat[0]; c->mat[1] = k.mat[1];
+        c->stateDirty = true;
+        pfBindTexture(k.texture);
+        pfBegin(k.mode);
+        for (size_t j = 0; j < k.col.size(); j++) {
+            pfColor4ubv((const PFubyte *)&k.col[j]);
+            pfTexCoordfv(&k.uv[2 * j]);
+            pfNormal3fv(&k.nrm[3 * j]);
+            pfVertex4fv(&k.pos[4 * j]);
+        }
+        pfEnd();
+    }
+    ctx_restore(c);
+}
 
 // --- readback, post-process -----------------------------------------------------
 void pfFinish(void) { if (G) flush(G); }

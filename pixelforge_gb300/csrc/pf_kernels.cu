@@ -31,7 +31,8 @@ namespace {
 
 #include "pf_common.cuh"
 
-static_assert((unsigned)PFP_DEPTH_TEST == (unsigned)PFS_DEPTH_TEST, "points and lines reuse the draw-state depth-test bit");
+static_assert((unsigned)PFP_DEPTH_TEST == (unsigned)PFS_DEPTH_TEST && (unsigned)PFP_BLEND == (unsigned)PFS_BLEND &&
+              (unsigned)PFP_DEPTH_WRITE == (unsigned)PFS_DEPTH_MASK, "host-set records carry draw-state bits");
 
 
 // ---------------------------------------------------------------------------
@@ -899,8 +900,9 @@ __device__ __forceinline__ void derive_chunk_prim(const PFPrim &P, uint32_t ox, 
     cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
     const PFDrawState &St = states[P.flags >> 8];
     cp.rstate = (St.flags & 0xffffu) | ((uint32_t)St.depthFunc << 16) | ((uint32_t)St.blendMode << 24);
-    // points and lines carry their own depth-test bit (a thick line's centre is always tested)
-    if (P.flags & PFP_KIND) cp.rstate = (cp.rstate & ~(uint32_t)PFS_DEPTH_TEST) | (P.flags & PFP_DEPTH_TEST);
+    // host-set records carry their own depth test, blending and depth write
+    // (a thick line's centre is always tested; pfRectf does none of them)
+    if (P.flags & PFP_KIND) cp.rstate = (cp.rstate & ~(uint32_t)PFP_OPS) | (P.flags & PFP_OPS);
     dp.e0[0] = cp.e0[0]; dp.e0[1] = cp.e0[1]; dp.e0[2] = cp.e0[2];
     dp.ex0 = cp.ex[0]; dp.ex1 = cp.ex[1]; dp.ex2 = cp.ex[2];
     dp.ey0 = cp.ey[0]; dp.ey1 = cp.ey[1]; dp.ey2 = cp.ey[2];
@@ -1003,6 +1005,7 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
 // ---------------------------------------------------------------------------
 __device__ __noinline__ bool lp_covers(const PFPrim &P, int32_t X, int32_t Y)
 {
+    if ((P.flags & PFP_KIND) == PFP_BLIT) return true;          // every pixel of its box
     if ((P.flags & PFP_KIND) == PFP_POINT) {                     // points.c:106-183
         const int32_t dx = X - P.x1, dy = Y - P.y1;
         if (P.x2 < 0) return dx == 0 && dy == 0;
@@ -1027,9 +1030,31 @@ __device__ __forceinline__ float lp_t(const PFPrim &P, int32_t X, int32_t Y)
     return (float)i * P.wInvSum;
 }
 
+// (PFsizei)(float) as the reference's x86-64 build converts it: a 64-bit
+// truncating conversion whose low 32 bits are kept; 0 for NaN / out of range.
+__device__ __forceinline__ uint32_t x86_ftou32(float x)
+{
+    if (!(x > -9.2e18f && x < 9.2e18f)) return 0u;
+    return (uint32_t)(unsigned long long)__float2ll_rz(x);
+}
+
+// A pfRectf record's colour, or the pfDrawPixels source pixel that lands on
+// (X, Y) (context.c:2044-2082): x1, y1 the raster position on screen, x2 the
+// image width, y2 / x3 width - 1 / height - 1, wInvSum / z2 the inverse
+// zoomed width / height.  Elements past the image read as 0.
+__device__ __forceinline__ uint32_t blit_color(const PFPrim &P, int32_t X, int32_t Y)
+{
+    if (!P.src) return P.c1;
+    const float v = (float)(int32_t)((uint32_t)Y - (uint32_t)P.y1) * P.z2;
+    const uint32_t ySrc = x86_ftou32(v * (float)(uint32_t)P.x3) * (uint32_t)P.x2;
+    const float u = (float)(int32_t)((uint32_t)X - (uint32_t)P.x1) * P.wInvSum;
+    const uint32_t o = ySrc + x86_ftou32(u * (float)(uint32_t)P.y2);
+    return o < P.nSrc ? __ldg(reinterpret_cast<const uint32_t *>(P.src) + o) : 0u;
+}
+
 __device__ __noinline__ float lp_depth(const PFPrim &P, int32_t X, int32_t Y)
 {
-    if ((P.flags & PFP_KIND) == PFP_POINT) return P.z1;
+    if ((P.flags & PFP_KIND) != PFP_LINE) return P.z1;
     const float t = lp_t(P, X, Y);
     return P.z1 + t * (P.z2 - P.z1);
 }
@@ -1038,6 +1063,7 @@ __device__ __noinline__ float lp_depth(const PFPrim &P, int32_t X, int32_t Y)
 __device__ __noinline__ uint32_t lp_color(const PFPrim &P, int32_t X, int32_t Y)
 {
     if ((P.flags & PFP_KIND) == PFP_POINT) return P.c1;
+    if ((P.flags & PFP_KIND) == PFP_BLIT) return blit_color(P, X, Y);
     const float t = lp_t(P, X, Y);
     int32_t o[4];
     for (int i = 0; i < 4; i++) {
@@ -1137,6 +1163,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ float fz[RASTER_THREADS / 32][FWIN];
     __shared__ uint32_t woff[RASTER_THREADS / 32][33];
     __shared__ int sDense, sAnyLP;
+    __shared__ uint32_t sBlit;                        // chunk records that are rectangles (not counted as fragments)
 
     if (a.cnt->abortCommand <= a.command) return;
     // the batch completed set-up without overflow: its sub-triangles count
@@ -1228,6 +1255,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 const bool has = lane < cn;
                 uint32_t bh = 0, area = 0;
                 const bool anyLP = __any_sync(0xffffffffu, has && (sprim[lane].flags & PFP_KIND));
+                const uint32_t blit = __ballot_sync(0xffffffffu, has && (sprim[lane].flags & PFP_KIND) == PFP_BLIT);
                 if (has) {
                     const PFPrim &P = sprim[lane];
                     ChunkPrim cp;
@@ -1247,7 +1275,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 // boxes that cover half a tile on average: test every
                 // (pixel, sub-triangle) pair instead of stepping rows
                 // (points and lines always take the row path)
-                if (lane == 0) { sDense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP; sAnyLP = anyLP; }
+                if (lane == 0) { sDense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP; sAnyLP = anyLP; sBlit = blit; }
             }
             __syncthreads();
             uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
@@ -1310,7 +1338,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 //    submission order, which leave the set of visible fragments
                 const uint32_t m = pmask[tid];
                 const uint32_t cntp = __popc(m);
-                frags += cntp;
+                frags += lpChunk ? __popc(m & ~sBlit) : cntp;
                 uint32_t myOff, wtotal;
                 warp_offsets(cntp, woff[warp], myOff, wtotal);
                 for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
@@ -1445,6 +1473,21 @@ __global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, 
             uint32_t r = 0;
             for (int ch = 0; ch < 4; ch++) r |= (((chn(c, ch) * k + chn(hp.color, ch) * (255u - k)) / 255u) & 255u) << (8 * ch);
             c = r;
+        } else if (hook == 3) {   // pfFogProcess (context.c:2288-2351)
+            const float d = depth[i];
+            const uint32_t alpha = hp.color >> 24, fc = hp.color & 0x00ffffffu;
+            if (d >= hp.end) {
+                const uint32_t f = fc | (alpha << 24);
+                c = alpha == 255u ? f : blend_sisd(1, f, c);
+            } else if (d > hp.start) {
+                float t = 0.0f;
+                const float invLen = 1.0f / (hp.end - hp.start);
+                if (hp.mode == 0) t = (d - hp.start) * invLen;
+                else if (hp.mode == 1) t = 1.0f - (float)exp((double)(-hp.density * (d - hp.start)));
+                else if (hp.mode == 2) t = 1.0f - (float)exp2((double)(-hp.density * (d - hp.start)));
+                const uint32_t a = (uint32_t)x86_cvt_trunc(t * (float)alpha) & 255u;
+                c = blend_sisd(1, fc | (a << 24), c);
+            }
         } else if (hook == 2) {   // grayscale
             uint32_t gy = (77u * chn(c, 0) + 150u * chn(c, 1) + 29u * chn(c, 2)) >> 8;
             c = gy | (gy << 8) | (gy << 16) | (c & 0xff000000u);

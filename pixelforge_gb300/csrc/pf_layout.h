@@ -131,15 +131,21 @@ typedef struct {
     uint32_t pad[2];
 } PFVertexOut;                    /* 64 bytes */
 
-/* PFPrim.flags bits: bit0 face (1 = BACK), bit1 3D path, bits 2-3 the kind
- * of primitive, bits 8.. the draw state.  Points and lines (set up on the
- * host) use the fields as noted in pf_host.cpp (lp_line_prim, lp_point_prim). */
+/* PFPrim.flags bits: bit0 face (1 = BACK), bit1 3D path, bits 6-7 the kind
+ * of record, bits 8.. the draw state.  Records other than triangles are set
+ * up on the host (pf_host.cpp: lp_point, lp_thin_line, pfRectf,
+ * pfDrawPixels) and carry their own per-fragment operations in bits 3-5,
+ * which stand in for the draw state's (same bit positions as PFS_*). */
 enum {
-    PFP_LINE = 1u << 2,           /* a thin line of the reference's 16.16 DDA */
-    PFP_POINT = 2u << 2,          /* a point: one pixel or a disc */
-    PFP_KIND = 3u << 2,
-    PFP_DEPTH_TEST = 1u << 4,     /* points and lines: depth-test this primitive */
-    PFP_Y_LONGER = 1u << 5        /* lines: y is the long axis */
+    PFP_Y_LONGER = 1u << 2,       /* lines: y is the long axis */
+    PFP_BLEND = 1u << 3,          /* blend (scalar rules) */
+    PFP_DEPTH_TEST = 1u << 4,     /* depth-test (scalar rules) */
+    PFP_DEPTH_WRITE = 1u << 5,    /* write depth */
+    PFP_OPS = PFP_BLEND | PFP_DEPTH_TEST | PFP_DEPTH_WRITE,
+    PFP_LINE = 1u << 6,           /* a thin line of the reference's 16.16 DDA */
+    PFP_POINT = 2u << 6,          /* a point: one pixel or a disc */
+    PFP_BLIT = 3u << 6,           /* a rectangle: pfRectf colour or pfDrawPixels image */
+    PFP_KIND = 3u << 6
 };
 
 /* Set-up sub-triangle, as read by the tile rasterizer. */
@@ -153,7 +159,9 @@ typedef struct {
     uint32_t c1, c2, c3, pad0;
     float u1, v1, u2, v2;
     float u3, v3, pad1, pad2;
-    float pad3[4];
+    uint64_t src;                 /* PFP_BLIT: device address of the RGBA8 image, 0 for a plain colour */
+    uint32_t nSrc;                /* PFP_BLIT: pixels in the image */
+    float pad3;
 } PFPrim;                         /* 128 bytes */
 
 typedef struct {

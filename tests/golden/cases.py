@@ -246,6 +246,11 @@ def lp(seed):
     return lambda lib: run_lp(lib, lp_case(seed))
 
 
+def px(seed):
+    from pixscenes import px_case, run_px
+    return lambda lib: run_px(lib, px_case(seed))
+
+
 def _scene(sc, **kw):
     return lambda lib: sc.render(lib, "fbo", **kw)
 
@@ -283,13 +288,19 @@ def cases() -> dict:
         c[f"mix_{s}"] = mix(5000 + s)
     for s in range(24):
         c[f"lp_{s}"] = lp(7000 + s)
+    for s in range(16):
+        c[f"px_{s}"] = px(9000 + s)
     return c
 
 
-# cases whose colour goes through the Gouraud specular powf of the host libm
+# cases whose colour goes through the host libm (the Gouraud specular powf,
+# the fog's expf / exp2f)
 def uses_host_powf(name: str) -> bool:
     if name.startswith("sphere"):
         return True
+    if name.startswith("px_"):
+        from pixscenes import px_case
+        return px_case(9000 + int(name.split("_")[1]))["kind"] in ("fog", "list")
     if name.startswith("mix_"):
         from mixscenes import mix_case
         return mix_case(5000 + int(name.split("_")[1]))["lighting"] == "gouraud"

@@ -110,6 +110,31 @@ def state_script(lib):
         lib.pfGetIntegerv(A.PF_BLEND_FUNC, v)
         out.append(("blend func", v[0]))
         out.append(("err end", lib.pfGetError()))
+        # raster position, pixel zoom, fog and render-list parameter errors
+        lib.pfRasterPos3f(2.75, -1.5, 0.25)
+        lib.pfGetFloatv(A.PF_CURRENT_RASTER_POSITION, f)
+        out.append(("raster pos f", [f[0], f[1]]))
+        lib.pfGetIntegerv(A.PF_CURRENT_RASTER_POSITION, v)
+        out.append(("raster pos i", [v[0], v[1]]))
+        lib.pfPixelZoom(2.5, 0.5)
+        for name, e in (("zoom x", 10032), ("zoom y", 10033)):
+            lib.pfGetFloatv(e, f)
+            out.append((name, f[0]))
+        for call in (lambda: lib.pfFogi(0, 3), lambda: lib.pfFogi(1, 2), lambda: lib.pfFogf(0, 1.0),
+                     lambda: lib.pfFogf(1, 1.5), lambda: lib.pfFogi(4, 1), lambda: lib.pfFogi(9, 1)):
+            call()
+            out.append(("fog param", lib.pfGetError()))
+        lib.pfNewList(None)
+        out.append(("new null list", lib.pfGetError()))
+        lib.pfEndList()
+        out.append(("end without list", lib.pfGetError()))
+        px = (C.c_uint8 * 16)()
+        lib.pfDrawPixels(0, 2, A.PF_RGBA, A.PF_UNSIGNED_BYTE, px)
+        out.append(("draw pixels empty", lib.pfGetError()))
+        lib.pfDrawPixels(2, 2, 11, A.PF_UNSIGNED_BYTE, px)
+        out.append(("draw pixels format", lib.pfGetError()))
+        lib.pfDrawPixels(2, 2, A.PF_RGBA, 2, px)
+        out.append(("draw pixels no getter", lib.pfGetError()))
         lib.pfMatrixMode(12345)
         out.append(("bad matrix mode", lib.pfGetError()))
         out.append(("error reset", lib.pfGetError()))

@@ -44,3 +44,13 @@ def test_oracle_equals_reference_points_lines(oracle, ref_shim, seed):
     from lpscenes import lp_case, run_lp
     case = lp_case(seed)
     same(run_lp(oracle, case), run_lp(ref_shim, case), f"points/lines {seed} {case}")
+
+
+@pytest.mark.parametrize("seed", range(0, 80))
+def test_oracle_equals_reference_lists_rects_pixels_fog(oracle, ref_shim, seed):
+    """Render lists, pfRect*, pfDrawPixels (every source format, zooms,
+    depth test and blending) and pfFog* / pfFogProcess, interleaved with
+    triangles."""
+    from pixscenes import px_case, run_px
+    case = px_case(seed)
+    same(run_px(oracle, case), run_px(ref_shim, case), f"extras {seed} {case}")

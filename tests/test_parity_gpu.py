@@ -183,3 +183,24 @@ def test_wireframe_1080(gpu, oracle, target):
     assert (ref.color.reshape(-1, 4)[:, :3].any(-1)).sum() > 100000       # drawn pixels
     assert_parity(got, ref, exact_color=True, label=f"wireframe {target}")
     assert got.stats["fragments"] == ref.stats["fragments"]
+
+
+@pytest.mark.parametrize("seed", range(0, 80))
+def test_lists_rects_pixels_fog(gpu, oracle, seed):
+    """Render lists, pfRect*, pfDrawPixels and pfFogProcess in order with
+    triangles: depth bit-exact, colour exact (within 1 LSB where it goes
+    through the host libm: the fog's e^x / 2^x, the lists' lit replays)."""
+    from pixscenes import px_case, run_px
+    case = px_case(seed)
+    got = run_px(gpu, case)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert_parity(got, run_px(oracle, case), exact_color=case["kind"] not in ("fog", "list"),
+                  label=f"extras {seed} {case}")
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_lists_rects_pixels_fog_main_target(gpu, oracle, seed):
+    from pixscenes import px_case, run_px
+    case = px_case(seed)
+    assert_parity(run_px(gpu, case, "main"), run_px(oracle, case, "main"), exact_color=case["kind"] not in ("fog", "list"),
+                  label=f"extras main {seed}")
