@@ -2653,19 +2653,111 @@ void pfCallList(const PFrenderlist pl)
 // --- readback, post-process -----------------------------------------------------
 void pfFinish(void) { if (G) flush(G); }
 
-void pfReadPixels(PFint x, PFint y, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, void *pixels)
+// pfmFloatToHalfI (src/pfm.h:108-126): round half up on the dropped bits,
+// flush below 2^-14, infinity from 2^16, all NaNs quiet.
+static uint16_t float_to_half(float x)
 {
-    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { G->err = PF_INVALID_ENUM; return; }
+    uint32_t ui; std::memcpy(&ui, &x, 4);
+    const int s = (int)((ui >> 16) & 0x8000u);
+    const int em = (int)(ui & 0x7fffffffu);
+    int h = (em - (112 << 23) + (1 << 12)) >> 13;
+    h = (em < (113 << 23)) ? 0 : h;
+    h = (em >= (143 << 23)) ? 0x7c00 : h;
+    h = (em > (255 << 23)) ? 0x7e00 : h;
+    return (uint16_t)(s | h);
+}
+
+// The reference's scalar pixel setter (src/internal/pixel.h:52-405) writing
+// RGBA8 colour col as element o of a buffer of format f / type t.
+#define FTOUB ftoub
+static void pixel_set_sisd(PFpixelformat f, PFdatatype t, void *dst, size_t o, uint32_t col)
+{
+    const float inv = (float)(1.0 / 255);
+    const uint32_t r = col & 255u, g = (col >> 8) & 255u, b = (col >> 16) & 255u, a = col >> 24;
+    uint8_t *p8 = (uint8_t *)dst;
+    uint16_t *p16 = (uint16_t *)dst;
+    float *pf = (float *)dst;
+    /* PF_COLOR_GARYSCALE (src/internal/pixel.h:69-74) */
+    const float gray = (float)r * inv * 0.299f + (float)g * inv * 0.587f + (float)b * inv * 0.114f;
+    uint32_t ch = 0;
+    switch (f) {
+    case PF_RED: ch = r; break;
+    case PF_GREEN: ch = g; break;
+    case PF_BLUE: ch = b; break;
+    case PF_ALPHA: ch = a; break;
+    default: break;
+    }
+    switch (f) {
+    case PF_RED: case PF_GREEN: case PF_BLUE: case PF_ALPHA:
+        if (t == PF_UNSIGNED_BYTE) p8[o] = (uint8_t)ch;
+        else if (t == PF_HALF_FLOAT) p16[o] = float_to_half((float)ch / 255.0f);
+        else pf[o] = (float)ch / 255.0f;
+        return;
+    case PF_LUMINANCE:
+        if (t == PF_UNSIGNED_BYTE) p8[o] = FTOUB(255.0f * gray);
+        else if (t == PF_HALF_FLOAT) p16[o] = float_to_half(gray);
+        else pf[o] = gray;
+        return;
+    case PF_LUMINANCE_ALPHA:
+        if (t == PF_UNSIGNED_BYTE) { p8[2 * o] = FTOUB(255 * gray); p8[2 * o + 1] = (uint8_t)a; }
+        else if (t == PF_HALF_FLOAT) { p16[2 * o] = float_to_half(gray); p16[2 * o + 1] = float_to_half((float)a * inv); }
+        else { pf[2 * o] = gray; pf[2 * o + 1] = (float)a * inv; }
+        return;
+    default: break;
+    }
+    /* PF_COLOR_{RGB,BGR,RGBA,BGRA}_NORMALIZE (pixel.h:36-66): the BGRA one keeps RGBA order */
+    const int bgr = (f == PF_BGR);
+    float n[4] = { (float)r * inv, (float)g * inv, (float)b * inv, (float)a * inv };
+    if (bgr) { n[0] = (float)b * inv; n[2] = (float)r * inv; }
+    if (t == PF_UNSIGNED_SHORT_5_6_5) {
+        const uint32_t c0 = (uint8_t)std::round(n[0] * 31.0f), c1 = (uint8_t)std::round(n[1] * 63.0f), c2 = (uint8_t)std::round(n[2] * 31.0f);
+        p16[o] = (uint16_t)(c0 << 11 | c1 << 5 | c2);
+        return;
+    }
+    if (t == PF_UNSIGNED_SHORT_5_5_5_1) {
+        const uint32_t c0 = (uint8_t)std::round(n[0] * 31.0f), c1 = (uint8_t)std::round(n[1] * 31.0f), c2 = (uint8_t)std::round(n[2] * 31.0f);
+        const uint32_t al = ((double)n[3] > (double)(float)50 * (1.0 / 255)) ? 1u : 0u;
+        p16[o] = (uint16_t)(c0 << 11 | c1 << 6 | c2 << 1 | al);
+        return;
+    }
+    if (t == PF_UNSIGNED_SHORT_4_4_4_4) {
+        const uint32_t c0 = (uint8_t)std::round(n[0] * 15.0f), c1 = (uint8_t)std::round(n[1] * 15.0f);
+        const uint32_t c2 = (uint8_t)std::round(n[2] * 15.0f), c3 = (uint8_t)std::round(n[3] * 15.0f);
+        p16[o] = (uint16_t)(c0 << 12 | c1 << 8 | c2 << 4 | c3);
+        return;
+    }
+    const int k = (f == PF_RGB || f == PF_BGR) ? 3 : 4;
+    if (t == PF_UNSIGNED_BYTE) {
+        const uint32_t v[4] = { (f == PF_BGR || f == PF_BGRA) ? b : r, g, (f == PF_BGR || f == PF_BGRA) ? r : b, a };
+        for (int i = 0; i < k; i++) p8[(size_t)k * o + (size_t)i] = (uint8_t)v[i];
+    } else if (t == PF_HALF_FLOAT) {
+        for (int i = 0; i < k; i++) p16[(size_t)k * o + (size_t)i] = float_to_half(n[i]);
+    } else {
+        for (int i = 0; i < k; i++) pf[(size_t)k * o + (size_t)i] = n[i];
+    }
+}
+#undef FTOUB
+
+void pfReadPixels(PFint x, PFint y, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, void *pixels)
+{                                                                    // context.c:2353-2395
+    if (!(f >= PF_RED && f <= PF_BGRA && t >= PF_UNSIGNED_BYTE && t <= PF_DOUBLE)) { G->err = PF_INVALID_ENUM; return; }
+    if (!texel_bytes(f, t)) { G->err = PF_INVALID_ENUM; return; }
     sync_host(G);
     const Tex *s = (const Tex *)G->current->texture;
     auto cl = [](PFint v, PFint lo, PFint hi) { return v < lo ? lo : (v > hi ? hi : v); };
     PFint xMin = cl(x, 0, (PFint)s->w - 1), yMin = cl(y, 0, (PFint)s->h - 1);
     PFint xMax = cl(x + (PFint)w, 0, (PFint)s->w), yMax = cl(y + (PFint)h, 0, (PFint)s->h);
     const uint32_t *src = (const uint32_t *)s->pixels;
-    uint32_t *dst = (uint32_t *)pixels;
+    if (f == PF_RGBA && t == PF_UNSIGNED_BYTE) {
+        uint32_t *dst = (uint32_t *)pixels;
+        for (PFint yy = yMin; yy < yMax; yy++)
+            for (PFint xx = xMin; xx < xMax; xx++)
+                dst[(size_t)(yy - yMin) * w + (size_t)(xx - xMin)] = src[(size_t)yy * s->w + (size_t)xx];
+        return;
+    }
     for (PFint yy = yMin; yy < yMax; yy++)
         for (PFint xx = xMin; xx < xMax; xx++)
-            dst[(size_t)(yy - yMin) * w + (size_t)(xx - xMin)] = src[(size_t)yy * s->w + (size_t)xx];
+            pixel_set_sisd(f, t, pixels, (size_t)(yy - yMin) * w + (size_t)(xx - xMin), src[(size_t)yy * s->w + (size_t)xx]);
 }
 
 void pfPostProcess(PFpostprocessfunc fn)                             // context.c:2397-2441

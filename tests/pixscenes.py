@@ -222,3 +222,31 @@ def run_px(lib: A.PixelForgeLib, case: dict, target: str = "fbo") -> Frame:
             th = C.c_void_p(tex)
             lib.pfDeleteTexture(C.byref(th), False)
         tg.close()
+
+
+_TYPE_BYTES = {0: 1, 2: 2, 3: 2, 4: 2, 9: 2, 10: 4}
+
+
+def run_readback(lib: A.PixelForgeLib, seed: int, target: str = "fbo") -> dict:
+    """A small scene read back with pfReadPixels into every format the
+    reference has a setter for, over regions partly outside the
+    framebuffer; returns the bytes of each read."""
+    r = np.random.default_rng(seed + 404)
+    W, H = 40, 30
+    tg = Target(lib, W, H, target)
+    out = {}
+    try:
+        lib.pfClearColor(10, 20, 30, 200)
+        lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+        lib.pfDisable(A.PF_CULL_FACE)
+        _soup(lib, r, 20, "default")
+        for fmt, typ in PIXEL_FORMATS:
+            x, y = int(r.integers(-5, 30)), int(r.integers(-5, 24))
+            w, h = int(r.integers(1, 30)), int(r.integers(1, 20))
+            n = w * h * (1 if typ in (2, 3, 4) else _COMPS[fmt]) * _TYPE_BYTES[typ]
+            buf = np.full(n + 16, 0xA5, np.uint8)
+            lib.pfReadPixels(x, y, w, h, fmt, typ, _ptr(buf))
+            out[(fmt, typ)] = (buf, lib.pfGetError())
+        return out
+    finally:
+        tg.close()

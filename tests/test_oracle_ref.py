@@ -54,3 +54,14 @@ def test_oracle_equals_reference_lists_rects_pixels_fog(oracle, ref_shim, seed):
     from pixscenes import px_case, run_px
     case = px_case(seed)
     same(run_px(oracle, case), run_px(ref_shim, case), f"extras {seed} {case}")
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_oracle_equals_reference_read_pixels(oracle, ref_shim, seed):
+    """pfReadPixels into every format / type with a setter, regions partly
+    outside the framebuffer."""
+    from pixscenes import run_readback
+    a, b = run_readback(oracle, seed), run_readback(ref_shim, seed)
+    for k in a:
+        assert a[k][1] == b[k][1] == 0, k
+        assert np.array_equal(a[k][0], b[k][0]), f"format/type {k}: bytes differ"

@@ -204,3 +204,12 @@ def test_lists_rects_pixels_fog_main_target(gpu, oracle, seed):
     case = px_case(seed)
     assert_parity(run_px(gpu, case, "main"), run_px(oracle, case, "main"), exact_color=case["kind"] not in ("fog", "list"),
                   label=f"extras main {seed}")
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_read_pixels_formats(gpu, oracle, seed):
+    from pixscenes import run_readback
+    a, b = run_readback(gpu, seed), run_readback(oracle, seed)
+    for k in a:
+        assert a[k][1] == b[k][1] == 0, k
+        assert np.array_equal(a[k][0], b[k][0]), f"format/type {k}: bytes differ"
