@@ -105,6 +105,34 @@ __device__ __forceinline__ void to_screen(const PFDrawState &S, float hx, float 
     sy = ((float)S.vpPos[1] + (1.0f - hy) * 0.5f * (float)S.vpDim[1]) + 0.5f;
 }
 
+// The per-fragment operations of a draw state, packed for the tile
+// rasterizer: PFS_* bits | depth function << 16 | blend mode << 24.
+__device__ __forceinline__ uint32_t raster_state(const PFDrawState &S)
+{
+    return (S.flags & 0xffffu) | ((uint32_t)S.depthFunc << 16) | ((uint32_t)S.blendMode << 24);
+}
+
+// A bound below which no fragment depth of the sub-triangle can fall, for
+// PF_LESS (and, one step lower, PF_LEQUAL).  The depth of a covered pixel is
+// 1 / ((z1 wN1 + z2 wN2) + z3 wN3) with wN >= 0 summing to 1 within a few
+// ulps, so the interpolated term lies in [min z, max z] widened by a
+// relative 1e-5; its reciprocal is bounded by the reciprocals of the ends
+// when they have one sign.  NaN (never rejects) otherwise.
+__device__ __forceinline__ float depth_reject_bound(const PFPrim &P, uint32_t rstate)
+{
+    const float qnan = __int_as_float(0x7fffffff);
+    const int func = (int)((rstate >> 16) & 255u);
+    if (!(rstate & PFS_DEPTH_TEST) || (func != 2 && func != 3)) return qnan;
+    const float lo = fminf(P.z1, fminf(P.z2, P.z3)), hi = fmaxf(P.z1, fmaxf(P.z2, P.z3));
+    if (!(fabsf(lo) < 1e30f && fabsf(hi) < 1e30f)) return qnan;
+    float b;
+    if (lo > 0.0f) b = __fdiv_rn(1.0f, hi * 1.00001f) * 0.99999f;         // interpolated term <= hi (1 + 1e-5)
+    else if (hi < 0.0f) b = __fdiv_rn(1.0f, hi * 0.99999f) * 1.00001f;    // term <= hi (1 - 1e-5) < 0
+    else return qnan;
+    if (!(fabsf(b) < 1e30f)) return qnan;
+    return func == 2 ? b : nextafterf(b, -INFINITY);
+}
+
 // Rasterize_Triangle set-up (triangles.c:287-349).  Returns false if culled.
 __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVert &a, const SVert &b,
                            const SVert &c, int stateIdx, PFPrim &P)
@@ -132,9 +160,11 @@ __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVer
     P.poolBase = -1;
     P.wInvSum = 1.0f / (float)(int32_t)(r1 + r2 + r3);
     P.z1 = a.z; P.z2 = b.z; P.z3 = c.z;
-    P.c1 = a.c; P.c2 = b.c; P.c3 = c.c; P.pad0 = 0;
+    P.c1 = a.c; P.c2 = b.c; P.c3 = c.c;
+    P.rstate = raster_state(S);
     P.u1 = a.u; P.v1 = a.v; P.u2 = b.u; P.v2 = b.v; P.u3 = c.u; P.v3 = c.v;
-    P.pad1 = P.pad2 = 0.0f;
+    P.zReject = depth_reject_bound(P, P.rstate);
+    P.pad2 = 0.0f;
     P.src = 0; P.nSrc = 0; P.pad3 = 0.0f;
     return true;
 }

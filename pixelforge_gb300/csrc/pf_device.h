@@ -31,6 +31,7 @@ struct PFBatchLaunch {
     PFPrimPhong *poolPh;
     uint32_t poolCap;
     uint32_t *binCount;       /* totalTiles */
+    uint32_t *tileList;       /* totalTiles: the tiles with a non-empty bin; NULL: queue every tile */
     uint32_t *bins;           /* totalTiles * cap */
     uint32_t cap;
     const PFTarget *targets;  /* device */

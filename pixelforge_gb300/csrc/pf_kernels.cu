@@ -375,7 +375,7 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (cnt->abortCommand != 0xffffffffu) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
-    if (g == 0) { cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0; }
+    if (g == 0) { cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0; cnt->tileListCount = 0; }
     const uint32_t g0 = blockIdx.x * blockDim.x;
     if (g0 >= nVerts) return;
     // the block's vertices usually belong to one segment: stage it and its
@@ -453,6 +453,7 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
 
 struct BinArgs {
     uint32_t *binCount;
+    uint32_t *tileList;        // tiles with a non-empty bin (NULL: not listed)
     uint32_t *bins;
     uint32_t cap;
     const PFTarget *targets;
@@ -499,6 +500,12 @@ __device__ __forceinline__ void bin_slot(const BinArgs &B, uint32_t t, uint32_t 
     }
 }
 
+// The first entry of a tile's bin puts the tile on the raster work list.
+__device__ __forceinline__ void list_tile(const BinArgs &B, uint32_t t)
+{
+    if (B.tileList) B.tileList[atomicAdd(&B.cnt->tileListCount, 1u)] = t;
+}
+
 // Append `key` to the bin of every tile the sub-triangle touches (one
 // thread; used by the clipping path).
 __device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, uint32_t key)
@@ -508,7 +515,9 @@ __device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, 
     for (uint32_t ty = ty0; ty < ty0 + nty; ty++)
         for (uint32_t tx = tx0; tx < tx0 + ntx; tx++) {
             const uint32_t t = T.tileBase + ty * T.tilesX + tx;
-            bin_slot(B, t, atomicAdd(&B.binCount[t], 1u), key);
+            const uint32_t slot = atomicAdd(&B.binCount[t], 1u);
+            if (slot == 0) list_tile(B, t);
+            bin_slot(B, t, slot, key);
         }
 }
 
@@ -532,7 +541,10 @@ __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, co
         if (!act) continue;
         const uint32_t leader = __ffs(grp) - 1;
         uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&B.binCount[t], (unsigned)__popc(grp));
+        if (lane == leader) {
+            base = atomicAdd(&B.binCount[t], (unsigned)__popc(grp));
+            if (base == 0) list_tile(B, t);
+        }
         base = __shfl_sync(grp, base, leader);
         bin_slot(B, t, base + __popc(grp & lt), key);
     }
@@ -704,6 +716,10 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
         const uint32_t r = (uint32_t)reinterpret_cast<const int4 *>(sg.explicitItems)[k].x;
         P = static_cast<const PFPrim *>(sg.prebuilt)[r];
         P.flags = (P.flags & 0xffu) | ((uint32_t)sg.state << 8);
+        // its own depth test, blending and depth write stand in for the
+        // state's (a thick line's centre is always tested; pfRectf does none)
+        P.rstate = (raster_state(S) & ~(uint32_t)PFP_OPS) | (P.flags & PFP_OPS);
+        P.zReject = __int_as_float(0x7fffffff);
         O.prims[g] = P;
         return true;
     }
@@ -816,6 +832,7 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 
 struct RasterArgs {
     const uint32_t *binCount;
+    const uint32_t *tileList;
     const uint32_t *bins;
     uint32_t cap;
     const PFPrim *prims;
@@ -831,11 +848,19 @@ struct RasterArgs {
     int anyPhong;
 };
 
+// A chunk record in shared memory, padded to 144 bytes: lane i's record
+// starts 4 banks after lane i-1's, so 16-byte loads of the records of 8
+// lanes touch all 32 banks once (with 128 bytes they would all start in
+// bank 0).
+struct __align__(16) SPrim {
+    PFPrim p;
+    int4 pad;
+};
+
 struct ChunkPrim {             // per-sub-triangle data derived for this tile
     int32_t e0[3];             // edge functions at the tile origin
     int32_t ex[3], ey[3];      // their x and y steps
     uint32_t bx0, by0, bw, bh; // bounding box clipped to the tile (tile-relative)
-    float invBw;
     uint32_t flags;            // face | is3D | state << 8
     uint32_t rstate;           // the state's PFS_* flags | depth function << 16 | blend mode << 24
 };
@@ -854,63 +879,44 @@ struct __align__(16) DenseP {
     float zReject;             // every covered fragment fails the depth test when zReject >= depth (NaN: never)
 };
 
-// A bound below which no fragment depth of the sub-triangle can fall, for
-// PF_LESS (and, one step lower, PF_LEQUAL).  The depth of a covered pixel is
-// 1 / ((z1 wN1 + z2 wN2) + z3 wN3) with wN >= 0 summing to 1 within a few
-// ulps, so the interpolated term lies in [min z, max z] widened by a
-// relative 1e-5; its reciprocal is bounded by the reciprocals of the ends
-// when they have one sign.  NaN (never rejects) otherwise.
-__device__ __forceinline__ float depth_reject_bound(const PFPrim &P, uint32_t rstate)
+// Tile-relative set-up of chunk record sp for the tile at (ox, oy), read
+// from shared memory in 16-byte words (the padded stride keeps them free of
+// bank conflicts across the warp).
+__device__ __forceinline__ void derive_chunk_prim(const SPrim *sp, uint32_t ox, uint32_t oy, uint32_t W, uint32_t H,
+                                                  ChunkPrim &cp, DenseP &dp)
 {
-    const float qnan = __int_as_float(0x7fffffff);
-    const int func = (int)((rstate >> 16) & 255u);
-    if (!(rstate & PFS_DEPTH_TEST) || (func != 2 && func != 3)) return qnan;
-    const float lo = fminf(P.z1, fminf(P.z2, P.z3)), hi = fmaxf(P.z1, fmaxf(P.z2, P.z3));
-    if (!(fabsf(lo) < 1e30f && fabsf(hi) < 1e30f)) return qnan;
-    float b;
-    if (lo > 0.0f) b = __fdiv_rn(1.0f, hi * 1.00001f) * 0.99999f;         // interpolated term <= hi (1 + 1e-5)
-    else if (hi < 0.0f) b = __fdiv_rn(1.0f, hi * 0.99999f) * 1.00001f;    // term <= hi (1 - 1e-5) < 0
-    else return qnan;
-    if (!(fabsf(b) < 1e30f)) return qnan;
-    return func == 2 ? b : nextafterf(b, -INFINITY);
-}
-
-// Tile-relative set-up of sub-triangle P for the tile at (ox, oy).
-__device__ __forceinline__ void derive_chunk_prim(const PFPrim &P, uint32_t ox, uint32_t oy, uint32_t W, uint32_t H,
-                                                  const PFDrawState *states, ChunkPrim &cp, DenseP &dp)
-{
-    cp.flags = P.flags;
-    const int face = P.flags & 1;
-    int32_t sx[3] = { P.y3 - P.y2, P.y1 - P.y3, P.y2 - P.y1 };
-    int32_t sy[3] = { P.x2 - P.x3, P.x3 - P.x1, P.x1 - P.x2 };
-    const int32_t rx[3] = { P.x2, P.x3, P.x1 }, ry[3] = { P.y2, P.y3, P.y1 };
+    const int4 *w = reinterpret_cast<const int4 *>(&sp->p);
+    const int4 q0 = w[0], q1 = w[1], q2 = w[2];        // x1 y1 x2 y2 | x3 y3 xMin yMin | xMax yMax flags -
+    const int32_t X1 = q0.x, Y1 = q0.y, X2 = q0.z, Y2 = q0.w, X3 = q1.x, Y3 = q1.y;
+    const uint32_t xMin = (uint32_t)q1.z, yMin = (uint32_t)q1.w, xMax = (uint32_t)q2.x, yMax = (uint32_t)q2.y;
+    const uint32_t flags = (uint32_t)q2.z;
+    cp.flags = flags;
+    const int face = flags & 1;
+    int32_t sx[3] = { Y3 - Y2, Y1 - Y3, Y2 - Y1 };
+    int32_t sy[3] = { X2 - X3, X3 - X1, X1 - X2 };
+    const int32_t rx[3] = { X2, X3, X1 }, ry[3] = { Y2, Y3, Y1 };
     for (int e = 0; e < 3; e++) {
         if (face) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
         cp.ex[e] = sx[e]; cp.ey[e] = sy[e];
         cp.e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
     }
     // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside tile and framebuffer
-    uint32_t x0 = max((uint32_t)P.xMin, ox), x1 = min(min((uint32_t)P.xMax, ox + PF_TILE), W);
-    uint32_t y0 = max((uint32_t)P.yMin, oy), y1e = min(min((uint32_t)P.yMax + 1u, oy + PF_TILE), H);
-    if ((uint32_t)P.yMax == 0xffffffffu) y1e = 0;    // yMax + 1 wrapped
-    const bool empty = (x0 >= x1) || (y0 >= y1e) || ((uint32_t)P.xMin >= (uint32_t)P.xMax) ||
-                       ((uint32_t)P.yMin > (uint32_t)P.yMax);
+    uint32_t x0 = max(xMin, ox), x1 = min(min(xMax, ox + PF_TILE), W);
+    uint32_t y0 = max(yMin, oy), y1e = min(min(yMax + 1u, oy + PF_TILE), H);
+    if (yMax == 0xffffffffu) y1e = 0;                 // yMax + 1 wrapped
+    const bool empty = (x0 >= x1) || (y0 >= y1e) || (xMin >= xMax) || (yMin > yMax);
     cp.bx0 = empty ? 0 : x0 - ox; cp.by0 = empty ? 0 : y0 - oy;
     cp.bw = empty ? 0 : x1 - x0; cp.bh = empty ? 0 : y1e - y0;
-    cp.invBw = cp.bw ? 1.0f / (float)cp.bw : 0.0f;
-    const PFDrawState &St = states[P.flags >> 8];
-    cp.rstate = (St.flags & 0xffffu) | ((uint32_t)St.depthFunc << 16) | ((uint32_t)St.blendMode << 24);
-    // host-set records carry their own depth test, blending and depth write
-    // (a thick line's centre is always tested; pfRectf does none of them)
-    if (P.flags & PFP_KIND) cp.rstate = (cp.rstate & ~(uint32_t)PFP_OPS) | (P.flags & PFP_OPS);
+    cp.rstate = sp->p.rstate;
     dp.e0[0] = cp.e0[0]; dp.e0[1] = cp.e0[1]; dp.e0[2] = cp.e0[2];
     dp.ex0 = cp.ex[0]; dp.ex1 = cp.ex[1]; dp.ex2 = cp.ex[2];
     dp.ey0 = cp.ey[0]; dp.ey1 = cp.ey[1]; dp.ey2 = cp.ey[2];
     dp.box = cp.bx0 | (cp.bw << 8) | (cp.by0 << 16) | (cp.bh << 24);
     dp.rstate = cp.rstate;
-    dp.wInvSum = P.wInvSum;
-    dp.z1 = P.z1; dp.z2 = P.z2; dp.z3 = P.z3;
-    dp.zReject = depth_reject_bound(P, cp.rstate);
+    const float4 zq = reinterpret_cast<const float4 *>(&sp->p)[3];     // wInvSum z1 z2 z3
+    dp.wInvSum = zq.x;
+    dp.z1 = zq.y; dp.z2 = zq.z; dp.z3 = zq.w;
+    dp.zReject = sp->p.zReject;
 }
 
 // Exclusive offsets of each lane's count within the warp (wo[0..31]) and
@@ -1127,7 +1133,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Issue the copies of chunk records keys[c0 .. c0 + cn) into sp (and their
 // per-fragment lighting data into sq when the launch has any).
 __device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uint32_t *keys, uint32_t c0, uint32_t cn,
-                                                  PFPrim *sp, PFPrimPhong *sq)
+                                                  SPrim *sp, PFPrimPhong *sq)
 {
     for (uint32_t w = threadIdx.x; w < cn * 8; w += RASTER_THREADS) {
         const uint32_t pi = w >> 3, part = w & 7;
@@ -1135,7 +1141,7 @@ __device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uin
         const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
         const PFPrim *src = &a.prims[item];
         if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-        cp_async16(reinterpret_cast<int4 *>(&sp[pi]) + part, reinterpret_cast<const int4 *>(src) + part);
+        cp_async16(reinterpret_cast<int4 *>(&sp[pi].p) + part, reinterpret_cast<const int4 *>(src) + part);
     }
     if (a.anyPhong) {
         for (uint32_t w = threadIdx.x; w < cn * 5; w += RASTER_THREADS) {
@@ -1153,7 +1159,7 @@ __device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uin
 __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
 {
     extern __shared__ uint32_t skeys[];               // [N] keys (+ [n] sorted copy when rank-sorting)
-    __shared__ __align__(16) PFPrim sprimBuf[2][CH];         // double-buffered chunk records
+    __shared__ SPrim sprimBuf[2][CH];                 // double-buffered chunk records
     __shared__ __align__(16) PFPrimPhong sphBuf[2][CH];
     __shared__ ChunkPrim scp[CH];
     __shared__ DenseP sdp[CH];
@@ -1172,14 +1178,56 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     const uint32_t lx = tid % PF_TILE, ly = tid / PF_TILE;
     unsigned long long frags = 0;
 
-    // persistent: CTAs take tiles of all targets from a shared work queue
+    // persistent: CTAs take tiles from a shared work queue -- the tiles the
+    // binning listed as non-empty (every tile when there is no list); the
+    // next entry is claimed while the current tile is rasterized
+    const bool listed = a.tileList != nullptr;
+    const uint32_t nQueue = listed ? min(a.cnt->tileListCount, a.totalTiles) : a.totalTiles;
     __shared__ uint32_t sNext;
+    uint32_t claim = 0;
+    if (tid == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
+    if (listed) {
+        // tiles with an empty bin only get their fused clear, if any: warp w
+        // of the grid takes the groups of 32 tiles w, w + 8 * gridDim, ...
+        // (no shared memory, no barrier, no atomics); the queue's dynamic
+        // schedule absorbs the few microseconds this costs the first CTAs
+        for (uint32_t t0 = (blockIdx.x * (RASTER_THREADS / 32) + (uint32_t)warp) * 32u; t0 < a.totalTiles;
+             t0 += gridDim.x * RASTER_THREADS) {
+            const uint32_t t = t0 + (uint32_t)lane;
+            int ti = 0;
+            bool clear = false;
+            if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
+                int tlo = 0, thi = a.nTargets - 1;
+                while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= t) tlo = mid; else thi = mid - 1; }
+                ti = tlo;
+                clear = a.targets[tlo].clearMode != 0;
+            }
+            for (uint32_t m = __ballot_sync(0xffffffffu, clear); m; m &= m - 1) {
+                const int src = __ffs(m) - 1;
+                const PFTarget &T = a.targets[__shfl_sync(0xffffffffu, ti, src)];
+                const uint32_t tile = t0 + (uint32_t)src - T.tileBase;
+                const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
+                for (uint32_t p = (uint32_t)lane; p < PF_TILE_PIXELS; p += 32) {
+                    const uint32_t px = ox + p % PF_TILE, py = oy + p / PF_TILE;
+                    if (px >= T.W || py >= T.H) continue;
+                    const size_t pidx = (size_t)py * T.W + px;
+                    if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
+                    T.color[pidx] = T.clearColor;
+                    T.depth[pidx] = T.clearDepth;
+                }
+            }
+        }
+    }
     for (;;) {
     __syncthreads();                                   // sNext and the previous tile's shared data are free
-    if (tid == 0) sNext = atomicAdd(&a.cnt->tileQueue, 1u);
+    if (tid == 0) {
+        const uint32_t q = claim;
+        sNext = q < nQueue ? (listed ? __ldg(a.tileList + q) : q) : 0xffffffffu;
+        if (q < nQueue) claim = atomicAdd(&a.cnt->tileQueue, 1u);
+    }
     __syncthreads();
     const uint32_t gt = sNext;
-    if (gt >= a.totalTiles) break;
+    if (gt == 0xffffffffu) break;
     int tlo = 0, thi = a.nTargets - 1;
     while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gt) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
@@ -1241,7 +1289,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
         stage_chunk_async(a, keys, 0, min((uint32_t)CH, n), sprimBuf[0], sphBuf[0]);
         for (uint32_t c0 = 0, it = 0; c0 < n; c0 += CH, it++) {
             const uint32_t cn = min((uint32_t)CH, n - c0);
-            PFPrim *const sprim = sprimBuf[it & 1];
+            SPrim *const sprim = sprimBuf[it & 1];
             PFPrimPhong *const sph = sphBuf[it & 1];
             cp_async_wait_all();
             __syncthreads();                                  // this chunk is staged; the previous one's data are free
@@ -1254,18 +1302,19 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             if (warp == 0) {
                 const bool has = lane < cn;
                 uint32_t bh = 0, area = 0;
-                const bool anyLP = __any_sync(0xffffffffu, has && (sprim[lane].flags & PFP_KIND));
-                const uint32_t blit = __ballot_sync(0xffffffffu, has && (sprim[lane].flags & PFP_KIND) == PFP_BLIT);
+                ChunkPrim cp;
+                DenseP dp;
+                uint32_t kind = 0;
                 if (has) {
-                    const PFPrim &P = sprim[lane];
-                    ChunkPrim cp;
-                    DenseP dp;
-                    derive_chunk_prim(P, ox, oy, T.W, T.H, a.states, cp, dp);
+                    derive_chunk_prim(&sprim[lane], ox, oy, T.W, T.H, cp, dp);
                     scp[lane] = cp;
                     sdp[lane] = dp;
                     bh = cp.bw ? cp.bh : 0;
                     area = cp.bw * cp.bh;
+                    kind = cp.flags & PFP_KIND;
                 }
+                const bool anyLP = __any_sync(0xffffffffu, kind != 0);
+                const uint32_t blit = __ballot_sync(0xffffffffu, kind == PFP_BLIT);
                 // prefix of clipped box rows; box area
                 uint32_t s = bh;
                 for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
@@ -1275,7 +1324,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 // boxes that cover half a tile on average: test every
                 // (pixel, sub-triangle) pair instead of stepping rows
                 // (points and lines always take the row path)
-                if (lane == 0) { sDense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP; sAnyLP = anyLP; sBlit = blit; }
+                const bool dense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP;
+                if (lane == 0) { sDense = dense; sAnyLP = anyLP; sBlit = blit; }
             }
             __syncthreads();
             uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
@@ -1324,7 +1374,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
                     if (lpChunk && (cp.flags & PFP_KIND)) {
                         for (uint32_t dx = 0; dx < cp.bw; dx++)
-                            if (lp_covers(sprim[lo], (int32_t)(ox + cp.bx0 + dx), (int32_t)(oy + Y))) atomicOr(row + dx, bit);
+                            if (lp_covers(sprim[lo].p, (int32_t)(ox + cp.bx0 + dx), (int32_t)(oy + Y))) atomicOr(row + dx, bit);
                         continue;
                     }
                     for (uint32_t dx = 0; dx < cp.bw; dx++) {
@@ -1349,8 +1399,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         float wn[3];
                         const uint32_t p = (uint32_t)(warp * 32 + lo);
                         fz[warp][f - b0] = (lpChunk && (scp[k].flags & PFP_KIND))
-                            ? lp_depth(sprim[k], (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
-                            : frag_depth(sprim[k], scp[k], p, wn);
+                            ? lp_depth(sprim[k].p, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
+                            : frag_depth(sprim[k].p, scp[k], p, wn);
                     }
                     __syncwarp();
                     if (cntp) {
@@ -1389,7 +1439,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     int lo; uint32_t k;
                     frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
                     float wn[3];
-                    const PFPrim &P = sprim[k];
+                    const PFPrim &P = sprim[k].p;
                     const uint32_t p = (uint32_t)(warp * 32 + lo);
                     if (lpChunk && (scp[k].flags & PFP_KIND)) {
                         fcol[warp][f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
@@ -1422,6 +1472,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     }
     if (inside) { T.color[pidx] = col; T.depth[pidx] = dep; }
     }   // tile loop
+
     // fragment counter: one atomic per CTA (same-address atomics serialise)
     __shared__ unsigned long long sFrags;
     if (tid == 0) sFrags = 0;
@@ -1528,7 +1579,7 @@ cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
-    BinArgs B{ L.binCount, L.bins, L.cap, L.targets, L.cnt, L.command };
+    BinArgs B{ L.binCount, L.tileList, L.bins, L.cap, L.targets, L.cnt, L.command };
     ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap };
     k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, O, B);
     return cudaGetLastError();
@@ -1545,7 +1596,7 @@ static size_t raster_smem(uint32_t cap)
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
-    RasterArgs a{ L.binCount, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
+    RasterArgs a{ L.binCount, L.tileList, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
                   L.totalTiles, L.cnt, L.command, L.anyPhong };
     const size_t smem = raster_smem(L.cap);
     cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

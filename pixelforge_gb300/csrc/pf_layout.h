@@ -156,9 +156,13 @@ typedef struct {
     uint32_t flags;               /* bit0 face (1 = BACK), bit1 is3D, bits 8.. state */
     int32_t poolBase;             /* clipped items: pool index of sub-triangle 1 */
     float wInvSum, z1, z2, z3;
-    uint32_t c1, c2, c3, pad0;
+    uint32_t c1, c2, c3;
+    uint32_t rstate;              /* the state's PFS_* bits | depth function << 16 | blend mode << 24,
+                                     with a host-set record's own operations in place of the state's */
     float u1, v1, u2, v2;
-    float u3, v3, pad1, pad2;
+    float u3, v3;
+    float zReject;                /* depth-test rejection bound (k_raster's dense path); NaN: none */
+    float pad2;
     uint64_t src;                 /* PFP_BLIT: device address of the RGBA8 image, 0 for a plain colour */
     uint32_t nSrc;                /* PFP_BLIT: pixels in the image */
     float pad3;
@@ -186,8 +190,8 @@ typedef struct {
     unsigned int maxBin;          /* largest tile bin count seen */
     unsigned int clipCount;       /* clipped sub-triangles allocated */
     unsigned long long batchRasterized;   /* sub-triangles set up by the current batch */
-    unsigned int tileQueue;       /* next tile of the current batch's raster work list */
-    unsigned int pad_;
+    unsigned int tileQueue;       /* next entry of the current batch's raster work list */
+    unsigned int tileListCount;   /* tiles with a non-empty bin, listed by the binning */
 } PFDevCounters;
 
 #endif /* PF_LAYOUT_H */
