@@ -165,7 +165,9 @@ struct Cmd {
     int segBegin, segEnd;              // CMD_DRAW: segments [segBegin, segEnd)
 };
 
-// Segment as recorded on the host: staging offsets instead of pointers.
+// Segment as recorded on the host: references instead of pointers.  A
+// reference is -1 (none), an offset >= 0 into the staging block, or the
+// negated address (< -1) of a device copy made at record time (upload()).
 struct SegRec {
     PFSegment seg;                     // pointer fields left null until the flush
     PFframebuffer *fb = nullptr;       // framebuffer the segment draws into
@@ -239,10 +241,18 @@ struct Renderer {
     std::vector<StateRec> states;
     std::vector<SegRec> segs;
     std::vector<Cmd> cmds;
-    struct SnapKey { const void *p; size_t bytes; int64_t off; };
+    struct SnapKey { const void *p; size_t bytes; int64_t off; int64_t maxU32; };   // maxU32: largest u32 element, -1 unknown
     std::vector<SnapKey> snaps;
     struct Conversion { int64_t rawOff, off; PFpixelformat format; PFdatatype type; };
     std::vector<Conversion> conversions;   // RGBA8 copies of textures of other formats in this recording          // dedup of texture / array snapshots in this recording
+
+    // caller arrays copied to the device at record time (upload()): device
+    // chunks reused from one recording to the next
+    struct UpChunk { void *p; size_t cap; };
+    std::vector<UpChunk> up;
+    size_t upChunk = 0, upOff = 0, upBytes = 0;
+    cudaStream_t upStream = nullptr;
+    cudaEvent_t upDone = nullptr;
 
     // device
     bool devInit = false, devOk = false;
@@ -505,8 +515,10 @@ public:
 private:
     Pool()
     {
+        // all cores but the caller's: the copies into staging are bound by
+        // per-core memory bandwidth
         unsigned hw = std::thread::hardware_concurrency();
-        int n = (int)std::min(7u, hw > 1 ? hw / 2 : 0u);
+        int n = (int)std::min(15u, hw > 1 ? hw - 1 : 0u);
         for (int i = 0; i < n; i++) threads_.emplace_back([this] { loop(); });
     }
     void work()
@@ -542,7 +554,7 @@ private:
     bool stop_ = false;
 };
 
-constexpr size_t kParallelChunk = (size_t)1 << 19;     // 512 KiB
+constexpr size_t kParallelChunk = (size_t)1 << 17;     // 128 KiB
 
 void par_memcpy(void *dst, const void *src, size_t bytes)
 {
@@ -567,6 +579,23 @@ bool par_equal(const void *a, const void *b, size_t bytes)
     return !diff.load();
 }
 
+// Largest of `count` u32 values.
+uint32_t par_max_u32(const uint32_t *src, size_t count)
+{
+    const size_t chunk = kParallelChunk / 4;
+    const int n = (int)((count + chunk - 1) / chunk);
+    std::vector<uint32_t> mx((size_t)std::max(n, 1), 0u);
+    Pool::get().run(n, [&](int i) {
+        size_t o = (size_t)i * chunk, len = std::min(chunk, count - o);
+        uint32_t m = 0;
+        for (size_t k = 0; k < len; k++) { uint32_t v = src[o + k]; m = v > m ? v : m; }
+        mx[(size_t)i] = m;
+    });
+    uint32_t m = 0;
+    for (uint32_t v : mx) m = std::max(m, v);
+    return m;
+}
+
 // u32 indices: copy and return the largest
 uint32_t par_copy_max_u32(uint32_t *dst, const uint32_t *src, size_t count)
 {
@@ -587,18 +616,84 @@ uint32_t par_copy_max_u32(uint32_t *dst, const uint32_t *src, size_t count)
 // ---------------------------------------------------------------------------
 // recording
 // ---------------------------------------------------------------------------
-// Copy `bytes` of caller memory into staging, reusing an identical snapshot
-// taken earlier in the same recording.
-int64_t snapshot(Renderer *r, const void *p, size_t bytes)
+bool device_init(Renderer *r);
+
+inline int64_t dev_ref(const void *p) { return -(int64_t)(uintptr_t)p; }
+
+constexpr size_t kUploadMin = (size_t)64 << 10;          // smaller arrays go through staging
+constexpr size_t kUploadBudget = (size_t)8 << 30;        // per recording; beyond it, staging with de-duplication
+constexpr size_t kUploadChunk = (size_t)64 << 20;
+
+// Copy `bytes` of caller memory to the device now, straight from where it
+// lies (one cudaMemcpyAsync; on this platform that is several times faster
+// than a host copy into pinned staging followed by the upload).  From
+// pageable memory the call returns only once the bytes are read, which is
+// the snapshot the reference's draw-time read implies; from page-locked or
+// device memory it would return earlier, so the copy is waited for.
+// Returns the device reference, or -1 (the caller takes the staging path).
+int64_t upload(Renderer *r, const void *p, size_t bytes)
 {
+    if (bytes < kUploadMin || r->upBytes + bytes > kUploadBudget || !device_init(r)) return -1;
+    if (r->upBytes == 0) {               // a new recording: the last flush's device data is overwritten
+        r->lastOps.clear();
+        r->graphValid = false;
+    }
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    while (r->upChunk < r->up.size() && r->upOff + need > r->up[r->upChunk].cap) { r->upChunk++; r->upOff = 0; }
+    if (r->upChunk == r->up.size()) {
+        Renderer::UpChunk c{ nullptr, std::max(kUploadChunk, need) };
+        if (cudaMalloc(&c.p, c.cap) != cudaSuccess) { cudaGetLastError(); return -1; }
+        r->up.push_back(c);
+        r->upOff = 0;
+    }
+    uint8_t *dst = (uint8_t *)r->up[r->upChunk].p + r->upOff;
+    cudaPointerAttributes attr{};
+    const bool pageable = cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeUnregistered;
+    cudaGetLastError();
+    if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
+    if (!pageable) cudaStreamSynchronize(r->upStream);
+    r->upOff += need;
+    r->upBytes += bytes;
+    return dev_ref(dst);
+}
+
+// Copy `bytes` of caller memory for the device: uploaded now (large arrays;
+// device_ok), or into staging, reusing an identical snapshot taken earlier
+// in the same recording.
+int64_t snapshot(Renderer *r, const void *p, size_t bytes, bool device_ok = true)
+{
+    if (device_ok) {
+        const int64_t ref = upload(r, p, bytes);
+        if (ref != -1) return ref;
+    }
     for (auto &s : r->snaps)
         if (s.p == p && s.bytes == bytes && par_equal(r->staging.base + s.off, p, bytes)) return s.off;
     int64_t off = r->staging.alloc(bytes);
     par_memcpy(r->staging.base + off, p, bytes);
-    r->snaps.push_back({ p, bytes, off });
+    r->snaps.push_back({ p, bytes, off, -1 });
     return off;
 }
 int64_t snapshot(Ctx *c, const void *p, size_t bytes) { return snapshot(c->rend, p, bytes); }
+
+// Snapshot of `count` u32 indices and their largest value (kept with the
+// snapshot, so a draw that repeats the indices compares instead of copying).
+int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
+{
+    const size_t bytes = count * 4;
+    if (bytes >= kUploadMin) {
+        const int64_t ref = upload(r, p, bytes);
+        if (ref != -1) { mx = par_max_u32(p, count); return ref; }
+    }
+    for (auto &s : r->snaps)
+        if (s.p == p && s.bytes == bytes && s.maxU32 >= 0 && par_equal(r->staging.base + s.off, p, bytes)) {
+            mx = (uint32_t)s.maxU32;
+            return s.off;
+        }
+    const int64_t off = r->staging.alloc(bytes);
+    mx = par_copy_max_u32((uint32_t *)(r->staging.base + off), p, count);
+    r->snaps.push_back({ p, bytes, off, (int64_t)mx });
+    return off;
+}
 
 // RGBA8 snapshot of a texture: its own bytes, or the converted texels of
 // another format (from a snapshot of its bytes, converted once per recording).
@@ -606,7 +701,7 @@ int64_t snapshot_texture(Renderer *r, const Tex *t)
 {
     const size_t n = (size_t)t->w * t->h;
     if (t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE) return snapshot(r, t->pixels, n * 4);
-    const int64_t raw = snapshot(r, t->pixels, n * (size_t)texel_bytes(t->format, t->type));
+    const int64_t raw = snapshot(r, t->pixels, n * (size_t)texel_bytes(t->format, t->type), false);   // read here
     for (auto &cv : r->conversions)
         if (cv.rawOff == raw && cv.format == t->format && cv.type == t->type) return cv.off;
     const int64_t off = r->staging.alloc(n * 4);
@@ -1107,6 +1202,8 @@ bool device_init(Renderer *r)
         return false;
     }
     e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->upStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->upDone, cudaEventDisableTiming);
     if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); r->devStatus |= PF_DEVICE_NO_GPU; return false; }
     if (!r->counters.ensure(sizeof(PFDevCounters))) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
     if (cudaMallocHost((void **)&r->hostCounters, sizeof(PFDevCounters)) != cudaSuccess) {
@@ -1126,6 +1223,10 @@ void release_renderer(Renderer *r)
         if (r->evStart) { cudaEventDestroy(r->evStart); cudaEventDestroy(r->evEnd); }
         for (auto &pr : r->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
         if (r->stream) cudaStreamDestroy(r->stream);
+        if (r->upStream) cudaStreamDestroy(r->upStream);
+        if (r->upDone) cudaEventDestroy(r->upDone);
+        for (auto &u : r->up) cudaFree(u.p);
+        r->up.clear();
         for (void *q : r->splitMem) cudaFree(q);
         r->splitMem.clear();
     }
@@ -1181,6 +1282,10 @@ void discard_recording(Renderer *r)
 {
     r->states.clear(); r->segs.clear(); r->cmds.clear(); r->snaps.clear(); r->conversions.clear();
     r->staging.used = 0;
+    if (r->upBytes) {
+        cudaStreamSynchronize(r->upStream);
+        r->upChunk = r->upOff = r->upBytes = 0;
+    }
 }
 
 // One unit of device work of a flush: a multi-target raster batch (a run of
@@ -1292,7 +1397,10 @@ bool flush(Renderer *r)
     const size_t total = r->staging.used;
     if (!r->arena.ensure(total)) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return fail("cudaMalloc(arena)", cudaErrorMemoryAllocation); }
     uint8_t *dbase = (uint8_t *)r->arena.p;
-    auto dptr = [&](int64_t off) -> const void * { return off < 0 ? nullptr : (const void *)(dbase + off); };
+    auto dptr = [&](int64_t off) -> const void * {
+        if (off < -1) return (const void *)(uintptr_t)(-off);    // uploaded at record time
+        return off < 0 ? nullptr : (const void *)(dbase + off);
+    };
     PFDrawState *hs = (PFDrawState *)(r->staging.base + statesOff);
     for (size_t i = 0; i < nStates; i++) {
         hs[i] = r->states[i].st;
@@ -1377,6 +1485,10 @@ bool flush(Renderer *r)
         maxVerts = std::max(maxVerts, v); maxItems = std::max(maxItems, it); maxTiles = std::max(maxTiles, tiles);
     }
     cudaError_t e = cudaMemcpyAsync(dbase, r->staging.base, total, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && r->upBytes) {            // the record-time uploads come first
+        e = cudaEventRecord(r->upDone, r->upStream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, r->upDone, 0);
+    }
     if (e != cudaSuccess) return fail("cudaMemcpyAsync(staging)", e);
 
     // --- framebuffers: bring host content to the device unless the first
@@ -2224,17 +2336,19 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     int64_t idxOff = -1;
     size_t nverts;
     if (indices) {
-        idxOff = c->rend->staging.alloc((size_t)count * 4);
-        uint32_t *dst = (uint32_t *)(c->rend->staging.base + idxOff);
         uint32_t mx = 0;
         if (itype == PF_UNSIGNED_INT) {
-            mx = par_copy_max_u32(dst, (const uint32_t *)indices, count);
-        } else if (itype == PF_UNSIGNED_SHORT) {
-            const uint16_t *s = (const uint16_t *)indices;
-            for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
+            idxOff = snapshot_u32(c->rend, (const uint32_t *)indices, (size_t)count, mx);
         } else {
-            const uint8_t *s = (const uint8_t *)indices;
-            for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
+            idxOff = c->rend->staging.alloc((size_t)count * 4);
+            uint32_t *dst = (uint32_t *)(c->rend->staging.base + idxOff);
+            if (itype == PF_UNSIGNED_SHORT) {
+                const uint16_t *s = (const uint16_t *)indices;
+                for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
+            } else {
+                const uint8_t *s = (const uint8_t *)indices;
+                for (PFsizei i = 0; i < count; i++) { dst[i] = s[i]; mx = std::max(mx, dst[i]); }
+            }
         }
         nverts = (size_t)mx + 1;
         first = 0;

@@ -827,7 +827,7 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 // ---------------------------------------------------------------------------
 #define RASTER_THREADS PF_TILE_PIXELS
 #define CH 32
-#define FWIN 256
+#define FWIN 2048
 #define RANK_SORT_MAX 1024
 
 struct RasterArgs {
@@ -919,29 +919,35 @@ __device__ __forceinline__ void derive_chunk_prim(const SPrim *sp, uint32_t ox, 
     dp.zReject = sp->p.zReject;
 }
 
-// Exclusive offsets of each lane's count within the warp (wo[0..31]) and
-// the warp total (wo[32]).
-__device__ __forceinline__ void warp_offsets(uint32_t cnt, uint32_t *wo, uint32_t &myOff, uint32_t &total)
+// Exclusive offset of this thread's count within the CTA, and the CTA
+// total (one barrier; wsum must not be in use by another call).
+__device__ __forceinline__ uint32_t cta_offsets(uint32_t cnt, uint32_t *wsum, uint32_t &total)
 {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t s = cnt;
     for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
-    __syncwarp();                                      // previous readers of wo are done
-    myOff = s - cnt;
-    wo[lane] = myOff;
-    if (lane == 31) wo[32] = s;
-    __syncwarp();
-    total = wo[32];
+    if (lane == 31) wsum[warp] = s;
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+    for (int w = 0; w < RASTER_THREADS / 32; w++) {
+        const uint32_t v = wsum[w];
+        before += (w < warp) ? v : 0u;
+        tot += v;
+    }
+    total = tot;
+    return before + s - cnt;
 }
 
-// Owner lane of the f-th fragment of a warp's compacted list and its chunk
-// sub-triangle (the owner's n-th set mask bit).
-__device__ __forceinline__ void frag_owner(const uint32_t *wo, const uint32_t *masks, uint32_t f, int &lo, uint32_t &k)
+// Write this pixel's fragments (set bits of mask, in order) to entries
+// off, off + 1, ... of the fragment list, as far as they fall in the
+// window [b0, bEnd): pixel << 5 | chunk record.
+__device__ __forceinline__ void list_fragments(uint32_t mask, uint32_t off, uint32_t b0, uint32_t bEnd, uint16_t *fdesc)
 {
-    int l = 0, h = 31;                                 // largest L with wo[L] <= f
-    while (l < h) { int mid = (l + h + 1) >> 1; if (wo[mid] <= f) l = mid; else h = mid - 1; }
-    lo = l;
-    k = __fns(masks[l], 0, (int)(f - wo[l]) + 1) & (CH - 1);
+    const uint32_t cnt = __popc(mask);
+    if (!cnt || off >= bEnd || off + cnt <= b0) return;
+    uint32_t f = off;
+    for (uint32_t mm = mask; mm && f < bEnd; mm &= mm - 1, f++)
+        if (f >= b0) fdesc[f - b0] = (uint16_t)((threadIdx.x << 5) | (uint32_t)(__ffs(mm) - 1));
 }
 
 // Weights and depth of a covered fragment at tile pixel p (triangles.c:426-438).
@@ -1165,9 +1171,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ DenseP sdp[CH];
     __shared__ uint32_t sarea[CH + 1];
     __shared__ uint32_t pmask[RASTER_THREADS];
-    __shared__ uint32_t fcol[RASTER_THREADS / 32][FWIN];
-    __shared__ float fz[RASTER_THREADS / 32][FWIN];
-    __shared__ uint32_t woff[RASTER_THREADS / 32][33];
+    __shared__ uint16_t fdesc[FWIN];                  // listed fragments: pixel << 5 | chunk record
+    __shared__ uint32_t fval[FWIN];                   // their depth (pass 3) or colour (pass 4)
+    __shared__ uint32_t wsum[RASTER_THREADS / 32];
     __shared__ int sDense, sAnyLP;
     __shared__ uint32_t sBlit;                        // chunk records that are rectangles (not counted as fragments)
 
@@ -1361,8 +1367,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             } else {
                 // 2. coverage: one work item per (sub-triangle, row of its clipped
                 //    box); edge functions stepped along the row
-                const uint32_t total = sarea[CH];
-                for (uint32_t t = tid; t < total; t += RASTER_THREADS) {
+                const uint32_t nRows = sarea[CH];
+                for (uint32_t t = tid; t < nRows; t += RASTER_THREADS) {
                     int lo = 0, hi = CH - 1;                          // largest k with sarea[k] <= t
                     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
                     const ChunkPrim &cp = scp[lo];
@@ -1383,27 +1389,30 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     }
                 }
                 __syncthreads();
-                // 3. per warp, depth first: the depth of every covered fragment
-                //    (dense over the warp), then each pixel's depth tests in
-                //    submission order, which leave the set of visible fragments
+                // 3. depth first, over the whole CTA: the chunk's covered
+                //    fragments, listed pixel by pixel in submission order,
+                //    get their depth computed densely by all threads; then
+                //    each pixel runs its depth tests in order, which leave
+                //    the set of visible fragments
                 const uint32_t m = pmask[tid];
                 const uint32_t cntp = __popc(m);
                 frags += lpChunk ? __popc(m & ~sBlit) : cntp;
-                uint32_t myOff, wtotal;
-                warp_offsets(cntp, woff[warp], myOff, wtotal);
-                for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
-                    const uint32_t bEnd = min(wtotal, b0 + FWIN);
-                    for (uint32_t f = b0 + lane; f < bEnd; f += 32) {
-                        int lo; uint32_t k;
-                        frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
+                uint32_t total;
+                const uint32_t myOff = cta_offsets(cntp, wsum, total);
+                for (uint32_t b0 = 0; b0 < total; b0 += FWIN) {
+                    const uint32_t bEnd = min(total, b0 + FWIN);
+                    list_fragments(m, myOff, b0, bEnd, fdesc);
+                    __syncthreads();
+                    for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
+                        const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
                         float wn[3];
-                        const uint32_t p = (uint32_t)(warp * 32 + lo);
-                        fz[warp][f - b0] = (lpChunk && (scp[k].flags & PFP_KIND))
+                        const float z = (lpChunk && (scp[k].flags & PFP_KIND))
                             ? lp_depth(sprim[k].p, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
                             : frag_depth(sprim[k].p, scp[k], p, wn);
+                        fval[f - b0] = __float_as_uint(z);
                     }
-                    __syncwarp();
-                    if (cntp) {
+                    __syncthreads();
+                    if (cntp && myOff < bEnd && myOff + cntp > b0) {
                         uint32_t f = myOff, mm = m;
                         while (mm) {
                             const uint32_t k = __ffs(mm) - 1;
@@ -1411,7 +1420,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                             if (f >= bEnd) break;
                             if (f >= b0) {
                                 const uint32_t rs = scp[k].rstate;
-                                const float z = fz[warp][f - b0];
+                                const float z = __uint_as_float(fval[f - b0]);
                                 const int func = (int)((rs >> 16) & 255u);
                                 if (!(rs & PFS_DEPTH_TEST) ||
                                     ((lpChunk && (scp[k].flags & PFP_KIND)) ? depth_sisd(func, z, dep)
@@ -1423,41 +1432,39 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                             f++;
                         }
                     }
-                    __syncwarp();
+                    __syncthreads();                          // fdesc and fval are free
                 }
             }
-            // 4. shade the visible fragments (dense over the warp) and blend
-            //    them in submission order
-            __syncwarp();
-            pmask[tid] = vis;
-            const uint32_t cntv = __popc(vis);
-            uint32_t myOff, wtotal;
-            warp_offsets(cntv, woff[warp], myOff, wtotal);
-            for (uint32_t b0 = 0; b0 < wtotal; b0 += FWIN) {
-                const uint32_t bEnd = min(wtotal, b0 + FWIN);
-                for (uint32_t f = b0 + lane; f < bEnd; f += 32) {
-                    int lo; uint32_t k;
-                    frag_owner(woff[warp], &pmask[warp * 32], f, lo, k);
-                    float wn[3];
+            // 4. shade the visible fragments (densely over the CTA) and blend
+            //    each pixel's in submission order
+            uint32_t totalv;
+            const uint32_t myOffV = cta_offsets(__popc(vis), wsum, totalv);
+            for (uint32_t b0 = 0; b0 < totalv; b0 += FWIN) {
+                const uint32_t bEnd = min(totalv, b0 + FWIN);
+                list_fragments(vis, myOffV, b0, bEnd, fdesc);
+                __syncthreads();
+                for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
+                    const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
                     const PFPrim &P = sprim[k].p;
-                    const uint32_t p = (uint32_t)(warp * 32 + lo);
                     if (lpChunk && (scp[k].flags & PFP_KIND)) {
-                        fcol[warp][f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
+                        fval[f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
                         continue;
                     }
+                    float wn[3];
                     const float z = frag_depth(P, scp[k], p, wn);
-                    fcol[warp][f - b0] = shade_fragment(P, &sph[k], a.states[P.flags >> 8], wn[0], wn[1], wn[2], z);
+                    fval[f - b0] = shade_fragment(P, &sph[k], a.states[P.flags >> 8], wn[0], wn[1], wn[2], z);
                 }
-                __syncwarp();
-                if (cntv) {
-                    uint32_t f = myOff, mm = vis;
+                __syncthreads();
+                const uint32_t cntv = __popc(vis);
+                if (cntv && myOffV < bEnd && myOffV + cntv > b0) {
+                    uint32_t f = myOffV, mm = vis;
                     while (mm) {
                         const uint32_t k = __ffs(mm) - 1;
                         mm &= mm - 1;
                         if (f >= bEnd) break;
                         if (f >= b0) {
                             const uint32_t rs = scp[k].rstate;
-                            uint32_t frag = fcol[warp][f - b0];
+                            uint32_t frag = fval[f - b0];
                             if (rs & PFS_BLEND)
                                 frag = (lpChunk && (scp[k].flags & PFP_KIND)) ? blend_sisd((int)(rs >> 24), frag, col)
                                                                   : blend_simd((int)(rs >> 24), frag, col);
@@ -1466,7 +1473,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         f++;
                     }
                 }
-                __syncwarp();
+                __syncthreads();                              // fdesc and fval are free
             }
         }
     }
