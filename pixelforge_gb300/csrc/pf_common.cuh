@@ -164,7 +164,15 @@ __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVer
     P.rstate = raster_state(S);
     P.u1 = a.u; P.v1 = a.v; P.u2 = b.u; P.v2 = b.v; P.u3 = c.u; P.v3 = c.v;
     P.zReject = depth_reject_bound(P, P.rstate);
-    P.pad2 = 0.0f;
-    P.src = 0; P.nSrc = 0; P.pad3 = 0.0f;
+    // the texture's parameters travel with the record: the rasterizer
+    // samples without reading the draw state
+    P.src = 0; P.nSrc = 0; P.texTx = 0.0f; P.texTy = 0.0f;
+    if (S.flags & PFS_TEXTURE) {
+        P.src = (uint64_t)(uintptr_t)S.tex;
+        P.texTx = S.texTx; P.texTy = S.texTy;
+        P.rstate |= ((uint32_t)S.texWrap & 3u) << PFR_WRAP_SHIFT | (S.texFilter ? (uint32_t)PFR_FILTER : 0u);
+        if (S.texW < 65536u && S.texH < 65536u) P.nSrc = S.texW | (S.texH << 16);
+        else P.rstate |= PFR_TEX_FROM_STATE;
+    }
     return true;
 }

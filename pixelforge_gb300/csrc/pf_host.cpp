@@ -1590,7 +1590,7 @@ bool flush(Renderer *r)
             !r->primsPh.ensure(anyPhong ? (size_t)maxItems * sizeof(PFPrimPhong) + 128 : 128) ||
             !r->pool.ensure((size_t)r->poolCap * sizeof(PFPrim)) ||
             !r->poolPh.ensure(anyPhong ? (size_t)r->poolCap * sizeof(PFPrimPhong) : 128) ||
-            !r->binCount.ensure((size_t)maxTiles * 8 + 128) ||       // bin counters, then the tile list
+            !r->binCount.ensure((size_t)(((size_t)maxTiles + 31) & ~(size_t)31) * 16) ||   // bin counters, three tile lists
             !r->bins.ensure((size_t)maxTiles * r->cap * 4 + 64)) {
             r->devStatus |= PF_DEVICE_ALLOC_FAIL;
             return fail("cudaMalloc(scratch)", cudaErrorMemoryAllocation);
@@ -1624,7 +1624,8 @@ bool flush(Renderer *r)
                 L.prims = (PFPrim *)r->prims.p; L.primsPh = (PFPrimPhong *)r->primsPh.p;
                 L.pool = (PFPrim *)r->pool.p; L.poolPh = (PFPrimPhong *)r->poolPh.p; L.poolCap = r->poolCap;
                 L.binCount = (uint32_t *)r->binCount.p; L.bins = (uint32_t *)r->bins.p; L.cap = r->cap;
-                L.tileList = (uint32_t *)r->binCount.p + (((size_t)maxTiles + 31) & ~(size_t)31);
+                L.listStride = (uint32_t)(((size_t)maxTiles + 31) & ~(size_t)31);
+                L.tileList = (uint32_t *)r->binCount.p + L.listStride;
                 L.rasterCtasPerSM = r->rasterCtasPerSM;
                 L.anyPhong = anyPhong ? 1 : 0;
                 L.cnt = dcnt;

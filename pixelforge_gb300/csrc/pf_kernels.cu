@@ -172,13 +172,39 @@ __device__ __forceinline__ bool depth_simd(int f, float src, float dst)
 }
 
 
+// A texture as the rasterizer samples it.
+struct TexDesc {
+    const uint32_t *tex;
+    uint32_t w, h;
+    int32_t wrap, filter;
+    float tx, ty;
+};
+
+// From the set-up record (texture parameters copied there by setup_prim),
+// or from the draw state when they did not fit.
+__device__ __forceinline__ TexDesc tex_desc(const PFPrim &P, const PFDrawState *states)
+{
+    TexDesc d;
+    if (!(P.rstate & PFR_TEX_FROM_STATE)) {
+        d.tex = reinterpret_cast<const uint32_t *>(P.src);
+        d.w = P.nSrc & 0xffffu; d.h = P.nSrc >> 16;
+        d.wrap = (int32_t)((P.rstate >> PFR_WRAP_SHIFT) & 3u); d.filter = (P.rstate & PFR_FILTER) ? 1 : 0;
+        d.tx = P.texTx; d.ty = P.texTy;
+    } else {
+        const PFDrawState &S = states[P.flags >> 8];
+        d.tex = S.tex; d.w = S.texW; d.h = S.texH; d.wrap = S.texWrap; d.filter = S.texFilter;
+        d.tx = S.texTx; d.ty = S.texTy;
+    }
+    return d;
+}
+
 // Texel at linear offset y*w + x; offsets outside the texture read as 0
 // (the reference reads past its buffer there).
-__device__ __forceinline__ uint32_t tex_fetch(const PFDrawState &S, int32_t x, int32_t y)
+__device__ __forceinline__ uint32_t tex_fetch(const TexDesc &T, int32_t x, int32_t y)
 {
-    int32_t off = (int32_t)((uint32_t)y * S.texW + (uint32_t)x);
-    if (off < 0 || (uint32_t)off >= S.texW * S.texH) return 0u;
-    return __ldg(S.tex + off);
+    int32_t off = (int32_t)((uint32_t)y * T.w + (uint32_t)x);
+    if (off < 0 || (uint32_t)off >= T.w * T.h) return 0u;
+    return __ldg(T.tex + off);
 }
 
 __device__ __forceinline__ uint32_t lerp_color(uint32_t a, uint32_t b, float t)
@@ -194,19 +220,19 @@ __device__ __forceinline__ uint32_t lerp_color(uint32_t a, uint32_t b, float t)
     return pack4(o);
 }
 
-__device__ uint32_t tex_sample(const PFDrawState &S, float u, float v)
+__device__ uint32_t tex_sample(const TexDesc &T, float u, float v)
 {
     int32_t x0, y0;
-    tex_map(S, u, v, x0, y0);
-    if (S.texFilter == 0) return tex_fetch(S, x0, y0);
+    tex_map_wh(T.w, T.h, T.wrap, u, v, x0, y0);
+    if (T.filter == 0) return tex_fetch(T, x0, y0);
     int32_t x1, y1;
-    tex_map(S, u + S.texTx, v + S.texTy, x1, y1);
-    float fx = u * (float)S.texW - (float)x0;
-    float fy = v * (float)S.texH - (float)y0;
+    tex_map_wh(T.w, T.h, T.wrap, u + T.tx, v + T.ty, x1, y1);
+    float fx = u * (float)T.w - (float)x0;
+    float fy = v * (float)T.h - (float)y0;
     fx = x86_min(x86_max(fx, 0.0f), 1.0f);
     fy = x86_min(x86_max(fy, 0.0f), 1.0f);
-    uint32_t c00 = tex_fetch(S, x0, y0), c10 = tex_fetch(S, x1, y0);
-    uint32_t c01 = tex_fetch(S, x0, y1), c11 = tex_fetch(S, x1, y1);
+    uint32_t c00 = tex_fetch(T, x0, y0), c10 = tex_fetch(T, x1, y0);
+    uint32_t c01 = tex_fetch(T, x0, y1), c11 = tex_fetch(T, x1, y1);
     return lerp_color(lerp_color(c00, c10, fx), lerp_color(c01, c11, fx), fy);
 }
 
@@ -375,7 +401,10 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (cnt->abortCommand != 0xffffffffu) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
-    if (g == 0) { cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0; cnt->tileListCount = 0; }
+    if (g == 0) {
+        cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0;
+        cnt->tileListCount = 0; cnt->heavyCount1 = 0; cnt->heavyCount2 = 0;
+    }
     const uint32_t g0 = blockIdx.x * blockDim.x;
     if (g0 >= nVerts) return;
     // the block's vertices usually belong to one segment: stage it and its
@@ -453,7 +482,8 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
 
 struct BinArgs {
     uint32_t *binCount;
-    uint32_t *tileList;        // tiles with a non-empty bin (NULL: not listed)
+    uint32_t *tileList;        // the raster work lists (NULL: not listed)
+    uint32_t listStride;
     uint32_t *bins;
     uint32_t cap;
     const PFTarget *targets;
@@ -500,10 +530,18 @@ __device__ __forceinline__ void bin_slot(const BinArgs &B, uint32_t t, uint32_t 
     }
 }
 
-// The first entry of a tile's bin puts the tile on the raster work list.
-__device__ __forceinline__ void list_tile(const BinArgs &B, uint32_t t)
+// Raster work lists: a tile's bin growing from `before` to `before + added`
+// entries puts the tile on the list of non-empty tiles (first entry) and on
+// the lists of heavy tiles (PF_HEAVY1 and PF_HEAVY2 entries), which the
+// rasterizer takes first so that the longest tiles do not start last.
+__device__ __forceinline__ void list_tile(const BinArgs &B, uint32_t t, uint32_t before, uint32_t added)
 {
-    if (B.tileList) B.tileList[atomicAdd(&B.cnt->tileListCount, 1u)] = t;
+    if (!B.tileList) return;
+    if (before == 0) B.tileList[atomicAdd(&B.cnt->tileListCount, 1u)] = t;
+    if (before < PF_HEAVY1 && before + added >= PF_HEAVY1)
+        B.tileList[B.listStride + atomicAdd(&B.cnt->heavyCount1, 1u)] = t;
+    if (before < PF_HEAVY2 && before + added >= PF_HEAVY2)
+        B.tileList[2 * B.listStride + atomicAdd(&B.cnt->heavyCount2, 1u)] = t;
 }
 
 // Append `key` to the bin of every tile the sub-triangle touches (one
@@ -516,7 +554,7 @@ __device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, 
         for (uint32_t tx = tx0; tx < tx0 + ntx; tx++) {
             const uint32_t t = T.tileBase + ty * T.tilesX + tx;
             const uint32_t slot = atomicAdd(&B.binCount[t], 1u);
-            if (slot == 0) list_tile(B, t);
+            list_tile(B, t, slot, 1u);
             bin_slot(B, t, slot, key);
         }
 }
@@ -543,7 +581,7 @@ __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, co
         uint32_t base = 0;
         if (lane == leader) {
             base = atomicAdd(&B.binCount[t], (unsigned)__popc(grp));
-            if (base == 0) list_tile(B, t);
+            list_tile(B, t, base, (uint32_t)__popc(grp));
         }
         base = __shfl_sync(grp, base, leader);
         bin_slot(B, t, base + __popc(grp & lt), key);
@@ -833,6 +871,7 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 struct RasterArgs {
     const uint32_t *binCount;
     const uint32_t *tileList;
+    uint32_t listStride;
     const uint32_t *bins;
     uint32_t cap;
     const PFPrim *prims;
@@ -965,10 +1004,10 @@ __device__ __forceinline__ float frag_depth(const PFPrim &P, const ChunkPrim &cp
 
 // Source colour of one fragment (triangles.c:500-521): colour interpolation,
 // texturing, per-fragment lighting.  Independent of the destination pixel.
-__device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrimPhong *Q, const PFDrawState &S,
+__device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrimPhong *Q, const PFDrawState *states,
                                                    float wn1, float wn2, float wn3, float z)
 {
-    const uint32_t fl = S.flags;
+    const uint32_t fl = P.rstate;
     uint32_t frag;
     if (fl & PFS_SMOOTH) {
         // covered pixels have weights in [0, 1]: the conversions are in range
@@ -991,9 +1030,10 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
         float tv = P.v1 * wn1 + P.v2 * wn2;
         tv = tv + P.v3 * wn3;
         if (P.flags & 2) { tu = tu * z; tv = tv * z; }
-        frag = blend_simd(4, tex_sample(S, tu, tv), frag);
+        frag = blend_simd(4, tex_sample(tex_desc(P, states), tu, tv), frag);
     }
     if (fl & PFS_PHONG) {
+        const PFDrawState &S = states[P.flags >> 8];
         float N[3], Pp[3];
         for (int i = 0; i < 3; i++) {
             float t0 = Q->n1[i] * wn1 + Q->n2[i] * wn2; N[i] = t0 + Q->n3[i] * wn3;
@@ -1173,8 +1213,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ uint32_t pmask[RASTER_THREADS];
     __shared__ uint16_t fdesc[FWIN];                  // listed fragments: pixel << 5 | chunk record
     __shared__ uint32_t fval[FWIN];                   // their depth (pass 3) or colour (pass 4)
+    __shared__ uint32_t fcolv[FWIN];                  // their colour (passes 3 and 4 in one)
     __shared__ uint32_t wsum[RASTER_THREADS / 32];
-    __shared__ int sDense, sAnyLP;
+    __shared__ int sDense, sAnyLP, sPhong;
     __shared__ uint32_t sBlit;                        // chunk records that are rectangles (not counted as fragments)
 
     if (a.cnt->abortCommand <= a.command) return;
@@ -1188,7 +1229,12 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     // binning listed as non-empty (every tile when there is no list); the
     // next entry is claimed while the current tile is rasterized
     const bool listed = a.tileList != nullptr;
-    const uint32_t nQueue = listed ? min(a.cnt->tileListCount, a.totalTiles) : a.totalTiles;
+    // queue entries: the tiles with >= PF_HEAVY2 entries, then those with
+    // >= PF_HEAVY1, then every non-empty tile; a tile is rasterized from
+    // the first list it is on and skipped on the later ones
+    const uint32_t nH2 = listed ? min(a.cnt->heavyCount2, a.totalTiles) : 0u;
+    const uint32_t nH1 = listed ? min(a.cnt->heavyCount1, a.totalTiles) : 0u;
+    const uint32_t nQueue = listed ? nH2 + nH1 + min(a.cnt->tileListCount, a.totalTiles) : a.totalTiles;
     __shared__ uint32_t sNext;
     uint32_t claim = 0;
     if (tid == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
@@ -1228,12 +1274,25 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __syncthreads();                                   // sNext and the previous tile's shared data are free
     if (tid == 0) {
         const uint32_t q = claim;
-        sNext = q < nQueue ? (listed ? __ldg(a.tileList + q) : q) : 0xffffffffu;
-        if (q < nQueue) claim = atomicAdd(&a.cnt->tileQueue, 1u);
+        uint32_t next = 0xffffffffu;
+        if (q < nQueue) {
+            claim = atomicAdd(&a.cnt->tileQueue, 1u);
+            if (!listed) next = q;
+            else {
+                const uint32_t level = q < nH2 ? 2u : (q < nH2 + nH1 ? 1u : 0u);
+                const uint32_t idx = level == 2u ? 2u * a.listStride + q : (level == 1u ? a.listStride + q - nH2 : q - nH2 - nH1);
+                next = __ldg(a.tileList + idx);
+                const uint32_t c = __ldg(a.binCount + next);
+                const uint32_t own = c >= PF_HEAVY2 ? 2u : (c >= PF_HEAVY1 ? 1u : 0u);
+                if (own != level) next = 0xfffffffeu;            // rasterized from an earlier list
+            }
+        }
+        sNext = next;
     }
     __syncthreads();
     const uint32_t gt = sNext;
     if (gt == 0xffffffffu) break;
+    if (gt == 0xfffffffeu) continue;
     int tlo = 0, thi = a.nTargets - 1;
     while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gt) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
@@ -1320,6 +1379,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     kind = cp.flags & PFP_KIND;
                 }
                 const bool anyLP = __any_sync(0xffffffffu, kind != 0);
+                const bool anyPhong = __any_sync(0xffffffffu, has && (cp.rstate & PFS_PHONG));
                 const uint32_t blit = __ballot_sync(0xffffffffu, kind == PFP_BLIT);
                 // prefix of clipped box rows; box area
                 uint32_t s = bh;
@@ -1331,7 +1391,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 // (pixel, sub-triangle) pair instead of stepping rows
                 // (points and lines always take the row path)
                 const bool dense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP;
-                if (lane == 0) { sDense = dense; sAnyLP = anyLP; sBlit = blit; }
+                if (lane == 0) { sDense = dense; sAnyLP = anyLP; sBlit = blit; sPhong = anyPhong; }
             }
             __syncthreads();
             uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
@@ -1389,91 +1449,145 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     }
                 }
                 __syncthreads();
-                // 3. depth first, over the whole CTA: the chunk's covered
-                //    fragments, listed pixel by pixel in submission order,
-                //    get their depth computed densely by all threads; then
-                //    each pixel runs its depth tests in order, which leave
-                //    the set of visible fragments
                 const uint32_t m = pmask[tid];
                 const uint32_t cntp = __popc(m);
                 frags += lpChunk ? __popc(m & ~sBlit) : cntp;
                 uint32_t total;
                 const uint32_t myOff = cta_offsets(cntp, wsum, total);
-                for (uint32_t b0 = 0; b0 < total; b0 += FWIN) {
-                    const uint32_t bEnd = min(total, b0 + FWIN);
-                    list_fragments(m, myOff, b0, bEnd, fdesc);
+                if (!sPhong) {
+                    // 3+4. shading is cheap (no per-fragment lighting): every
+                    //    covered fragment, listed pixel by pixel in
+                    //    submission order, gets its depth and colour
+                    //    densely over the CTA; then each pixel applies its
+                    //    fragments in order (depth test, blend, depth write)
+                    for (uint32_t b0 = 0; b0 < total; b0 += FWIN) {
+                        const uint32_t bEnd = min(total, b0 + FWIN);
+                        list_fragments(m, myOff, b0, bEnd, fdesc);
+                        __syncthreads();
+                        for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
+                            const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
+                            const PFPrim &P = sprim[k].p;
+                            if (lpChunk && (scp[k].flags & PFP_KIND)) {
+                                const int32_t X = (int32_t)(ox + p % PF_TILE), Y = (int32_t)(oy + p / PF_TILE);
+                                fval[f - b0] = __float_as_uint(lp_depth(P, X, Y));
+                                fcolv[f - b0] = lp_color(P, X, Y);
+                                continue;
+                            }
+                            float wn[3];
+                            const float z = frag_depth(P, scp[k], p, wn);
+                            fval[f - b0] = __float_as_uint(z);
+                            fcolv[f - b0] = shade_fragment(P, &sph[k], a.states, wn[0], wn[1], wn[2], z);
+                        }
+                        __syncthreads();
+                        if (cntp && myOff < bEnd && myOff + cntp > b0) {
+                            uint32_t f = myOff, mm = m;
+                            while (mm) {
+                                const uint32_t k = __ffs(mm) - 1;
+                                mm &= mm - 1;
+                                if (f >= bEnd) break;
+                                if (f >= b0) {
+                                    const uint32_t rs = scp[k].rstate;
+                                    const float z = __uint_as_float(fval[f - b0]);
+                                    const int func = (int)((rs >> 16) & 255u);
+                                    const bool lpk = lpChunk && (scp[k].flags & PFP_KIND);
+                                    if (!(rs & PFS_DEPTH_TEST) || (lpk ? depth_sisd(func, z, dep) : depth_simd(func, z, dep))) {
+                                        uint32_t frag = fcolv[f - b0];
+                                        if (rs & PFS_BLEND)
+                                            frag = lpk ? blend_sisd((int)(rs >> 24), frag, col) : blend_simd((int)(rs >> 24), frag, col);
+                                        col = frag;
+                                        if (rs & PFS_DEPTH_MASK) dep = z;
+                                    }
+                                }
+                                f++;
+                            }
+                        }
+                        __syncthreads();                      // fdesc, fval and fcolv are free
+                    }
+                } else {
+                    // 3. with per-fragment lighting, depth first, over the
+                    //    whole CTA: the chunk's covered fragments, listed
+                    //    pixel by pixel in submission order, get their depth
+                    //    computed densely by all threads; then each pixel
+                    //    runs its depth tests in order, which leave the set
+                    //    of visible fragments for pass 4
+                    for (uint32_t b0 = 0; b0 < total; b0 += FWIN) {
+                        const uint32_t bEnd = min(total, b0 + FWIN);
+                        list_fragments(m, myOff, b0, bEnd, fdesc);
+                        __syncthreads();
+                        for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
+                            const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
+                            float wn[3];
+                            const float z = (lpChunk && (scp[k].flags & PFP_KIND))
+                                ? lp_depth(sprim[k].p, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
+                                : frag_depth(sprim[k].p, scp[k], p, wn);
+                            fval[f - b0] = __float_as_uint(z);
+                        }
+                        __syncthreads();
+                        if (cntp && myOff < bEnd && myOff + cntp > b0) {
+                            uint32_t f = myOff, mm = m;
+                            while (mm) {
+                                const uint32_t k = __ffs(mm) - 1;
+                                mm &= mm - 1;
+                                if (f >= bEnd) break;
+                                if (f >= b0) {
+                                    const uint32_t rs = scp[k].rstate;
+                                    const float z = __uint_as_float(fval[f - b0]);
+                                    const int func = (int)((rs >> 16) & 255u);
+                                    if (!(rs & PFS_DEPTH_TEST) ||
+                                        ((lpChunk && (scp[k].flags & PFP_KIND)) ? depth_sisd(func, z, dep)
+                                                                                 : depth_simd(func, z, dep))) {
+                                        vis |= 1u << k;
+                                        if (rs & PFS_DEPTH_MASK) dep = z;
+                                    }
+                                }
+                                f++;
+                            }
+                        }
+                        __syncthreads();                          // fdesc and fval are free
+                    }
+                }
+            }
+            // 4. shade the visible fragments (densely over the CTA) and blend
+            //    each pixel's in submission order
+            if (sDense || sPhong) {
+                uint32_t totalv;
+                const uint32_t myOffV = cta_offsets(__popc(vis), wsum, totalv);
+                for (uint32_t b0 = 0; b0 < totalv; b0 += FWIN) {
+                    const uint32_t bEnd = min(totalv, b0 + FWIN);
+                    list_fragments(vis, myOffV, b0, bEnd, fdesc);
                     __syncthreads();
                     for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
                         const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
+                        const PFPrim &P = sprim[k].p;
+                        if (lpChunk && (scp[k].flags & PFP_KIND)) {
+                            fval[f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
+                            continue;
+                        }
                         float wn[3];
-                        const float z = (lpChunk && (scp[k].flags & PFP_KIND))
-                            ? lp_depth(sprim[k].p, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
-                            : frag_depth(sprim[k].p, scp[k], p, wn);
-                        fval[f - b0] = __float_as_uint(z);
+                        const float z = frag_depth(P, scp[k], p, wn);
+                        fval[f - b0] = shade_fragment(P, &sph[k], a.states, wn[0], wn[1], wn[2], z);
                     }
                     __syncthreads();
-                    if (cntp && myOff < bEnd && myOff + cntp > b0) {
-                        uint32_t f = myOff, mm = m;
+                    const uint32_t cntv = __popc(vis);
+                    if (cntv && myOffV < bEnd && myOffV + cntv > b0) {
+                        uint32_t f = myOffV, mm = vis;
                         while (mm) {
                             const uint32_t k = __ffs(mm) - 1;
                             mm &= mm - 1;
                             if (f >= bEnd) break;
                             if (f >= b0) {
                                 const uint32_t rs = scp[k].rstate;
-                                const float z = __uint_as_float(fval[f - b0]);
-                                const int func = (int)((rs >> 16) & 255u);
-                                if (!(rs & PFS_DEPTH_TEST) ||
-                                    ((lpChunk && (scp[k].flags & PFP_KIND)) ? depth_sisd(func, z, dep)
-                                                                             : depth_simd(func, z, dep))) {
-                                    vis |= 1u << k;
-                                    if (rs & PFS_DEPTH_MASK) dep = z;
-                                }
+                                uint32_t frag = fval[f - b0];
+                                if (rs & PFS_BLEND)
+                                    frag = (lpChunk && (scp[k].flags & PFP_KIND)) ? blend_sisd((int)(rs >> 24), frag, col)
+                                                                      : blend_simd((int)(rs >> 24), frag, col);
+                                col = frag;
                             }
                             f++;
                         }
                     }
                     __syncthreads();                          // fdesc and fval are free
                 }
-            }
-            // 4. shade the visible fragments (densely over the CTA) and blend
-            //    each pixel's in submission order
-            uint32_t totalv;
-            const uint32_t myOffV = cta_offsets(__popc(vis), wsum, totalv);
-            for (uint32_t b0 = 0; b0 < totalv; b0 += FWIN) {
-                const uint32_t bEnd = min(totalv, b0 + FWIN);
-                list_fragments(vis, myOffV, b0, bEnd, fdesc);
-                __syncthreads();
-                for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                    const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
-                    const PFPrim &P = sprim[k].p;
-                    if (lpChunk && (scp[k].flags & PFP_KIND)) {
-                        fval[f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
-                        continue;
-                    }
-                    float wn[3];
-                    const float z = frag_depth(P, scp[k], p, wn);
-                    fval[f - b0] = shade_fragment(P, &sph[k], a.states[P.flags >> 8], wn[0], wn[1], wn[2], z);
-                }
-                __syncthreads();
-                const uint32_t cntv = __popc(vis);
-                if (cntv && myOffV < bEnd && myOffV + cntv > b0) {
-                    uint32_t f = myOffV, mm = vis;
-                    while (mm) {
-                        const uint32_t k = __ffs(mm) - 1;
-                        mm &= mm - 1;
-                        if (f >= bEnd) break;
-                        if (f >= b0) {
-                            const uint32_t rs = scp[k].rstate;
-                            uint32_t frag = fval[f - b0];
-                            if (rs & PFS_BLEND)
-                                frag = (lpChunk && (scp[k].flags & PFP_KIND)) ? blend_sisd((int)(rs >> 24), frag, col)
-                                                                  : blend_simd((int)(rs >> 24), frag, col);
-                            col = frag;
-                        }
-                        f++;
-                    }
-                }
-                __syncthreads();                              // fdesc and fval are free
             }
         }
     }
@@ -1586,7 +1700,7 @@ cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
-    BinArgs B{ L.binCount, L.tileList, L.bins, L.cap, L.targets, L.cnt, L.command };
+    BinArgs B{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.targets, L.cnt, L.command };
     ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap };
     k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, O, B);
     return cudaGetLastError();
@@ -1603,7 +1717,7 @@ static size_t raster_smem(uint32_t cap)
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
-    RasterArgs a{ L.binCount, L.tileList, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
+    RasterArgs a{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
                   L.totalTiles, L.cnt, L.command, L.anyPhong };
     const size_t smem = raster_smem(L.cap);
     cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -19,6 +19,8 @@
 #define PF_MAX_SUBTRIS     10          /* fan of a triangle clipped by 7 planes */
 #define PF_CLIP_MAXV       12          /* polygon capacity during clipping */
 #define PF_SUB_BITS        4           /* bin key = item << 4 | sub-triangle */
+#define PF_HEAVY1          48          /* bin sizes from which a tile is rasterized early */
+#define PF_HEAVY2          96
 
 /* draw-state flag bits */
 enum {
@@ -162,11 +164,20 @@ typedef struct {
     float u1, v1, u2, v2;
     float u3, v3;
     float zReject;                /* depth-test rejection bound (k_raster's dense path); NaN: none */
-    float pad2;
-    uint64_t src;                 /* PFP_BLIT: device address of the RGBA8 image, 0 for a plain colour */
-    uint32_t nSrc;                /* PFP_BLIT: pixels in the image */
-    float pad3;
+    float texTx;                  /* textured triangles: 1 / texture width (the bilinear step) */
+    uint64_t src;                 /* textured triangles: the texels; PFP_BLIT: the RGBA8 image, 0 for a colour */
+    uint32_t nSrc;                /* textured triangles: width | height << 16; PFP_BLIT: pixels in the image */
+    float texTy;                  /* textured triangles: 1 / texture height */
 } PFPrim;                         /* 128 bytes */
+
+/* PFPrim.rstate bits above the state's PFS_* flags: the texture's wrap mode
+ * and filter, and whether its parameters must be read from the draw state
+ * (a side of 65536 texels or more does not fit nSrc). */
+enum {
+    PFR_WRAP_SHIFT = 8,
+    PFR_FILTER = 1u << 10,
+    PFR_TEX_FROM_STATE = 1u << 11
+};
 
 typedef struct {
     float n1[3], n2[3], n3[3];
@@ -192,6 +203,8 @@ typedef struct {
     unsigned long long batchRasterized;   /* sub-triangles set up by the current batch */
     unsigned int tileQueue;       /* next entry of the current batch's raster work list */
     unsigned int tileListCount;   /* tiles with a non-empty bin, listed by the binning */
+    unsigned int heavyCount1;     /* tiles whose bin reached PF_HEAVY1 entries */
+    unsigned int heavyCount2;     /* tiles whose bin reached PF_HEAVY2 entries */
 } PFDevCounters;
 
 #endif /* PF_LAYOUT_H */
