@@ -1214,7 +1214,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ uint16_t fdesc[FWIN];                  // listed fragments: pixel << 5 | chunk record
     __shared__ uint32_t fval[FWIN];                   // their depth (pass 3) or colour (pass 4)
     __shared__ uint32_t fcolv[FWIN];                  // their colour (passes 3 and 4 in one)
-    __shared__ uint32_t wsum[RASTER_THREADS / 32];
+    __shared__ uint32_t wsum[2][RASTER_THREADS / 32];    // pass 3 (and the merged pass), pass 4
     __shared__ int sDense, sAnyLP, sPhong;
     __shared__ uint32_t sBlit;                        // chunk records that are rectangles (not counted as fragments)
 
@@ -1453,7 +1453,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 const uint32_t cntp = __popc(m);
                 frags += lpChunk ? __popc(m & ~sBlit) : cntp;
                 uint32_t total;
-                const uint32_t myOff = cta_offsets(cntp, wsum, total);
+                const uint32_t myOff = cta_offsets(cntp, wsum[0], total);
                 if (!sPhong) {
                     // 3+4. shading is cheap (no per-fragment lighting): every
                     //    covered fragment, listed pixel by pixel in
@@ -1501,7 +1501,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                                 f++;
                             }
                         }
-                        __syncthreads();                      // fdesc, fval and fcolv are free
+                        // (no barrier: the next window's list build touches only
+                        // fdesc, and its compute starts after a barrier)
                     }
                 } else {
                     // 3. with per-fragment lighting, depth first, over the
@@ -1543,7 +1544,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                                 f++;
                             }
                         }
-                        __syncthreads();                          // fdesc and fval are free
+                        // (no barrier needed before the next window or pass 4)
                     }
                 }
             }
@@ -1551,7 +1552,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             //    each pixel's in submission order
             if (sDense || sPhong) {
                 uint32_t totalv;
-                const uint32_t myOffV = cta_offsets(__popc(vis), wsum, totalv);
+                const uint32_t myOffV = cta_offsets(__popc(vis), wsum[1], totalv);
                 for (uint32_t b0 = 0; b0 < totalv; b0 += FWIN) {
                     const uint32_t bEnd = min(totalv, b0 + FWIN);
                     list_fragments(vis, myOffV, b0, bEnd, fdesc);
@@ -1586,7 +1587,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                             f++;
                         }
                     }
-                    __syncthreads();                          // fdesc and fval are free
+                    // (no barrier: the next chunk starts with one)
                 }
             }
         }
