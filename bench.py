@@ -167,7 +167,8 @@ def run_gpu(args):
     peak, peak_kind = _peaks()
     raster_ms = st["raster_ms"] / max(st["raster_launches"], 1)
     achieved = fb["raster"] / (raster_ms / 1e3) / 1e9
-    h2d = (2 * (scene.pos.nbytes * 2 + scene.uv.nbytes + scene.idx.nbytes) + scene.tex.nbytes)
+    # each draw copies what it references: positions, normals, uvs, indices, texture
+    h2d = 2 * (scene.pos.nbytes * 2 + scene.uv.nbytes + scene.idx.nbytes + scene.tex.nbytes)
     d2h = scene.width * scene.height * 4
     out = {
         "metric": "fragments/s",

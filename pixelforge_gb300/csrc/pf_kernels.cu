@@ -399,6 +399,7 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
     __shared__ __align__(16) PFDrawState sState;
     __shared__ int sUniform;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // the previous kernel of the stream is done
     if (cnt->abortCommand != 0xffffffffu) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
     if (g == 0) {
@@ -809,6 +810,7 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
     __shared__ __align__(16) PFDrawState sState;
     __shared__ int sUniform;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // k_vertex is done
     if (B.cnt->abortCommand != 0xffffffffu) return;
     const uint32_t g0 = blockIdx.x * blockDim.x;
     if (threadIdx.x == 0) {
@@ -1218,6 +1220,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ int sDense, sAnyLP, sPhong;
     __shared__ uint32_t sBlit;                        // chunk records that are rectangles (not counted as fragments)
 
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // k_items is done
     if (a.cnt->abortCommand <= a.command) return;
     // the batch completed set-up without overflow: its sub-triangles count
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.cnt->rasterized, a.cnt->batchRasterized);
@@ -1676,6 +1679,30 @@ __global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, 
 // ---------------------------------------------------------------------------
 static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
+// The three pipeline kernels are launched with programmatic stream
+// serialization: a kernel's CTAs may be scheduled as the previous kernel's
+// last CTAs exit (no early trigger is issued, so every CTA of the previous
+// grid has left its SM by then), and each kernel starts with
+// griddepcontrol.wait, which returns once the previous grid has completed
+// and its memory is visible.  What this hides is the launch gap between
+// the kernels of a frame.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_serialized(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                                     cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 int pfd_sm_count(void)
 {
     static int sms = 0;
@@ -1693,9 +1720,8 @@ cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 {
     const uint32_t nTiles = L.totalTiles;
     const size_t work = L.nVerts > nTiles ? L.nVerts : nTiles;
-    k_vertex<<<grid_for(work, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nVerts, L.cnt,
-                                                  L.binCount, nTiles);
-    return cudaGetLastError();
+    return launch_serialized(k_vertex, grid_for(work, 128), 128, 0, st, L.segs, L.nSegs, L.states, L.vout, L.nVerts,
+                             L.cnt, L.binCount, nTiles);
 }
 
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
@@ -1703,8 +1729,8 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
     if (L.nItems == 0) return cudaSuccess;
     BinArgs B{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.targets, L.cnt, L.command };
     ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap };
-    k_items<<<grid_for(L.nItems, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nItems, O, B);
-    return cudaGetLastError();
+    return launch_serialized(k_items, grid_for(L.nItems, 128), 128, 0, st, L.segs, L.nSegs, L.states,
+                             (const PFVertexOut *)L.vout, L.nItems, O, B);
 }
 
 static size_t raster_smem(uint32_t cap)
@@ -1725,8 +1751,7 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
     if (e != cudaSuccess) return e;
     const uint32_t per = (uint32_t)(L.rasterCtasPerSM > 0 ? L.rasterCtasPerSM : 4);
     const uint32_t grid = min(L.totalTiles, (uint32_t)pfd_sm_count() * per);
-    k_raster<<<grid, RASTER_THREADS, smem, st>>>(a);
-    return cudaGetLastError();
+    return launch_serialized(k_raster, grid, RASTER_THREADS, smem, st, a);
 }
 
 cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
