@@ -201,11 +201,54 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, samples=2)
     tg.close()
+    if not args.no_phong:
+        out["phong"] = run_phong(lib)
     if not args.no_batched:
         out["batched"] = run_batched(lib)
     if not args.no_adjoint:
         out["adjoint"] = run_adjoint(args)
     return out
+
+
+def run_phong(lib, warmup: int = 2, steps: int = 5) -> dict:
+    """The fragment-heavy Phong workload at 1080p: 1.3M-triangle displaced
+    icosphere, 8 point lights per fragment, 2048^2 nearest mirrored texture,
+    30% of the triangles additive, device fog hook.  Device time of the
+    frame's kernels (events), fragments counted on the device, and the end-
+    to-end time of the API calls, uploads and write-back."""
+    import torch
+    from pixelforge_gb300 import abi as A
+    from pixelforge_gb300.scenes import PhongScene, Target
+    sc = PhongScene()
+    tg = Target(lib, sc.width, sc.height, "main")
+    sc.setup(lib)
+    lib.pfEnableTiming(True)
+    l2_flush = torch.empty(512 << 20, dtype=torch.uint8, device=torch.device("cuda:0"))
+    for _ in range(warmup):
+        sc.frame(lib)
+        lib.pfFinish()
+    lib.pfResetStats()
+    wall = 0.0
+    for _ in range(steps):
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc.frame(lib)
+        lib.pfFinish()
+        wall += time.perf_counter() - t0
+    s = A.PFstats()
+    lib.pfGetStats(s)
+    status = lib.pfGetDeviceStatus()
+    sc.teardown(lib)
+    tg.close()
+    if status != 0:
+        raise RuntimeError(f"device status {status:#x}")
+    return {"workload": f"phong1080: displaced icosphere subdiv 8 ({sc.ntris} triangles), 8 point lights per "
+                        "fragment, 2048^2 nearest mirrored-repeat texture, 30% additive, device fog",
+            "ms_per_frame": s.device_ms / steps, "fragments_per_frame": s.fragments / steps,
+            "fragments_per_s": s.fragments / (s.device_ms / 1e3),
+            "raster_ms_per_frame": s.raster_ms / steps,
+            "e2e_ms_per_frame": wall * 1e3 / steps, "l2": "flushed between frames"}
 
 
 def run_adjoint(args) -> dict:
@@ -385,6 +428,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-context batch measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the fitting-iteration measurement")
+    ap.add_argument("--no-phong", action="store_true", help="skip the Phong 1080p measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -31,8 +31,9 @@ struct PFBatchLaunch {
     PFPrimPhong *poolPh;
     uint32_t poolCap;
     uint32_t *binCount;       /* totalTiles */
-    uint32_t *tileList;       /* three lists of listStride entries: the tiles with a non-empty bin,
-                                 with >= PF_HEAVY1, with >= PF_HEAVY2 entries; NULL: queue every tile */
+    uint32_t *tileList;       /* 1 + PF_HEAVY_LEVELS lists of listStride entries: the tiles with a
+                                 non-empty bin, then those whose bin reached each heavy level;
+                                 NULL: queue every tile */
     uint32_t listStride;
     uint32_t *bins;           /* totalTiles * cap */
     uint32_t cap;

@@ -1590,7 +1590,7 @@ bool flush(Renderer *r)
             !r->primsPh.ensure(anyPhong ? (size_t)maxItems * sizeof(PFPrimPhong) + 128 : 128) ||
             !r->pool.ensure((size_t)r->poolCap * sizeof(PFPrim)) ||
             !r->poolPh.ensure(anyPhong ? (size_t)r->poolCap * sizeof(PFPrimPhong) : 128) ||
-            !r->binCount.ensure((size_t)(((size_t)maxTiles + 31) & ~(size_t)31) * 16) ||   // bin counters, three tile lists
+            !r->binCount.ensure((size_t)(((size_t)maxTiles + 31) & ~(size_t)31) * 4 * (2 + PF_HEAVY_LEVELS)) ||   // bin counters, tile lists
             !r->bins.ensure((size_t)maxTiles * r->cap * 4 + 64)) {
             r->devStatus |= PF_DEVICE_ALLOC_FAIL;
             return fail("cudaMalloc(scratch)", cudaErrorMemoryAllocation);

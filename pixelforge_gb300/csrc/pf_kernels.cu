@@ -404,7 +404,8 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
     if (g == 0) {
         cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0;
-        cnt->tileListCount = 0; cnt->heavyCount1 = 0; cnt->heavyCount2 = 0;
+        cnt->tileListCount = 0;
+        for (int l = 0; l < PF_HEAVY_LEVELS; l++) cnt->heavyCount[l] = 0;
     }
     const uint32_t g0 = blockIdx.x * blockDim.x;
     if (g0 >= nVerts) return;
@@ -533,16 +534,22 @@ __device__ __forceinline__ void bin_slot(const BinArgs &B, uint32_t t, uint32_t 
 
 // Raster work lists: a tile's bin growing from `before` to `before + added`
 // entries puts the tile on the list of non-empty tiles (first entry) and on
-// the lists of heavy tiles (PF_HEAVY1 and PF_HEAVY2 entries), which the
-// rasterizer takes first so that the longest tiles do not start last.
+// the list of each heavy level it reaches (32, 128, 512, 2048 entries),
+// which the rasterizer takes first, heaviest level first, so that the
+// longest tiles do not start last.
+__device__ __forceinline__ uint32_t heavy_level(uint32_t count)
+{
+    uint32_t l = 0;
+    for (uint32_t th = PF_HEAVY_BASE; l < PF_HEAVY_LEVELS && count >= th; th <<= 2) l++;
+    return l;                                          // 0: below the first level
+}
+
 __device__ __forceinline__ void list_tile(const BinArgs &B, uint32_t t, uint32_t before, uint32_t added)
 {
     if (!B.tileList) return;
     if (before == 0) B.tileList[atomicAdd(&B.cnt->tileListCount, 1u)] = t;
-    if (before < PF_HEAVY1 && before + added >= PF_HEAVY1)
-        B.tileList[B.listStride + atomicAdd(&B.cnt->heavyCount1, 1u)] = t;
-    if (before < PF_HEAVY2 && before + added >= PF_HEAVY2)
-        B.tileList[2 * B.listStride + atomicAdd(&B.cnt->heavyCount2, 1u)] = t;
+    for (uint32_t l = heavy_level(before) + 1; l <= heavy_level(before + added); l++)
+        B.tileList[l * B.listStride + atomicAdd(&B.cnt->heavyCount[l - 1], 1u)] = t;
 }
 
 // Append `key` to the bin of every tile the sub-triangle touches (one
@@ -1232,12 +1239,16 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     // binning listed as non-empty (every tile when there is no list); the
     // next entry is claimed while the current tile is rasterized
     const bool listed = a.tileList != nullptr;
-    // queue entries: the tiles with >= PF_HEAVY2 entries, then those with
-    // >= PF_HEAVY1, then every non-empty tile; a tile is rasterized from
-    // the first list it is on and skipped on the later ones
-    const uint32_t nH2 = listed ? min(a.cnt->heavyCount2, a.totalTiles) : 0u;
-    const uint32_t nH1 = listed ? min(a.cnt->heavyCount1, a.totalTiles) : 0u;
-    const uint32_t nQueue = listed ? nH2 + nH1 + min(a.cnt->tileListCount, a.totalTiles) : a.totalTiles;
+    // queue entries: the tiles of the heaviest level, then of each lighter
+    // level, then every non-empty tile; a tile is rasterized from the first
+    // list it is on and skipped on the later ones
+    uint32_t levelEnd[PF_HEAVY_LEVELS + 1];           // queue index past level l's entries, heaviest first
+    uint32_t nQueue = 0;
+    if (listed) {
+        for (int l = PF_HEAVY_LEVELS; l >= 1; l--) { nQueue += min(a.cnt->heavyCount[l - 1], a.totalTiles); levelEnd[l] = nQueue; }
+        nQueue += min(a.cnt->tileListCount, a.totalTiles);
+        levelEnd[0] = nQueue;
+    } else nQueue = a.totalTiles;
     __shared__ uint32_t sNext;
     uint32_t claim = 0;
     if (tid == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
@@ -1282,12 +1293,10 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             claim = atomicAdd(&a.cnt->tileQueue, 1u);
             if (!listed) next = q;
             else {
-                const uint32_t level = q < nH2 ? 2u : (q < nH2 + nH1 ? 1u : 0u);
-                const uint32_t idx = level == 2u ? 2u * a.listStride + q : (level == 1u ? a.listStride + q - nH2 : q - nH2 - nH1);
-                next = __ldg(a.tileList + idx);
-                const uint32_t c = __ldg(a.binCount + next);
-                const uint32_t own = c >= PF_HEAVY2 ? 2u : (c >= PF_HEAVY1 ? 1u : 0u);
-                if (own != level) next = 0xfffffffeu;            // rasterized from an earlier list
+                uint32_t level = PF_HEAVY_LEVELS, begin = 0;
+                while (q >= levelEnd[level]) { begin = levelEnd[level]; level--; }
+                next = __ldg(a.tileList + (size_t)level * a.listStride + (q - begin));
+                if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
             }
         }
         sNext = next;

@@ -19,8 +19,8 @@
 #define PF_MAX_SUBTRIS     10          /* fan of a triangle clipped by 7 planes */
 #define PF_CLIP_MAXV       12          /* polygon capacity during clipping */
 #define PF_SUB_BITS        4           /* bin key = item << 4 | sub-triangle */
-#define PF_HEAVY1          48          /* bin sizes from which a tile is rasterized early */
-#define PF_HEAVY2          96
+#define PF_HEAVY_LEVELS    4           /* bin sizes from which a tile is rasterized early: */
+#define PF_HEAVY_BASE      32          /* 32, 128, 512, 2048 entries (x4 per level) */
 
 /* draw-state flag bits */
 enum {
@@ -203,8 +203,7 @@ typedef struct {
     unsigned long long batchRasterized;   /* sub-triangles set up by the current batch */
     unsigned int tileQueue;       /* next entry of the current batch's raster work list */
     unsigned int tileListCount;   /* tiles with a non-empty bin, listed by the binning */
-    unsigned int heavyCount1;     /* tiles whose bin reached PF_HEAVY1 entries */
-    unsigned int heavyCount2;     /* tiles whose bin reached PF_HEAVY2 entries */
+    unsigned int heavyCount[PF_HEAVY_LEVELS];   /* tiles whose bin reached 32 << 2 l entries */
 } PFDevCounters;
 
 #endif /* PF_LAYOUT_H */
