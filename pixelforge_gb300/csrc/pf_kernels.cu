@@ -873,9 +873,11 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 //      blend, depth write) on its colour and depth held in registers.
 // ---------------------------------------------------------------------------
 #define RASTER_THREADS PF_TILE_PIXELS
-#define CH 32
-#define FWIN 2048
+#define CH 64
+#define FWIN 1024
 #define RANK_SORT_MAX 1024
+
+typedef unsigned long long ChunkMask;      // bit k: chunk record k (CH = 64 records per chunk)
 
 struct RasterArgs {
     const uint32_t *binCount;
@@ -989,13 +991,13 @@ __device__ __forceinline__ uint32_t cta_offsets(uint32_t cnt, uint32_t *wsum, ui
 // Write this pixel's fragments (set bits of mask, in order) to entries
 // off, off + 1, ... of the fragment list, as far as they fall in the
 // window [b0, bEnd): pixel << 5 | chunk record.
-__device__ __forceinline__ void list_fragments(uint32_t mask, uint32_t off, uint32_t b0, uint32_t bEnd, uint16_t *fdesc)
+__device__ __forceinline__ void list_fragments(ChunkMask mask, uint32_t off, uint32_t b0, uint32_t bEnd, uint16_t *fdesc)
 {
-    const uint32_t cnt = __popc(mask);
+    const uint32_t cnt = __popcll(mask);
     if (!cnt || off >= bEnd || off + cnt <= b0) return;
     uint32_t f = off;
-    for (uint32_t mm = mask; mm && f < bEnd; mm &= mm - 1, f++)
-        if (f >= b0) fdesc[f - b0] = (uint16_t)((threadIdx.x << 5) | (uint32_t)(__ffs(mm) - 1));
+    for (ChunkMask mm = mask; mm && f < bEnd; mm &= mm - 1, f++)
+        if (f >= b0) fdesc[f - b0] = (uint16_t)((threadIdx.x << 6) | (uint32_t)(__ffsll(mm) - 1));
 }
 
 // Weights and depth of a covered fragment at tile pixel p (triangles.c:426-438).
@@ -1219,13 +1221,13 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     __shared__ ChunkPrim scp[CH];
     __shared__ DenseP sdp[CH];
     __shared__ uint32_t sarea[CH + 1];
-    __shared__ uint32_t pmask[RASTER_THREADS];
+    __shared__ ChunkMask pmask[RASTER_THREADS];
     __shared__ uint16_t fdesc[FWIN];                  // listed fragments: pixel << 5 | chunk record
     __shared__ uint32_t fval[FWIN];                   // their depth (pass 3) or colour (pass 4)
     __shared__ uint32_t fcolv[FWIN];                  // their colour (passes 3 and 4 in one)
     __shared__ uint32_t wsum[2][RASTER_THREADS / 32];    // pass 3 (and the merged pass), pass 4
     __shared__ int sDense, sAnyLP, sPhong;
-    __shared__ uint32_t sBlit;                        // chunk records that are rectangles (not counted as fragments)
+    __shared__ ChunkMask sBlit;                        // chunk records that are rectangles (not counted as fragments)
 
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_items is done
     if (a.cnt->abortCommand <= a.command) return;
@@ -1374,39 +1376,44 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 stage_chunk_async(a, keys, c0 + CH, min((uint32_t)CH, n - c0 - CH), sprimBuf[(it + 1) & 1],
                                   sphBuf[(it + 1) & 1]);
             pmask[tid] = 0;
-            // 1. warp 0 derives the chunk's tile-relative set-up (one
-            //    sub-triangle per lane)
+            // 1. warp 0 derives the chunk's tile-relative set-up (two
+            //    records per lane)
             if (warp == 0) {
-                const bool has = lane < cn;
-                uint32_t bh = 0, area = 0;
-                ChunkPrim cp;
-                DenseP dp;
-                uint32_t kind = 0;
-                if (has) {
-                    derive_chunk_prim(&sprim[lane], ox, oy, T.W, T.H, cp, dp);
-                    scp[lane] = cp;
-                    sdp[lane] = dp;
-                    bh = cp.bw ? cp.bh : 0;
-                    area = cp.bw * cp.bh;
-                    kind = cp.flags & PFP_KIND;
+                uint32_t area = 0, kinds = 0;
+                bool phong = false;
+                ChunkMask blit = 0;
+                uint32_t base = 0;                            // rows of the first half
+                for (int h = 0; h < CH / 32; h++) {
+                    const uint32_t k = (uint32_t)(h * 32 + lane);
+                    const bool has = k < cn;
+                    uint32_t bh = 0, kind = 0;
+                    if (has) {
+                        ChunkPrim cp;
+                        DenseP dp;
+                        derive_chunk_prim(&sprim[k], ox, oy, T.W, T.H, cp, dp);
+                        scp[k] = cp;
+                        sdp[k] = dp;
+                        bh = cp.bw ? cp.bh : 0;
+                        area += cp.bw * cp.bh;
+                        kind = cp.flags & PFP_KIND;
+                        phong = phong || (cp.rstate & PFS_PHONG);
+                    }
+                    kinds |= kind;
+                    blit |= (ChunkMask)__ballot_sync(0xffffffffu, kind == PFP_BLIT) << (32 * h);
+                    uint32_t sc = bh;
+                    for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, sc, o); if (lane >= o) sc += t; }
+                    sarea[k + 1] = base + sc;
+                    base += __shfl_sync(0xffffffffu, sc, 31);
                 }
-                const bool anyLP = __any_sync(0xffffffffu, kind != 0);
-                const bool anyPhong = __any_sync(0xffffffffu, has && (cp.rstate & PFS_PHONG));
-                const uint32_t blit = __ballot_sync(0xffffffffu, kind == PFP_BLIT);
-                // prefix of clipped box rows; box area
-                uint32_t s = bh;
-                for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
-                sarea[lane + 1] = s;
                 if (lane == 0) sarea[0] = 0;
+                const bool anyLP = __any_sync(0xffffffffu, kinds != 0);
+                const bool anyPhong = __any_sync(0xffffffffu, phong);
                 for (int o = 16; o > 0; o >>= 1) area += __shfl_xor_sync(0xffffffffu, area, o);
-                // boxes that cover half a tile on average: test every
-                // (pixel, sub-triangle) pair instead of stepping rows
-                // (points and lines always take the row path)
                 const bool dense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP;
                 if (lane == 0) { sDense = dense; sAnyLP = anyLP; sBlit = blit; sPhong = anyPhong; }
             }
             __syncthreads();
-            uint32_t vis = 0;                                 // chunk sub-triangles visible at my pixel
+            ChunkMask vis = 0;                                // chunk sub-triangles visible at my pixel
             const bool lpChunk = sAnyLP != 0;                 // the chunk holds points or lines
             if (sDense) {
                 // 2+3 (large sub-triangles). Each thread walks the chunk in
@@ -1431,7 +1438,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     const float z = 1.0f / zs;
                     const uint32_t rs = (uint32_t)q2.z;
                     if (!(rs & PFS_DEPTH_TEST) || depth_simd((int)((rs >> 16) & 255u), z, dep)) {
-                        vis |= 1u << k;
+                        vis |= 1ull << k;
                         if (rs & PFS_DEPTH_MASK) dep = z;
                     }
                 }
@@ -1445,11 +1452,11 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
                     const ChunkPrim &cp = scp[lo];
                     const uint32_t Y = cp.by0 + (t - sarea[lo]);
-                    const uint32_t bit = 1u << lo;
+                    const ChunkMask bit = 1ull << lo;
                     uint32_t w1 = (uint32_t)cp.e0[0] + cp.bx0 * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0];
                     uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
                     uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
-                    uint32_t *row = &pmask[Y * PF_TILE + cp.bx0];
+                    ChunkMask *row = &pmask[Y * PF_TILE + cp.bx0];
                     if (lpChunk && (cp.flags & PFP_KIND)) {
                         for (uint32_t dx = 0; dx < cp.bw; dx++)
                             if (lp_covers(sprim[lo].p, (int32_t)(ox + cp.bx0 + dx), (int32_t)(oy + Y))) atomicOr(row + dx, bit);
@@ -1461,9 +1468,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     }
                 }
                 __syncthreads();
-                const uint32_t m = pmask[tid];
-                const uint32_t cntp = __popc(m);
-                frags += lpChunk ? __popc(m & ~sBlit) : cntp;
+                const ChunkMask m = pmask[tid];
+                const uint32_t cntp = __popcll(m);
+                frags += lpChunk ? __popcll(m & ~sBlit) : cntp;
                 uint32_t total;
                 const uint32_t myOff = cta_offsets(cntp, wsum[0], total);
                 if (!sPhong) {
@@ -1477,7 +1484,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         list_fragments(m, myOff, b0, bEnd, fdesc);
                         __syncthreads();
                         for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                            const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
+                            const uint32_t d = fdesc[f - b0], p = d >> 6, k = d & 63u;
                             const PFPrim &P = sprim[k].p;
                             if (lpChunk && (scp[k].flags & PFP_KIND)) {
                                 const int32_t X = (int32_t)(ox + p % PF_TILE), Y = (int32_t)(oy + p / PF_TILE);
@@ -1492,9 +1499,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         }
                         __syncthreads();
                         if (cntp && myOff < bEnd && myOff + cntp > b0) {
-                            uint32_t f = myOff, mm = m;
+                            uint32_t f = myOff; ChunkMask mm = m;
                             while (mm) {
-                                const uint32_t k = __ffs(mm) - 1;
+                                const uint32_t k = __ffsll(mm) - 1;
                                 mm &= mm - 1;
                                 if (f >= bEnd) break;
                                 if (f >= b0) {
@@ -1528,7 +1535,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         list_fragments(m, myOff, b0, bEnd, fdesc);
                         __syncthreads();
                         for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                            const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
+                            const uint32_t d = fdesc[f - b0], p = d >> 6, k = d & 63u;
                             float wn[3];
                             const float z = (lpChunk && (scp[k].flags & PFP_KIND))
                                 ? lp_depth(sprim[k].p, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
@@ -1537,9 +1544,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         }
                         __syncthreads();
                         if (cntp && myOff < bEnd && myOff + cntp > b0) {
-                            uint32_t f = myOff, mm = m;
+                            uint32_t f = myOff; ChunkMask mm = m;
                             while (mm) {
-                                const uint32_t k = __ffs(mm) - 1;
+                                const uint32_t k = __ffsll(mm) - 1;
                                 mm &= mm - 1;
                                 if (f >= bEnd) break;
                                 if (f >= b0) {
@@ -1549,7 +1556,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                                     if (!(rs & PFS_DEPTH_TEST) ||
                                         ((lpChunk && (scp[k].flags & PFP_KIND)) ? depth_sisd(func, z, dep)
                                                                                  : depth_simd(func, z, dep))) {
-                                        vis |= 1u << k;
+                                        vis |= 1ull << k;
                                         if (rs & PFS_DEPTH_MASK) dep = z;
                                     }
                                 }
@@ -1564,13 +1571,13 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             //    each pixel's in submission order
             if (sDense || sPhong) {
                 uint32_t totalv;
-                const uint32_t myOffV = cta_offsets(__popc(vis), wsum[1], totalv);
+                const uint32_t myOffV = cta_offsets(__popcll(vis), wsum[1], totalv);
                 for (uint32_t b0 = 0; b0 < totalv; b0 += FWIN) {
                     const uint32_t bEnd = min(totalv, b0 + FWIN);
                     list_fragments(vis, myOffV, b0, bEnd, fdesc);
                     __syncthreads();
                     for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                        const uint32_t d = fdesc[f - b0], p = d >> 5, k = d & 31u;
+                        const uint32_t d = fdesc[f - b0], p = d >> 6, k = d & 63u;
                         const PFPrim &P = sprim[k].p;
                         if (lpChunk && (scp[k].flags & PFP_KIND)) {
                             fval[f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
@@ -1581,11 +1588,11 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                         fval[f - b0] = shade_fragment(P, &sph[k], a.states, wn[0], wn[1], wn[2], z);
                     }
                     __syncthreads();
-                    const uint32_t cntv = __popc(vis);
+                    const uint32_t cntv = __popcll(vis);
                     if (cntv && myOffV < bEnd && myOffV + cntv > b0) {
-                        uint32_t f = myOffV, mm = vis;
+                        uint32_t f = myOffV; ChunkMask mm = vis;
                         while (mm) {
-                            const uint32_t k = __ffs(mm) - 1;
+                            const uint32_t k = __ffsll(mm) - 1;
                             mm &= mm - 1;
                             if (f >= bEnd) break;
                             if (f >= b0) {

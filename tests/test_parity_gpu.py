@@ -74,6 +74,15 @@ def test_phong_fog_540(gpu, oracle):
     assert_parity(got, ref, exact_color=True, label="phong fog")
 
 
+def test_phong_fog_1080_full_size(gpu, oracle):
+    """The fragment-heavy workload at its full size (1.3M triangles, tile
+    bins of 2,000-3,300 entries rasterized in halves)."""
+    sc = PhongScene()
+    got, ref = sc.render(gpu), sc.render(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert_parity(got, ref, exact_color=True, label="phong fog 1080")
+
+
 @pytest.mark.parametrize("seed", range(60))
 def test_feature_mix(gpu, oracle, seed):
     case = mix_case(seed, bilinear=True)
