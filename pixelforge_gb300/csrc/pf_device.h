@@ -41,6 +41,7 @@ struct PFBatchLaunch {
     int nTargets;
     uint32_t totalTiles;
     int rasterCtasPerSM;      /* persistent raster grid: SMs x this */
+    int chunk;                /* records per raster chunk: 64, or 32 (the default) */
     int anyPhong;             /* some state of the launch lights per fragment */
     PFDevCounters *cnt;
     uint32_t command;

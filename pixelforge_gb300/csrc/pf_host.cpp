@@ -1627,6 +1627,10 @@ bool flush(Renderer *r)
                 L.listStride = (uint32_t)(((size_t)maxTiles + 31) & ~(size_t)31);
                 L.tileList = (uint32_t *)r->binCount.p + L.listStride;
                 L.rasterCtasPerSM = r->rasterCtasPerSM;
+                // long bins of small triangles (more than 24 items per tile on
+                // average) take 64-record chunks; bigger triangles, whose
+                // bins need more capacity, the smaller footprint of 32
+                L.chunk = (uint64_t)L.nItems >= 24ull * L.totalTiles ? 64 : 32;
                 L.anyPhong = anyPhong ? 1 : 0;
                 L.cnt = dcnt;
                 rop.L = L;

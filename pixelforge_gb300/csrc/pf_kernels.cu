@@ -859,7 +859,7 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 // ---------------------------------------------------------------------------
 // k_raster: one CTA per 16x16 tile
 //
-// For each chunk of CH sub-triangles (in submission order):
+// For each chunk of CHN sub-triangles (in submission order):
 //   1. stage the records in shared memory, with each one's bounding box
 //      clipped to the tile and its edge functions at the tile origin;
 //   2. coverage, prim-parallel: the (sub-triangle, pixel) pairs of all
@@ -873,11 +873,13 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 //      blend, depth write) on its colour and depth held in registers.
 // ---------------------------------------------------------------------------
 #define RASTER_THREADS PF_TILE_PIXELS
-#define CH 64
+// records per chunk: 64 (64-bit fragment masks) where tiles are long
+// lists of small triangles, 32 (less shared memory, so bigger bins at full
+// occupancy) otherwise; chosen per launch (PFBatchLaunch.chunk)
 #define FWIN 1024
 #define RANK_SORT_MAX 1024
 
-typedef unsigned long long ChunkMask;      // bit k: chunk record k (CH = 64 records per chunk)
+typedef unsigned long long ChunkMask;      // bit k: chunk record k
 
 struct RasterArgs {
     const uint32_t *binCount;
@@ -1213,14 +1215,15 @@ __device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uin
     cp_async_commit();
 }
 
+template <int CHN>
 __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
 {
     extern __shared__ uint32_t skeys[];               // [N] keys (+ [n] sorted copy when rank-sorting)
-    __shared__ SPrim sprimBuf[2][CH];                 // double-buffered chunk records
-    __shared__ __align__(16) PFPrimPhong sphBuf[2][CH];
-    __shared__ ChunkPrim scp[CH];
-    __shared__ DenseP sdp[CH];
-    __shared__ uint32_t sarea[CH + 1];
+    __shared__ SPrim sprimBuf[2][CHN];                 // double-buffered chunk records
+    __shared__ __align__(16) PFPrimPhong sphBuf[2][CHN];
+    __shared__ ChunkPrim scp[CHN];
+    __shared__ DenseP sdp[CHN];
+    __shared__ uint32_t sarea[CHN + 1];
     __shared__ ChunkMask pmask[RASTER_THREADS];
     __shared__ uint16_t fdesc[FWIN];                  // listed fragments: pixel << 5 | chunk record
     __shared__ uint32_t fval[FWIN];                   // their depth (pass 3) or colour (pass 4)
@@ -1365,15 +1368,15 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             }
         }
 
-        stage_chunk_async(a, keys, 0, min((uint32_t)CH, n), sprimBuf[0], sphBuf[0]);
-        for (uint32_t c0 = 0, it = 0; c0 < n; c0 += CH, it++) {
-            const uint32_t cn = min((uint32_t)CH, n - c0);
+        stage_chunk_async(a, keys, 0, min((uint32_t)CHN, n), sprimBuf[0], sphBuf[0]);
+        for (uint32_t c0 = 0, it = 0; c0 < n; c0 += CHN, it++) {
+            const uint32_t cn = min((uint32_t)CHN, n - c0);
             SPrim *const sprim = sprimBuf[it & 1];
             PFPrimPhong *const sph = sphBuf[it & 1];
             cp_async_wait_all();
             __syncthreads();                                  // this chunk is staged; the previous one's data are free
-            if (c0 + CH < n)
-                stage_chunk_async(a, keys, c0 + CH, min((uint32_t)CH, n - c0 - CH), sprimBuf[(it + 1) & 1],
+            if (c0 + CHN < n)
+                stage_chunk_async(a, keys, c0 + CHN, min((uint32_t)CHN, n - c0 - CHN), sprimBuf[(it + 1) & 1],
                                   sphBuf[(it + 1) & 1]);
             pmask[tid] = 0;
             // 1. warp 0 derives the chunk's tile-relative set-up (two
@@ -1383,7 +1386,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                 bool phong = false;
                 ChunkMask blit = 0;
                 uint32_t base = 0;                            // rows of the first half
-                for (int h = 0; h < CH / 32; h++) {
+                for (int h = 0; h < CHN / 32; h++) {
                     const uint32_t k = (uint32_t)(h * 32 + lane);
                     const bool has = k < cn;
                     uint32_t bh = 0, kind = 0;
@@ -1446,9 +1449,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             } else {
                 // 2. coverage: one work item per (sub-triangle, row of its clipped
                 //    box); edge functions stepped along the row
-                const uint32_t nRows = sarea[CH];
+                const uint32_t nRows = sarea[CHN];
                 for (uint32_t t = tid; t < nRows; t += RASTER_THREADS) {
-                    int lo = 0, hi = CH - 1;                          // largest k with sarea[k] <= t
+                    int lo = 0, hi = CHN - 1;                          // largest k with sarea[k] <= t
                     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
                     const ChunkPrim &cp = scp[lo];
                     const uint32_t Y = cp.by0 + (t - sarea[lo]);
@@ -1763,11 +1766,12 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
     RasterArgs a{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
                   L.totalTiles, L.cnt, L.command, L.anyPhong };
     const size_t smem = raster_smem(L.cap);
-    cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    void (*kernel)(RasterArgs) = L.chunk == 64 ? k_raster<64> : k_raster<32>;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const uint32_t per = (uint32_t)(L.rasterCtasPerSM > 0 ? L.rasterCtasPerSM : 4);
     const uint32_t grid = min(L.totalTiles, (uint32_t)pfd_sm_count() * per);
-    return launch_serialized(k_raster, grid, RASTER_THREADS, smem, st, a);
+    return launch_serialized(kernel, grid, RASTER_THREADS, smem, st, a);
 }
 
 cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
