@@ -13,6 +13,10 @@
 
 #include <stdint.h>
 
+/* Records read and written whole by the kernels are 16-byte aligned, so
+ * that copies of them compile to 128-bit loads and stores. */
+#define PF_ALIGN16 __attribute__((aligned(16)))
+
 #define PF_MAX_LIGHTS      8
 #define PF_TILE            16          /* tile edge in pixels (one CTA per tile) */
 #define PF_TILE_PIXELS     (PF_TILE * PF_TILE)
@@ -67,7 +71,7 @@ typedef struct {
 } PFDrawState;
 
 /* Vertex record for immediate mode and for converted vertex arrays. */
-typedef struct {
+typedef struct PF_ALIGN16 {
     float pos[4];
     float normal[3];
     float uv[2];
@@ -124,7 +128,7 @@ typedef struct {
 } PFTarget;                       /* 64 bytes */
 
 /* Transformed vertex. */
-typedef struct {
+typedef struct PF_ALIGN16 {
     float h[4];                   /* clip-space position */
     float uv[2];
     uint32_t col[2];              /* lit colour for PF_FRONT, PF_BACK */
@@ -151,7 +155,7 @@ enum {
 };
 
 /* Set-up sub-triangle, as read by the tile rasterizer. */
-typedef struct {
+typedef struct PF_ALIGN16 {
     int32_t x1, y1, x2, y2;
     int32_t x3, y3, xMin, yMin;
     int32_t xMax, yMax;           /* x in [xMin, xMax), y in [yMin, yMax] */
@@ -179,7 +183,7 @@ enum {
     PFR_TEX_FROM_STATE = 1u << 11
 };
 
-typedef struct {
+typedef struct PF_ALIGN16 {
     float n1[3], n2[3], n3[3];
     float p1[3], p2[3], p3[3];
     float pad[2];
