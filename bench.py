@@ -181,8 +181,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32+u8",
         "data": "synthetic (seeded UV sphere and noise texture)",
-        "config": {"workload": "sphere1080: 1920x1080 textured Gouraud UV sphere 256x128, two draws "
-                               "(opaque + alpha 0.5 scaled 1.05), 1024^2 bilinear repeat texture",
+        "config": {"workload": SPHERE_WORKLOAD,
                    "fragments_per_frame": frags / args.steps,
                    "l2": "flushed between frames (512 MiB write)", "parallelism": "single GPU"},
         "e2e": {"value": frags / wall, "unit": "fragments/s", "ms_per_step": wall * 1e3 / args.steps,
@@ -208,6 +207,10 @@ def run_gpu(args):
     if not args.no_adjoint:
         out["adjoint"] = run_adjoint(args)
     return out
+
+
+SPHERE_WORKLOAD = ("sphere1080: 1920x1080 textured Gouraud UV sphere 256x128, two draws "
+                   "(opaque + alpha 0.5 scaled 1.05), 1024^2 bilinear repeat texture")
 
 
 def run_phong(lib, warmup: int = 2, steps: int = 5) -> dict:
@@ -414,7 +417,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": cb["ms_per_frame"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+u8", "data": "synthetic (seeded UV sphere and noise texture)",
-            "config": {"workload": "sphere1080 (same scene, CPU)"},
+            "config": {"workload": SPHERE_WORKLOAD, "parallelism": "host CPU cores"},
             "cpu_baseline": {k: cb[k] for k in ("kind", "cores", "sample", "value", "unit")},
             "e2e": {"value": cb["value"], "unit": "fragments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
