@@ -27,7 +27,7 @@
  *     (the reference reads past its buffer: its SIMD mirrored and clamped
  *     maps round a coordinate of exactly 1.0 to row h,
  *     src/internal/sampler.h:222-258).
- * Only RGBA / UNSIGNED_BYTE framebuffers and textures are supported.
+ * Framebuffer formats: see fb_format_ok.
  */
 #include "pixelforge.h"
 #include "pfref_internal.h"
@@ -481,6 +481,100 @@ static uint32_t texel_rgba8(const RTex *t, int64_t o)
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* framebuffer formats                                                       */
+/* ------------------------------------------------------------------------ */
+
+static uint32_t pixel_sisd(PFpixelformat f, PFdatatype t, const void *p, size_t o);
+static void pixel_set_sisd(PFpixelformat f, PFdatatype t, void *dst, size_t o, uint32_t col);
+static uint16_t float_to_half(float x);
+
+/* Formats a framebuffer may have.  The reference draws triangles through
+ * the framebuffer format's SIMD getter and setter (triangles.c:378-379,
+ * 525-528) and everything else through the scalar ones.  Refused, because
+ * one pixel's result would depend on other pixels or on its SIMD lane:
+ * single-channel and luminance(-alpha) unsigned byte (their SIMD getters
+ * read the texel three places on, or the next texel, pixel.h:2253-2420),
+ * single-channel and luminance half / float (their SIMD setters rewrite,
+ * requantised, the pixels of the vector that the mask leaves out,
+ * pixel.h:905-970, 1219-1490) and BGRA unsigned byte (lane-dependent
+ * shuffle, pixel.h:2070-2078, 2916-2921). */
+static int fb_format_ok(PFpixelformat f, PFdatatype t)
+{
+    if (!texel_bytes(f, t)) return 0;
+    switch (f) {
+    case PF_RGB: case PF_BGR: case PF_RGBA: return 1;
+    case PF_BGRA: return t != PF_UNSIGNED_BYTE;
+    case PF_LUMINANCE_ALPHA: return t == PF_HALF_FLOAT || t == PF_FLOAT;
+    default: return 0;
+    }
+}
+static inline int fb_rgba8(const RTex *t) { return t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE; }
+
+/* Destination colour as the SIMD getter reads it (blending of triangles). */
+static inline uint32_t fb_get_simd(const RTex *t, size_t o)
+{
+    return fb_rgba8(t) ? ((const uint32_t *)t->pixels)[o] : texel_rgba8(t, (int64_t)o);
+}
+
+/* The SIMD setter writing one unmasked lane (pixel.h:976-1090, 1492-2250):
+ * 8-bit channels to 5/6/4 bits by (c * (2^n - 1)) >> 8, the 1-bit alpha
+ * a > 127, half / float channels c * (1/255) (BGR half / float keep R first,
+ * BGR unsigned byte and BGRA of every type put B first), luminance
+ * (77 r + 150 g + 29 b) >> 8 (color.h:206-240). */
+static void fb_set_simd(RTex *t, size_t o, uint32_t col)
+{
+    if (fb_rgba8(t)) { ((uint32_t *)t->pixels)[o] = col; return; }
+    const uint32_t r = col & 255u, g = (col >> 8) & 255u, b = (col >> 16) & 255u, a = col >> 24;
+    uint8_t *p8 = (uint8_t *)t->pixels;
+    uint16_t *p16 = (uint16_t *)t->pixels;
+    float *pf = (float *)t->pixels;
+    const PFpixelformat f = t->format;
+    const int bFirst = f == PF_BGRA || (f == PF_BGR && (t->type == PF_UNSIGNED_BYTE ||
+                                                        t->type == PF_UNSIGNED_SHORT_5_6_5));
+    const uint32_t c0 = bFirst ? b : r, c2 = bFirst ? r : b;
+    switch (t->type) {
+    case PF_UNSIGNED_SHORT_5_6_5:
+        p16[o] = (uint16_t)(((c0 * 31u) >> 8) << 11 | ((g * 63u) >> 8) << 5 | ((c2 * 31u) >> 8));
+        return;
+    case PF_UNSIGNED_SHORT_5_5_5_1:
+        p16[o] = (uint16_t)(((c0 * 31u) >> 8) << 11 | ((g * 31u) >> 8) << 6 | ((c2 * 31u) >> 8) << 1 | (a > 127u ? 1u : 0u));
+        return;
+    case PF_UNSIGNED_SHORT_4_4_4_4:
+        p16[o] = (uint16_t)(((c0 * 15u) >> 8) << 12 | ((g * 15u) >> 8) << 8 | ((c2 * 15u) >> 8) << 4 | ((a * 15u) >> 8));
+        return;
+    case PF_UNSIGNED_BYTE:                                  /* RGB, BGR */
+        p8[3 * o] = (uint8_t)c0; p8[3 * o + 1] = (uint8_t)g; p8[3 * o + 2] = (uint8_t)c2;
+        return;
+    default: break;
+    }
+    float n[4];
+    int k;
+    if (f == PF_LUMINANCE_ALPHA) {
+        const uint32_t gray = (b * 29u + g * 150u + r * 77u) >> 8;
+        n[0] = (float)(gray & 255u) * INV255; n[1] = (float)a * INV255; k = 2;
+    } else {
+        n[0] = (float)c0 * INV255; n[1] = (float)g * INV255; n[2] = (float)c2 * INV255; n[3] = (float)a * INV255;
+        k = (f == PF_RGB || f == PF_BGR) ? 3 : 4;
+    }
+    for (int i = 0; i < k; i++) {
+        if (t->type == PF_HALF_FLOAT) p16[(size_t)k * o + (size_t)i] = float_to_half(n[i]);
+        else pf[(size_t)k * o + (size_t)i] = n[i];
+    }
+}
+
+/* The scalar getter and setter (points, lines, rectangles, pixel
+ * transfers, fog, post-processing, the framebuffer functions). */
+static inline uint32_t fb_get(const RTex *t, size_t o)
+{
+    return fb_rgba8(t) ? ((const uint32_t *)t->pixels)[o] : pixel_sisd(t->format, t->type, t->pixels, o);
+}
+static inline void fb_set(RTex *t, size_t o, uint32_t col)
+{
+    if (fb_rgba8(t)) ((uint32_t *)t->pixels)[o] = col;
+    else pixel_set_sisd(t->format, t->type, t->pixels, o, col);
+}
+
 static uint32_t tex_fetch(const RTex *t, int32_t x, int32_t y)
 {
     int64_t off = (int64_t)(int32_t)((uint32_t)y * t->w + (uint32_t)x);
@@ -699,7 +793,6 @@ static void raster_tri(RCtx *c, PFface face, int is3D, const RVert *v1, const RV
     const float z1 = v1->homogeneous[2], z2 = v2->homogeneous[2], z3 = v3->homogeneous[2];
 
     RTex *fbt = (RTex *)c->current->texture;
-    uint32_t *pb = (uint32_t *)fbt->pixels;
     float *zb = c->current->zbuffer;
     const uint32_t W = fbt->w, H = fbt->h;
 
@@ -761,8 +854,8 @@ static void raster_tri(RCtx *c, PFface face, int is3D, const RVert *v1, const RV
                 }
                 frag = light_phong(c, frag, fm, viewPos, P, N);
             }
-            if (blending) frag = blend_simd(c->blend, frag, pb[p]);
-            pb[p] = frag;
+            if (blending) frag = blend_simd(c->blend, frag, fb_get_simd(fbt, p));
+            fb_set_simd(fbt, p, frag);
             if (c->depthMask) zb[p] = z;
         }
     }
@@ -974,12 +1067,11 @@ static void lp_pixel(RCtx *c, int32_t x, int32_t y, float z, uint32_t col, int t
     RTex *fbt = (RTex *)c->current->texture;
     if (x < 0 || y < 0 || (uint32_t)x >= fbt->w || (uint32_t)y >= fbt->h) return;
     const size_t p = (size_t)y * fbt->w + (size_t)x;
-    uint32_t *pb = (uint32_t *)fbt->pixels;
     float *zb = c->current->zbuffer;
     c->stats.fragments++;
     if (test && !depth_sisd(c->depthFunc, z, zb[p])) return;
-    if (c->state & PF_BLEND) col = blend_sisd(c->blend, col, pb[p]);
-    pb[p] = col;
+    if (c->state & PF_BLEND) col = blend_sisd(c->blend, col, fb_get(fbt, p));
+    fb_set(fbt, p, col);
     if (c->depthMask) zb[p] = z;
 }
 
@@ -1270,11 +1362,11 @@ static void update_matrices(RCtx *c, int withNormal)   /* context.c:96-111 */
 
 static int texel_bytes(PFpixelformat f, PFdatatype t);
 
-/* Framebuffers are RGBA / unsigned byte; textures may use any format the
- * reference has a SIMD getter for. */
+/* Textures may use any format the reference has a SIMD getter for,
+ * framebuffers the formats fb_format_ok accepts. */
 static RTex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, int sampled)
 {
-    if (sampled ? !texel_bytes(f, t) : !(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) {
+    if (sampled ? !texel_bytes(f, t) : !fb_format_ok(f, t)) {
         if (G) G->err = PF_INVALID_ENUM;
         return NULL;
     }
@@ -1590,10 +1682,18 @@ void pfClear(PFclearflag flag)
     RTex *t = (RTex *)G->current->texture;
     size_t size = (size_t)t->w * t->h;
     size_t aligned = size - (size % 8);
-    uint32_t *pb = (uint32_t *)t->pixels; float *zb = G->current->zbuffer;
-    uint32_t cc = col_pack(G->clearColor);
-    for (size_t i = 8; i < aligned; i++) { pb[i] = cc; zb[i] = G->clearDepth; }
-    for (size_t i = aligned; i < size; i++) { pb[i] = pb[0]; zb[i] = zb[0]; }
+    float *zb = G->current->zbuffer;
+    const uint32_t cc = col_pack(G->clearColor);
+    const size_t bpp = (size_t)texel_bytes(t->format, t->type);
+    uint8_t *pb = (uint8_t *)t->pixels;
+    /* The tail copy steps by pfiGetPixelBytes (pixel.h:3156-3210), components
+     * x type size: 6 or 8 bytes for the packed 16-bit types, whose pixels
+     * are 2 bytes, so that there it writes past the pixels (outside the
+     * buffer) and the tail pixels keep their values. */
+    const int packed = t->type == PF_UNSIGNED_SHORT_5_6_5 || t->type == PF_UNSIGNED_SHORT_5_5_5_1 ||
+                       t->type == PF_UNSIGNED_SHORT_4_4_4_4;
+    for (size_t i = 8; i < aligned; i++) { fb_set_simd(t, i, cc); zb[i] = G->clearDepth; }
+    for (size_t i = aligned; i < size; i++) { if (!packed) memcpy(pb + i * bpp, pb, bpp); zb[i] = zb[0]; }
 }
 void pfClearDepth(PFfloat d) { G->clearDepth = d; }
 void pfClearColor(PFubyte r, PFubyte g, PFubyte b, PFubyte a) { PFcolor c = { r, g, b, a }; G->clearColor = c; }
@@ -1884,7 +1984,7 @@ static void put_pixel(RCtx *c, int64_t x, int64_t y, uint32_t col)
 {
     RTex *fbt = (RTex *)c->current->texture;
     if (x < 0 || y < 0 || x >= (int64_t)fbt->w || y >= (int64_t)fbt->h) return;
-    ((uint32_t *)fbt->pixels)[(size_t)y * fbt->w + (size_t)x] = col;
+    fb_set(fbt, (size_t)y * fbt->w + (size_t)x, col);
 }
 
 /* pfRectf (context.c:1936-1981): the two corners through the MVP to screen
@@ -2005,7 +2105,6 @@ void pfDrawPixels(PFsizei width, PFsizei height, PFpixelformat format, PFdatatyp
     const uint32_t widthM1 = width - 1, heightM1 = height - 1;
     RTex *dst = (RTex *)c->current->texture;
     float *zb = c->current->zbuffer;
-    uint32_t *pb = (uint32_t *)dst->pixels;
     const int test = (c->state & PF_DEPTH_TEST) != 0;
     const size_t nSrc = (size_t)width * height;
     for (int64_t y = yMin; y <= yMax; y++) {
@@ -2019,8 +2118,8 @@ void pfDrawPixels(PFsizei width, PFsizei height, PFpixelformat format, PFdatatyp
             const uint32_t src = ySrc + ox_ftou32(u * (float)widthM1);
             if (c->depthMask) zb[p] = zPos;
             uint32_t col = src < nSrc ? pixel_sisd(format, type, pixels, src) : 0u;
-            if (c->state & PF_BLEND) col = blend_sisd(c->blend, col, pb[p]);
-            pb[p] = col;
+            if (c->state & PF_BLEND) col = blend_sisd(c->blend, col, fb_get(dst, p));
+            fb_set(dst, p, col);
         }
     }
 }
@@ -2099,7 +2198,6 @@ void pfFogProcess(void)
 {
     RCtx *c = G;
     RTex *t = (RTex *)c->current->texture;
-    uint32_t *pb = (uint32_t *)t->pixels;
     const float *zb = c->current->zbuffer;
     const float density = c->fog.density, start = c->fog.start, end = c->fog.end;
     const float invLen = 1 / (end - start);
@@ -2108,7 +2206,7 @@ void pfFogProcess(void)
         const float depth = zb[o];
         if (depth >= end) {
             const uint32_t f = fc | alpha << 24;
-            pb[o] = alpha == 255 ? f : blend_alpha_sisd(f, pb[o]);
+            fb_set(t, o, alpha == 255 ? f : blend_alpha_sisd(f, fb_get(t, o)));
         } else if (depth > start) {
             float tt = 0;
             switch (c->fog.mode) {
@@ -2118,7 +2216,7 @@ void pfFogProcess(void)
             default: break;
             }
             const uint32_t a = ox_ftoub(tt * (float)alpha);
-            pb[o] = blend_alpha_sisd(fc | a << 24, pb[o]);
+            fb_set(t, o, blend_alpha_sisd(fc | a << 24, fb_get(t, o)));
         }
     }
 }
@@ -2314,20 +2412,19 @@ void pfReadPixels(PFint x, PFint y, PFsizei w, PFsizei h, PFpixelformat f, PFdat
 #define CLAMPR(v, lo, hi) ((v) < (lo) ? (lo) : ((v) > (hi) ? (hi) : (v)))
     PFint xMin = CLAMPR(x, 0, (PFint)s->w - 1), yMin = CLAMPR(y, 0, (PFint)s->h - 1);
     PFint xMax = CLAMPR(x + (PFint)w, 0, (PFint)s->w), yMax = CLAMPR(y + (PFint)h, 0, (PFint)s->h);
-    const uint32_t *src = (const uint32_t *)s->pixels;
     for (PFint yy = yMin; yy < yMax; yy++)
         for (PFint xx = xMin; xx < xMax; xx++)
-            pixel_set_sisd(f, t, pixels, (size_t)(yy - yMin) * w + (size_t)(xx - xMin), src[(size_t)yy * s->w + (size_t)xx]);
+            pixel_set_sisd(f, t, pixels, (size_t)(yy - yMin) * w + (size_t)(xx - xMin), fb_get(s, (size_t)yy * s->w + (size_t)xx));
 }
 
 void pfPostProcess(PFpostprocessfunc fn)   /* context.c:2397-2441 */
 {
     RTex *t = (RTex *)G->current->texture;
-    uint32_t *pb = (uint32_t *)t->pixels; const float *zb = G->current->zbuffer;
+    const float *zb = G->current->zbuffer;
     for (PFint y = 0; y < (PFint)t->h; y++)
         for (PFint x = 0; x < (PFint)t->w; x++) {
             size_t o = (size_t)y * t->w + (size_t)x;
-            pb[o] = col_pack(fn(x, y, zb[o], col_unpack(pb[o])));
+            fb_set(t, o, col_pack(fn(x, y, zb[o], col_unpack(fb_get(t, o)))));
         }
 }
 
@@ -2379,8 +2476,8 @@ void pfEnableTiming(PFboolean enable) { (void)enable; }
 PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
 {
     PFframebuffer fb = { NULL, NULL };
-    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { if (G) G->err = PF_INVALID_ENUM; return fb; }
-    void *px = calloc((size_t)w * h, 4);
+    if (!fb_format_ok(f, t)) { if (G) G->err = PF_INVALID_ENUM; return fb; }
+    void *px = calloc((size_t)w * h, (size_t)texel_bytes(f, t));
     fb.texture = tex_new(px, w, h, f, t, 0);
     fb.zbuffer = (float *)malloc((size_t)w * h * sizeof(float));
     for (size_t i = 0; i < (size_t)w * h; i++) fb.zbuffer[i] = FLT_MAX;
@@ -2401,12 +2498,12 @@ void pfClearFramebuffer(PFframebuffer *fb, PFcolor col, PFfloat d)
 {
     RTex *t = (RTex *)fb->texture;
     uint32_t cc = col_pack(col);
-    for (size_t i = 0; i < (size_t)t->w * t->h; i++) { ((uint32_t *)t->pixels)[i] = cc; fb->zbuffer[i] = d; }
+    for (size_t i = 0; i < (size_t)t->w * t->h; i++) { fb_set(t, i, cc); fb->zbuffer[i] = d; }
 }
 PFcolor pfGetFramebufferPixel(const PFframebuffer *fb, PFsizei x, PFsizei y)
 {
     const RTex *t = (const RTex *)fb->texture;
-    return col_unpack(((const uint32_t *)t->pixels)[(size_t)y * t->w + x]);
+    return col_unpack(fb_get(t, (size_t)y * t->w + x));
 }
 PFfloat pfGetFramebufferDepth(const PFframebuffer *fb, PFsizei x, PFsizei y)
 {
@@ -2426,17 +2523,17 @@ void pfSetFramebufferPixelDepthTest(PFframebuffer *fb, PFsizei x, PFsizei y, PFf
     case PF_GREATER: pass = z > fb->zbuffer[o]; break;
     default: pass = z >= fb->zbuffer[o]; break;
     }
-    if (pass) { ((uint32_t *)t->pixels)[o] = col_pack(col); fb->zbuffer[o] = z; }
+    if (pass) { fb_set(t, o, col_pack(col)); fb->zbuffer[o] = z; }
 }
 void pfSetFramebufferPixelDepth(PFframebuffer *fb, PFsizei x, PFsizei y, PFfloat z, PFcolor col)
 {
     RTex *t = (RTex *)fb->texture; size_t o = (size_t)y * t->w + x;
-    ((uint32_t *)t->pixels)[o] = col_pack(col); fb->zbuffer[o] = z;
+    fb_set(t, o, col_pack(col)); fb->zbuffer[o] = z;
 }
 void pfSetFramebufferPixel(PFframebuffer *fb, PFsizei x, PFsizei y, PFcolor col)
 {
     RTex *t = (RTex *)fb->texture;
-    ((uint32_t *)t->pixels)[(size_t)y * t->w + x] = col_pack(col);
+    fb_set(t, (size_t)y * t->w + x, col_pack(col));
 }
 
 PFtexture pfGenTexture(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t) { return tex_new(pixels, w, h, f, t, 1); }

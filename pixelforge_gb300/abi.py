@@ -71,7 +71,17 @@ PF_EMISSION, PF_SHININESS = 5, 6
 PF_POSITION, PF_SPOT_DIRECTION = 7, 8
 PF_SPOT_INNER_CUTOFF, PF_SPOT_OUTER_CUTOFF = 10, 11
 PF_CONSTANT_ATTENUATION, PF_LINEAR_ATTENUATION, PF_QUADRATIC_ATTENUATION = 12, 13, 14
-PF_RGBA = 7
+(PF_RED, PF_GREEN, PF_BLUE, PF_ALPHA, PF_LUMINANCE, PF_LUMINANCE_ALPHA, PF_RGB, PF_RGBA,
+ PF_BGR, PF_BGRA) = range(10)
+PF_UNSIGNED_SHORT_5_6_5, PF_UNSIGNED_SHORT_5_5_5_1, PF_UNSIGNED_SHORT_4_4_4_4 = 2, 3, 4
+
+
+def pixel_bytes(fmt: int, typ: int) -> int:
+    """Bytes of one pixel of a format / type pair (0: no such pixel)."""
+    comps = [1, 1, 1, 1, 1, 2, 3, 4, 3, 4][fmt] if 0 <= fmt < 10 else 0
+    if typ in (PF_UNSIGNED_SHORT_5_6_5, PF_UNSIGNED_SHORT_5_5_5_1, PF_UNSIGNED_SHORT_4_4_4_4):
+        return 2
+    return comps * {PF_UNSIGNED_BYTE: 1, PF_HALF_FLOAT: 2, PF_FLOAT: 4}.get(typ, 0)
 (PF_VIEWPORT, PF_COLOR_CLEAR_VALUE, PF_DEPTH_CLEAR_VALUE, PF_CULL_FACE_MODE, PF_CURRENT_COLOR,
  PF_CURRENT_NORMAL, PF_CURRENT_TEXTURE_COORDS, PF_CURRENT_RASTER_POSITION, PF_BLEND_FUNC, PF_DEPTH_FUNC,
  PF_POLYGON_MODE, PF_POINT_SIZE, PF_LINE_WIDTH, PF_MATRIX_MODE, PF_PROJECTION_MATRIX, PF_MODELVIEW_MATRIX,

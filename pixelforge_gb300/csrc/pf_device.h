@@ -43,6 +43,7 @@ struct PFBatchLaunch {
     int rasterCtasPerSM;      /* persistent raster grid: SMs x this */
     int chunk;                /* records per raster chunk: 64, or 32 (the default) */
     int anyPhong;             /* some state of the launch lights per fragment */
+    int generic;              /* some target is not RGBA / unsigned byte (32-record chunks) */
     PFDevCounters *cnt;
     uint32_t command;
 };
@@ -55,9 +56,11 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);
 /* Number of SMs of the current device (cached). */
 int pfd_sm_count(void);
-cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
+/* pfClear (all = false) or pfClearFramebuffer (all = true) of a framebuffer
+ * of format fmt (PFF_*); cc is the clear colour as stored. */
+cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,
                              const PFDevCounters *cnt, uint32_t command, cudaStream_t st);
-cudaError_t pfd_launch_hook(uint32_t *color, const float *depth, size_t n, int hook, const PFHookParams &hp,
+cudaError_t pfd_launch_hook(void *color, uint32_t fmt, const float *depth, size_t n, int hook, const PFHookParams &hp,
                             const PFDevCounters *cnt, uint32_t command, cudaStream_t st);
 
 #endif /* PF_DEVICE_H */

@@ -35,6 +35,7 @@
 #include "pixelforge.h"
 #include "pf_layout.h"
 #include "pf_device.h"
+#include "pf_pixfmt.h"
 
 namespace {
 
@@ -146,7 +147,9 @@ struct FBMirror {
     Tex *tex = nullptr;
     float *hostDepth = nullptr;
     bool depthUserVisible = false;     // pfGenFramebuffer: zbuffer is a public host pointer
-    uint32_t *dColor = nullptr;
+    void *dColor = nullptr;            // pixels of format fmt
+    uint32_t fmt = PFF_RGBA8;
+    size_t bpp = 4;
     float *dDepth = nullptr;
     size_t w = 0, h = 0;
     bool depthOnDevice = false;        // device depth already holds the authoritative copy
@@ -164,6 +167,15 @@ struct Cmd {
     PFHookParams hp;
     int segBegin, segEnd;              // CMD_DRAW: segments [segBegin, segEnd)
 };
+
+// The clear colour of a CMD_CLEAR (pfClear: the SIMD setter,
+// context.c:700-710) or CMD_FILL (pfClearFramebuffer: the scalar setter,
+// framebuffer.c:89-102) as a framebuffer of format fmt stores it.
+void clear_raw(uint32_t fmt, const Cmd &cmd, uint32_t raw[4])
+{
+    if (cmd.kind == CMD_FILL) pff_set_sisd(fmt, cmd.color, raw);
+    else pff_set_simd(fmt, cmd.color, raw);
+}
 
 // Segment as recorded on the host: references instead of pointers.  A
 // reference is -1 (none), an offset >= 0 into the staging block, or the
@@ -268,8 +280,8 @@ struct Renderer {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> rasterEv;   // per raster launch, reused
 
     // the device work of the last successful flush, for graph replay
-    struct Op { int kind; int cmd; PFBatchLaunch L; size_t n; uint32_t *color; float *depth;
-                uint32_t cc; float cd; bool all; int hook; PFHookParams hp; };
+    struct Op { int kind; int cmd; PFBatchLaunch L; size_t n; void *color; uint32_t fmt; float *depth;
+                uint32_t cc[4]; float cd; bool all; int hook; PFHookParams hp; };
     std::vector<Op> lastOps;
     std::vector<void *> splitMem;        // device segments/targets of draw groups split by the last flush
     cudaGraphExec_t graph = nullptr;
@@ -472,11 +484,49 @@ uint32_t texel_rgba8(PFpixelformat f, PFdatatype t, const TexelSrc &s, int64_t o
     }
 }
 
-// Framebuffers are RGBA / unsigned byte; textures may use any format the
-// reference has a SIMD getter for.
+// The PFF_* code of a framebuffer format, -1 for the formats a framebuffer
+// may not have: those for which one pixel's result would depend on other
+// pixels or on its SIMD lane in the reference -- single-channel and
+// luminance(-alpha) unsigned byte (their SIMD getters read the texel three
+// places on, or the next texel, src/internal/pixel.h:2253-2420),
+// single-channel and luminance half / float (their SIMD setters rewrite,
+// requantised, the pixels of the vector that the mask leaves out,
+// pixel.h:905-970, 1219-1490) and BGRA unsigned byte (lane-dependent
+// shuffle, pixel.h:2070-2078, 2916-2921).
+int fb_code(PFpixelformat f, PFdatatype t)
+{
+    switch (t) {
+    case PF_UNSIGNED_BYTE: return f == PF_RGBA ? PFF_RGBA8 : f == PF_RGB ? PFF_RGB8 : f == PF_BGR ? PFF_BGR8 : -1;
+    case PF_UNSIGNED_SHORT_5_6_5: return f == PF_RGB ? PFF_RGB565 : f == PF_BGR ? PFF_BGR565 : -1;
+    case PF_UNSIGNED_SHORT_5_5_5_1: return f == PF_RGBA ? PFF_RGBA5551 : f == PF_BGRA ? PFF_BGRA5551 : -1;
+    case PF_UNSIGNED_SHORT_4_4_4_4: return f == PF_RGBA ? PFF_RGBA4444 : f == PF_BGRA ? PFF_BGRA4444 : -1;
+    case PF_HALF_FLOAT:
+        switch (f) {
+        case PF_LUMINANCE_ALPHA: return PFF_LA16F;
+        case PF_RGB: return PFF_RGB16F;
+        case PF_BGR: return PFF_BGR16F;
+        case PF_RGBA: return PFF_RGBA16F;
+        case PF_BGRA: return PFF_BGRA16F;
+        default: return -1;
+        }
+    case PF_FLOAT:
+        switch (f) {
+        case PF_LUMINANCE_ALPHA: return PFF_LA32F;
+        case PF_RGB: return PFF_RGB32F;
+        case PF_BGR: return PFF_BGR32F;
+        case PF_RGBA: return PFF_RGBA32F;
+        case PF_BGRA: return PFF_BGRA32F;
+        default: return -1;
+        }
+    default: return -1;
+    }
+}
+
+// Textures may use any format the reference has a SIMD getter for,
+// framebuffers the formats fb_code accepts.
 Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, bool sampled)
 {
-    if (sampled ? !texel_bytes(f, t) : !(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { set_err(PF_INVALID_ENUM); return nullptr; }
+    if (sampled ? !texel_bytes(f, t) : fb_code(f, t) < 0) { set_err(PF_INVALID_ENUM); return nullptr; }
     Tex *x = new Tex();
     x->pixels = pixels; x->w = w; x->h = h; x->format = f; x->type = t;
     x->tx = 1.0f / (float)w; x->ty = 1.0f / (float)h;
@@ -1240,13 +1290,17 @@ FBMirror *mirror_for(Renderer *r, PFframebuffer *fb)
     Tex *t = (Tex *)fb->texture;
     FBMirror &m = gMirrors[t];
     const size_t w = t->w, h = t->h;
-    if (m.dColor && (m.w != w || m.h != h)) { cudaFree(m.dColor); cudaFree(m.dDepth); m.dColor = nullptr; m.dDepth = nullptr; }
+    const uint32_t fmt = (uint32_t)fb_code(t->format, t->type);
+    const size_t bpp = (size_t)pff_bytes(fmt);
+    if (m.dColor && (m.w != w || m.h != h || m.fmt != fmt)) {
+        cudaFree(m.dColor); cudaFree(m.dDepth); m.dColor = nullptr; m.dDepth = nullptr;
+    }
     if (!m.dColor) {
-        if (cudaMalloc((void **)&m.dColor, w * h * 4) != cudaSuccess ||
+        if (cudaMalloc(&m.dColor, w * h * bpp) != cudaSuccess ||
             cudaMalloc((void **)&m.dDepth, w * h * 4) != cudaSuccess) {
             cudaGetLastError(); r->devStatus |= PF_DEVICE_ALLOC_FAIL; return nullptr;
         }
-        m.w = w; m.h = h; m.depthOnDevice = false;
+        m.w = w; m.h = h; m.fmt = fmt; m.bpp = bpp; m.depthOnDevice = false;
     }
     m.tex = t;
     m.hostDepth = fb->zbuffer;
@@ -1254,7 +1308,7 @@ FBMirror *mirror_for(Renderer *r, PFframebuffer *fb)
     if (m.registered != t->pixels && !t->ownsPinned) {
         if (m.registered) cudaHostUnregister(m.registered);
         m.registered = nullptr;
-        if (cudaHostRegister(t->pixels, w * h * 4, cudaHostRegisterDefault) == cudaSuccess) m.registered = t->pixels;
+        if (cudaHostRegister(t->pixels, w * h * bpp, cudaHostRegisterDefault) == cudaSuccess) m.registered = t->pixels;
         else cudaGetLastError();
     }
     return &m;
@@ -1463,14 +1517,16 @@ bool flush(Renderer *r)
             FBMirror *m = mirrorOf(o.targets[k]);
             PFTarget &T = htg[tgCursor + k];
             std::memset(&T, 0, sizeof T);
-            T.color = m->dColor; T.depth = m->dDepth;
+            T.color = m->dColor; T.depth = m->dDepth; T.fmt = m->fmt;
+            if (m->fmt != PFF_RGBA8) L.generic = 1;
             T.W = (uint32_t)m->w; T.H = (uint32_t)m->h;
             T.tilesX = (T.W + PF_TILE - 1) / PF_TILE; T.tilesY = (T.H + PF_TILE - 1) / PF_TILE;
             T.tileBase = tiles;
             tiles += T.tilesX * T.tilesY;
             if (o.clearCmd[k] >= 0) {
                 const Cmd &cl = cmds[o.clearCmd[k]];
-                T.clearMode = (cl.kind == CMD_FILL) ? 2 : 1; T.clearColor = cl.color; T.clearDepth = cl.depth;
+                T.clearMode = (cl.kind == CMD_FILL) ? 2 : 1; T.clearDepth = cl.depth;
+                clear_raw(m->fmt, cl, T.clearRaw);
             }
         }
         L.segs = (const PFSegment *)(dbase + segsOff) + o.segBegin;
@@ -1505,10 +1561,10 @@ bool flush(Renderer *r)
         } else if (first->kind == CMD_CLEAR) {
             // the clear leaves pixels 0..7 (and reads pixel 0 for the tail)
             const size_t k = std::min<size_t>(8, n);
-            cudaMemcpyAsync(m->dColor, m->tex->pixels, k * 4, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(m->dColor, m->tex->pixels, k * m->bpp, cudaMemcpyHostToDevice, st);
             if (uploadDepth) cudaMemcpyAsync(m->dDepth, m->hostDepth, k * 4, cudaMemcpyHostToDevice, st);
         } else {
-            cudaMemcpyAsync(m->dColor, m->tex->pixels, n * 4, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(m->dColor, m->tex->pixels, n * m->bpp, cudaMemcpyHostToDevice, st);
             if (uploadDepth) cudaMemcpyAsync(m->dDepth, m->hostDepth, n * 4, cudaMemcpyHostToDevice, st);
         }
         m->depthOnDevice = true;
@@ -1613,11 +1669,12 @@ bool flush(Renderer *r)
             if (o.kind == 1 || o.kind == 2) {
                 const Cmd &cmd = cmds[o.cmd];
                 FBMirror *m = mirrorOf(cmd.fb);
-                rop.n = m->w * m->h; rop.color = m->dColor; rop.depth = m->dDepth;
-                rop.cc = cmd.color; rop.cd = cmd.depth; rop.all = cmd.kind == CMD_FILL; rop.hook = cmd.hook; rop.hp = cmd.hp;
+                rop.n = m->w * m->h; rop.color = m->dColor; rop.fmt = m->fmt; rop.depth = m->dDepth;
+                clear_raw(m->fmt, cmd, rop.cc);
+                rop.cd = cmd.depth; rop.all = cmd.kind == CMD_FILL; rop.hook = cmd.hook; rop.hp = cmd.hp;
                 r->stats.kernel_launches += 1;
-                e = (o.kind == 1) ? pfd_launch_clear(rop.color, rop.depth, rop.n, rop.cc, rop.cd, rop.all, dcnt, (uint32_t)oi, st)
-                                  : pfd_launch_hook(rop.color, rop.depth, rop.n, rop.hook, rop.hp, dcnt, (uint32_t)oi, st);
+                e = (o.kind == 1) ? pfd_launch_clear(rop.color, rop.fmt, rop.depth, rop.n, rop.cc, rop.cd, rop.all, dcnt, (uint32_t)oi, st)
+                                  : pfd_launch_hook(rop.color, rop.fmt, rop.depth, rop.n, rop.hook, rop.hp, dcnt, (uint32_t)oi, st);
             } else {
                 PFBatchLaunch L = launches[oi];
                 L.vout = (PFVertexOut *)r->vout.p;
@@ -1658,7 +1715,7 @@ bool flush(Renderer *r)
         for (FBMirror *m : mirrors) {
             if (e != cudaSuccess) break;
             const size_t n = m->w * m->h;
-            e = cudaMemcpyAsync(m->tex->pixels, m->dColor, n * 4, cudaMemcpyDeviceToHost, st);
+            e = cudaMemcpyAsync(m->tex->pixels, m->dColor, n * m->bpp, cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess && m->depthUserVisible)
                 e = cudaMemcpyAsync(m->hostDepth, m->dDepth, n * 4, cudaMemcpyDeviceToHost, st);
         }
@@ -1740,8 +1797,8 @@ float replay(Renderer *r, uint32_t n)
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return -1.0f; }
         cudaMemcpyAsync(dcnt, r->hostCounters, sizeof(PFDevCounters), cudaMemcpyHostToDevice, st);
         for (const auto &op : r->lastOps) {
-            if (op.kind == 1) pfd_launch_clear(op.color, op.depth, op.n, op.cc, op.cd, op.all, dcnt, (uint32_t)op.cmd, st);
-            else if (op.kind == 2) pfd_launch_hook(op.color, op.depth, op.n, op.hook, op.hp, dcnt, (uint32_t)op.cmd, st);
+            if (op.kind == 1) pfd_launch_clear(op.color, op.fmt, op.depth, op.n, op.cc, op.cd, op.all, dcnt, (uint32_t)op.cmd, st);
+            else if (op.kind == 2) pfd_launch_hook(op.color, op.fmt, op.depth, op.n, op.hook, op.hp, dcnt, (uint32_t)op.cmd, st);
             else {
                 pfd_launch_vertex(op.L, st);
                 pfd_launch_items(op.L, st);
@@ -2858,6 +2915,23 @@ static void pixel_set_sisd(PFpixelformat f, PFdatatype t, void *dst, size_t o, u
 }
 #undef FTOUB
 
+// A framebuffer's scalar getter and setter for pixel o (host side: the
+// framebuffer functions, pfReadPixels, host post-processing).
+static uint32_t fb_get(const Tex *t, size_t o)
+{
+    uint32_t raw[4];
+    const uint32_t f = (uint32_t)fb_code(t->format, t->type);
+    pff_load(f, t->pixels, o, raw);
+    return pff_get_sisd(f, raw);
+}
+static void fb_set(Tex *t, size_t o, uint32_t col)
+{
+    uint32_t raw[4];
+    const uint32_t f = (uint32_t)fb_code(t->format, t->type);
+    pff_set_sisd(f, col, raw);
+    pff_store(f, t->pixels, o, raw);
+}
+
 void pfReadPixels(PFint x, PFint y, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, void *pixels)
 {                                                                    // context.c:2353-2395
     if (!(f >= PF_RED && f <= PF_BGRA && t >= PF_UNSIGNED_BYTE && t <= PF_DOUBLE)) { G->err = PF_INVALID_ENUM; return; }
@@ -2867,17 +2941,16 @@ void pfReadPixels(PFint x, PFint y, PFsizei w, PFsizei h, PFpixelformat f, PFdat
     auto cl = [](PFint v, PFint lo, PFint hi) { return v < lo ? lo : (v > hi ? hi : v); };
     PFint xMin = cl(x, 0, (PFint)s->w - 1), yMin = cl(y, 0, (PFint)s->h - 1);
     PFint xMax = cl(x + (PFint)w, 0, (PFint)s->w), yMax = cl(y + (PFint)h, 0, (PFint)s->h);
-    const uint32_t *src = (const uint32_t *)s->pixels;
     if (f == PF_RGBA && t == PF_UNSIGNED_BYTE) {
         uint32_t *dst = (uint32_t *)pixels;
         for (PFint yy = yMin; yy < yMax; yy++)
             for (PFint xx = xMin; xx < xMax; xx++)
-                dst[(size_t)(yy - yMin) * w + (size_t)(xx - xMin)] = src[(size_t)yy * s->w + (size_t)xx];
+                dst[(size_t)(yy - yMin) * w + (size_t)(xx - xMin)] = fb_get(s, (size_t)yy * s->w + (size_t)xx);
         return;
     }
     for (PFint yy = yMin; yy < yMax; yy++)
         for (PFint xx = xMin; xx < xMax; xx++)
-            pixel_set_sisd(f, t, pixels, (size_t)(yy - yMin) * w + (size_t)(xx - xMin), src[(size_t)yy * s->w + (size_t)xx]);
+            pixel_set_sisd(f, t, pixels, (size_t)(yy - yMin) * w + (size_t)(xx - xMin), fb_get(s, (size_t)yy * s->w + (size_t)xx));
 }
 
 void pfPostProcess(PFpostprocessfunc fn)                             // context.c:2397-2441
@@ -2885,12 +2958,11 @@ void pfPostProcess(PFpostprocessfunc fn)                             // context.
     sync_host(G);
     if (G->current == &G->mainFB) pull_main_depth(G);
     Tex *t = (Tex *)G->current->texture;
-    uint32_t *pb = (uint32_t *)t->pixels;
     const float *zb = G->current->zbuffer;
     for (PFint y = 0; y < (PFint)t->h; y++)
         for (PFint x = 0; x < (PFint)t->w; x++) {
             size_t o = (size_t)y * t->w + (size_t)x;
-            pb[o] = pack(fn(x, y, zb[o], unpack(pb[o])));
+            fb_set(t, o, pack(fn(x, y, zb[o], unpack(fb_get(t, o)))));
         }
 }
 
@@ -2977,13 +3049,14 @@ PFuint pfGetDeviceStatus(void) { return G ? G->own.devStatus : 0; }
 PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
 {
     PFframebuffer fb{ nullptr, nullptr };
-    if (!(f == PF_RGBA && t == PF_UNSIGNED_BYTE)) { set_err(PF_INVALID_ENUM); return fb; }
-    const size_t n = (size_t)w * h;
+    const int code = fb_code(f, t);
+    if (code < 0) { set_err(PF_INVALID_ENUM); return fb; }
+    const size_t n = (size_t)w * h, bytes = n * (size_t)pff_bytes((uint32_t)code);
     void *px = nullptr;
-    bool pinned = cudaMallocHost(&px, n * 4) == cudaSuccess;
-    if (!pinned) { cudaGetLastError(); px = std::malloc(n * 4); }
+    bool pinned = cudaMallocHost(&px, bytes) == cudaSuccess;
+    if (!pinned) { cudaGetLastError(); px = std::malloc(bytes); }
     if (!px) { set_err(PF_ERROR_OUT_OF_MEMORY); return fb; }
-    std::memset(px, 0, n * 4);
+    std::memset(px, 0, bytes);
     Tex *tx = tex_new(px, w, h, f, t, false);
     tx->ownsPinned = pinned;
     float *z = nullptr;
@@ -3025,7 +3098,7 @@ PFcolor pfGetFramebufferPixel(const PFframebuffer *fb, PFsizei x, PFsizei y)
 {
     if (G) sync_host(G);
     const Tex *t = (const Tex *)fb->texture;
-    return unpack(((const uint32_t *)t->pixels)[(size_t)y * t->w + x]);
+    return unpack(fb_get(t, (size_t)y * t->w + x));
 }
 PFfloat pfGetFramebufferDepth(const PFframebuffer *fb, PFsizei x, PFsizei y)
 {
@@ -3048,20 +3121,20 @@ void pfSetFramebufferPixelDepthTest(PFframebuffer *fb, PFsizei x, PFsizei y, PFf
     case PF_GREATER: pass = z > fb->zbuffer[o]; break;
     default: pass = z >= fb->zbuffer[o]; break;
     }
-    if (pass) { ((uint32_t *)t->pixels)[o] = pack(col); fb->zbuffer[o] = z; }
+    if (pass) { fb_set(t, o, pack(col)); fb->zbuffer[o] = z; }
 }
 void pfSetFramebufferPixelDepth(PFframebuffer *fb, PFsizei x, PFsizei y, PFfloat z, PFcolor col)
 {
     if (G) { sync_host(G); if (fb == &G->mainFB) pull_main_depth(G); }
     Tex *t = (Tex *)fb->texture;
     size_t o = (size_t)y * t->w + x;
-    ((uint32_t *)t->pixels)[o] = pack(col); fb->zbuffer[o] = z;
+    fb_set(t, o, pack(col)); fb->zbuffer[o] = z;
 }
 void pfSetFramebufferPixel(PFframebuffer *fb, PFsizei x, PFsizei y, PFcolor col)
 {
     if (G) sync_host(G);
     Tex *t = (Tex *)fb->texture;
-    ((uint32_t *)t->pixels)[(size_t)y * t->w + x] = pack(col);
+    fb_set(t, (size_t)y * t->w + x, pack(col));
 }
 
 // --- textures (texture.c) --------------------------------------------------------

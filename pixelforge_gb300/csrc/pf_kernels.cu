@@ -15,6 +15,10 @@
 //   k_clear, k_fill, k_hook  framebuffer-wide passes (pfClear,
 //              pfClearFramebuffer, device post-process hooks)
 //
+// Framebuffers of other formats than RGBA / unsigned byte keep their raw
+// pixels in HBM; the kernels read and write them through the format's
+// getters and setters (pf_pixfmt.h).
+//
 // Arithmetic parity.  The file is compiled with -fmad=false so that no
 // multiply-add is contracted (the reference is built for AVX2 without FMA);
 // every floating-point expression keeps the reference's operation order.
@@ -26,6 +30,7 @@
 #include <stdint.h>
 #include "pf_layout.h"
 #include "pf_device.h"
+#include "pf_pixfmt.h"
 
 namespace {
 
@@ -1215,7 +1220,34 @@ __device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uin
     cp_async_commit();
 }
 
-template <int CHN>
+// The colour of the pixel a k_raster thread owns, as the framebuffer holds
+// it.  RGBA / unsigned byte: the packed colour, whose getters and setters
+// are the identity.  Other formats: the raw pixel, read for blending through
+// the SIMD getter (triangles) or the scalar one (points, lines, rectangles,
+// images) and written through the matching setter.
+template <bool GEN> struct FbPixel;
+template <> struct FbPixel<false> {
+    uint32_t c;
+    __device__ __forceinline__ void load(const PFTarget &T, size_t i) { c = ((const uint32_t *)T.color)[i]; }
+    __device__ __forceinline__ void clear(const PFTarget &T) { c = T.clearRaw[0]; }
+    __device__ __forceinline__ void store(const PFTarget &T, size_t i) const { ((uint32_t *)T.color)[i] = c; }
+    __device__ __forceinline__ uint32_t get(bool) const { return c; }
+    __device__ __forceinline__ void set(bool, uint32_t v) { c = v; }
+};
+template <> struct FbPixel<true> {
+    uint32_t r[4];
+    uint32_t f;
+    __device__ __forceinline__ void load(const PFTarget &T, size_t i) { f = T.fmt; pff_load(f, T.color, i, r); }
+    __device__ __forceinline__ void clear(const PFTarget &T)
+    {
+        f = T.fmt; r[0] = T.clearRaw[0]; r[1] = T.clearRaw[1]; r[2] = T.clearRaw[2]; r[3] = T.clearRaw[3];
+    }
+    __device__ __forceinline__ void store(const PFTarget &T, size_t i) const { pff_store(f, T.color, i, r); }
+    __device__ __forceinline__ uint32_t get(bool scalar) const { return scalar ? pff_get_sisd(f, r) : pff_get_simd(f, r); }
+    __device__ __forceinline__ void set(bool scalar, uint32_t v) { if (scalar) pff_set_sisd(f, v, r); else pff_set_simd(f, v, r); }
+};
+
+template <int CHN, bool GEN>
 __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
 {
     extern __shared__ uint32_t skeys[];               // [N] keys (+ [n] sorted copy when rank-sorting)
@@ -1283,7 +1315,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                     if (px >= T.W || py >= T.H) continue;
                     const size_t pidx = (size_t)py * T.W + px;
                     if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
-                    T.color[pidx] = T.clearColor;
+                    if (GEN) pff_store(T.fmt, T.color, pidx, T.clearRaw);
+                    else ((uint32_t *)T.color)[pidx] = T.clearRaw[0];
                     T.depth[pidx] = T.clearDepth;
                 }
             }
@@ -1323,10 +1356,10 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
     const size_t pidx = (size_t)py * T.W + px;
 
     // pixel state in registers
-    uint32_t col = 0; float dep = 0.0f;
+    FbPixel<GEN> col{}; float dep = 0.0f;
     if (inside) {
-        if (T.clearMode == 2 || (T.clearMode == 1 && pidx >= 8)) { col = T.clearColor; dep = T.clearDepth; }
-        else { col = T.color[pidx]; dep = T.depth[pidx]; }
+        if (T.clearMode == 2 || (T.clearMode == 1 && pidx >= 8)) { col.clear(T); dep = T.clearDepth; }
+        else { col.load(T, pidx); dep = T.depth[pidx]; }
     }
 
     if (n > 0) {
@@ -1515,8 +1548,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                                     if (!(rs & PFS_DEPTH_TEST) || (lpk ? depth_sisd(func, z, dep) : depth_simd(func, z, dep))) {
                                         uint32_t frag = fcolv[f - b0];
                                         if (rs & PFS_BLEND)
-                                            frag = lpk ? blend_sisd((int)(rs >> 24), frag, col) : blend_simd((int)(rs >> 24), frag, col);
-                                        col = frag;
+                                            frag = lpk ? blend_sisd((int)(rs >> 24), frag, col.get(true))
+                                                       : blend_simd((int)(rs >> 24), frag, col.get(false));
+                                        col.set(lpk, frag);
                                         if (rs & PFS_DEPTH_MASK) dep = z;
                                     }
                                 }
@@ -1601,10 +1635,11 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
                             if (f >= b0) {
                                 const uint32_t rs = scp[k].rstate;
                                 uint32_t frag = fval[f - b0];
+                                const bool lpk = lpChunk && (scp[k].flags & PFP_KIND);
                                 if (rs & PFS_BLEND)
-                                    frag = (lpChunk && (scp[k].flags & PFP_KIND)) ? blend_sisd((int)(rs >> 24), frag, col)
-                                                                      : blend_simd((int)(rs >> 24), frag, col);
-                                col = frag;
+                                    frag = lpk ? blend_sisd((int)(rs >> 24), frag, col.get(true))
+                                               : blend_simd((int)(rs >> 24), frag, col.get(false));
+                                col.set(lpk, frag);
                             }
                             f++;
                         }
@@ -1614,7 +1649,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
             }
         }
     }
-    if (inside) { T.color[pidx] = col; T.depth[pidx] = dep; }
+    if (inside) { col.store(T, pidx); T.depth[pidx] = dep; }
     }   // tile loop
 
     // fragment counter: one atomic per CTA (same-address atomics serialise)
@@ -1631,35 +1666,53 @@ __global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
 // framebuffer-wide passes
 // ---------------------------------------------------------------------------
 // pfClear, SIMD build (context.c:680-745): pixels [8, n - n%8) take the clear
-// values, the tail copies pixel 0, pixels 0..7 are left as they are.
-__global__ void k_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd,
+// value (as the SIMD setter stores it), the tail copies pixel 0's bytes,
+// pixels 0..7 are left as they are.  For the packed 16-bit formats the
+// reference steps the tail copy by components x 2 bytes (pixel.h:3156-3210),
+// past the pixels: their tail keeps its colour (the depth tail is copied).
+__global__ void k_clear(void *color, uint32_t fmt, float *depth, size_t n, uint4 cc, float cd,
                         const PFDevCounters *cnt, uint32_t command)
 {
     if (cnt->abortCommand <= command) return;
     const size_t aligned = n - (n % 8);
+    const uint32_t craw[4] = { cc.x, cc.y, cc.z, cc.w };
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (i < 8) continue;
-        if (i < aligned) { color[i] = cc; depth[i] = cd; }
-        else { color[i] = color[0]; depth[i] = depth[0]; }
+        if (fmt == PFF_RGBA8) {
+            uint32_t *c32 = (uint32_t *)color;
+            if (i < aligned) c32[i] = cc.x; else c32[i] = c32[0];
+        } else if (i < aligned) pff_store(fmt, color, i, craw);
+        else if (pff_bytes(fmt) != 2) { uint32_t r[4]; pff_load(fmt, color, 0, r); pff_store(fmt, color, i, r); }
+        depth[i] = (i < aligned) ? cd : depth[0];
     }
 }
 
-// pfClearFramebuffer (framebuffer.c:89-102): every pixel.
-__global__ void k_fill(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd,
+// pfClearFramebuffer (framebuffer.c:89-102): every pixel, through the
+// scalar setter.
+__global__ void k_fill(void *color, uint32_t fmt, float *depth, size_t n, uint4 cc, float cd,
+                       const PFDevCounters *cnt, uint32_t command)
+{
+    if (cnt->abortCommand <= command) return;
+    const uint32_t craw[4] = { cc.x, cc.y, cc.z, cc.w };
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (fmt == PFF_RGBA8) ((uint32_t *)color)[i] = cc.x;
+        else pff_store(fmt, color, i, craw);
+        depth[i] = cd;
+    }
+}
+
+// Post-process hooks (pfPostProcess, context.c:2397-2441) and pfFogProcess
+// (context.c:2288-2351), through the scalar getter and setter.  The hooks
+// rewrite every pixel; the fog writes only the pixels past its start.
+__global__ void k_hook(void *color, uint32_t fmt, const float *depth, size_t n, int hook, PFHookParams hp,
                        const PFDevCounters *cnt, uint32_t command)
 {
     if (cnt->abortCommand <= command) return;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        color[i] = cc; depth[i] = cd;
-    }
-}
-
-__global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, PFHookParams hp,
-                       const PFDevCounters *cnt, uint32_t command)
-{
-    if (cnt->abortCommand <= command) return;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        uint32_t c = color[i];
+        uint32_t raw[4];
+        pff_load(fmt, color, i, raw);
+        uint32_t c = pff_get_sisd(fmt, raw);
+        bool write = true;
         if (hook == 1) {          // linear fog on depth
             float d = (depth[i] + hp.znear) / (hp.zfar + hp.znear);
             float f = (hp.end - d) / (hp.end - hp.start);
@@ -1670,6 +1723,7 @@ __global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, 
             c = r;
         } else if (hook == 3) {   // pfFogProcess (context.c:2288-2351)
             const float d = depth[i];
+            write = d > hp.start;
             const uint32_t alpha = hp.color >> 24, fc = hp.color & 0x00ffffffu;
             if (d >= hp.end) {
                 const uint32_t f = fc | (alpha << 24);
@@ -1687,7 +1741,10 @@ __global__ void k_hook(uint32_t *color, const float *depth, size_t n, int hook, 
             uint32_t gy = (77u * chn(c, 0) + 150u * chn(c, 1) + 29u * chn(c, 2)) >> 8;
             c = gy | (gy << 8) | (gy << 16) | (c & 0xff000000u);
         }
-        color[i] = c;
+        if (write) {
+            pff_set_sisd(fmt, c, raw);
+            pff_store(fmt, color, i, raw);
+        }
     }
 }
 
@@ -1766,7 +1823,7 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
     RasterArgs a{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
                   L.totalTiles, L.cnt, L.command, L.anyPhong };
     const size_t smem = raster_smem(L.cap);
-    void (*kernel)(RasterArgs) = L.chunk == 64 ? k_raster<64> : k_raster<32>;
+    void (*kernel)(RasterArgs) = L.generic ? k_raster<32, true> : L.chunk == 64 ? k_raster<64, false> : k_raster<32, false>;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const uint32_t per = (uint32_t)(L.rasterCtasPerSM > 0 ? L.rasterCtasPerSM : 4);
@@ -1774,21 +1831,22 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
     return launch_serialized(kernel, grid, RASTER_THREADS, smem, st, a);
 }
 
-cudaError_t pfd_launch_clear(uint32_t *color, float *depth, size_t n, uint32_t cc, float cd, bool all,
+cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,
                              const PFDevCounters *cnt, uint32_t command, cudaStream_t st)
 {
     unsigned grid = (unsigned)min((size_t)152 * 8, (n + 255) / 256);
     if (grid == 0) return cudaSuccess;
-    if (all) k_fill<<<grid, 256, 0, st>>>(color, depth, n, cc, cd, cnt, command);
-    else k_clear<<<grid, 256, 0, st>>>(color, depth, n, cc, cd, cnt, command);
+    const uint4 c4 = make_uint4(cc[0], cc[1], cc[2], cc[3]);
+    if (all) k_fill<<<grid, 256, 0, st>>>(color, fmt, depth, n, c4, cd, cnt, command);
+    else k_clear<<<grid, 256, 0, st>>>(color, fmt, depth, n, c4, cd, cnt, command);
     return cudaGetLastError();
 }
 
-cudaError_t pfd_launch_hook(uint32_t *color, const float *depth, size_t n, int hook, const PFHookParams &hp,
+cudaError_t pfd_launch_hook(void *color, uint32_t fmt, const float *depth, size_t n, int hook, const PFHookParams &hp,
                             const PFDevCounters *cnt, uint32_t command, cudaStream_t st)
 {
     unsigned grid = (unsigned)min((size_t)152 * 8, (n + 255) / 256);
     if (grid == 0) return cudaSuccess;
-    k_hook<<<grid, 256, 0, st>>>(color, depth, n, hook, hp, cnt, command);
+    k_hook<<<grid, 256, 0, st>>>(color, fmt, depth, n, hook, hp, cnt, command);
     return cudaGetLastError();
 }

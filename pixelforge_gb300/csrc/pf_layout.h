@@ -116,15 +116,15 @@ typedef struct {
 /* A framebuffer rendered by a batch.  Its tiles are numbered
  * tileBase .. tileBase + tilesX*tilesY - 1 in the batch's bin arrays. */
 typedef struct {
-    uint32_t *color;
+    void *color;                  /* pixels of format fmt (pf_pixfmt.h) */
     float *depth;
     uint32_t W, H;
     uint32_t tilesX, tilesY;
     uint32_t tileBase;
     int32_t clearMode;            /* 0 keep, 1 fused pfClear (pixels 0..7 kept), 2 fused full fill */
-    uint32_t clearColor;
+    uint32_t clearRaw[4];         /* the clear colour as stored: SIMD setter (pfClear), scalar (fill) */
     float clearDepth;
-    uint32_t pad_[4];
+    uint32_t fmt;                 /* PFF_* framebuffer format */
 } PFTarget;                       /* 64 bytes */
 
 /* Transformed vertex. */

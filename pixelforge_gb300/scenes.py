@@ -51,16 +51,24 @@ class Target:
     """
 
     def __init__(self, lib: A.PixelForgeLib, width: int, height: int, kind: str = "fbo",
-                 init: np.ndarray | None = None):
+                 init: np.ndarray | None = None, fmt: tuple = (A.PF_RGBA, A.PF_UNSIGNED_BYTE)):
         self.lib, self.w, self.h, self.kind = lib, width, height, kind
-        self.main = np.zeros((height, width, 4), np.uint8) if init is None else init.copy()
-        self.ctx = lib.pfCreateContext(_ptr(self.main), width, height, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+        self.fmt, self.bpp = fmt, A.pixel_bytes(*fmt)
+        # packed 16-bit formats: the reference's pfClear copies its tail at
+        # components x 2 bytes per pixel (src/internal/pixel.h:3156-3210),
+        # past the pixels; the buffer gets room for those writes
+        n = height * width * self.bpp
+        self._backing = np.zeros(n * (4 if self.bpp == 2 else 1), np.uint8)
+        self.main = self._backing[:n].reshape(height, width, self.bpp)
+        if init is not None:
+            self.main[...] = init
+        self.ctx = lib.pfCreateContext(_ptr(self.main), width, height, *fmt)
         if not self.ctx:
             raise RuntimeError("pfCreateContext failed")
         lib.pfMakeCurrent(self.ctx)
         self.fb = None
         if kind == "fbo":
-            self.fb = lib.pfGenFramebuffer(width, height, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            self.fb = lib.pfGenFramebuffer(width, height, *fmt)
             self._fbref = C.pointer(self.fb)
             lib.pfBindFramebuffer(self._fbref)
             lib.pfEnable(A.PF_FRAMEBUFFER)
@@ -80,7 +88,7 @@ class Target:
             px.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             base = px(self.fb.texture, None, None, None, None)
             color = np.ctypeslib.as_array(C.cast(base, C.POINTER(C.c_uint8)),
-                                          shape=(self.h, self.w, 4)).copy()
+                                          shape=(self.h, self.w, self.bpp)).copy()
             depth = np.ctypeslib.as_array(self.fb.zbuffer, shape=(self.h, self.w)).copy()
             return Frame(color, depth, stats)
         return Frame(self.main.copy(), None, stats)
@@ -324,8 +332,8 @@ class SphereScene:
         th = C.c_void_p(self.texh)
         lib.pfDeleteTexture(C.byref(th), False)
 
-    def render(self, lib, target: str = "fbo") -> Frame:
-        tg = Target(lib, self.width, self.height, target)
+    def render(self, lib, target: str = "fbo", fmt: tuple = (A.PF_RGBA, A.PF_UNSIGNED_BYTE)) -> Frame:
+        tg = Target(lib, self.width, self.height, target, fmt=fmt)
         try:
             self.setup(lib)
             self.frame(lib)

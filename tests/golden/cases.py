@@ -290,6 +290,9 @@ def cases() -> dict:
         c[f"lp_{s}"] = lp(7000 + s)
     for s in range(16):
         c[f"px_{s}"] = px(9000 + s)
+    from fbscenes import FB_FORMATS, fb_frame
+    for s in range(len(FB_FORMATS)):
+        c[f"fb_{s}"] = fb_frame(11000 + s)
     return c
 
 

@@ -182,3 +182,16 @@ def test_static_entry_rejects_oversize_without_device(lib):
     assert f(dummy, dummy, 8193, dummy, dummy, dummy, 64, 64, 0, 0, None) == -1    # too many triangles
     assert f(dummy, dummy, 1, dummy, dummy, dummy, 513, 64, 0, 0, None) == -1      # too wide
     assert f(None, dummy, 1, dummy, dummy, dummy, 64, 64, 0, 0, None) == -2        # no positions
+
+
+def test_framebuffer_formats_refused(lib, oracle):
+    """Framebuffer formats whose reference results depend on other pixels or
+    on the SIMD lane are refused with PF_INVALID_ENUM, by the library and
+    the oracle alike; every accepted pair is a valid pixel format."""
+    from fbscenes import FB_FORMATS, FB_REFUSED, refused_formats
+    for lb in (lib, oracle):
+        res = refused_formats(lb)
+        assert len(res) == len(FB_REFUSED)
+        for pair, null, err in res:
+            assert null and err == A.PF_INVALID_ENUM, pair
+    assert len(FB_FORMATS) == 19 and all(A.pixel_bytes(*p) for p in FB_FORMATS)

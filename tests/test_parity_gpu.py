@@ -222,3 +222,36 @@ def test_read_pixels_formats(gpu, oracle, seed):
     for k in a:
         assert a[k][1] == b[k][1] == 0, k
         assert np.array_equal(a[k][0], b[k][0]), f"format/type {k}: bytes differ"
+
+
+@pytest.mark.parametrize("seed", range(0, 95))
+def test_framebuffer_formats(gpu, oracle, seed):
+    """Framebuffers of every accepted format (5 seeds each, main buffers and
+    framebuffer objects, odd sizes): clears and fills, triangles through the
+    format's SIMD getter / setter in k_raster, points, lines, rectangles and
+    images through the scalar ones, linear fog and the grayscale device
+    hook, the per-pixel framebuffer functions and pfReadPixels.  Raw pixels,
+    depth and every read bit-exact."""
+    from fbscenes import fb_case, run_fb
+    case = fb_case(seed)
+    a, b = run_fb(gpu, case), run_fb(oracle, case)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert a["err"] == b["err"] == 0
+    for k in ("color", "depth", "read", "get"):
+        if k in b:
+            x, y = a[k].view(np.uint8), b[k].view(np.uint8)
+            assert np.array_equal(x, y), f"{case}: {k} differs in {int((x != y).sum())} bytes"
+
+
+@pytest.mark.parametrize("fmt", [(A.PF_RGBA, A.PF_HALF_FLOAT), (A.PF_RGB, A.PF_UNSIGNED_SHORT_5_6_5),
+                                 (A.PF_BGRA, A.PF_FLOAT)])
+def test_framebuffer_formats_sphere1080(gpu, oracle, fmt):
+    """The textured, alpha-blended sphere at 1920x1080 (unlit: no host powf)
+    into a framebuffer of another format: raw pixels and depth bit-exact
+    against the oracle."""
+    sc = SphereScene(filt=A.PF_NEAREST, lighting=None)
+    got, ref = sc.render(gpu, "fbo", fmt=fmt), sc.render(oracle, "fbo", fmt=fmt)
+    assert got.color.shape == (1080, 1920, A.pixel_bytes(*fmt))
+    assert np.array_equal(got.depth.view(np.uint32), ref.depth.view(np.uint32))
+    nd = int((got.color != ref.color).any(-1).sum())
+    assert nd == 0, f"{fmt}: {nd} pixels differ"
