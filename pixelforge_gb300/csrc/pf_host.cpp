@@ -1559,9 +1559,14 @@ bool flush(Renderer *r)
         if (first->kind == CMD_FILL) {
             // every pixel is overwritten first
         } else if (first->kind == CMD_CLEAR) {
-            // the clear leaves pixels 0..7 (and reads pixel 0 for the tail)
+            // the clear leaves pixels 0..7 (and reads pixel 0 for the tail;
+            // the packed 16-bit formats keep their tail, see k_clear)
             const size_t k = std::min<size_t>(8, n);
             cudaMemcpyAsync(m->dColor, m->tex->pixels, k * m->bpp, cudaMemcpyHostToDevice, st);
+            const size_t aligned = n - n % 8;
+            if (m->bpp == 2 && aligned < n && aligned >= k)
+                cudaMemcpyAsync((uint8_t *)m->dColor + aligned * 2, (const uint8_t *)m->tex->pixels + aligned * 2,
+                                (n - aligned) * 2, cudaMemcpyHostToDevice, st);
             if (uploadDepth) cudaMemcpyAsync(m->dDepth, m->hostDepth, k * 4, cudaMemcpyHostToDevice, st);
         } else {
             cudaMemcpyAsync(m->dColor, m->tex->pixels, n * m->bpp, cudaMemcpyHostToDevice, st);
