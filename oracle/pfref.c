@@ -1428,6 +1428,7 @@ void pfDeleteContext(PFcontext ctx)
 void pfSetMainBuffer(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
 {
     if (!buf || !w || !h) { G->err = PF_INVALID_VALUE; return; }
+    if (!fb_format_ok(f, t)) { G->err = PF_INVALID_ENUM; return; }   /* the main buffer stays as it was */
     RTex *old = (RTex *)G->main.texture;
     if (old->w != w || old->h != h) {
         free(G->main.zbuffer);

@@ -1918,6 +1918,7 @@ void pfDeleteContext(PFcontext ctx)
 void pfSetMainBuffer(void *buf, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t)
 {
     if (!buf || !w || !h) { G->err = PF_INVALID_VALUE; return; }
+    if (fb_code(f, t) < 0) { G->err = PF_INVALID_ENUM; return; }   // the main buffer stays as it was
     flush(G);
     pull_main_depth(G);
     Tex *old = (Tex *)G->mainFB.texture;
