@@ -265,6 +265,10 @@ struct Renderer {
     size_t upChunk = 0, upOff = 0, upBytes = 0;
     cudaStream_t upStream = nullptr;
     cudaEvent_t upDone = nullptr;
+    unsigned *dMax = nullptr, *hMax = nullptr;   // largest uploaded index: device word, page-locked result
+    bool readsHostMemory = false;        // the device reads pageable memory through the CPU's page tables
+    int uploadScopes = 0;                // > 0: uploads that read caller memory in place are waited for at scope exit
+    bool uploadsInFlight = false;        // such uploads not yet waited for
 
     // device
     bool devInit = false, devOk = false;
@@ -674,12 +678,34 @@ constexpr size_t kUploadMin = (size_t)64 << 10;          // smaller arrays go th
 constexpr size_t kUploadBudget = (size_t)8 << 30;        // per recording; beyond it, staging with de-duplication
 constexpr size_t kUploadChunk = (size_t)64 << 20;
 
+// Wait for the uploads that read caller memory in place.
+void upload_wait(Renderer *r)
+{
+    if (!r->uploadsInFlight) return;
+    if (cudaStreamSynchronize(r->upStream) != cudaSuccess) cudaGetLastError();
+    r->uploadsInFlight = false;
+}
+
+// Within an API call that may upload several arrays (a draw): their in-place
+// copies run together and are waited for once, when the call returns.
+struct UploadScope {
+    Renderer *r;
+    explicit UploadScope(Renderer *rr) : r(rr) { r->uploadScopes++; }
+    ~UploadScope() { if (--r->uploadScopes == 0) upload_wait(r); }
+    UploadScope(const UploadScope &) = delete;
+    UploadScope &operator=(const UploadScope &) = delete;
+};
+
 // Copy `bytes` of caller memory to the device now, straight from where it
-// lies (one cudaMemcpyAsync; on this platform that is several times faster
-// than a host copy into pinned staging followed by the upload).  From
-// pageable memory the call returns only once the bytes are read, which is
-// the snapshot the reference's draw-time read implies; from page-locked or
-// device memory it would return earlier, so the copy is waited for.
+// lies: where the device reads pageable memory through the CPU's page
+// tables, a copy kernel reads it in place (16-byte aligned sources); else
+// one cudaMemcpyAsync (on this platform either is several times faster than
+// a host copy into pinned staging followed by the upload).  The call that
+// records the draw returns only once the bytes are read -- the snapshot the
+// reference's draw-time read implies: a pageable cudaMemcpyAsync returns
+// then by itself, an in-place copy is waited for (upload_wait, at the end of
+// the enclosing UploadScope or at once without one), a copy from page-locked
+// or device memory at once.
 // Returns the device reference, or -1 (the caller takes the staging path).
 int64_t upload(Renderer *r, const void *p, size_t bytes)
 {
@@ -700,8 +726,14 @@ int64_t upload(Renderer *r, const void *p, size_t bytes)
     cudaPointerAttributes attr{};
     const bool pageable = cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeUnregistered;
     cudaGetLastError();
-    if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
-    if (!pageable) cudaStreamSynchronize(r->upStream);
+    if (pageable && r->readsHostMemory && (uintptr_t)p % 16 == 0 && pfd_copy_host(dst, p, bytes, r->upStream) == cudaSuccess) {
+        r->uploadsInFlight = true;
+        if (r->uploadScopes == 0) upload_wait(r);
+    } else {
+        cudaGetLastError();
+        if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
+        if (!pageable) cudaStreamSynchronize(r->upStream);
+    }
     r->upOff += need;
     r->upBytes += bytes;
     return dev_ref(dst);
@@ -725,6 +757,22 @@ int64_t snapshot(Renderer *r, const void *p, size_t bytes, bool device_ok = true
 }
 int64_t snapshot(Ctx *c, const void *p, size_t bytes) { return snapshot(c->rend, p, bytes); }
 
+// The largest of `count` indices uploaded to d, reduced on the device (a
+// few microseconds after the copy lands; a host scan of the caller's array
+// takes several times longer).  False if the device could not do it.
+bool device_max_u32(Renderer *r, const uint32_t *d, size_t count, uint32_t &mx)
+{
+    if (!r->dMax && cudaMalloc((void **)&r->dMax, sizeof(unsigned)) != cudaSuccess) { cudaGetLastError(); r->dMax = nullptr; return false; }
+    if (!r->hMax && cudaMallocHost((void **)&r->hMax, sizeof(unsigned)) != cudaSuccess) { cudaGetLastError(); r->hMax = nullptr; return false; }
+    if (pfd_max_u32(d, count, r->dMax, r->hMax, r->upStream) != cudaSuccess || cudaStreamSynchronize(r->upStream) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    r->uploadsInFlight = false;          // the synchronisation completed every upload before it
+    mx = *r->hMax;
+    return true;
+}
+
 // Snapshot of `count` u32 indices and their largest value (kept with the
 // snapshot, so a draw that repeats the indices compares instead of copying).
 int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
@@ -732,7 +780,10 @@ int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
     const size_t bytes = count * 4;
     if (bytes >= kUploadMin) {
         const int64_t ref = upload(r, p, bytes);
-        if (ref != -1) { mx = par_max_u32(p, count); return ref; }
+        if (ref != -1) {
+            if (!device_max_u32(r, (const uint32_t *)(uintptr_t)(-ref), count, mx)) mx = par_max_u32(p, count);
+            return ref;
+        }
     }
     for (auto &s : r->snaps)
         if (s.p == p && s.bytes == bytes && s.maxU32 >= 0 && par_equal(r->staging.base + s.off, p, bytes)) {
@@ -1255,6 +1306,14 @@ bool device_init(Renderer *r)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->upStream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->upDone, cudaEventDisableTiming);
     if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); r->devStatus |= PF_DEVICE_NO_GPU; return false; }
+    {
+        int dev = 0, pageable = 0, hostTables = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess)
+            r->readsHostMemory = pageable == 1 && hostTables == 1;
+        cudaGetLastError();
+    }
     if (!r->counters.ensure(sizeof(PFDevCounters))) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
     if (cudaMallocHost((void **)&r->hostCounters, sizeof(PFDevCounters)) != cudaSuccess) {
         cudaGetLastError(); r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false;
@@ -1275,6 +1334,9 @@ void release_renderer(Renderer *r)
         if (r->stream) cudaStreamDestroy(r->stream);
         if (r->upStream) cudaStreamDestroy(r->upStream);
         if (r->upDone) cudaEventDestroy(r->upDone);
+        if (r->dMax) cudaFree(r->dMax);
+        if (r->hMax) cudaFreeHost(r->hMax);
+        r->dMax = r->hMax = nullptr;
         for (auto &u : r->up) cudaFree(u.p);
         r->up.clear();
         for (void *q : r->splitMem) cudaFree(q);
@@ -2382,6 +2444,7 @@ static void assemble_arrays(Ctx *c, PFdrawmode mode, PFsizei count, const void *
 static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first)
 {
     Ctx *c = G;
+    UploadScope uploads(c->rend);        // the arrays' copies are waited for once, on return
     update_matrices(c, !(mode == PF_POINTS || mode == PF_LINES));     // pfBegin inside the draw
     c->drawMode = mode; c->vcount = 0;
     c->stateDirty = true;

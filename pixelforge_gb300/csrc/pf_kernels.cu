@@ -1748,6 +1748,32 @@ __global__ void k_hook(void *color, uint32_t fmt, const float *depth, size_t n, 
     }
 }
 
+// Copy of n16 16-byte blocks of caller memory that the GPU reads in place
+// through the CPU's page tables (the host's source is 16-byte aligned, so
+// the last, partial block lies in the page of the array's last byte).
+__global__ void k_copy_host(uint4 *dst, const uint4 *src, size_t n16)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// The largest of n u32 indices (already on the device, 16-byte aligned):
+// per-warp maxima folded into *out with one atomic per warp.
+__global__ void k_max_u32(const uint32_t *src, size_t n, unsigned *out)
+{
+    const size_t n4 = n / 4;
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    unsigned m = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const uint4 v = __ldg(s4 + i);
+        m = max(m, max(max(v.x, v.y), max(v.z, v.w)));
+    }
+    for (size_t i = n4 * 4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride) m = max(m, __ldg(src + i));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1848,5 +1874,27 @@ cudaError_t pfd_launch_hook(void *color, uint32_t fmt, const float *depth, size_
     unsigned grid = (unsigned)min((size_t)152 * 8, (n + 255) / 256);
     if (grid == 0) return cudaSuccess;
     k_hook<<<grid, 256, 0, st>>>(color, fmt, depth, n, hook, hp, cnt, command);
+    return cudaGetLastError();
+}
+
+cudaError_t pfd_max_u32(const uint32_t *d, size_t n, unsigned *dWord, unsigned *hWord, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(dWord, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    if (n) {
+        const unsigned grid = (unsigned)min((size_t)pfd_sm_count() * 2, (n / 4 + 255) / 256 + 1);
+        k_max_u32<<<grid, 256, 0, st>>>(d, n, dWord);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaMemcpyAsync(hWord, dWord, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+}
+
+cudaError_t pfd_copy_host(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    const size_t n16 = (bytes + 15) / 16;
+    if (n16 == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)min((size_t)pfd_sm_count() * 4, (n16 + 255) / 256);
+    k_copy_host<<<grid, 256, 0, st>>>((uint4 *)dst, (const uint4 *)src, n16);
     return cudaGetLastError();
 }
