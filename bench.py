@@ -202,6 +202,8 @@ def run_gpu(args):
     tg.close()
     if not args.no_phong:
         out["phong"] = run_phong(lib)
+    if not args.no_formats:
+        out["framebuffer_formats"] = run_formats(lib)
     if not args.no_batched:
         out["batched"] = run_batched(lib)
     if not args.no_adjoint:
@@ -252,6 +254,46 @@ def run_phong(lib, warmup: int = 2, steps: int = 5) -> dict:
             "fragments_per_s": s.fragments / (s.device_ms / 1e3),
             "raster_ms_per_frame": s.raster_ms / steps,
             "e2e_ms_per_frame": wall * 1e3 / steps, "l2": "flushed between frames"}
+
+
+def run_formats(lib, warmup: int = 2, steps: int = 5) -> dict:
+    """The sphere frame into main buffers of other formats: device ms per
+    frame, raster ms and end-to-end ms (the write-back moves the format's
+    bytes); RGBA / unsigned byte runs the plain kernel, the others the
+    generic-format raster kernel."""
+    import torch
+    from pixelforge_gb300 import abi as A
+    from pixelforge_gb300.scenes import SphereScene, Target
+    l2_flush = torch.empty(512 << 20, dtype=torch.uint8, device=torch.device("cuda:0"))
+    out = {}
+    for name, fmt in (("RGBA8", (A.PF_RGBA, A.PF_UNSIGNED_BYTE)), ("RGB565", (A.PF_RGB, A.PF_UNSIGNED_SHORT_5_6_5)),
+                      ("RGBA16F", (A.PF_RGBA, A.PF_HALF_FLOAT)), ("RGBA32F", (A.PF_RGBA, A.PF_FLOAT))):
+        sc = SphereScene()
+        tg = Target(lib, sc.width, sc.height, "main", fmt=fmt)
+        sc.setup(lib)
+        lib.pfEnableTiming(True)
+        for _ in range(warmup):
+            sc.frame(lib)
+            lib.pfFinish()
+        lib.pfResetStats()
+        wall = 0.0
+        for _ in range(steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sc.frame(lib)
+            lib.pfFinish()
+            wall += time.perf_counter() - t0
+        s = A.PFstats()
+        lib.pfGetStats(s)
+        status = lib.pfGetDeviceStatus()
+        sc.teardown(lib)
+        tg.close()
+        if status != 0:
+            raise RuntimeError(f"device status {status:#x}")
+        out[name] = {"bytes_per_pixel": A.pixel_bytes(*fmt), "ms_per_frame": s.device_ms / steps,
+                     "raster_ms_per_frame": s.raster_ms / steps, "e2e_ms_per_frame": wall * 1e3 / steps}
+    return {"workload": SPHERE_WORKLOAD + ", main buffer of each format", **out}
 
 
 def run_adjoint(args) -> dict:
@@ -432,6 +474,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-context batch measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the fitting-iteration measurement")
     ap.add_argument("--no-phong", action="store_true", help="skip the Phong 1080p measurement")
+    ap.add_argument("--no-formats", action="store_true", help="skip the framebuffer-format measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

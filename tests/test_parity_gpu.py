@@ -255,3 +255,68 @@ def test_framebuffer_formats_sphere1080(gpu, oracle, fmt):
     assert np.array_equal(got.depth.view(np.uint32), ref.depth.view(np.uint32))
     nd = int((got.color != ref.color).any(-1).sum())
     assert nd == 0, f"{fmt}: {nd} pixels differ"
+
+
+def _aligned(n_bytes: int, misalign: int) -> np.ndarray:
+    """A byte array whose data starts `misalign` bytes past a 64-byte boundary."""
+    raw = np.zeros(n_bytes + 128, np.uint8)
+    start = (-raw.ctypes.data) % 64 + misalign
+    return raw[start:start + n_bytes]
+
+
+@pytest.mark.parametrize("misalign", [0, 4])
+def test_draw_time_snapshot_of_large_arrays(gpu, oracle, misalign):
+    """Arrays of 64 KiB and more are copied to the device during the draw
+    call (in place from 16-byte-aligned pageable memory, else by
+    cudaMemcpyAsync): the caller overwrites positions, colours, texcoords,
+    indices and texture right after each draw, and the image must be the
+    one the reference draws from the contents at each call."""
+    from pixelforge_gb300.scenes import Target, _ptr
+    ntri, W, H = 20000, 256, 192
+    nv = ntri * 3
+    pos = _aligned(nv * 12, misalign).view(np.float32).reshape(nv, 3)
+    uv = _aligned(nv * 8, misalign).view(np.float32).reshape(nv, 2)
+    col = _aligned(nv * 4, misalign).reshape(nv, 4)
+    idx = _aligned(nv * 4, misalign).view(np.uint32)
+    tex = _aligned(256 * 256 * 4, misalign).reshape(256, 256, 4)
+
+    def fill(seed):
+        r = np.random.default_rng(seed)
+        pos[...] = r.uniform(-1.1, 1.1, (nv, 3)).astype(np.float32) * np.float32([1, 1, 0.8])
+        uv[...] = r.uniform(-1, 2, (nv, 2)).astype(np.float32)
+        col[...] = r.integers(0, 256, (nv, 4)).astype(np.uint8)
+        idx[...] = r.permutation(nv).astype(np.uint32)
+        tex[...] = r.integers(0, 256, (256, 256, 4)).astype(np.uint8)
+
+    def run(lib):
+        tg = Target(lib, W, H, "fbo")
+        th = None
+        try:
+            lib.pfDisable(A.PF_CULL_FACE)
+            lib.pfEnable(A.PF_DEPTH_TEST)
+            lib.pfEnable(A.PF_BLEND)
+            lib.pfBlendFunc(A.PF_BLEND_ALPHA)
+            lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+            th = lib.pfGenTexture(_ptr(tex), 256, 256, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            lib.pfBindTexture(th)
+            lib.pfEnable(A.PF_TEXTURE_2D)
+            lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_TEXTURE_COORD_ARRAY | A.PF_COLOR_ARRAY)
+            lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(pos))
+            lib.pfTexCoordPointer(A.PF_FLOAT, 0, _ptr(uv))
+            lib.pfColorPointer(4, A.PF_UNSIGNED_BYTE, 0, _ptr(col))
+            for seed in (1, 2, 3):
+                fill(seed)
+                lib.pfDrawElements(A.PF_TRIANGLES, nv // (1 + seed % 2), A.PF_UNSIGNED_INT, _ptr(idx))
+            fill(99)                                   # after the last draw, before the flush
+            return tg.finish()
+        finally:
+            if th:
+                h = C.c_void_p(th)
+                lib.pfDeleteTexture(C.byref(h), False)
+            tg.close()
+
+    import ctypes as C
+    got, ref = run(gpu), run(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert (ref.depth < 1e30).sum() > 10000
+    assert_parity(got, ref, exact_color=True, label=f"snapshot misalign={misalign}")
