@@ -62,6 +62,10 @@ int pfd_sm_count(void);
  * tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables).  The caller
  * must keep src valid until st has completed the copy. */
 cudaError_t pfd_copy_host(void *dst, const void *src, size_t bytes, cudaStream_t st);
+/* pfd_copy_host for `count` u32 indices, their largest into the page-locked
+ * *hWord through the device word *dWord; complete once st is. */
+cudaError_t pfd_copy_host_max_u32(uint32_t *dst, const uint32_t *src, size_t count, unsigned *dWord, unsigned *hWord,
+                                  cudaStream_t st);
 /* The largest of n u32 values at d (device, 16-byte aligned) into the
  * page-locked *hWord, through the device word *dWord; complete once st is. */
 cudaError_t pfd_max_u32(const uint32_t *d, size_t n, unsigned *dWord, unsigned *hWord, cudaStream_t st);

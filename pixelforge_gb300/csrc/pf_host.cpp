@@ -707,9 +707,11 @@ struct UploadScope {
 // the enclosing UploadScope or at once without one), a copy from page-locked
 // or device memory at once.
 // Returns the device reference, or -1 (the caller takes the staging path).
-int64_t upload(Renderer *r, const void *p, size_t bytes)
+// Room for `bytes` in the upload chunks, or nullptr (the caller takes the
+// staging path); upload_commit takes it.
+uint8_t *upload_room(Renderer *r, size_t bytes)
 {
-    if (bytes < kUploadMin || r->upBytes + bytes > kUploadBudget || !device_init(r)) return -1;
+    if (bytes < kUploadMin || r->upBytes + bytes > kUploadBudget || !device_init(r)) return nullptr;
     if (r->upBytes == 0) {               // a new recording: the last flush's device data is overwritten
         r->lastOps.clear();
         r->graphValid = false;
@@ -718,14 +720,30 @@ int64_t upload(Renderer *r, const void *p, size_t bytes)
     while (r->upChunk < r->up.size() && r->upOff + need > r->up[r->upChunk].cap) { r->upChunk++; r->upOff = 0; }
     if (r->upChunk == r->up.size()) {
         Renderer::UpChunk c{ nullptr, std::max(kUploadChunk, need) };
-        if (cudaMalloc(&c.p, c.cap) != cudaSuccess) { cudaGetLastError(); return -1; }
+        if (cudaMalloc(&c.p, c.cap) != cudaSuccess) { cudaGetLastError(); return nullptr; }
         r->up.push_back(c);
         r->upOff = 0;
     }
-    uint8_t *dst = (uint8_t *)r->up[r->upChunk].p + r->upOff;
+    return (uint8_t *)r->up[r->upChunk].p + r->upOff;
+}
+void upload_commit(Renderer *r, size_t bytes)
+{
+    r->upOff += (bytes + 255) & ~(size_t)255;
+    r->upBytes += bytes;
+}
+bool is_pageable(const void *p)
+{
     cudaPointerAttributes attr{};
     const bool pageable = cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeUnregistered;
     cudaGetLastError();
+    return pageable;
+}
+
+int64_t upload(Renderer *r, const void *p, size_t bytes)
+{
+    uint8_t *dst = upload_room(r, bytes);
+    if (!dst) return -1;
+    const bool pageable = is_pageable(p);
     if (pageable && r->readsHostMemory && (uintptr_t)p % 16 == 0 && pfd_copy_host(dst, p, bytes, r->upStream) == cudaSuccess) {
         r->uploadsInFlight = true;
         if (r->uploadScopes == 0) upload_wait(r);
@@ -734,8 +752,7 @@ int64_t upload(Renderer *r, const void *p, size_t bytes)
         if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
         if (!pageable) cudaStreamSynchronize(r->upStream);
     }
-    r->upOff += need;
-    r->upBytes += bytes;
+    upload_commit(r, bytes);
     return dev_ref(dst);
 }
 
@@ -760,10 +777,25 @@ int64_t snapshot(Ctx *c, const void *p, size_t bytes) { return snapshot(c->rend,
 // The largest of `count` indices uploaded to d, reduced on the device (a
 // few microseconds after the copy lands; a host scan of the caller's array
 // takes several times longer).  False if the device could not do it.
+// The device word and page-locked word that return an index maximum.
+bool max_words(Renderer *r)
+{
+    if (!r->dMax) {
+        unsigned *d = nullptr;
+        if (cudaMalloc((void **)&d, sizeof(unsigned)) != cudaSuccess) { cudaGetLastError(); return false; }
+        r->dMax = d;
+    }
+    if (!r->hMax) {
+        unsigned *h = nullptr;
+        if (cudaMallocHost((void **)&h, sizeof(unsigned)) != cudaSuccess) { cudaGetLastError(); return false; }
+        r->hMax = h;
+    }
+    return true;
+}
+
 bool device_max_u32(Renderer *r, const uint32_t *d, size_t count, uint32_t &mx)
 {
-    if (!r->dMax && cudaMalloc((void **)&r->dMax, sizeof(unsigned)) != cudaSuccess) { cudaGetLastError(); r->dMax = nullptr; return false; }
-    if (!r->hMax && cudaMallocHost((void **)&r->hMax, sizeof(unsigned)) != cudaSuccess) { cudaGetLastError(); r->hMax = nullptr; return false; }
+    if (!max_words(r)) return false;
     if (pfd_max_u32(d, count, r->dMax, r->hMax, r->upStream) != cudaSuccess || cudaStreamSynchronize(r->upStream) != cudaSuccess) {
         cudaGetLastError();
         return false;
@@ -778,6 +810,21 @@ bool device_max_u32(Renderer *r, const uint32_t *d, size_t count, uint32_t &mx)
 int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
 {
     const size_t bytes = count * 4;
+    if (bytes >= kUploadMin && device_init(r) && r->readsHostMemory && (uintptr_t)p % 16 == 0 && is_pageable(p)) {
+        // copied in place, the largest index found by the same kernel; the
+        // wait also completes the uploads issued before it
+        uint8_t *dst = upload_room(r, bytes);
+        if (dst && max_words(r) &&
+            pfd_copy_host_max_u32((uint32_t *)dst, p, count, r->dMax, r->hMax, r->upStream) == cudaSuccess &&
+            cudaStreamSynchronize(r->upStream) == cudaSuccess) {
+            r->uploadsInFlight = false;
+            upload_commit(r, bytes);
+            mx = *r->hMax;
+            return dev_ref(dst);
+        }
+        cudaGetLastError();
+        upload_wait(r);
+    }
     if (bytes >= kUploadMin) {
         const int64_t ref = upload(r, p, bytes);
         if (ref != -1) {
@@ -2463,6 +2510,10 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
         return;
     }
 
+    // the segment and its draw state first: the texture's copy then runs
+    // while the indices are copied and their range is found
+    const int si = new_segment(c, PF_SRC_ARRAYS, mode == PF_TRIANGLES ? PF_ITEMS_TRIS : PF_ITEMS_EXPLICIT);
+
     // indices: stage as u32 and find the vertex range
     int64_t idxOff = -1;
     size_t nverts;
@@ -2490,7 +2541,6 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     const bool useN = (c->state & PF_NORMAL_ARRAY) && c->normals.buf;
     const bool useC = (c->state & PF_COLOR_ARRAY) && c->colors.buf;
 
-    const int si = new_segment(c, PF_SRC_ARRAYS, mode == PF_TRIANGLES ? PF_ITEMS_TRIS : PF_ITEMS_EXPLICIT);
     SegRec &r = c->rend->segs[si];
     r.posOff = stage_float_attr(c, c->positions, c->positions.size, (size_t)first, nverts);
     if (useN) r.nrmOff = stage_float_attr(c, c->normals, 3, (size_t)first, nverts);
