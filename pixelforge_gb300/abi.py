@@ -35,7 +35,8 @@ class PFstats(C.Structure):
                 ("rasterized", C.c_uint64), ("flushes", C.c_uint64),
                 ("bin_overflows", C.c_uint64), ("device_ms", C.c_double),
                 ("raster_ms", C.c_double), ("raster_launches", C.c_uint64),
-                ("kernel_launches", C.c_uint64), ("draw_splits", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("draw_splits", C.c_uint64),
+                ("copy_launches", C.c_uint64)]
 
 
 class PFhookfog(C.Structure):

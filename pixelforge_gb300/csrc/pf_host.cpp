@@ -745,7 +745,7 @@ int64_t upload(Renderer *r, const void *p, size_t bytes)
     if (!dst) return -1;
     const bool pageable = is_pageable(p);
     if (pageable && r->readsHostMemory && (uintptr_t)p % 16 == 0 && pfd_copy_host(dst, p, bytes, r->upStream) == cudaSuccess) {
-        r->stats.kernel_launches += 1;
+        r->stats.kernel_launches += 1; r->stats.copy_launches += 1;
         r->uploadsInFlight = true;
         if (r->uploadScopes == 0) upload_wait(r);
     } else {
@@ -801,7 +801,7 @@ bool device_max_u32(Renderer *r, const uint32_t *d, size_t count, uint32_t &mx)
         cudaGetLastError();
         return false;
     }
-    r->stats.kernel_launches += 1;
+    r->stats.kernel_launches += 1; r->stats.copy_launches += 1;
     r->uploadsInFlight = false;          // the synchronisation completed every upload before it
     mx = *r->hMax;
     return true;
@@ -820,7 +820,7 @@ int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
             pfd_copy_host_max_u32((uint32_t *)dst, p, count, r->dMax, r->hMax, r->upStream) == cudaSuccess &&
             cudaStreamSynchronize(r->upStream) == cudaSuccess) {
             r->uploadsInFlight = false;
-            r->stats.kernel_launches += 1;
+            r->stats.kernel_launches += 1; r->stats.copy_launches += 1;
             upload_commit(r, bytes);
             mx = *r->hMax;
             return dev_ref(dst);
