@@ -474,6 +474,7 @@ class BatchScene:
     tri_sigma: float = 1.0
     tri_clip: tuple = (100, 50000)
     tex_size: int = 256
+    fmts: tuple = ()                 # framebuffer (format, type) of context i: fmts[i % len]; RGBA8 if empty
 
     def __post_init__(self):
         rng = np.random.default_rng(self.seed)
@@ -507,8 +508,9 @@ class BatchScene:
     def create(self, lib):
         for i in range(self.n):
             s = int(self.sides[i])
-            b = np.zeros((s, s, 4), np.uint8)
-            c = lib.pfCreateContext(_ptr(b), s, s, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            fmt = self.fmts[i % len(self.fmts)] if self.fmts else (A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            b = np.zeros((s, s, A.pixel_bytes(*fmt)), np.uint8)
+            c = lib.pfCreateContext(_ptr(b), s, s, *fmt)
             lib.pfMakeCurrent(c)
             t = lib.pfGenTexture(_ptr(self.tex[i]), self.tex_size, self.tex_size, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
             lib.pfTextureParameter(t, int(self.wraps[i]), int(self.filters[i]))

@@ -56,6 +56,34 @@ def test_batch_vs_oracle(gpu, oracle):
         sc_o.destroy(oracle)
 
 
+def test_batch_mixed_framebuffer_formats_vs_oracle(gpu, oracle):
+    """One batch whose contexts have main buffers of different formats (the
+    raster launch takes the generic-format kernel, each target its own
+    format): raw pixels bit-exact against the oracle context by context."""
+    fmts = ((A.PF_RGBA, A.PF_UNSIGNED_BYTE), (A.PF_RGB, A.PF_UNSIGNED_SHORT_5_6_5), (A.PF_RGBA, A.PF_HALF_FLOAT),
+            (A.PF_BGR, A.PF_UNSIGNED_BYTE), (A.PF_BGRA, A.PF_FLOAT), (A.PF_LUMINANCE_ALPHA, A.PF_HALF_FLOAT),
+            (A.PF_RGBA, A.PF_UNSIGNED_SHORT_4_4_4_4))
+    sc_g = BatchScene(n=14, max_side=192, tri_clip=(100, 900), seed=34, fmts=fmts)
+    sc_o = BatchScene(n=14, max_side=192, tri_clip=(100, 900), seed=34, fmts=fmts)
+    sc_g.create(gpu)
+    sc_o.create(oracle)
+    try:
+        batch = gpu.pfgbBatchCreate()
+        try:
+            got = sc_g.render_batch(gpu, batch)
+        finally:
+            gpu.pfgbBatchDelete(batch)
+        assert gpu.pfGetDeviceStatus() == 0
+        ref = sc_o.render_loop(oracle)
+        for i, (g, r) in enumerate(zip(got, ref)):
+            assert g.shape == r.shape and g.shape[2] == A.pixel_bytes(*fmts[i % len(fmts)])
+            nd = int((g != r).any(-1).sum())
+            assert nd == 0, f"context {i} {fmts[i % len(fmts)]}: {nd} pixels differ"
+    finally:
+        sc_g.destroy(gpu)
+        sc_o.destroy(oracle)
+
+
 def test_batch_replay_and_reuse(gpu):
     sc = BatchScene(n=24, max_side=192, tri_clip=(100, 2000), seed=33)
     sc.create(gpu)
