@@ -2,6 +2,7 @@
 profilers and quick checks).
 
     python -m pixelforge_gb300.run_workload sphere --frames 4
+    python -m pixelforge_gb300.run_workload sphere --frames 4 --format RGBA16F
     python -m pixelforge_gb300.run_workload phong --frames 2 --width 960 --height 540
     python -m pixelforge_gb300.run_workload batch --contexts 64 --repeat 2
     python -m pixelforge_gb300.run_workload fit --views 8 --iters 2
@@ -14,6 +15,10 @@ import argparse
 import sys
 
 
+FORMATS = {"RGBA8": (7, 0), "RGB8": (6, 0), "RGB565": (6, 2), "RGBA5551": (7, 3), "RGBA4444": (7, 4),
+           "RGBA16F": (7, 9), "RGBA32F": (7, 10), "LA16F": (5, 9)}
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("workload", choices=["sphere", "phong", "batch", "fit"])
@@ -24,6 +29,8 @@ def main(argv=None) -> int:
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--views", type=int, default=8)
     ap.add_argument("--iters", type=int, default=2)
+    ap.add_argument("--format", default="RGBA8", choices=sorted(FORMATS),
+                    help="format of the main buffer (sphere and phong)")
     a = ap.parse_args(argv)
 
     from . import load_library
@@ -65,7 +72,7 @@ def main(argv=None) -> int:
     from .scenes import PhongScene, SphereScene, Target
     sc = SphereScene(width=a.width, height=a.height) if a.workload == "sphere" else \
         PhongScene(width=a.width, height=a.height)
-    tg = Target(lib, sc.width, sc.height, "main")
+    tg = Target(lib, sc.width, sc.height, "main", fmt=FORMATS[a.format])
     sc.setup(lib)
     for _ in range(a.frames):
         sc.frame(lib)
@@ -73,7 +80,7 @@ def main(argv=None) -> int:
     status = lib.pfGetDeviceStatus()
     sc.teardown(lib)
     tg.close()
-    print(f"{a.workload}: {a.frames} frames at {a.width}x{a.height}, status {status}")
+    print(f"{a.workload}: {a.frames} frames at {a.width}x{a.height} ({a.format}), status {status}")
     return 1 if status else 0
 
 
