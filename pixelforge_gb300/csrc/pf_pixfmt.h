@@ -9,9 +9,11 @@
  * rectangles, pixel transfers, fog, post-processing and the framebuffer
  * functions use the scalar getter and setter (src/internal/pixel.h:52-760).
  *
- * Compiled by nvcc for the kernels and by the host compiler for the clear
- * values the host precomputes; both follow the reference's x86-64 build:
- * CVTPS2DQ / CVTTSS2SI conversions, no fused multiply-add.
+ * Compiled by nvcc for the kernels and by the host compiler for what the
+ * host does with framebuffer pixels (the clear values it precomputes, the
+ * framebuffer functions, pfReadPixels, host post-processing); both follow
+ * the reference's x86-64 build: CVTPS2DQ / CVTTSS2SI conversions, no fused
+ * multiply-add.
  */
 #ifndef PF_PIXFMT_H
 #define PF_PIXFMT_H
