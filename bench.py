@@ -158,6 +158,18 @@ def run_gpu(args):
     torch.cuda.synchronize()
     ck = clocks.stop()
     st = stats()
+    # fragments of the opaque draw alone (one frame outside the timed region),
+    # for the immediate-mode byte count: the blended draw also reads colour
+    f_all = st["fragments"] / args.steps
+    if scene.second_draw:
+        lib.pfResetStats()
+        scene.second_draw = False
+        scene.frame(lib)
+        lib.pfFinish()
+        scene.second_draw = True
+        f_opaque = stats()["fragments"]
+    else:
+        f_opaque = f_all
     if lib.pfGetDeviceStatus() != 0:
         raise RuntimeError(f"device status {lib.pfGetDeviceStatus():#x}")
     frags = st["fragments"]
@@ -167,6 +179,9 @@ def run_gpu(args):
     peak, peak_kind = _peaks()
     raster_ms = st["raster_ms"] / max(st["raster_launches"], 1)
     achieved = fb["raster"] / (raster_ms / 1e3) / 1e9
+    # immediate-mode bytes: per fragment depth read + write and colour write
+    # (12 B), 16 texel bytes (bilinear), colour read when blending (4 B)
+    immediate = f_all * (12 + 16) + (f_all - f_opaque) * 4
     # each draw copies what it references: positions, normals, uvs, indices, texture
     h2d = 2 * (scene.pos.nbytes * 2 + scene.uv.nbytes + scene.idx.nbytes + scene.tex.nbytes)
     d2h = scene.width * scene.height * 4
@@ -194,7 +209,10 @@ def run_gpu(args):
                      "launch_share_of_frame": (st["raster_ms"] / max(st["device_ms"], 1e-9)),
                      "algorithmic_bytes_per_launch": fb["raster"], "launch_ms": raster_ms,
                      "frame_algorithmic_bytes": fb["total"],
-                     "frame_frac": fb["total"] / (ms_frame / 1e3) / 1e9 / peak},
+                     "frame_frac": fb["total"] / (ms_frame / 1e3) / 1e9 / peak,
+                     "frac_of_nominal_8000_gbs": achieved / 8000.0,
+                     "immediate_mode_bytes_per_launch": immediate,
+                     "immediate_mode_frac": immediate / (raster_ms / 1e3) / 1e9 / peak},
         "clocks": ck,
     }
     if not args.no_cpu_baseline:
