@@ -376,7 +376,8 @@ typedef struct {
     PFuint64 kernel_launches;  /* all kernels launched by this library */
     PFuint64 draw_splits;      /* draw groups rendered in two passes because a tile held more
                                   sub-triangles than one bin can sort */
-    PFuint64 copy_launches;    /* of kernel_launches: draw-time copies of caller arrays */
+    PFuint64 copy_launches;    /* of kernel_launches: kernels run while draws are recorded
+                                  (the index range of an uploaded index array) */
 } PFstats;
 
 PF_API void pfGetStats(PFstats* stats);

@@ -56,16 +56,6 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);
 /* Number of SMs of the current device (cached). */
 int pfd_sm_count(void);
-/* Copy bytes of pageable caller memory at src (16-byte aligned) to dst
- * (device, room for the size rounded up to 16) with a kernel that reads the
- * caller's memory in place; only where the device walks the CPU's page
- * tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables).  The caller
- * must keep src valid until st has completed the copy. */
-cudaError_t pfd_copy_host(void *dst, const void *src, size_t bytes, cudaStream_t st);
-/* pfd_copy_host for `count` u32 indices, their largest into the page-locked
- * *hWord through the device word *dWord; complete once st is. */
-cudaError_t pfd_copy_host_max_u32(uint32_t *dst, const uint32_t *src, size_t count, unsigned *dWord, unsigned *hWord,
-                                  cudaStream_t st);
 /* The largest of n u32 values at d (device, 16-byte aligned) into the
  * page-locked *hWord, through the device word *dWord; complete once st is. */
 cudaError_t pfd_max_u32(const uint32_t *d, size_t n, unsigned *dWord, unsigned *hWord, cudaStream_t st);

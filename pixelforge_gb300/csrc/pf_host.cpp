@@ -124,6 +124,7 @@ struct Tex {
     float tx, ty;
     int wrap, filter;
     bool ownsPinned;     // colour of a pfGenFramebuffer framebuffer (pinned host memory)
+    bool depthPinned;    // its depth buffer is pinned host memory (else malloc)
     bool isMain;         // a context's main framebuffer (its depth is internal)
 };
 
@@ -266,9 +267,6 @@ struct Renderer {
     cudaStream_t upStream = nullptr;
     cudaEvent_t upDone = nullptr;
     unsigned *dMax = nullptr, *hMax = nullptr;   // largest uploaded index: device word, page-locked result
-    bool readsHostMemory = false;        // the device reads pageable memory through the CPU's page tables
-    int uploadScopes = 0;                // > 0: uploads that read caller memory in place are waited for at scope exit
-    bool uploadsInFlight = false;        // such uploads not yet waited for
 
     // device
     bool devInit = false, devOk = false;
@@ -534,7 +532,7 @@ Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, 
     Tex *x = new Tex();
     x->pixels = pixels; x->w = w; x->h = h; x->format = f; x->type = t;
     x->tx = 1.0f / (float)w; x->ty = 1.0f / (float)h;
-    x->wrap = PF_REPEAT; x->filter = PF_NEAREST; x->ownsPinned = false; x->isMain = false;
+    x->wrap = PF_REPEAT; x->filter = PF_NEAREST; x->ownsPinned = false; x->depthPinned = false; x->isMain = false;
     return x;
 }
 
@@ -678,34 +676,12 @@ constexpr size_t kUploadMin = (size_t)64 << 10;          // smaller arrays go th
 constexpr size_t kUploadBudget = (size_t)8 << 30;        // per recording; beyond it, staging with de-duplication
 constexpr size_t kUploadChunk = (size_t)64 << 20;
 
-// Wait for the uploads that read caller memory in place.
-void upload_wait(Renderer *r)
-{
-    if (!r->uploadsInFlight) return;
-    if (cudaStreamSynchronize(r->upStream) != cudaSuccess) cudaGetLastError();
-    r->uploadsInFlight = false;
-}
-
-// Within an API call that may upload several arrays (a draw): their in-place
-// copies run together and are waited for once, when the call returns.
-struct UploadScope {
-    Renderer *r;
-    explicit UploadScope(Renderer *rr) : r(rr) { r->uploadScopes++; }
-    ~UploadScope() { if (--r->uploadScopes == 0) upload_wait(r); }
-    UploadScope(const UploadScope &) = delete;
-    UploadScope &operator=(const UploadScope &) = delete;
-};
-
 // Copy `bytes` of caller memory to the device now, straight from where it
-// lies: where the device reads pageable memory through the CPU's page
-// tables, a copy kernel reads it in place (16-byte aligned sources); else
-// one cudaMemcpyAsync (on this platform either is several times faster than
-// a host copy into pinned staging followed by the upload).  The call that
-// records the draw returns only once the bytes are read -- the snapshot the
-// reference's draw-time read implies: a pageable cudaMemcpyAsync returns
-// then by itself, an in-place copy is waited for (upload_wait, at the end of
-// the enclosing UploadScope or at once without one), a copy from page-locked
-// or device memory at once.
+// lies (one cudaMemcpyAsync; on this platform that is several times faster
+// than a host copy into pinned staging followed by the upload).  From
+// pageable memory the call returns only once the bytes are read, which is
+// the snapshot the reference's draw-time read implies; from page-locked or
+// device memory it would return earlier, so the copy is waited for.
 // Returns the device reference, or -1 (the caller takes the staging path).
 // Room for `bytes` in the upload chunks, or nullptr (the caller takes the
 // staging path); upload_commit takes it.
@@ -744,15 +720,8 @@ int64_t upload(Renderer *r, const void *p, size_t bytes)
     uint8_t *dst = upload_room(r, bytes);
     if (!dst) return -1;
     const bool pageable = is_pageable(p);
-    if (pageable && r->readsHostMemory && (uintptr_t)p % 16 == 0 && pfd_copy_host(dst, p, bytes, r->upStream) == cudaSuccess) {
-        r->stats.kernel_launches += 1; r->stats.copy_launches += 1;
-        r->uploadsInFlight = true;
-        if (r->uploadScopes == 0) upload_wait(r);
-    } else {
-        cudaGetLastError();
-        if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
-        if (!pageable) cudaStreamSynchronize(r->upStream);
-    }
+    if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
+    if (!pageable) cudaStreamSynchronize(r->upStream);
     upload_commit(r, bytes);
     return dev_ref(dst);
 }
@@ -802,7 +771,6 @@ bool device_max_u32(Renderer *r, const uint32_t *d, size_t count, uint32_t &mx)
         return false;
     }
     r->stats.kernel_launches += 1; r->stats.copy_launches += 1;
-    r->uploadsInFlight = false;          // the synchronisation completed every upload before it
     mx = *r->hMax;
     return true;
 }
@@ -812,22 +780,6 @@ bool device_max_u32(Renderer *r, const uint32_t *d, size_t count, uint32_t &mx)
 int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
 {
     const size_t bytes = count * 4;
-    if (bytes >= kUploadMin && device_init(r) && r->readsHostMemory && (uintptr_t)p % 16 == 0 && is_pageable(p)) {
-        // copied in place, the largest index found by the same kernel; the
-        // wait also completes the uploads issued before it
-        uint8_t *dst = upload_room(r, bytes);
-        if (dst && max_words(r) &&
-            pfd_copy_host_max_u32((uint32_t *)dst, p, count, r->dMax, r->hMax, r->upStream) == cudaSuccess &&
-            cudaStreamSynchronize(r->upStream) == cudaSuccess) {
-            r->uploadsInFlight = false;
-            r->stats.kernel_launches += 1; r->stats.copy_launches += 1;
-            upload_commit(r, bytes);
-            mx = *r->hMax;
-            return dev_ref(dst);
-        }
-        cudaGetLastError();
-        upload_wait(r);
-    }
     if (bytes >= kUploadMin) {
         const int64_t ref = upload(r, p, bytes);
         if (ref != -1) {
@@ -1356,14 +1308,6 @@ bool device_init(Renderer *r)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->upStream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->upDone, cudaEventDisableTiming);
     if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); r->devStatus |= PF_DEVICE_NO_GPU; return false; }
-    {
-        int dev = 0, pageable = 0, hostTables = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess)
-            r->readsHostMemory = pageable == 1 && hostTables == 1;
-        cudaGetLastError();
-    }
     if (!r->counters.ensure(sizeof(PFDevCounters))) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
     if (cudaMallocHost((void **)&r->hostCounters, sizeof(PFDevCounters)) != cudaSuccess) {
         cudaGetLastError(); r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false;
@@ -2494,7 +2438,6 @@ static void assemble_arrays(Ctx *c, PFdrawmode mode, PFsizei count, const void *
 static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first)
 {
     Ctx *c = G;
-    UploadScope uploads(c->rend);        // the arrays' copies are waited for once, on return
     update_matrices(c, !(mode == PF_POINTS || mode == PF_LINES));     // pfBegin inside the draw
     c->drawMode = mode; c->vcount = 0;
     c->stateDirty = true;
@@ -2513,8 +2456,8 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
         return;
     }
 
-    // the segment and its draw state first: the texture's copy then runs
-    // while the indices are copied and their range is found
+    // the segment and its draw state first: the texture's copy is then
+    // under way while the indices are copied and their range is found
     const int si = new_segment(c, PF_SRC_ARRAYS, mode == PF_TRIANGLES ? PF_ITEMS_TRIS : PF_ITEMS_EXPLICIT);
 
     // indices: stage as u32 and find the vertex range
@@ -3185,6 +3128,7 @@ PFframebuffer pfGenFramebuffer(PFsizei w, PFsizei h, PFpixelformat f, PFdatatype
     bool zp = cudaMallocHost((void **)&z, n * 4) == cudaSuccess;
     if (!zp) { cudaGetLastError(); z = (float *)std::malloc(n * 4); }
     for (size_t i = 0; i < n; i++) z[i] = FLT_MAX;
+    tx->depthPinned = zp;
     fb.texture = tx; fb.zbuffer = z;
     return fb;
 }
@@ -3197,7 +3141,10 @@ void pfDeleteFramebuffer(PFframebuffer *fb)
     if (t) {
         drop_mirror(t);
         if (t->ownsPinned) cudaFreeHost(t->pixels); else std::free(t->pixels);
-        if (fb->zbuffer) { if (cudaFreeHost(fb->zbuffer) != cudaSuccess) { cudaGetLastError(); std::free(fb->zbuffer); } }
+        if (fb->zbuffer) {
+            if (t->depthPinned) { if (cudaFreeHost(fb->zbuffer) != cudaSuccess) cudaGetLastError(); }
+            else std::free(fb->zbuffer);
+        }
         delete t;
     }
     fb->texture = nullptr; fb->zbuffer = nullptr;

@@ -1748,33 +1748,6 @@ __global__ void k_hook(void *color, uint32_t fmt, const float *depth, size_t n, 
     }
 }
 
-// Copy of n16 16-byte blocks of caller memory that the GPU reads in place
-// through the CPU's page tables (the host's source is 16-byte aligned, so
-// the last, partial block lies in the page of the array's last byte).
-__global__ void k_copy_host(uint4 *dst, const uint4 *src, size_t n16)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = src[i];
-}
-
-// The same for u32 indices, also folding the largest of the first `count`
-// (the last block may carry bytes past the array) into *out.
-__global__ void k_copy_host_max_u32(uint4 *dst, const uint4 *src, size_t n16, size_t count, unsigned *out)
-{
-    unsigned m = 0;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x) {
-        const uint4 v = src[i];
-        dst[i] = v;
-        const size_t e = i * 4;
-        m = max(m, v.x);
-        if (e + 1 < count) m = max(m, v.y);
-        if (e + 2 < count) m = max(m, v.z);
-        if (e + 3 < count) m = max(m, v.w);
-    }
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
-}
-
 // The largest of n u32 indices (already on the device, 16-byte aligned):
 // per-warp maxima folded into *out with one atomic per warp.
 __global__ void k_max_u32(const uint32_t *src, size_t n, unsigned *out)
@@ -1908,26 +1881,4 @@ cudaError_t pfd_max_u32(const uint32_t *d, size_t n, unsigned *dWord, unsigned *
     return cudaMemcpyAsync(hWord, dWord, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
 }
 
-cudaError_t pfd_copy_host(void *dst, const void *src, size_t bytes, cudaStream_t st)
-{
-    const size_t n16 = (bytes + 15) / 16;
-    if (n16 == 0) return cudaSuccess;
-    const unsigned grid = (unsigned)min((size_t)pfd_sm_count() * 4, (n16 + 255) / 256);
-    k_copy_host<<<grid, 256, 0, st>>>((uint4 *)dst, (const uint4 *)src, n16);
-    return cudaGetLastError();
-}
 
-cudaError_t pfd_copy_host_max_u32(uint32_t *dst, const uint32_t *src, size_t count, unsigned *dWord, unsigned *hWord,
-                                  cudaStream_t st)
-{
-    const size_t n16 = (count * 4 + 15) / 16;
-    cudaError_t e = cudaMemsetAsync(dWord, 0, sizeof(unsigned), st);
-    if (e != cudaSuccess) return e;
-    if (n16) {
-        const unsigned grid = (unsigned)min((size_t)pfd_sm_count() * 4, (n16 + 255) / 256);
-        k_copy_host_max_u32<<<grid, 256, 0, st>>>((uint4 *)dst, (const uint4 *)src, n16, count, dWord);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    return cudaMemcpyAsync(hWord, dWord, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-}
