@@ -195,3 +195,37 @@ def test_framebuffer_formats_refused(lib, oracle):
         for pair, null, err in res:
             assert null and err == A.PF_INVALID_ENUM, pair
     assert len(FB_FORMATS) == 19 and all(A.pixel_bytes(*p) for p in FB_FORMATS)
+
+
+def test_framebuffer_pixel_functions_every_format(lib, oracle):
+    """pfSetFramebufferPixel / pfGetFramebufferPixel and the stored bytes of
+    a framebuffer object of every accepted format, library against oracle
+    (host-side: the scalar setter and getter of pf_pixfmt.h, no device)."""
+    from fbscenes import FB_FORMATS
+    rng = np.random.default_rng(77)
+    cols = rng.integers(0, 256, (64, 4)).astype(np.uint8)
+    for fmt in FB_FORMATS:
+        res = []
+        for lb in (lib, oracle):
+            buf = np.zeros((4, 4, 4), np.uint8)
+            ctx = lb.pfCreateContext(buf.ctypes.data_as(C.c_void_p), 4, 4, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            lb.pfMakeCurrent(ctx)
+            fb = lb.pfGenFramebuffer(8, 8, *fmt)
+            ref = C.pointer(fb)
+            got = []
+            for i, c in enumerate(cols):
+                lb.pfSetFramebufferPixel(ref, i % 8, i // 8, A.PFcolor(*map(int, c)))
+                g = lb.pfGetFramebufferPixel(ref, i % 8, i // 8)
+                got.append((g.r, g.g, g.b, g.a))
+            px = lb.raw("pfGetTexturePixels")
+            px.restype = C.c_void_p
+            px.argtypes = [C.c_void_p] * 5
+            base = px(fb.texture, None, None, None, None)
+            raw = np.ctypeslib.as_array(C.cast(base, C.POINTER(C.c_uint8)), shape=(64 * A.pixel_bytes(*fmt),)).copy()
+            res.append((np.array(got), raw, lb.pfGetError()))
+            lb.pfDeleteFramebuffer(ref)
+            lb.pfDeleteContext(ctx)
+        (g1, r1, e1), (g2, r2, e2) = res
+        assert e1 == e2 == A.PF_NO_ERROR, fmt
+        assert np.array_equal(r1, r2), f"{fmt}: stored bytes differ"
+        assert np.array_equal(g1, g2), f"{fmt}: read-back colours differ"
