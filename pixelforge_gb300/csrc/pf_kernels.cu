@@ -1677,7 +1677,9 @@ __global__ void k_clear(void *color, uint32_t fmt, float *depth, size_t n, uint4
     const size_t aligned = n - (n % 8);
     const uint32_t craw[4] = { cc.x, cc.y, cc.z, cc.w };
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (i < 8) continue;
+        // the vector loop starts at pixel 8; the tail starts at `aligned`,
+        // which is 0 below 8 pixels (then every pixel takes pixel 0's value)
+        if (i < aligned ? i < 8 : i == 0) continue;
         if (fmt == PFF_RGBA8) {
             uint32_t *c32 = (uint32_t *)color;
             if (i < aligned) c32[i] = cc.x; else c32[i] = c32[0];

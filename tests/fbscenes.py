@@ -181,3 +181,31 @@ def fb_frame(seed: int):
         out = run_fb(lib, fb_case(seed), device_hook=False)
         return Frame(out["color"], out.get("depth"))
     return run
+
+
+# ragged framebuffers: fewer than 8 pixels (pfClear's vector loop does not
+# run and its tail copies pixel 0 over every pixel), a single row or column,
+# sides that are no multiple of the 16-pixel tile
+TINY_SIZES = [(1, 1), (2, 3), (7, 1), (1, 9), (17, 5), (33, 2), (5, 31)]
+TINY_FORMATS = [(A.PF_RGBA, 0), (A.PF_RGB, 0), (A.PF_RGBA, A.PF_HALF_FLOAT), (A.PF_BGRA, A.PF_FLOAT),
+                (A.PF_RGB, 2), (A.PF_RGBA, 4)]
+
+
+def tiny_case(k: int) -> dict:
+    """Case k of the ragged-size set: every size with every format of
+    TINY_FORMATS, except the packed 16-bit formats below 10 pixels (there the
+    reference's pfClear tail, stepped by components x 2 bytes, writes pixels
+    inside the buffer at 3-4x their index; not reproduced)."""
+    cases = []
+    for (W, H) in TINY_SIZES:
+        for fmt in TINY_FORMATS:
+            if fmt[1] in (2, 3, 4) and W * H < 10:
+                continue
+            cases.append((W, H, fmt))
+    W, H, fmt = cases[k]
+    r = np.random.default_rng(2000 + k)
+    return dict(seed=2000 + k, fmt=fmt, W=W, H=H, target=["main", "fbo"][k % 2],
+                depth=int(r.integers(-1, 6)), blend=int(r.integers(-1, 8)))
+
+
+TINY_CASES = sum(1 for (W, H) in TINY_SIZES for f in TINY_FORMATS if not (f[1] in (2, 3, 4) and W * H < 10))

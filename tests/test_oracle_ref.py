@@ -80,3 +80,15 @@ def test_oracle_equals_reference_framebuffer_formats(oracle, ref_shim, seed):
     for k in ("color", "depth", "read", "get"):
         if k in a:
             assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), f"{case}: {k} differs"
+
+
+def test_oracle_equals_reference_ragged_framebuffers(oracle, ref_shim):
+    """Framebuffers of 1 to 165 pixels (single rows and columns, fewer pixels
+    than pfClear's 8-wide vector) in six formats: raw bytes bit-exact."""
+    from fbscenes import TINY_CASES, run_fb, tiny_case
+    for k in range(TINY_CASES):
+        case = tiny_case(k)
+        a, b = run_fb(oracle, case, device_hook=False), run_fb(ref_shim, case, device_hook=False)
+        for key in ("color", "depth", "read", "get"):
+            if key in a:
+                assert np.array_equal(a[key].view(np.uint8), b[key].view(np.uint8)), f"{case}: {key} differs"

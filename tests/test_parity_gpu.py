@@ -320,3 +320,18 @@ def test_draw_time_snapshot_of_large_arrays(gpu, oracle, misalign):
     assert gpu.pfGetDeviceStatus() == 0
     assert (ref.depth < 1e30).sum() > 10000
     assert_parity(got, ref, exact_color=True, label=f"snapshot misalign={misalign}")
+
+
+def test_ragged_framebuffers(gpu, oracle):
+    """Framebuffers of 1 to 165 pixels in six formats (main buffers and
+    framebuffer objects): raw pixels, depth and reads bit-exact against the
+    oracle."""
+    from fbscenes import TINY_CASES, run_fb, tiny_case
+    for k in range(TINY_CASES):
+        case = tiny_case(k)
+        a, b = run_fb(gpu, case), run_fb(oracle, case)
+        assert gpu.pfGetDeviceStatus() == 0
+        for key in ("color", "depth", "read", "get"):
+            if key in b:
+                x, y = a[key].view(np.uint8), b[key].view(np.uint8)
+                assert np.array_equal(x, y), f"{case}: {key} differs in {int((x != y).sum())} bytes"
