@@ -335,3 +335,53 @@ def test_ragged_framebuffers(gpu, oracle):
             if key in b:
                 x, y = a[key].view(np.uint8), b[key].view(np.uint8)
                 assert np.array_equal(x, y), f"{case}: {key} differs in {int((x != y).sum())} bytes"
+
+
+def test_large_framebuffer_and_empty_draws(gpu, oracle):
+    """An 8192x4096 framebuffer object (524,288 tiles): clear, blended and
+    depth-tested triangles, empty draws (a pfBegin/pfEnd without vertices,
+    pfDrawArrays of 0 and of 2 vertices), points; colour and depth bit-exact
+    against the oracle."""
+    import ctypes as C
+    from pixelforge_gb300.scenes import Target, _ptr
+
+    def run(lib):
+        r = np.random.default_rng(4242)
+        tg = Target(lib, 8192, 4096, "fbo")
+        try:
+            lib.pfClearColor(10, 20, 30, 255)
+            lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+            lib.pfDisable(A.PF_CULL_FACE)
+            lib.pfEnable(A.PF_DEPTH_TEST)
+            lib.pfEnable(A.PF_BLEND)
+            lib.pfBlendFunc(A.PF_BLEND_ALPHA)
+            lib.pfBegin(A.PF_TRIANGLES)
+            lib.pfEnd()                                        # no vertices
+            pos = r.uniform(-1, 1, (6, 3)).astype(np.float32)
+            lib.pfEnable(A.PF_VERTEX_ARRAY)
+            lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(pos))
+            lib.pfDrawArrays(A.PF_TRIANGLES, 0, 0)             # nothing
+            lib.pfDrawArrays(A.PF_TRIANGLES, 0, 2)             # less than a triangle
+            lib.pfDisable(A.PF_VERTEX_ARRAY)
+            lib.pfBegin(A.PF_TRIANGLES)
+            for _ in range(24):
+                c = r.integers(0, 256, 4)
+                lib.pfColor4ub(int(c[0]), int(c[1]), int(c[2]), int(r.integers(100, 256)))
+                for _k in range(3):
+                    p = r.uniform(-1.1, 1.1, 2)
+                    lib.pfVertex3f(float(p[0]) * 0.6, float(p[1]) * 0.6, float(r.uniform(-0.9, 0.9)))
+            lib.pfEnd()
+            lib.pfPointSize(3.0)
+            lib.pfBegin(A.PF_POINTS)
+            for _ in range(50):
+                p = r.uniform(-1, 1, 2)
+                lib.pfVertex2f(float(p[0]), float(p[1]))
+            lib.pfEnd()
+            return tg.finish()
+        finally:
+            tg.close()
+
+    got, ref = run(gpu), run(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert (ref.depth < 1e30).sum() > 1_000_000
+    assert_parity(got, ref, exact_color=True, label="8192x4096")
