@@ -196,9 +196,9 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32+u8",
         "data": "synthetic (seeded UV sphere and noise texture)",
-        "config": {"workload": SPHERE_WORKLOAD,
-                   "fragments_per_frame": frags / args.steps,
-                   "l2": "flushed between frames (512 MiB write)", "parallelism": "single GPU"},
+        "config": SPHERE_CONFIG,
+        "parallelism": "one GPU per rank (replicas)",
+        "fragments_per_frame": frags / args.steps,
         "e2e": {"value": frags / wall, "unit": "fragments/s", "ms_per_step": wall * 1e3 / args.steps,
                 "record_ms_per_step": rec * 1e3 / args.steps,
                 "flush_ms_per_step": (wall - rec) * 1e3 / args.steps,
@@ -218,6 +218,8 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, samples=2)
     tg.close()
+    if not args.no_soup:
+        out["soup256"] = run_soup(lib)
     if not args.no_phong:
         out["phong"] = run_phong(lib)
     if not args.no_formats:
@@ -231,6 +233,71 @@ def run_gpu(args):
 
 SPHERE_WORKLOAD = ("sphere1080: 1920x1080 textured Gouraud UV sphere 256x128, two draws "
                    "(opaque + alpha 0.5 scaled 1.05), 1024^2 bilinear repeat texture")
+# identical in both arms: the same scene, frames and L2 handling
+SPHERE_CONFIG = {"workload": SPHERE_WORKLOAD, "frame": "clear + opaque draw + blended draw without depth writes",
+                 "l2": "flushed between frames (512 MiB device write); inputs larger than L2 on the host arm"}
+
+
+def _soup_frames(lib, steps: int, warmup: int, timing: bool):
+    """Frames of the 256x256 soup (immediate mode, 2,000 triangles) into a
+    main buffer: the recording time (the pf* calls, made from Python), the
+    flush time, and the library's statistics."""
+    from pixelforge_gb300 import abi as A
+    from pixelforge_gb300.scenes import SoupScene, Target
+    sc = SoupScene()
+    tg = Target(lib, sc.width, sc.height, "main")
+    if timing:
+        lib.pfEnableTiming(True)
+    for _ in range(warmup):
+        sc.record(lib)
+        if lib.has("pfFinish"):
+            lib.pfFinish()
+    if lib.has("pfResetStats"):
+        lib.pfResetStats()
+    rec = flush = 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        sc.record(lib)
+        t1 = time.perf_counter()
+        if lib.has("pfFinish"):
+            lib.pfFinish()
+        else:
+            lib.pfReadPixels(0, 0, 1, 1, A.PF_RGBA, A.PF_UNSIGNED_BYTE, tg.main.ctypes.data)
+        t2 = time.perf_counter()
+        rec += t1 - t0
+        flush += t2 - t1
+    st = None
+    if lib.has("pfGetStats"):
+        st = A.PFstats()
+        lib.pfGetStats(st)
+    status = lib.pfGetDeviceStatus() if lib.has("pfGetDeviceStatus") else 0
+    tg.close()
+    if status != 0:
+        raise RuntimeError(f"device status {status:#x}")
+    return rec, flush, st
+
+
+def run_soup(lib, warmup: int = 3, steps: int = 20) -> dict:
+    """The small plain workload (256x256, 2,000-triangle immediate-mode soup,
+    Gouraud colours, depth LESS, the reference's default cull and
+    projection): device ms/frame and fragments/s on the GPU, the recording
+    and flush time through the C ABI, and the same frames on the reference's
+    CPU path (the oracle port or the reference build) on the host cores."""
+    rec, flush, st = _soup_frames(lib, steps, warmup, True)
+    out = {"workload": "soup256: 256x256 RGBA8 + FP32 depth, 2,000-triangle seeded soup via pfBegin(PF_TRIANGLES), "
+                       "default projection, Gouraud colours, depth LESS, back faces culled",
+           "ms_per_frame": st.device_ms / steps, "fragments_per_frame": st.fragments / steps,
+           "fragments_per_s": st.fragments / (st.device_ms / 1e3),
+           "record_ms_per_frame": rec * 1e3 / steps, "flush_ms_per_frame": flush * 1e3 / steps,
+           "note": "recording is 12,000 pf* calls per frame made through ctypes from Python"}
+    cpu, kind = _reference_lib()
+    crec, cflush, cst = _soup_frames(cpu, steps, 1, False)
+    cms = (crec + cflush) * 1e3 / steps
+    cfr = (cst.fragments / steps) if cst is not None else out["fragments_per_frame"]
+    out["cpu"] = {"kind": kind, "ms_per_frame": cms, "fragments_per_s": cfr / (cms / 1e3),
+                  "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                  "sample": f"{steps} frames through the same Python recording loop, {platform.machine()} host"}
+    return out
 
 
 def run_phong(lib, warmup: int = 2, steps: int = 5) -> dict:
@@ -441,30 +508,36 @@ def _reference_lib():
     return PixelForgeLib(str(ROOT / "oracle" / "_build" / "libpfref.so")), "port"
 
 
-def cpu_baseline(args, samples: int = 2) -> dict:
+def cpu_baseline(args, samples: int = 2, warmup: int = 1) -> dict:
+    """The reference's CPU path on this host's cores, on the GPU arm's scene:
+    the second draw runs without depth writes through pfDepthMask, which
+    the oracle port has; the reference's own build (x86-64 only) has no
+    depth mask and writes depth there (same fragments, same work)."""
     from pixelforge_gb300.scenes import SphereScene, Target
     lib, kind = _reference_lib()
-    scene = SphereScene(depth_mask_off=False)
+    scene = SphereScene(depth_mask_off=lib.has("pfDepthMask"))
     tg = Target(lib, scene.width, scene.height, "main")
     scene.setup(lib)
-    scene.frame(lib)                      # warm caches
+    for _ in range(max(1, warmup)):       # warm caches
+        scene.frame(lib)
+    if lib.has("pfResetStats"):
+        lib.pfResetStats()
     t0 = time.perf_counter()
-    frags = 0
     for _ in range(samples):
         scene.frame(lib)
     dt = time.perf_counter() - t0
     frags = None
-    if lib.has("pfGetStats"):
+    if lib.has("pfGetStats") and lib.has("pfResetStats"):
         from pixelforge_gb300 import abi as A
         s = A.PFstats()
         lib.pfGetStats(s)
-        frags = s.fragments / (samples + 1)
+        frags = s.fragments / samples
     tg.close()
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     fr = frags if frags else 846563.0
     return {"value": fr * samples / dt, "unit": "fragments/s", "cores": threads, "kind": kind,
-            "ms_per_frame": dt * 1e3 / samples,
-            "sample": f"{samples} frames of the sphere1080 workload after one warm-up frame, "
+            "ms_per_frame": dt * 1e3 / samples, "fragments_per_frame": fr,
+            "sample": f"{samples} frames of the sphere1080 workload after {max(1, warmup)} warm-up frame(s), "
                       f"{platform.machine()} host, OMP_NUM_THREADS={threads}"}
 
 
@@ -472,12 +545,13 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    cb = cpu_baseline(args, samples=max(1, min(args.steps, 5)))
+    cb = cpu_baseline(args, samples=max(1, args.steps), warmup=max(1, args.warmup))
     return {"impl": "reference", "metric": "fragments/s", "value": cb["value"], "unit": "fragments/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": cb["ms_per_frame"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+u8", "data": "synthetic (seeded UV sphere and noise texture)",
-            "config": {"workload": SPHERE_WORKLOAD, "parallelism": "host CPU cores"},
+            "config": SPHERE_CONFIG, "parallelism": "host CPU cores",
+            "fragments_per_frame": cb["fragments_per_frame"],
             "cpu_baseline": {k: cb[k] for k in ("kind", "cores", "sample", "value", "unit")},
             "e2e": {"value": cb["value"], "unit": "fragments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -493,6 +567,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the fitting-iteration measurement")
     ap.add_argument("--no-phong", action="store_true", help="skip the Phong 1080p measurement")
     ap.add_argument("--no-formats", action="store_true", help="skip the framebuffer-format measurement")
+    ap.add_argument("--no-soup", action="store_true", help="skip the 256x256 soup measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -436,11 +436,12 @@ PF_API PFfloat   pfgbReplay(PFuint n);
  *
  * pfgbDrawTrianglesStatic renders `ntris` triangles straight into device
  * colour (RGBA8, width*height words) and depth (float) buffers that the
- * caller owns, and allocates nothing: for callers that cannot call
- * cudaMalloc -- inside someone else's stream capture, on a real-time frame
- * path where an allocation may block and synchronise the device, or in a
- * host that only lends out pre-allocated buffers.  It runs the same kernels
- * as the pf* API and gives the same pixels as
+ * caller owns, and allocates nothing.  It is for callers that cannot call
+ * cudaMalloc: a real-time frame path, where an allocation may block and
+ * synchronise the whole device, or an engine or plugin host that owns all
+ * device memory through its own pool and only lends out pre-allocated
+ * buffers.  It runs the same kernels as the pf* API and gives the same
+ * pixels as
  *     pfMatrixMode(PF_PROJECTION); pfLoadIdentity(); pfMultMatrixf(mvp);
  *     pfMatrixMode(PF_MODELVIEW);  pfLoadIdentity();
  *     depthFunc < 0 ? pfDisable(PF_DEPTH_TEST) : pfEnable + pfDepthFunc(depthFunc);
@@ -451,7 +452,9 @@ PF_API PFfloat   pfgbReplay(PFuint n);
  *
  * positions: device, 9 floats per triangle (object-space x, y, z of its 3
  * vertices); colors: device, one packed RGBA8 word per vertex; mvp: host,
- * 16 floats in the reference's layout; stream: a cudaStream_t or NULL.
+ * 16 floats in the reference's layout; stream: a cudaStream_t or NULL.  The
+ * call reads its overflow counters back and waits for `stream` before it
+ * returns.
  *
  * Its intermediates live in one file-scope __device__ array of
  * PFGB_STATIC_SCRATCH_BYTES that every GPU loading the library holds until
@@ -461,16 +464,18 @@ PF_API PFfloat   pfgbReplay(PFuint n);
  * that overlap on the GPU (other streams, other threads) race and corrupt
  * each other, so issue them one after another.  Returns 0, or a negative
  * PFGB_STATIC_E_* code; sizes beyond the limits below are rejected. */
-#define PFGB_STATIC_MAX_TRIANGLES   8192
+#define PFGB_STATIC_MAX_TRIANGLES   8192      /* culling off: 16,384 face items */
 #define PFGB_STATIC_MAX_WIDTH       512
 #define PFGB_STATIC_MAX_HEIGHT      512
 #define PFGB_STATIC_BIN_CAPACITY    2048      /* sub-triangles per 16x16 tile */
-#define PFGB_STATIC_SCRATCH_BYTES   15210240  /* 14.5 MiB */
+#define PFGB_STATIC_CLIP_CAPACITY   32768     /* extra sub-triangles of clipped triangles */
+#define PFGB_STATIC_SCRATCH_BYTES   16258816  /* 15.5 MiB */
 #define PFGB_STATIC_E_TOO_LARGE     (-1)      /* more triangles or pixels than the limits */
 #define PFGB_STATIC_E_INVALID       (-2)      /* null pointer or invalid mode */
 #define PFGB_STATIC_E_CUDA          (-3)      /* a CUDA call failed */
-#define PFGB_STATIC_E_CAPACITY      (-4)      /* a tile needed more than PFGB_STATIC_BIN_CAPACITY entries;
-                                                 the buffers were not modified */
+#define PFGB_STATIC_E_CAPACITY      (-4)      /* a tile needed more than PFGB_STATIC_BIN_CAPACITY entries,
+                                                 or clipping more than PFGB_STATIC_CLIP_CAPACITY
+                                                 sub-triangles; the buffers were not modified */
 PF_API int pfgbDrawTrianglesStatic(const float* positions, const uint32_t* colors, uint32_t ntris,
                                    const float* mvp, uint32_t* color, float* depth,
                                    uint32_t width, uint32_t height, int depthFunc, int cullMode,

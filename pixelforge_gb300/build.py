@@ -41,7 +41,7 @@ CUDA_UNITS = ("pf_kernels.cu", "pf_noalloc.cu", "pf_grad.cu")
 
 def _sources():
     return [*(CSRC / u for u in CUDA_UNITS), CSRC / "pf_host.cpp", CSRC / "pf_layout.h", CSRC / "pf_device.h",
-            CSRC / "pf_common.cuh", INCLUDE / "pixelforge.h", INCLUDE / "pixelforge_grad.h", Path(__file__)]
+            CSRC / "pf_common.cuh", CSRC / "pf_pixfmt.h", INCLUDE / "pixelforge.h", INCLUDE / "pixelforge_grad.h", Path(__file__)]
 
 
 def up_to_date() -> bool:

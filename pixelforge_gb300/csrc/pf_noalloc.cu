@@ -1,22 +1,24 @@
 // pf_noalloc.cu -- pfgbDrawTrianglesStatic: the triangle pipeline without any
 // allocation.
 //
-// Some callers cannot allocate device memory: code that runs inside a CUDA
-// graph being captured by someone else, a real-time renderer that must not
-// call cudaMalloc on its frame path (it can block and synchronise the
-// device), or a host that only hands out pre-allocated buffers.  For them
-// this entry point renders a soup of smooth-coloured triangles straight
-// into device colour and depth buffers the caller owns,
-// with the same kernels as the pf* API (k_vertex, k_items, k_raster), and
-// keeps every intermediate -- transformed vertices, set-up sub-triangles,
-// tile bins, counters -- in one file-scope __device__ array of fixed size.
+// Some callers cannot allocate device memory.  A real-time renderer must not
+// call cudaMalloc on its frame path, because an allocation can block and
+// synchronise the whole device; an engine or plugin host that owns all
+// device memory through its own pool only lends out pre-allocated buffers.
+// For them this entry point renders a soup of smooth-coloured triangles
+// straight into device colour and depth buffers the caller owns, with the
+// same kernels as the pf* API (k_vertex, k_items, k_raster), and keeps every
+// intermediate -- transformed vertices, set-up sub-triangles, tile bins,
+// counters -- in one file-scope __device__ array of fixed size.
 //
 // That array exists once per GPU that loads the library and stays allocated
 // until the process exits.  Every call uses it, so two calls that run at the
 // same time on the GPU (on different streams, or from different threads)
 // race on it and corrupt each other's results; issue calls one after another
 // on one stream.  A call leaves its intermediates in the array; everything a
-// call needs zeroed (bin counters, device counters) it clears itself.
+// call needs zeroed (bin counters, device counters) it clears itself.  The
+// call reads the device counters back and waits for its stream before it
+// returns.
 
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -32,7 +34,9 @@ constexpr uint32_t kMaxTris = PFGB_STATIC_MAX_TRIANGLES;
 constexpr uint32_t kMaxW = PFGB_STATIC_MAX_WIDTH, kMaxH = PFGB_STATIC_MAX_HEIGHT;
 constexpr uint32_t kMaxTiles = ((kMaxW + PF_TILE - 1) / PF_TILE) * ((kMaxH + PF_TILE - 1) / PF_TILE);
 constexpr uint32_t kBinCap = PFGB_STATIC_BIN_CAPACITY;
-constexpr uint32_t kPoolCap = 4 * kMaxTris;
+// culling off sets up every triangle twice (FRONT then BACK face items)
+constexpr uint32_t kMaxItems = 2 * kMaxTris;
+constexpr uint32_t kPoolCap = PFGB_STATIC_CLIP_CAPACITY;
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffState = 0;
@@ -41,7 +45,7 @@ constexpr size_t kOffCnt = align256(kOffSeg + sizeof(PFSegment));
 constexpr size_t kOffTarget = align256(kOffCnt + sizeof(PFDevCounters));
 constexpr size_t kOffVout = align256(kOffTarget + sizeof(PFTarget));
 constexpr size_t kOffPrims = align256(kOffVout + sizeof(PFVertexOut) * 3 * (size_t)kMaxTris);
-constexpr size_t kOffPool = align256(kOffPrims + sizeof(PFPrim) * (size_t)kMaxTris);
+constexpr size_t kOffPool = align256(kOffPrims + sizeof(PFPrim) * (size_t)kMaxItems);
 constexpr size_t kOffPh = align256(kOffPool + sizeof(PFPrim) * (size_t)kPoolCap);
 constexpr size_t kOffBinCount = align256(kOffPh + sizeof(PFPrimPhong));
 constexpr size_t kOffBins = align256(kOffBinCount + sizeof(uint32_t) * (size_t)kMaxTiles);

@@ -182,6 +182,8 @@ def test_static_entry_rejects_oversize_without_device(lib):
     assert f(dummy, dummy, 8193, dummy, dummy, dummy, 64, 64, 0, 0, None) == -1    # too many triangles
     assert f(dummy, dummy, 1, dummy, dummy, dummy, 513, 64, 0, 0, None) == -1      # too wide
     assert f(None, dummy, 1, dummy, dummy, dummy, 64, 64, 0, 0, None) == -2        # no positions
+    assert f(dummy, dummy, 1, dummy, dummy, dummy, 64, 64, 6, 0, None) == -2       # depth function
+    assert f(dummy, dummy, 1, dummy, dummy, dummy, 64, 64, 2, 3, None) == -2       # cull mode
 
 
 def test_framebuffer_formats_refused(lib, oracle):
