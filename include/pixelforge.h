@@ -467,9 +467,9 @@ PF_API PFfloat   pfgbReplay(PFuint n);
 #define PFGB_STATIC_MAX_TRIANGLES   8192      /* culling off: 16,384 face items */
 #define PFGB_STATIC_MAX_WIDTH       512
 #define PFGB_STATIC_MAX_HEIGHT      512
-#define PFGB_STATIC_BIN_CAPACITY    2048      /* sub-triangles per 16x16 tile */
+#define PFGB_STATIC_BIN_CAPACITY    512       /* sub-triangles per 8x8 tile */
 #define PFGB_STATIC_CLIP_CAPACITY   32768     /* extra sub-triangles of clipped triangles */
-#define PFGB_STATIC_SCRATCH_BYTES   16258816  /* 15.5 MiB */
+#define PFGB_STATIC_SCRATCH_BYTES   16353024  /* 15.6 MiB */
 #define PFGB_STATIC_E_TOO_LARGE     (-1)      /* more triangles or pixels than the limits */
 #define PFGB_STATIC_E_INVALID       (-2)      /* null pointer or invalid mode */
 #define PFGB_STATIC_E_CUDA          (-3)      /* a CUDA call failed */

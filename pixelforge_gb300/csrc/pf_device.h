@@ -32,18 +32,16 @@ struct PFBatchLaunch {
     uint32_t poolCap;
     uint32_t *binCount;       /* totalTiles */
     uint32_t *tileList;       /* 1 + PF_HEAVY_LEVELS lists of listStride entries: the tiles with a
-                                 non-empty bin, then those whose bin reached each heavy level;
-                                 NULL: queue every tile */
+                                 non-empty bin, then those whose bin reached each heavy level */
     uint32_t listStride;
     uint32_t *bins;           /* totalTiles * cap */
     uint32_t cap;
     const PFTarget *targets;  /* device */
     int nTargets;
     uint32_t totalTiles;
-    int rasterCtasPerSM;      /* persistent raster grid: SMs x this */
-    int chunk;                /* records per raster chunk: 64, or 32 (the default) */
+    int rasterCtasPerSM;      /* persistent raster grid: SMs x this, at most as many as fit (0: as many as fit) */
     int anyPhong;             /* some state of the launch lights per fragment */
-    int generic;              /* some target is not RGBA / unsigned byte (32-record chunks) */
+    int generic;              /* some target is not RGBA / unsigned byte */
     PFDevCounters *cnt;
     uint32_t command;
 };
@@ -51,6 +49,9 @@ struct PFBatchLaunch {
 /* k_vertex also zeroes the tile bin counters and the batch counters. */
 cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st);
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
+/* Bins that reached 128 entries put back into submission order (k_items
+ * appends in atomic order; shorter bins are sorted by the raster). */
+cudaError_t pfd_launch_binsort(const PFBatchLaunch &L, cudaStream_t st);
 /* Persistent tile raster over every tile of every target; each target's
  * clearMode says how its tiles start (see PFTarget). */
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);

@@ -273,7 +273,7 @@ struct Renderer {
     cudaStream_t stream = nullptr;
     DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters;
     uint32_t cap = 256, poolCap = 4096;
-    int rasterCtasPerSM = 4;
+    int rasterCtasPerSM = 0;                // 0: as many raster CTAs per SM as fit
     PFDevCounters *hostCounters = nullptr;
     PFstats stats{};
     PFuint devStatus = 0;
@@ -1745,16 +1745,13 @@ bool flush(Renderer *r)
                 L.listStride = (uint32_t)(((size_t)maxTiles + 31) & ~(size_t)31);
                 L.tileList = (uint32_t *)r->binCount.p + L.listStride;
                 L.rasterCtasPerSM = r->rasterCtasPerSM;
-                // long bins of small triangles (more than 24 items per tile on
-                // average) take 64-record chunks; bigger triangles, whose
-                // bins need more capacity, the smaller footprint of 32
-                L.chunk = (uint64_t)L.nItems >= 24ull * L.totalTiles ? 64 : 32;
                 L.anyPhong = anyPhong ? 1 : 0;
                 L.cnt = dcnt;
                 rop.L = L;
-                r->stats.kernel_launches += 3;
+                r->stats.kernel_launches += 4;
                 e = pfd_launch_vertex(L, st);
                 if (e == cudaSuccess) e = pfd_launch_items(L, st);
+                if (e == cudaSuccess) e = pfd_launch_binsort(L, st);
                 if (r->timing) {
                     if (r->rasterEv.size() <= nRaster) {
                         cudaEvent_t ev0, ev1; cudaEventCreate(&ev0); cudaEventCreate(&ev1);
@@ -1863,6 +1860,7 @@ float replay(Renderer *r, uint32_t n)
             else {
                 pfd_launch_vertex(op.L, st);
                 pfd_launch_items(op.L, st);
+                pfd_launch_binsort(op.L, st);
                 pfd_launch_raster(op.L, st);
             }
         }

@@ -404,11 +404,11 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
     __shared__ __align__(16) PFDrawState sState;
     __shared__ int sUniform;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    asm volatile("griddepcontrol.wait;" ::: "memory");   // the previous kernel of the stream is done
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // (no-op unless launched programmatically serialized)
     if (cnt->abortCommand != 0xffffffffu) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
     if (g == 0) {
-        cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0;
+        cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0; cnt->sortQueue = 0;
         cnt->tileListCount = 0;
         for (int l = 0; l < PF_HEAVY_LEVELS; l++) cnt->heavyCount[l] = 0;
     }
@@ -489,7 +489,7 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
 
 struct BinArgs {
     uint32_t *binCount;
-    uint32_t *tileList;        // the raster work lists (NULL: not listed)
+    uint32_t *tileList;        // the raster work lists
     uint32_t listStride;
     uint32_t *bins;
     uint32_t cap;
@@ -551,7 +551,6 @@ __device__ __forceinline__ uint32_t heavy_level(uint32_t count)
 
 __device__ __forceinline__ void list_tile(const BinArgs &B, uint32_t t, uint32_t before, uint32_t added)
 {
-    if (!B.tileList) return;
     if (before == 0) B.tileList[atomicAdd(&B.cnt->tileListCount, 1u)] = t;
     for (uint32_t l = heavy_level(before) + 1; l <= heavy_level(before + added); l++)
         B.tileList[l * B.listStride + atomicAdd(&B.cnt->heavyCount[l - 1], 1u)] = t;
@@ -574,30 +573,73 @@ __device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, 
 
 // Warp-cooperative binning: lanes whose sub-triangles touch the same tile
 // share one atomic on its counter (neighbouring triangles of a mesh usually
-// do); slots within a group follow lane order.  Every lane of the warp must
-// call it (lanes with nothing to bin pass n = 0).
+// do); slots within a group follow lane order.  The counters of up to
+// BIN_BURST tiles are claimed before any of their slots is written, so that
+// the atomics' round trips overlap.  A sub-triangle touching more than
+// BIN_WIDE tiles is binned by the whole warp, 32 of its tiles at a time.
+// Every lane of the warp must call it (lanes with nothing to bin pass
+// has = false).
+#define BIN_BURST 8
+#define BIN_WIDE 32
 __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, const PFPrim &P, uint32_t key)
 {
-    uint32_t tx0 = 0, ty0 = 0, ntx = 0, nty = 0;
+    uint32_t tx0 = 0, ty0 = 0, ntx = 1, nty = 0;
     if (has && !tile_range(T, P, tx0, ty0, ntx, nty)) has = false;
-    const uint32_t n = has ? ntx * nty : 0;
+    uint32_t n = has ? ntx * nty : 0;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1;
+    // large sub-triangles, one after the other: each lane takes tiles of it,
+    // each with its own counter (independent atomics)
+    for (uint32_t wide = __ballot_sync(0xffffffffu, n > BIN_WIDE); wide; wide &= wide - 1) {
+        const int src = __ffs(wide) - 1;
+        const uint32_t wx0 = __shfl_sync(0xffffffffu, tx0, src), wy0 = __shfl_sync(0xffffffffu, ty0, src);
+        const uint32_t wnx = __shfl_sync(0xffffffffu, ntx, src), wn = __shfl_sync(0xffffffffu, n, src);
+        const uint32_t wkey = __shfl_sync(0xffffffffu, key, src);
+        // the tile space of that lane's framebuffer (the lanes of a batch's
+        // warp may draw into different ones)
+        const uint32_t wbase = __shfl_sync(0xffffffffu, T.tileBase, src), wtx = __shfl_sync(0xffffffffu, T.tilesX, src);
+        for (uint32_t i0 = 0; i0 < wn; i0 += 32u * BIN_BURST) {
+            uint32_t tt[BIN_BURST], bb[BIN_BURST];
+#pragma unroll
+            for (int u = 0; u < BIN_BURST; u++) {
+                const uint32_t i = i0 + 32u * (uint32_t)u + lane;
+                tt[u] = i < wn ? wbase + (wy0 + i / wnx) * wtx + (wx0 + i % wnx) : 0xffffffffu;
+                bb[u] = i < wn ? atomicAdd(&B.binCount[tt[u]], 1u) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < BIN_BURST; u++) {
+                if (tt[u] == 0xffffffffu) continue;
+                list_tile(B, tt[u], bb[u], 1u);
+                bin_slot(B, tt[u], bb[u], wkey);
+            }
+        }
+    }
+    if (n > BIN_WIDE) n = 0;
     uint32_t most = n;
     for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
-    for (uint32_t i = 0; i < most; i++) {
-        const bool act = i < n;
-        const uint32_t t = act ? T.tileBase + (ty0 + i / ntx) * T.tilesX + (tx0 + i % ntx) : 0xffffffffu;
-        const uint32_t grp = __match_any_sync(0xffffffffu, t);
-        if (!act) continue;
-        const uint32_t leader = __ffs(grp) - 1;
-        uint32_t base = 0;
-        if (lane == leader) {
-            base = atomicAdd(&B.binCount[t], (unsigned)__popc(grp));
-            list_tile(B, t, base, (uint32_t)__popc(grp));
+    for (uint32_t i0 = 0; i0 < most; i0 += BIN_BURST) {
+        uint32_t tt[BIN_BURST], gg[BIN_BURST], bb[BIN_BURST];
+#pragma unroll
+        for (int u = 0; u < BIN_BURST; u++) {
+            const uint32_t i = i0 + (uint32_t)u;
+            tt[u] = 0xffffffffu; gg[u] = 0; bb[u] = 0;
+            if (i >= most) continue;                           // uniform over the warp
+            const bool act = i < n;
+            const uint32_t t = act ? T.tileBase + (ty0 + i / ntx) * T.tilesX + (tx0 + i % ntx) : 0xffffffffu;
+            const uint32_t grp = __match_any_sync(0xffffffffu, t);
+            tt[u] = t; gg[u] = grp;
+            if (act && lane == (uint32_t)(__ffs(grp) - 1)) bb[u] = atomicAdd(&B.binCount[t], (unsigned)__popc(grp));
         }
-        base = __shfl_sync(grp, base, leader);
-        bin_slot(B, t, base + __popc(grp & lt), key);
+#pragma unroll
+        for (int u = 0; u < BIN_BURST; u++) {
+            const uint32_t i = i0 + (uint32_t)u;
+            if (i >= most) continue;
+            const uint32_t grp = gg[u], leader = (uint32_t)(__ffs(grp) - 1);
+            const uint32_t base = __shfl_sync(0xffffffffu, bb[u], leader);
+            if (i >= n) continue;
+            if (lane == leader) list_tile(B, tt[u], base, (uint32_t)__popc(grp));
+            bin_slot(B, tt[u], base + __popc(grp & lt), key);
+        }
     }
 }
 
@@ -862,35 +904,47 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// k_raster: one CTA per 16x16 tile
+// k_binsort and k_raster
 //
-// For each chunk of CHN sub-triangles (in submission order):
-//   1. stage the records in shared memory, with each one's bounding box
-//      clipped to the tile and its edge functions at the tile origin;
-//   2. coverage, prim-parallel: the (sub-triangle, pixel) pairs of all
-//      clipped boxes are spread over the CTA's threads; a covered pair sets
-//      bit k of the pixel's 32-bit mask, so a pixel's fragments are ordered
-//      by bit position = submission order;
-//   3. shading, fragment-parallel: each warp compacts the fragments of its 32
-//      pixels and shades them densely (texture, Gouraud / Phong colour) --
-//      the source colour does not depend on the destination;
-//   4. resolve: every pixel applies its fragments in order (depth test,
-//      blend, depth write) on its colour and depth held in registers.
+// k_items appends a tile's bin entries (order keys item << 4 | sub-triangle)
+// in atomic order.  k_binsort puts every bin that reached REG_SORT_MAX
+// entries back into submission order, in place (one CTA per bin); shorter
+// bins are sorted by the rasterizing warp itself, in registers.
+//
+// k_raster: one warp per 8x8 tile, two pixels per lane, warps independent
+// of each other (a CTA only groups four of them).  A warp takes a tile from
+// the work queue and walks its bin in batches of 32 sub-triangles in
+// submission order:
+//   1. every lane loads one record of the batch into the warp's shared
+//      memory and derives its edge functions at the tile origin and its
+//      bounding box clipped to the tile;
+//   2. each lane walks the batch in order at its own two pixels: coverage
+//      with the reference's integer edge functions, depth, depth test and
+//      depth write (triangles.c:398-438) -- which leaves, per pixel, the
+//      fragments that passed;
+//   3. the passing fragments are listed pixel by pixel in submission order
+//      and shaded densely over the warp (texture, Gouraud / Phong colour:
+//      the source colour does not depend on the destination);
+//   4. every pixel blends its listed fragments in order into its colour,
+//      held in registers with its depth for the whole tile.
 // ---------------------------------------------------------------------------
-#define RASTER_THREADS PF_TILE_PIXELS
-// records per chunk: 64 (64-bit fragment masks) where tiles are long
-// lists of small triangles, 32 (less shared memory, so bigger bins at full
-// occupancy) otherwise; chosen per launch (PFBatchLaunch.chunk)
-#define FWIN 1024
-#define RANK_SORT_MAX 1024
+#define RASTER_THREADS 128          // four independent warps
+#define RASTER_WARPS (RASTER_THREADS / 32)
+#define QCHN 32                     // records per batch (bit k of a pixel's 32-bit masks)
+#define QFW 128                     // fragment window of a warp
+#define SORT_THREADS 256
+#define REG_SORT_MAX 128            // bins shorter than this are sorted by the raster warp (four keys a lane)
+#define REG_SORT_LEVEL 2            // the heavy-level list of bins that reached REG_SORT_MAX entries
+#define RANK_SORT_MAX 256           // k_binsort: bins up to this size are rank-sorted, longer ones bitonic-sorted
 
-typedef unsigned long long ChunkMask;      // bit k: chunk record k
+static_assert(PF_TILE == 8 && PF_TILE_PIXELS == 64, "a warp owns a tile: two pixels per lane");
+static_assert(REG_SORT_MAX == (PF_HEAVY_BASE << (2 * (REG_SORT_LEVEL - 1))), "k_binsort takes one heavy-level list");
 
 struct RasterArgs {
     const uint32_t *binCount;
     const uint32_t *tileList;
     uint32_t listStride;
-    const uint32_t *bins;
+    uint32_t *bins;
     uint32_t cap;
     const PFPrim *prims;
     const PFPrimPhong *primsPh;
@@ -905,8 +959,8 @@ struct RasterArgs {
     int anyPhong;
 };
 
-// A chunk record in shared memory, padded to 144 bytes: lane i's record
-// starts 4 banks after lane i-1's, so 16-byte loads of the records of 8
+// A batch record in shared memory, padded to 144 bytes: lane i's record
+// starts 4 banks after lane i-1's, so 16-byte accesses of the records of 8
 // lanes touch all 32 banks once (with 128 bytes they would all start in
 // bank 0).
 struct __align__(16) SPrim {
@@ -914,106 +968,67 @@ struct __align__(16) SPrim {
     int4 pad;
 };
 
-struct ChunkPrim {             // per-sub-triangle data derived for this tile
-    int32_t e0[3];             // edge functions at the tile origin
-    int32_t ex[3], ey[3];      // their x and y steps
-    uint32_t bx0, by0, bw, bh; // bounding box clipped to the tile (tile-relative)
-    uint32_t flags;            // face | is3D | state << 8
-    uint32_t rstate;           // the state's PFS_* flags | depth function << 16 | blend mode << 24
-};
-
-// The per-pixel pass's view of a chunk sub-triangle, four 16-byte words:
-// edge functions at the tile origin and their steps, the clipped box
-// (x0 | width << 8 | y0 << 16 | height << 24), the state bits, wInvSum, the
-// three depth terms and a depth-test rejection bound.
-struct __align__(16) DenseP {
+// A batch record's coverage view, three 16-byte words: edge functions at the
+// tile origin and their x / y steps, the box clipped to the tile
+// (x0 | width << 4 | y0 << 8 | height << 12) with the record's kind above
+// (bits 16-17), the raster state and the depth-test rejection bound.
+struct __align__(16) QEdge {
     int32_t e0[3], ex0;
     int32_t ex1, ex2, ey0, ey1;
     int32_t ey2;
     uint32_t box, rstate;
-    float wInvSum;
-    float z1, z2, z3;
     float zReject;             // every covered fragment fails the depth test when zReject >= depth (NaN: never)
 };
 
-// Tile-relative set-up of chunk record sp for the tile at (ox, oy), read
-// from shared memory in 16-byte words (the padded stride keeps them free of
-// bank conflicts across the warp).
-__device__ __forceinline__ void derive_chunk_prim(const SPrim *sp, uint32_t ox, uint32_t oy, uint32_t W, uint32_t H,
-                                                  ChunkPrim &cp, DenseP &dp)
+// Shared memory of one warp.
+struct QWarp {
+    SPrim rec[QCHN];
+    QEdge edge[QCHN];
+    uint16_t fdesc[QFW];       // listed fragments: tile pixel << 5 | record
+    uint32_t fc[QFW];          // their colour
+};
+
+// Edge set-up of a record (its first three 16-byte words: x1 y1 x2 y2 |
+// x3 y3 xMin yMin | xMax yMax flags -) for the tile at (ox, oy) of a W x H
+// framebuffer (triangles.c:336-349, 398-420: the integer edge functions,
+// stepped from the tile origin).
+__device__ __forceinline__ void tile_edge(const int4 q0, const int4 q1, const int4 q2, uint32_t rstate, float zReject,
+                                          uint32_t ox, uint32_t oy, uint32_t W, uint32_t H, QEdge &E)
 {
-    const int4 *w = reinterpret_cast<const int4 *>(&sp->p);
-    const int4 q0 = w[0], q1 = w[1], q2 = w[2];        // x1 y1 x2 y2 | x3 y3 xMin yMin | xMax yMax flags -
     const int32_t X1 = q0.x, Y1 = q0.y, X2 = q0.z, Y2 = q0.w, X3 = q1.x, Y3 = q1.y;
     const uint32_t xMin = (uint32_t)q1.z, yMin = (uint32_t)q1.w, xMax = (uint32_t)q2.x, yMax = (uint32_t)q2.y;
-    const uint32_t flags = (uint32_t)q2.z;
-    cp.flags = flags;
-    const int face = flags & 1;
+    const uint32_t flags = (uint32_t)q2.z, face = flags & 1u;
     int32_t sx[3] = { Y3 - Y2, Y1 - Y3, Y2 - Y1 };
     int32_t sy[3] = { X2 - X3, X3 - X1, X1 - X2 };
     const int32_t rx[3] = { X2, X3, X1 }, ry[3] = { Y2, Y3, Y1 };
+    int32_t e0[3];
     for (int e = 0; e < 3; e++) {
         if (face) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
-        cp.ex[e] = sx[e]; cp.ey[e] = sy[e];
-        cp.e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
+        e0[e] = (int32_t)((ox - (uint32_t)rx[e]) * (uint32_t)sx[e] + (oy - (uint32_t)ry[e]) * (uint32_t)sy[e]);
     }
-    // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside tile and framebuffer
-    uint32_t x0 = max(xMin, ox), x1 = min(min(xMax, ox + PF_TILE), W);
-    uint32_t y0 = max(yMin, oy), y1e = min(min(yMax + 1u, oy + PF_TILE), H);
-    if (yMax == 0xffffffffu) y1e = 0;                 // yMax + 1 wrapped
+    // pixels x in [xMin, xMax), y in [yMin, yMax] (unsigned), inside the tile and the framebuffer
+    const uint32_t x0 = max(xMin, ox), x1 = min(min(xMax, ox + PF_TILE), W);
+    const uint32_t y0 = max(yMin, oy);
+    uint32_t y1e = min(min(yMax + 1u, oy + PF_TILE), H);
+    if (yMax == 0xffffffffu) y1e = 0;                  // yMax + 1 wrapped
     const bool empty = (x0 >= x1) || (y0 >= y1e) || (xMin >= xMax) || (yMin > yMax);
-    cp.bx0 = empty ? 0 : x0 - ox; cp.by0 = empty ? 0 : y0 - oy;
-    cp.bw = empty ? 0 : x1 - x0; cp.bh = empty ? 0 : y1e - y0;
-    cp.rstate = sp->p.rstate;
-    dp.e0[0] = cp.e0[0]; dp.e0[1] = cp.e0[1]; dp.e0[2] = cp.e0[2];
-    dp.ex0 = cp.ex[0]; dp.ex1 = cp.ex[1]; dp.ex2 = cp.ex[2];
-    dp.ey0 = cp.ey[0]; dp.ey1 = cp.ey[1]; dp.ey2 = cp.ey[2];
-    dp.box = cp.bx0 | (cp.bw << 8) | (cp.by0 << 16) | (cp.bh << 24);
-    dp.rstate = cp.rstate;
-    const float4 zq = reinterpret_cast<const float4 *>(&sp->p)[3];     // wInvSum z1 z2 z3
-    dp.wInvSum = zq.x;
-    dp.z1 = zq.y; dp.z2 = zq.z; dp.z3 = zq.w;
-    dp.zReject = sp->p.zReject;
+    const uint32_t bx0 = empty ? 0 : x0 - ox, by0 = empty ? 0 : y0 - oy;
+    const uint32_t bw = empty ? 0 : x1 - x0, bh = empty ? 0 : y1e - y0;
+    E.e0[0] = e0[0]; E.e0[1] = e0[1]; E.e0[2] = e0[2];
+    E.ex0 = sx[0]; E.ex1 = sx[1]; E.ex2 = sx[2];
+    E.ey0 = sy[0]; E.ey1 = sy[1]; E.ey2 = sy[2];
+    E.box = bx0 | (bw << 4) | (by0 << 8) | (bh << 12) | (((flags & PFP_KIND) >> 6) << 16);
+    E.rstate = rstate;
+    E.zReject = zReject;
 }
 
-// Exclusive offset of this thread's count within the CTA, and the CTA
-// total (one barrier; wsum must not be in use by another call).
-__device__ __forceinline__ uint32_t cta_offsets(uint32_t cnt, uint32_t *wsum, uint32_t &total)
+// Normalised weights and depth of a covered fragment at tile pixel (X, Y)
+// (triangles.c:421-438).
+__device__ __forceinline__ float tile_depth(const QEdge &E, const PFPrim &P, uint32_t X, uint32_t Y, float *wn)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t s = cnt;
-    for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
-    if (lane == 31) wsum[warp] = s;
-    __syncthreads();
-    uint32_t before = 0, tot = 0;
-    for (int w = 0; w < RASTER_THREADS / 32; w++) {
-        const uint32_t v = wsum[w];
-        before += (w < warp) ? v : 0u;
-        tot += v;
-    }
-    total = tot;
-    return before + s - cnt;
-}
-
-// Write this pixel's fragments (set bits of mask, in order) to entries
-// off, off + 1, ... of the fragment list, as far as they fall in the
-// window [b0, bEnd): pixel << 5 | chunk record.
-__device__ __forceinline__ void list_fragments(ChunkMask mask, uint32_t off, uint32_t b0, uint32_t bEnd, uint16_t *fdesc)
-{
-    const uint32_t cnt = __popcll(mask);
-    if (!cnt || off >= bEnd || off + cnt <= b0) return;
-    uint32_t f = off;
-    for (ChunkMask mm = mask; mm && f < bEnd; mm &= mm - 1, f++)
-        if (f >= b0) fdesc[f - b0] = (uint16_t)((threadIdx.x << 6) | (uint32_t)(__ffsll(mm) - 1));
-}
-
-// Weights and depth of a covered fragment at tile pixel p (triangles.c:426-438).
-__device__ __forceinline__ float frag_depth(const PFPrim &P, const ChunkPrim &cp, uint32_t p, float *wn)
-{
-    const uint32_t X = p % PF_TILE, Y = p / PF_TILE;
-    const int32_t w1 = (int32_t)((uint32_t)cp.e0[0] + X * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0]);
-    const int32_t w2 = (int32_t)((uint32_t)cp.e0[1] + X * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1]);
-    const int32_t w3 = (int32_t)((uint32_t)cp.e0[2] + X * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2]);
+    const int32_t w1 = (int32_t)((uint32_t)E.e0[0] + X * (uint32_t)E.ex0 + Y * (uint32_t)E.ey0);
+    const int32_t w2 = (int32_t)((uint32_t)E.e0[1] + X * (uint32_t)E.ex1 + Y * (uint32_t)E.ey1);
+    const int32_t w3 = (int32_t)((uint32_t)E.e0[2] + X * (uint32_t)E.ex2 + Y * (uint32_t)E.ey2);
     wn[0] = (float)w1 * P.wInvSum; wn[1] = (float)w2 * P.wInvSum; wn[2] = (float)w3 * P.wInvSum;
     float zs = P.z1 * wn[0] + P.z2 * wn[1];
     zs = zs + P.z3 * wn[2];
@@ -1184,42 +1199,6 @@ __device__ __noinline__ uint32_t blend_sisd(int mode, uint32_t src, uint32_t dst
     return pack4(o);
 }
 
-// 16-byte global-to-shared copies that complete asynchronously (cp.async):
-// the next chunk's records are fetched while the current one is rasterized.
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-// Issue the copies of chunk records keys[c0 .. c0 + cn) into sp (and their
-// per-fragment lighting data into sq when the launch has any).
-__device__ __forceinline__ void stage_chunk_async(const RasterArgs &a, const uint32_t *keys, uint32_t c0, uint32_t cn,
-                                                  SPrim *sp, PFPrimPhong *sq)
-{
-    for (uint32_t w = threadIdx.x; w < cn * 8; w += RASTER_THREADS) {
-        const uint32_t pi = w >> 3, part = w & 7;
-        const uint32_t key = keys[c0 + pi];
-        const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
-        const PFPrim *src = &a.prims[item];
-        if (sub != 0) src = &a.pool[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-        cp_async16(reinterpret_cast<int4 *>(&sp[pi].p) + part, reinterpret_cast<const int4 *>(src) + part);
-    }
-    if (a.anyPhong) {
-        for (uint32_t w = threadIdx.x; w < cn * 5; w += RASTER_THREADS) {
-            const uint32_t pi = w / 5, part = w % 5;
-            const uint32_t key = keys[c0 + pi];
-            const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
-            const PFPrimPhong *src = &a.primsPh[item];
-            if (sub != 0) src = &a.poolPh[(uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1];
-            cp_async16(reinterpret_cast<int4 *>(&sq[pi]) + part, reinterpret_cast<const int4 *>(src) + part);
-        }
-    }
-    cp_async_commit();
-}
-
 // The colour of the pixel a k_raster thread owns, as the framebuffer holds
 // it.  RGBA / unsigned byte: the packed colour, whose getters and setters
 // are the identity.  Other formats: the raw pixel, read for blending through
@@ -1247,409 +1226,352 @@ template <> struct FbPixel<true> {
     __device__ __forceinline__ void set(bool scalar, uint32_t v) { if (scalar) pff_set_sisd(f, v, r); else pff_set_simd(f, v, r); }
 };
 
-template <int CHN, bool GEN>
-__global__ void __launch_bounds__(RASTER_THREADS, 4) k_raster(RasterArgs a)
+// k_binsort: one CTA per bin that reached REG_SORT_MAX entries (a
+// heavy-level list), taken from a queue: its keys are put back into
+// submission order in place -- rank sort up to RANK_SORT_MAX entries,
+// bitonic sort in shared memory beyond.
+__global__ void __launch_bounds__(SORT_THREADS) k_binsort(RasterArgs a)
 {
-    extern __shared__ uint32_t skeys[];               // [N] keys (+ [n] sorted copy when rank-sorting)
-    __shared__ SPrim sprimBuf[2][CHN];                 // double-buffered chunk records
-    __shared__ __align__(16) PFPrimPhong sphBuf[2][CHN];
-    __shared__ ChunkPrim scp[CHN];
-    __shared__ DenseP sdp[CHN];
-    __shared__ uint32_t sarea[CHN + 1];
-    __shared__ ChunkMask pmask[RASTER_THREADS];
-    __shared__ uint16_t fdesc[FWIN];                  // listed fragments: pixel << 5 | chunk record
-    __shared__ uint32_t fval[FWIN];                   // their depth (pass 3) or colour (pass 4)
-    __shared__ uint32_t fcolv[FWIN];                  // their colour (passes 3 and 4 in one)
-    __shared__ uint32_t wsum[2][RASTER_THREADS / 32];    // pass 3 (and the merged pass), pass 4
-    __shared__ int sDense, sAnyLP, sPhong;
-    __shared__ ChunkMask sBlit;                        // chunk records that are rectangles (not counted as fragments)
-
+    extern __shared__ uint32_t sbuf[];                // a bin's keys (room for a bitonic sort)
+    __shared__ uint32_t sTile;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_items is done
     if (a.cnt->abortCommand <= a.command) return;
-    // the batch completed set-up without overflow: its sub-triangles count
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.cnt->rasterized, a.cnt->batchRasterized);
+    const int tid = threadIdx.x;
+    const uint32_t nList = min(a.cnt->heavyCount[REG_SORT_LEVEL - 1], a.totalTiles);
+    for (;;) {
+        if (tid == 0) {
+            const uint32_t q = atomicAdd(&a.cnt->sortQueue, 1u);
+            sTile = q < nList ? __ldg(a.tileList + (size_t)REG_SORT_LEVEL * a.listStride + q) : 0xffffffffu;
+        }
+        __syncthreads();
+        const uint32_t t = sTile;
+        if (t == 0xffffffffu) break;
+        const uint32_t n = min(__ldg(a.binCount + t), a.cap);
+        uint32_t *bin = a.bins + (size_t)t * a.cap;
+        for (uint32_t i = tid; i < n; i += SORT_THREADS) sbuf[i] = bin[i];
+        __syncthreads();
+        int unsorted = 0;
+        for (uint32_t i = tid; i + 1 < n; i += SORT_THREADS) unsorted |= (sbuf[i] > sbuf[i + 1]);
+        if (__syncthreads_or(unsorted)) {
+            if (n <= RANK_SORT_MAX) {
+                // keys are unique: a key's place is the number of smaller keys
+                for (uint32_t i = tid; i < n; i += SORT_THREADS) {
+                    const uint32_t k = sbuf[i];
+                    uint32_t r = 0;
+                    for (uint32_t j = 0; j < n; j++) r += (sbuf[j] < k);
+                    bin[r] = k;
+                }
+            } else {
+                uint32_t N = 1; while (N < n) N <<= 1;
+                for (uint32_t i = n + tid; i < N; i += SORT_THREADS) sbuf[i] = 0xffffffffu;
+                __syncthreads();
+                for (uint32_t k = 2; k <= N; k <<= 1)
+                    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                        for (uint32_t i = tid; i < N; i += SORT_THREADS) {
+                            const uint32_t ixj = i ^ j;
+                            if (ixj > i) {
+                                const uint32_t x = sbuf[i], y = sbuf[ixj];
+                                if ((x > y) == ((i & k) == 0)) { sbuf[i] = y; sbuf[ixj] = x; }
+                            }
+                        }
+                        __syncthreads();
+                    }
+                for (uint32_t i = tid; i < n; i += SORT_THREADS) bin[i] = sbuf[i];
+            }
+        }
+        __syncthreads();                               // sTile and sbuf are free
+    }
+}
+
+// List this lane's fragments (bit 32 s + k of m: record k at its pixel of
+// slot s), in order, as entries off, off + 1, ... of the warp's fragment
+// list, as far as they fall in the window [b0, bEnd).
+__device__ __forceinline__ void tile_list(unsigned long long m, uint32_t off, uint32_t b0, uint32_t bEnd,
+                                          uint16_t *fdesc)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t cnt = __popcll(m);
+    if (!cnt || off >= bEnd || off + cnt <= b0) return;
+    uint32_t f = off;
+    for (unsigned long long mm = m; mm && f < bEnd; mm &= mm - 1, f++) {
+        if (f < b0) continue;
+        const uint32_t b = (uint32_t)(__ffsll(mm) - 1);
+        fdesc[f - b0] = (uint16_t)(((lane + 32u * (b >> 5)) << 5) | (b & 31u));
+    }
+}
+
+// Warp-wide exclusive prefix sum of v; total gets the sum over the warp.
+__device__ __forceinline__ uint32_t warp_offsets(uint32_t v, uint32_t &total)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t s = v;
+    for (int o = 1; o < 32; o <<= 1) { const uint32_t t = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += t; }
+    total = __shfl_sync(0xffffffffu, s, 31);
+    return s - v;
+}
+
+template <bool GEN>
+__global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
+{
+    extern __shared__ __align__(16) unsigned char rsmem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t lx = tid % PF_TILE, ly = tid / PF_TILE;
+    QWarp &Q = reinterpret_cast<QWarp *>(rsmem)[warp];
+    PFPrimPhong *const ph = reinterpret_cast<PFPrimPhong *>(rsmem + RASTER_WARPS * sizeof(QWarp)) + warp * QCHN;
+
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // k_binsort is done
+    if (a.cnt->abortCommand <= a.command) return;
+    // the batch completed set-up without overflow: its sub-triangles count
+    if (blockIdx.x == 0 && tid == 0) atomicAdd(&a.cnt->rasterized, a.cnt->batchRasterized);
+    const uint32_t lx = (uint32_t)lane & 7u, ly = (uint32_t)lane >> 3;     // my pixels: (lx, ly) and (lx, ly + 4)
     unsigned long long frags = 0;
 
-    // persistent: CTAs take tiles from a shared work queue -- the tiles the
-    // binning listed as non-empty (every tile when there is no list); the
-    // next entry is claimed while the current tile is rasterized
-    const bool listed = a.tileList != nullptr;
-    // queue entries: the tiles of the heaviest level, then of each lighter
-    // level, then every non-empty tile; a tile is rasterized from the first
-    // list it is on and skipped on the later ones
+    // persistent: warps take tiles from a shared work queue -- the tiles the
+    // binning listed as non-empty, those of the heaviest level first, then
+    // of each lighter level, then the rest; a tile is rasterized from the
+    // first list it is on and skipped on the later ones
     uint32_t levelEnd[PF_HEAVY_LEVELS + 1];           // queue index past level l's entries, heaviest first
     uint32_t nQueue = 0;
-    if (listed) {
-        for (int l = PF_HEAVY_LEVELS; l >= 1; l--) { nQueue += min(a.cnt->heavyCount[l - 1], a.totalTiles); levelEnd[l] = nQueue; }
-        nQueue += min(a.cnt->tileListCount, a.totalTiles);
-        levelEnd[0] = nQueue;
-    } else nQueue = a.totalTiles;
-    __shared__ uint32_t sNext;
+    for (int l = PF_HEAVY_LEVELS; l >= 1; l--) { nQueue += min(a.cnt->heavyCount[l - 1], a.totalTiles); levelEnd[l] = nQueue; }
+    nQueue += min(a.cnt->tileListCount, a.totalTiles);
+    levelEnd[0] = nQueue;
     uint32_t claim = 0;
-    if (tid == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
-    if (listed) {
-        // tiles with an empty bin only get their fused clear, if any: warp w
-        // of the grid takes the groups of 32 tiles w, w + 8 * gridDim, ...
-        // (no shared memory, no barrier, no atomics); the queue's dynamic
-        // schedule absorbs the few microseconds this costs the first CTAs
-        for (uint32_t t0 = (blockIdx.x * (RASTER_THREADS / 32) + (uint32_t)warp) * 32u; t0 < a.totalTiles;
-             t0 += gridDim.x * RASTER_THREADS) {
-            const uint32_t t = t0 + (uint32_t)lane;
-            int ti = 0;
-            bool clear = false;
-            if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
-                int tlo = 0, thi = a.nTargets - 1;
-                while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= t) tlo = mid; else thi = mid - 1; }
-                ti = tlo;
-                clear = a.targets[tlo].clearMode != 0;
-            }
-            for (uint32_t m = __ballot_sync(0xffffffffu, clear); m; m &= m - 1) {
-                const int src = __ffs(m) - 1;
-                const PFTarget &T = a.targets[__shfl_sync(0xffffffffu, ti, src)];
-                const uint32_t tile = t0 + (uint32_t)src - T.tileBase;
-                const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
-                for (uint32_t p = (uint32_t)lane; p < PF_TILE_PIXELS; p += 32) {
-                    const uint32_t px = ox + p % PF_TILE, py = oy + p / PF_TILE;
-                    if (px >= T.W || py >= T.H) continue;
-                    const size_t pidx = (size_t)py * T.W + px;
-                    if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
-                    if (GEN) pff_store(T.fmt, T.color, pidx, T.clearRaw);
-                    else ((uint32_t *)T.color)[pidx] = T.clearRaw[0];
-                    T.depth[pidx] = T.clearDepth;
-                }
+    if (lane == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
+    // tiles with an empty bin only get their fused clear, if any: warp w of
+    // the grid takes the groups of 32 tiles w, w + warps of the grid, ...;
+    // the queue's dynamic schedule absorbs the time this costs
+    for (uint32_t t0 = (blockIdx.x * RASTER_WARPS + (uint32_t)warp) * 32u; t0 < a.totalTiles;
+         t0 += gridDim.x * RASTER_THREADS) {
+        const uint32_t t = t0 + (uint32_t)lane;
+        int ti = 0;
+        bool clear = false;
+        if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
+            int tlo = 0, thi = a.nTargets - 1;
+            while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= t) tlo = mid; else thi = mid - 1; }
+            ti = tlo;
+            clear = a.targets[tlo].clearMode != 0;
+        }
+        for (uint32_t m = __ballot_sync(0xffffffffu, clear); m; m &= m - 1) {
+            const int src = __ffs(m) - 1;
+            const PFTarget &T = a.targets[__shfl_sync(0xffffffffu, ti, src)];
+            const uint32_t tile = t0 + (uint32_t)src - T.tileBase;
+            const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
+            for (uint32_t p = (uint32_t)lane; p < PF_TILE_PIXELS; p += 32) {
+                const uint32_t px = ox + p % PF_TILE, py = oy + p / PF_TILE;
+                if (px >= T.W || py >= T.H) continue;
+                const size_t pidx = (size_t)py * T.W + px;
+                if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
+                if (GEN) pff_store(T.fmt, T.color, pidx, T.clearRaw);
+                else ((uint32_t *)T.color)[pidx] = T.clearRaw[0];
+                T.depth[pidx] = T.clearDepth;
             }
         }
     }
+
     for (;;) {
-    __syncthreads();                                   // sNext and the previous tile's shared data are free
-    if (tid == 0) {
+    uint32_t next = 0xffffffffu;
+    if (lane == 0) {
         const uint32_t q = claim;
-        uint32_t next = 0xffffffffu;
         if (q < nQueue) {
             claim = atomicAdd(&a.cnt->tileQueue, 1u);
-            if (!listed) next = q;
-            else {
-                uint32_t level = PF_HEAVY_LEVELS, begin = 0;
-                while (q >= levelEnd[level]) { begin = levelEnd[level]; level--; }
-                next = __ldg(a.tileList + (size_t)level * a.listStride + (q - begin));
-                if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
-            }
+            uint32_t level = PF_HEAVY_LEVELS, begin = 0;
+            while (q >= levelEnd[level]) { begin = levelEnd[level]; level--; }
+            next = __ldg(a.tileList + (size_t)level * a.listStride + (q - begin));
+            if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
         }
-        sNext = next;
     }
-    __syncthreads();
-    const uint32_t gt = sNext;
+    const uint32_t gt = __shfl_sync(0xffffffffu, next, 0);
     if (gt == 0xffffffffu) break;
     if (gt == 0xfffffffeu) continue;
     int tlo = 0, thi = a.nTargets - 1;
     while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gt) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
     const uint32_t tile = gt - T.tileBase;
-    const uint32_t n = min(a.binCount[gt], a.cap);
+    const uint32_t n = min(__ldg(a.binCount + gt), a.cap);
     if (n == 0 && T.clearMode == 0) continue;
-    const uint32_t tx = tile % T.tilesX, ty = tile / T.tilesX;
-    const uint32_t ox = tx * PF_TILE, oy = ty * PF_TILE;
-    const uint32_t px = ox + lx, py = oy + ly;
-    const bool inside = px < T.W && py < T.H;
-    const size_t pidx = (size_t)py * T.W + px;
+    const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
+    const uint32_t W = T.W, H = T.H;
 
-    // pixel state in registers
-    FbPixel<GEN> col{}; float dep = 0.0f;
-    if (inside) {
-        if (T.clearMode == 2 || (T.clearMode == 1 && pidx >= 8)) { col.clear(T); dep = T.clearDepth; }
-        else { col.load(T, pidx); dep = T.depth[pidx]; }
+    FbPixel<GEN> col0{}, col1{};
+    float dep0 = 0.0f, dep1 = 0.0f;
+    const uint32_t X0 = ox + lx, Y0 = oy + ly, Y1 = Y0 + 4u;
+    const bool in0 = X0 < W && Y0 < H, in1 = X0 < W && Y1 < H;
+    const size_t pidx0 = (size_t)Y0 * W + X0, pidx1 = (size_t)Y1 * W + X0;
+    {
+        auto init = [&](FbPixel<GEN> &c, float &d, bool in, size_t pi) {
+            if (!in) return;
+            if (T.clearMode == 2 || (T.clearMode == 1 && pi >= 8)) { c.clear(T); d = T.clearDepth; }
+            else { c.load(T, pi); d = T.depth[pi]; }
+        };
+        init(col0, dep0, in0, pidx0);
+        init(col1, dep1, in1, pidx1);
     }
 
-    if (n > 0) {
-        const uint32_t *bin = a.bins + (size_t)gt * a.cap;
-        for (uint32_t i = tid; i < n; i += RASTER_THREADS) skeys[i] = bin[i];
-        __syncthreads();
-        // keys arrive in atomic order; restore submission order
-        int unsorted = 0;
-        for (uint32_t i = tid; i + 1 < n; i += RASTER_THREADS) unsorted |= (skeys[i] > skeys[i + 1]);
-        const uint32_t *keys = skeys;
-        if (__syncthreads_or(unsorted)) {
-            if (n <= RANK_SORT_MAX) {
-                // rank sort: keys are unique; rank = number of smaller keys
-                uint32_t *dst = skeys + RANK_SORT_MAX;
-                for (uint32_t i = tid; i < n; i += RASTER_THREADS) {
-                    const uint32_t k = skeys[i];
-                    uint32_t r = 0;
-                    for (uint32_t j = 0; j < n; j++) r += (skeys[j] < k);
-                    dst[r] = k;
-                }
-                __syncthreads();
-                keys = dst;
-            } else {
-                uint32_t N = 1; while (N < n) N <<= 1;
-                for (uint32_t i = n + tid; i < N; i += RASTER_THREADS) skeys[i] = 0xffffffffu;
-                __syncthreads();
-                for (uint32_t k = 2; k <= N; k <<= 1)
-                    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                        for (uint32_t i = tid; i < N; i += RASTER_THREADS) {
-                            uint32_t ixj = i ^ j;
-                            if (ixj > i) {
-                                uint32_t x = skeys[i], y = skeys[ixj];
-                                bool up = (i & k) == 0;
-                                if ((x > y) == up) { skeys[i] = y; skeys[ixj] = x; }
-                            }
-                        }
-                        __syncthreads();
-                    }
-            }
-        }
-
-        stage_chunk_async(a, keys, 0, min((uint32_t)CHN, n), sprimBuf[0], sphBuf[0]);
-        for (uint32_t c0 = 0, it = 0; c0 < n; c0 += CHN, it++) {
-            const uint32_t cn = min((uint32_t)CHN, n - c0);
-            SPrim *const sprim = sprimBuf[it & 1];
-            PFPrimPhong *const sph = sphBuf[it & 1];
-            cp_async_wait_all();
-            __syncthreads();                                  // this chunk is staged; the previous one's data are free
-            if (c0 + CHN < n)
-                stage_chunk_async(a, keys, c0 + CHN, min((uint32_t)CHN, n - c0 - CHN), sprimBuf[(it + 1) & 1],
-                                  sphBuf[(it + 1) & 1]);
-            pmask[tid] = 0;
-            // 1. warp 0 derives the chunk's tile-relative set-up (two
-            //    records per lane)
-            if (warp == 0) {
-                uint32_t area = 0, kinds = 0;
-                bool phong = false;
-                ChunkMask blit = 0;
-                uint32_t base = 0;                            // rows of the first half
-                for (int h = 0; h < CHN / 32; h++) {
-                    const uint32_t k = (uint32_t)(h * 32 + lane);
-                    const bool has = k < cn;
-                    uint32_t bh = 0, kind = 0;
-                    if (has) {
-                        ChunkPrim cp;
-                        DenseP dp;
-                        derive_chunk_prim(&sprim[k], ox, oy, T.W, T.H, cp, dp);
-                        scp[k] = cp;
-                        sdp[k] = dp;
-                        bh = cp.bw ? cp.bh : 0;
-                        area += cp.bw * cp.bh;
-                        kind = cp.flags & PFP_KIND;
-                        phong = phong || (cp.rstate & PFS_PHONG);
-                    }
-                    kinds |= kind;
-                    blit |= (ChunkMask)__ballot_sync(0xffffffffu, kind == PFP_BLIT) << (32 * h);
-                    uint32_t sc = bh;
-                    for (int o = 1; o < 32; o <<= 1) { uint32_t t = __shfl_up_sync(0xffffffffu, sc, o); if (lane >= o) sc += t; }
-                    sarea[k + 1] = base + sc;
-                    base += __shfl_sync(0xffffffffu, sc, 31);
-                }
-                if (lane == 0) sarea[0] = 0;
-                const bool anyLP = __any_sync(0xffffffffu, kinds != 0);
-                const bool anyPhong = __any_sync(0xffffffffu, phong);
-                for (int o = 16; o > 0; o >>= 1) area += __shfl_xor_sync(0xffffffffu, area, o);
-                const bool dense = area > cn * (PF_TILE_PIXELS / 2) && !anyLP;
-                if (lane == 0) { sDense = dense; sAnyLP = anyLP; sBlit = blit; sPhong = anyPhong; }
-            }
-            __syncthreads();
-            ChunkMask vis = 0;                                // chunk sub-triangles visible at my pixel
-            const bool lpChunk = sAnyLP != 0;                 // the chunk holds points or lines
-            if (sDense) {
-                // 2+3 (large sub-triangles). Each thread walks the chunk in
-                //    submission order at its own pixel: coverage, depth, test.
-                uint32_t cov = 0;
-                for (uint32_t k = 0; k < cn; k++) {
-                    const int4 *d4 = reinterpret_cast<const int4 *>(&sdp[k]);
-                    const int4 q0 = d4[0], q1 = d4[1], q2 = d4[2];
-                    const uint32_t box = (uint32_t)q2.y;
-                    if (lx - (box & 255u) >= ((box >> 8) & 255u) || ly - ((box >> 16) & 255u) >= (box >> 24)) continue;
-                    const int32_t w1 = (int32_t)((uint32_t)q0.x + lx * (uint32_t)q0.w + ly * (uint32_t)q1.z);
-                    const int32_t w2 = (int32_t)((uint32_t)q0.y + lx * (uint32_t)q1.x + ly * (uint32_t)q1.w);
-                    const int32_t w3 = (int32_t)((uint32_t)q0.z + lx * (uint32_t)q1.y + ly * (uint32_t)q2.x);
-                    if (!((w1 | w2 | w3) > 0)) continue;
-                    cov++;
-                    const float4 zq = reinterpret_cast<const float4 *>(&sdp[k])[3];
-                    if (zq.w >= dep) continue;                   // every fragment of it fails the depth test
-                    const float wInvSum = __int_as_float(q2.w);
-                    const float wn1 = (float)w1 * wInvSum, wn2 = (float)w2 * wInvSum, wn3 = (float)w3 * wInvSum;
-                    float zs = zq.x * wn1 + zq.y * wn2;
-                    zs = zs + zq.z * wn3;
-                    const float z = 1.0f / zs;
-                    const uint32_t rs = (uint32_t)q2.z;
-                    if (!(rs & PFS_DEPTH_TEST) || depth_simd((int)((rs >> 16) & 255u), z, dep)) {
-                        vis |= 1ull << k;
-                        if (rs & PFS_DEPTH_MASK) dep = z;
-                    }
-                }
-                frags += cov;
-            } else {
-                // 2. coverage: one work item per (sub-triangle, row of its clipped
-                //    box); edge functions stepped along the row
-                const uint32_t nRows = sarea[CHN];
-                for (uint32_t t = tid; t < nRows; t += RASTER_THREADS) {
-                    int lo = 0, hi = CHN - 1;                          // largest k with sarea[k] <= t
-                    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (sarea[mid] <= t) lo = mid; else hi = mid - 1; }
-                    const ChunkPrim &cp = scp[lo];
-                    const uint32_t Y = cp.by0 + (t - sarea[lo]);
-                    const ChunkMask bit = 1ull << lo;
-                    uint32_t w1 = (uint32_t)cp.e0[0] + cp.bx0 * (uint32_t)cp.ex[0] + Y * (uint32_t)cp.ey[0];
-                    uint32_t w2 = (uint32_t)cp.e0[1] + cp.bx0 * (uint32_t)cp.ex[1] + Y * (uint32_t)cp.ey[1];
-                    uint32_t w3 = (uint32_t)cp.e0[2] + cp.bx0 * (uint32_t)cp.ex[2] + Y * (uint32_t)cp.ey[2];
-                    ChunkMask *row = &pmask[Y * PF_TILE + cp.bx0];
-                    if (lpChunk && (cp.flags & PFP_KIND)) {
-                        for (uint32_t dx = 0; dx < cp.bw; dx++)
-                            if (lp_covers(sprim[lo].p, (int32_t)(ox + cp.bx0 + dx), (int32_t)(oy + Y))) atomicOr(row + dx, bit);
-                        continue;
-                    }
-                    for (uint32_t dx = 0; dx < cp.bw; dx++) {
-                        if ((int32_t)(w1 | w2 | w3) > 0) atomicOr(row + dx, bit);
-                        w1 += (uint32_t)cp.ex[0]; w2 += (uint32_t)cp.ex[1]; w3 += (uint32_t)cp.ex[2];
-                    }
-                }
-                __syncthreads();
-                const ChunkMask m = pmask[tid];
-                const uint32_t cntp = __popcll(m);
-                frags += lpChunk ? __popcll(m & ~sBlit) : cntp;
-                uint32_t total;
-                const uint32_t myOff = cta_offsets(cntp, wsum[0], total);
-                if (!sPhong) {
-                    // 3+4. shading is cheap (no per-fragment lighting): every
-                    //    covered fragment, listed pixel by pixel in
-                    //    submission order, gets its depth and colour
-                    //    densely over the CTA; then each pixel applies its
-                    //    fragments in order (depth test, blend, depth write)
-                    for (uint32_t b0 = 0; b0 < total; b0 += FWIN) {
-                        const uint32_t bEnd = min(total, b0 + FWIN);
-                        list_fragments(m, myOff, b0, bEnd, fdesc);
-                        __syncthreads();
-                        for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                            const uint32_t d = fdesc[f - b0], p = d >> 6, k = d & 63u;
-                            const PFPrim &P = sprim[k].p;
-                            if (lpChunk && (scp[k].flags & PFP_KIND)) {
-                                const int32_t X = (int32_t)(ox + p % PF_TILE), Y = (int32_t)(oy + p / PF_TILE);
-                                fval[f - b0] = __float_as_uint(lp_depth(P, X, Y));
-                                fcolv[f - b0] = lp_color(P, X, Y);
-                                continue;
-                            }
-                            float wn[3];
-                            const float z = frag_depth(P, scp[k], p, wn);
-                            fval[f - b0] = __float_as_uint(z);
-                            fcolv[f - b0] = shade_fragment(P, &sph[k], a.states, wn[0], wn[1], wn[2], z);
-                        }
-                        __syncthreads();
-                        if (cntp && myOff < bEnd && myOff + cntp > b0) {
-                            uint32_t f = myOff; ChunkMask mm = m;
-                            while (mm) {
-                                const uint32_t k = __ffsll(mm) - 1;
-                                mm &= mm - 1;
-                                if (f >= bEnd) break;
-                                if (f >= b0) {
-                                    const uint32_t rs = scp[k].rstate;
-                                    const float z = __uint_as_float(fval[f - b0]);
-                                    const int func = (int)((rs >> 16) & 255u);
-                                    const bool lpk = lpChunk && (scp[k].flags & PFP_KIND);
-                                    if (!(rs & PFS_DEPTH_TEST) || (lpk ? depth_sisd(func, z, dep) : depth_simd(func, z, dep))) {
-                                        uint32_t frag = fcolv[f - b0];
-                                        if (rs & PFS_BLEND)
-                                            frag = lpk ? blend_sisd((int)(rs >> 24), frag, col.get(true))
-                                                       : blend_simd((int)(rs >> 24), frag, col.get(false));
-                                        col.set(lpk, frag);
-                                        if (rs & PFS_DEPTH_MASK) dep = z;
-                                    }
-                                }
-                                f++;
-                            }
-                        }
-                        // (no barrier: the next window's list build touches only
-                        // fdesc, and its compute starts after a barrier)
+    // a bin shorter than REG_SORT_MAX is put into submission order here, in
+    // registers: a bitonic network over 32, 64 or 128 places, place
+    // 32 r + lane in key r of the lane; longer bins were sorted by k_binsort
+    const uint32_t *bin = a.bins + (size_t)gt * a.cap;
+    const bool regSort = n < REG_SORT_MAX;
+    uint32_t sk[4] = { 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu };
+    if (regSort) {
+        const uint32_t nk = n <= 32 ? 1u : n <= 64 ? 2u : 4u;    // keys a lane sorts: a power-of-two network
+        for (uint32_t r = 0; r < 4; r++)
+            if (32 * r + (uint32_t)lane < n) sk[r] = __ldg(bin + 32 * r + lane);
+        for (uint32_t k = 2; k <= 32 * nk; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                if (j >= 32) {
+                    // partners are keys of the same lane: places i and i + j
+                    const uint32_t dr = j >> 5;
+#pragma unroll
+                    for (uint32_t r = 0; r < 4; r++) {
+                        if (r & dr) continue;
+                        const uint32_t i = 32 * r + (uint32_t)lane;
+                        const uint32_t x = sk[r], y = sk[r + dr];
+                        const bool asc = (i & k) == 0;
+                        sk[r] = asc ? min(x, y) : max(x, y);
+                        sk[r + dr] = asc ? max(x, y) : min(x, y);
                     }
                 } else {
-                    // 3. with per-fragment lighting, depth first, over the
-                    //    whole CTA: the chunk's covered fragments, listed
-                    //    pixel by pixel in submission order, get their depth
-                    //    computed densely by all threads; then each pixel
-                    //    runs its depth tests in order, which leave the set
-                    //    of visible fragments for pass 4
-                    for (uint32_t b0 = 0; b0 < total; b0 += FWIN) {
-                        const uint32_t bEnd = min(total, b0 + FWIN);
-                        list_fragments(m, myOff, b0, bEnd, fdesc);
-                        __syncthreads();
-                        for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                            const uint32_t d = fdesc[f - b0], p = d >> 6, k = d & 63u;
-                            float wn[3];
-                            const float z = (lpChunk && (scp[k].flags & PFP_KIND))
-                                ? lp_depth(sprim[k].p, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE))
-                                : frag_depth(sprim[k].p, scp[k], p, wn);
-                            fval[f - b0] = __float_as_uint(z);
-                        }
-                        __syncthreads();
-                        if (cntp && myOff < bEnd && myOff + cntp > b0) {
-                            uint32_t f = myOff; ChunkMask mm = m;
-                            while (mm) {
-                                const uint32_t k = __ffsll(mm) - 1;
-                                mm &= mm - 1;
-                                if (f >= bEnd) break;
-                                if (f >= b0) {
-                                    const uint32_t rs = scp[k].rstate;
-                                    const float z = __uint_as_float(fval[f - b0]);
-                                    const int func = (int)((rs >> 16) & 255u);
-                                    if (!(rs & PFS_DEPTH_TEST) ||
-                                        ((lpChunk && (scp[k].flags & PFP_KIND)) ? depth_sisd(func, z, dep)
-                                                                                 : depth_simd(func, z, dep))) {
-                                        vis |= 1ull << k;
-                                        if (rs & PFS_DEPTH_MASK) dep = z;
-                                    }
-                                }
-                                f++;
-                            }
-                        }
-                        // (no barrier needed before the next window or pass 4)
+#pragma unroll
+                    for (uint32_t r = 0; r < 4; r++) {
+                        const uint32_t i = 32 * r + (uint32_t)lane;
+                        const uint32_t o = __shfl_xor_sync(0xffffffffu, sk[r], j);
+                        sk[r] = (((i & k) == 0) == ((i & j) == 0)) ? min(sk[r], o) : max(sk[r], o);
                     }
                 }
             }
-            // 4. shade the visible fragments (densely over the CTA) and blend
-            //    each pixel's in submission order
-            if (sDense || sPhong) {
-                uint32_t totalv;
-                const uint32_t myOffV = cta_offsets(__popcll(vis), wsum[1], totalv);
-                for (uint32_t b0 = 0; b0 < totalv; b0 += FWIN) {
-                    const uint32_t bEnd = min(totalv, b0 + FWIN);
-                    list_fragments(vis, myOffV, b0, bEnd, fdesc);
-                    __syncthreads();
-                    for (uint32_t f = b0 + tid; f < bEnd; f += RASTER_THREADS) {
-                        const uint32_t d = fdesc[f - b0], p = d >> 6, k = d & 63u;
-                        const PFPrim &P = sprim[k].p;
-                        if (lpChunk && (scp[k].flags & PFP_KIND)) {
-                            fval[f - b0] = lp_color(P, (int32_t)(ox + p % PF_TILE), (int32_t)(oy + p / PF_TILE));
-                            continue;
-                        }
-                        float wn[3];
-                        const float z = frag_depth(P, scp[k], p, wn);
-                        fval[f - b0] = shade_fragment(P, &sph[k], a.states, wn[0], wn[1], wn[2], z);
+    }
+
+    for (uint32_t c0 = 0; c0 < n; c0 += QCHN) {
+        const uint32_t cn = min((uint32_t)QCHN, n - c0);
+        // 1. my record: load, stage, derive its tile set-up
+        uint32_t kind = 0;
+        if ((uint32_t)lane < cn) {
+            uint32_t key;
+            if (!regSort) key = __ldg(bin + c0 + lane);
+            else key = c0 == 0 ? sk[0] : c0 == 32 ? sk[1] : c0 == 64 ? sk[2] : sk[3];
+            const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
+            const PFPrim *src = &a.prims[item];
+            uint32_t pi = item;
+            if (sub != 0) { pi = (uint32_t)__ldg(&a.prims[item].poolBase) + sub - 1; src = &a.pool[pi]; }
+            const int4 *s4 = reinterpret_cast<const int4 *>(src);
+            int4 r[8];
+            for (int i = 0; i < 8; i++) r[i] = __ldg(s4 + i);
+            int4 *d4 = reinterpret_cast<int4 *>(&Q.rec[lane].p);
+            for (int i = 0; i < 8; i++) d4[i] = r[i];
+            if (a.anyPhong) {
+                const int4 *p4 = reinterpret_cast<const int4 *>(sub != 0 ? &a.poolPh[pi] : &a.primsPh[item]);
+                int4 *q4 = reinterpret_cast<int4 *>(&ph[lane]);
+                for (int i = 0; i < 5; i++) q4[i] = __ldg(p4 + i);
+            }
+            QEdge E;
+            tile_edge(r[0], r[1], r[2], (uint32_t)r[4].w, __int_as_float(r[6].z), ox, oy, W, H, E);
+            Q.edge[lane] = E;
+            kind = (uint32_t)r[2].z & PFP_KIND;
+        }
+        const bool anyLP = __any_sync(0xffffffffu, kind != 0);
+        __syncwarp();
+        // 2. my two pixels walk the batch in submission order: coverage,
+        //    depth, depth test, depth write
+        unsigned long long vis = 0;                     // bit 32 s + k: record k passed at my pixel of slot s
+        uint32_t cov = 0;
+        for (uint32_t k = 0; k < cn; k++) {
+            const int4 *e4 = reinterpret_cast<const int4 *>(&Q.edge[k]);
+            const int4 q2 = e4[2];
+            const uint32_t box = (uint32_t)q2.y;
+            const uint32_t bx0 = box & 15u, bw = (box >> 4) & 15u, by0 = (box >> 8) & 15u, bh = (box >> 12) & 15u;
+            const bool r0 = ly - by0 < bh, r1 = ly + 4u - by0 < bh;
+            if (lx - bx0 >= bw || !(r0 || r1)) continue;
+            const uint32_t rs = (uint32_t)q2.z;
+            const int func = (int)((rs >> 16) & 255u);
+            if (((box >> 16) & 3u) == 0) {
+                const int4 q0 = e4[0], q1 = e4[1];
+                uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + ly * (uint32_t)q1.z;
+                uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + ly * (uint32_t)q1.w;
+                uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + ly * (uint32_t)q2.x;
+                const float4 zq = reinterpret_cast<const float4 *>(&Q.rec[k].p)[3];     // wInvSum z1 z2 z3
+                const float zRej = __int_as_float(q2.w);
+                auto test = [&](float &d, bool rowOK, int s) {
+                    if (!rowOK || !((int32_t)(w1 | w2 | w3) > 0)) return;
+                    cov++;
+                    if (zRej >= d) return;                      // every fragment of it fails the depth test
+                    const float wn1 = (float)(int32_t)w1 * zq.x, wn2 = (float)(int32_t)w2 * zq.x;
+                    const float wn3 = (float)(int32_t)w3 * zq.x;
+                    float zs = zq.y * wn1 + zq.z * wn2;
+                    zs = zs + zq.w * wn3;
+                    const float z = 1.0f / zs;
+                    if (!(rs & PFS_DEPTH_TEST) || depth_simd(func, z, d)) {
+                        vis |= 1ull << (32 * s + (int)k);
+                        if (rs & PFS_DEPTH_MASK) d = z;
                     }
-                    __syncthreads();
-                    const uint32_t cntv = __popcll(vis);
-                    if (cntv && myOffV < bEnd && myOffV + cntv > b0) {
-                        uint32_t f = myOffV; ChunkMask mm = vis;
-                        while (mm) {
-                            const uint32_t k = __ffsll(mm) - 1;
-                            mm &= mm - 1;
-                            if (f >= bEnd) break;
-                            if (f >= b0) {
-                                const uint32_t rs = scp[k].rstate;
-                                uint32_t frag = fval[f - b0];
-                                const bool lpk = lpChunk && (scp[k].flags & PFP_KIND);
-                                if (rs & PFS_BLEND)
-                                    frag = lpk ? blend_sisd((int)(rs >> 24), frag, col.get(true))
-                                               : blend_simd((int)(rs >> 24), frag, col.get(false));
-                                col.set(lpk, frag);
-                            }
-                            f++;
-                        }
+                };
+                test(dep0, r0, 0);
+                w1 += 4u * (uint32_t)q1.z; w2 += 4u * (uint32_t)q1.w; w3 += 4u * (uint32_t)q2.x;
+                test(dep1, r1, 1);
+            } else {
+                // a point, line or rectangle set up on the host: its own
+                // coverage and depth, the scalar depth test
+                const PFPrim &P = Q.rec[k].p;
+                const bool counted = ((box >> 16) & 3u) != (PFP_BLIT >> 6);   // rectangles are not fragments
+                auto test = [&](float &d, bool rowOK, uint32_t Y, int s) {
+                    if (!rowOK || !lp_covers(P, (int32_t)X0, (int32_t)Y)) return;
+                    if (counted) cov++;
+                    const float z = lp_depth(P, (int32_t)X0, (int32_t)Y);
+                    if (!(rs & PFS_DEPTH_TEST) || depth_sisd(func, z, d)) {
+                        vis |= 1ull << (32 * s + (int)k);
+                        if (rs & PFS_DEPTH_MASK) d = z;
                     }
-                    // (no barrier: the next chunk starts with one)
-                }
+                };
+                test(dep0, r0, Y0, 0);
+                test(dep1, r1, Y1, 1);
             }
         }
+        frags += cov;
+        // 3+4. shade the fragments that passed, densely over the warp, and
+        //      blend each pixel's in submission order
+        uint32_t totalv;
+        const uint32_t cntv = __popcll(vis);
+        const uint32_t offv = warp_offsets(cntv, totalv);
+        for (uint32_t b0 = 0; b0 < totalv; b0 += QFW) {
+            const uint32_t bEnd = min(totalv, b0 + QFW);
+            tile_list(vis, offv, b0, bEnd, Q.fdesc);
+            __syncwarp();
+            for (uint32_t f = b0 + (uint32_t)lane; f < bEnd; f += 32) {
+                const uint32_t d = Q.fdesc[f - b0], p = d >> 5, k = d & 31u;
+                const uint32_t X = p & 7u, Y = p >> 3;
+                const PFPrim &P = Q.rec[k].p;
+                if (anyLP && (P.flags & PFP_KIND)) {
+                    Q.fc[f - b0] = lp_color(P, (int32_t)(ox + X), (int32_t)(oy + Y));
+                    continue;
+                }
+                float wn[3];
+                const float z = tile_depth(Q.edge[k], P, X, Y, wn);
+                Q.fc[f - b0] = shade_fragment(P, &ph[k], a.states, wn[0], wn[1], wn[2], z);
+            }
+            __syncwarp();
+            if (cntv && offv < bEnd && offv + cntv > b0) {
+                uint32_t f = offv;
+                auto blend = [&](FbPixel<GEN> &c, uint32_t mm) {
+                    for (; mm && f < bEnd; mm &= mm - 1, f++) {
+                        if (f < b0) continue;
+                        const uint32_t k = (uint32_t)(__ffs(mm) - 1);
+                        const uint32_t rs = Q.edge[k].rstate;
+                        const bool lpk = anyLP && (Q.rec[k].p.flags & PFP_KIND);
+                        uint32_t frag = Q.fc[f - b0];
+                        if (rs & PFS_BLEND)
+                            frag = lpk ? blend_sisd((int)(rs >> 24), frag, c.get(true))
+                                       : blend_simd((int)(rs >> 24), frag, c.get(false));
+                        c.set(lpk, frag);
+                    }
+                };
+                blend(col0, (uint32_t)vis);
+                blend(col1, (uint32_t)(vis >> 32));
+            }
+            __syncwarp();                                  // the window's lists are free
+        }
+        __syncwarp();                                      // the batch's records are free
     }
-    if (inside) { col.store(T, pidx); T.depth[pidx] = dep; }
+    if (in0) { col0.store(T, pidx0); T.depth[pidx0] = dep0; }
+    if (in1) { col1.store(T, pidx1); T.depth[pidx1] = dep1; }
     }   // tile loop
 
     // fragment counter: one atomic per CTA (same-address atomics serialise)
@@ -1811,12 +1733,16 @@ int pfd_sm_count(void)
     return sms;
 }
 
+// k_vertex starts a launch's chain: its predecessors in the stream are the
+// uploads, the counter reset and the wait for the draw-time copies, so it
+// is launched without programmatic serialization (its griddepcontrol.wait
+// then returns at once).
 cudaError_t pfd_launch_vertex(const PFBatchLaunch &L, cudaStream_t st)
 {
     const uint32_t nTiles = L.totalTiles;
     const size_t work = L.nVerts > nTiles ? L.nVerts : nTiles;
-    return launch_serialized(k_vertex, grid_for(work, 128), 128, 0, st, L.segs, L.nSegs, L.states, L.vout, L.nVerts,
-                             L.cnt, L.binCount, nTiles);
+    k_vertex<<<grid_for(work, 128), 128, 0, st>>>(L.segs, L.nSegs, L.states, L.vout, L.nVerts, L.cnt, L.binCount, nTiles);
+    return cudaGetLastError();
 }
 
 cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
@@ -1828,26 +1754,57 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
                              (const PFVertexOut *)L.vout, L.nItems, O, B);
 }
 
-static size_t raster_smem(uint32_t cap)
+// Dynamic shared memory of k_raster: the warps' batch buffers and their
+// per-fragment lighting records when the launch has any.
+static size_t raster_smem(bool anyPhong)
 {
-    uint32_t N = 1; while (N < cap) N <<= 1;
-    size_t words = N > (uint32_t)RANK_SORT_MAX ? N : (size_t)2 * RANK_SORT_MAX;
-    if (cap <= RANK_SORT_MAX) words = (size_t)RANK_SORT_MAX + cap;
-    return words * sizeof(uint32_t);
+    return RASTER_WARPS * sizeof(QWarp) + (anyPhong ? RASTER_WARPS * QCHN * sizeof(PFPrimPhong) : 0);
+}
+
+static RasterArgs raster_args(const PFBatchLaunch &L)
+{
+    return RasterArgs{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states,
+                       L.targets, L.nTargets, L.totalTiles, L.cnt, L.command, L.anyPhong };
+}
+
+// Persistent grid of `kernel`: as many CTAs as fit on the GPU at once, at
+// most `perSM` per SM (0: as many as fit), at most `units`.
+static cudaError_t persistent_grid(const void *kernel, int block, size_t smem, int perSM, uint32_t units, uint32_t &grid)
+{
+    int fit = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, block, smem);
+    if (e != cudaSuccess) return e;
+    uint32_t per = (uint32_t)(fit > 0 ? fit : 1);
+    if (perSM > 0) per = min(per, (uint32_t)perSM);
+    grid = max(1u, min(units, (uint32_t)pfd_sm_count() * per));
+    return cudaSuccess;
+}
+
+cudaError_t pfd_launch_binsort(const PFBatchLaunch &L, cudaStream_t st)
+{
+    if (L.totalTiles == 0) return cudaSuccess;
+    uint32_t N = 1; while (N < L.cap) N <<= 1;
+    const size_t smem = (size_t)N * sizeof(uint32_t);
+    cudaError_t e = cudaFuncSetAttribute(k_binsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    uint32_t grid = 0;
+    if (e == cudaSuccess) e = persistent_grid((const void *)k_binsort, SORT_THREADS, smem, 4, L.totalTiles, grid);
+    if (e != cudaSuccess) return e;
+    return launch_serialized(k_binsort, grid, SORT_THREADS, smem, st, raster_args(L));
 }
 
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
-    RasterArgs a{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.prims, L.primsPh, L.pool, L.poolPh, L.states, L.targets, L.nTargets,
-                  L.totalTiles, L.cnt, L.command, L.anyPhong };
-    const size_t smem = raster_smem(L.cap);
-    void (*kernel)(RasterArgs) = L.generic ? k_raster<32, true> : L.chunk == 64 ? k_raster<64, false> : k_raster<32, false>;
+    const size_t smem = raster_smem(L.anyPhong != 0);
+    void (*kernel)(RasterArgs) = L.generic ? k_raster<true> : k_raster<false>;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)     // the CTAs' shared memory, not L1, bounds how many fit on an SM
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    uint32_t grid = 0;
+    if (e == cudaSuccess) e = persistent_grid((const void *)kernel, RASTER_THREADS, smem, L.rasterCtasPerSM,
+                                              (L.totalTiles + RASTER_WARPS - 1) / RASTER_WARPS, grid);
     if (e != cudaSuccess) return e;
-    const uint32_t per = (uint32_t)(L.rasterCtasPerSM > 0 ? L.rasterCtasPerSM : 4);
-    const uint32_t grid = min(L.totalTiles, (uint32_t)pfd_sm_count() * per);
-    return launch_serialized(kernel, grid, RASTER_THREADS, smem, st, a);
+    return launch_serialized(kernel, grid, RASTER_THREADS, smem, st, raster_args(L));
 }
 
 cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,

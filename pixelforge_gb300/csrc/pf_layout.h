@@ -18,7 +18,7 @@
 #define PF_ALIGN16 __attribute__((aligned(16)))
 
 #define PF_MAX_LIGHTS      8
-#define PF_TILE            16          /* tile edge in pixels (one CTA per tile) */
+#define PF_TILE            8           /* tile edge in pixels (one warp per tile) */
 #define PF_TILE_PIXELS     (PF_TILE * PF_TILE)
 #define PF_MAX_SUBTRIS     10          /* fan of a triangle clipped by 7 planes */
 #define PF_CLIP_MAXV       12          /* polygon capacity during clipping */
@@ -206,6 +206,7 @@ typedef struct {
     unsigned int clipCount;       /* clipped sub-triangles allocated */
     unsigned long long batchRasterized;   /* sub-triangles set up by the current batch */
     unsigned int tileQueue;       /* next entry of the current batch's raster work list */
+    unsigned int sortQueue;       /* next entry of the current batch's bin-sort list */
     unsigned int tileListCount;   /* tiles with a non-empty bin, listed by the binning */
     unsigned int heavyCount[PF_HEAVY_LEVELS];   /* tiles whose bin reached 32 << 2 l entries */
 } PFDevCounters;

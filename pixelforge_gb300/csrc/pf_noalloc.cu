@@ -47,8 +47,11 @@ constexpr size_t kOffVout = align256(kOffTarget + sizeof(PFTarget));
 constexpr size_t kOffPrims = align256(kOffVout + sizeof(PFVertexOut) * 3 * (size_t)kMaxTris);
 constexpr size_t kOffPool = align256(kOffPrims + sizeof(PFPrim) * (size_t)kMaxItems);
 constexpr size_t kOffPh = align256(kOffPool + sizeof(PFPrim) * (size_t)kPoolCap);
+// bin counters, then the raster's work lists (the non-empty tiles and those
+// of each heavy level), listStride entries each
+constexpr uint32_t kListStride = (kMaxTiles + 31) & ~31u;
 constexpr size_t kOffBinCount = align256(kOffPh + sizeof(PFPrimPhong));
-constexpr size_t kOffBins = align256(kOffBinCount + sizeof(uint32_t) * (size_t)kMaxTiles);
+constexpr size_t kOffBins = align256(kOffBinCount + sizeof(uint32_t) * (size_t)kListStride * (2 + PF_HEAVY_LEVELS));
 constexpr size_t kScratchBytes = align256(kOffBins + sizeof(uint32_t) * (size_t)kMaxTiles * kBinCap);
 static_assert(kScratchBytes == PFGB_STATIC_SCRATCH_BYTES, "header states the scratch size");
 
@@ -146,11 +149,13 @@ extern "C" int pfgbDrawTrianglesStatic(const float *positions, const uint32_t *c
     L.prims = (PFPrim *)(s + kOffPrims); L.primsPh = (PFPrimPhong *)(s + kOffPh);
     L.pool = (PFPrim *)(s + kOffPool); L.poolPh = (PFPrimPhong *)(s + kOffPh); L.poolCap = kPoolCap;
     L.binCount = (uint32_t *)(s + kOffBinCount); L.bins = (uint32_t *)(s + kOffBins); L.cap = kBinCap;
+    L.listStride = kListStride; L.tileList = L.binCount + kListStride;
     L.targets = (const PFTarget *)(s + kOffTarget); L.nTargets = 1; L.totalTiles = T.tilesX * T.tilesY;
-    L.rasterCtasPerSM = 4;
+    L.rasterCtasPerSM = 0;
     L.cnt = (PFDevCounters *)(s + kOffCnt); L.command = 0;
     e = pfd_launch_vertex(L, st);
     if (e == cudaSuccess) e = pfd_launch_items(L, st);
+    if (e == cudaSuccess) e = pfd_launch_binsort(L, st);
     if (e == cudaSuccess) e = pfd_launch_raster(L, st);
     if (e != cudaSuccess) { cudaGetLastError(); return PFGB_STATIC_E_CUDA; }
     // the counters say whether a tile bin or the clip pool overflowed

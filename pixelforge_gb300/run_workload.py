@@ -5,6 +5,7 @@ profilers and quick checks).
     python -m pixelforge_gb300.run_workload sphere --frames 4 --format RGBA16F
     python -m pixelforge_gb300.run_workload phong --frames 2 --width 960 --height 540
     python -m pixelforge_gb300.run_workload batch --contexts 64 --repeat 2
+    python -m pixelforge_gb300.run_workload soup --frames 4
     python -m pixelforge_gb300.run_workload fit --views 8 --iters 2
 
 Exits non-zero if the device reports an error.
@@ -21,7 +22,7 @@ FORMATS = {"RGBA8": (7, 0), "RGB8": (6, 0), "RGB565": (6, 2), "RGBA5551": (7, 3)
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["sphere", "phong", "batch", "fit"])
+    ap.add_argument("workload", choices=["sphere", "phong", "batch", "fit", "soup"])
     ap.add_argument("--frames", type=int, default=4)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
@@ -69,7 +70,17 @@ def main(argv=None) -> int:
         print(f"batch: {a.contexts} contexts x {a.repeat}, status {status}")
         return 1 if status else 0
 
-    from .scenes import PhongScene, SphereScene, Target
+    from .scenes import PhongScene, SoupScene, SphereScene, Target
+    if a.workload == "soup":
+        sc = SoupScene()
+        tg = Target(lib, sc.width, sc.height, "main")
+        for _ in range(a.frames):
+            sc.record(lib)
+            lib.pfFinish()
+        status = lib.pfGetDeviceStatus()
+        tg.close()
+        print(f"soup: {a.frames} frames at {sc.width}x{sc.height}, status {status}")
+        return 1 if status else 0
     sc = SphereScene(width=a.width, height=a.height) if a.workload == "sphere" else \
         PhongScene(width=a.width, height=a.height)
     tg = Target(lib, sc.width, sc.height, "main", fmt=FORMATS[a.format])

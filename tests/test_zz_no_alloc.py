@@ -70,8 +70,8 @@ def _soup(seed, ntris, near_share=0.0):
 
 
 def _one_tile_pile(seed, ntris):
-    """Triangles inside the first 16x16 tile of the ortho view (more of them
-    than a tile bin holds)."""
+    """Triangles inside the first 16x16 pixels of the ortho view (more of
+    them in each 8x8 tile than a tile bin holds)."""
     r = np.random.default_rng(seed)
     # in a 64x48 ortho view these land on pixels 0..14 of x and 0..14 of y
     x = r.uniform(-1.0, -0.55, (ntris, 3))
