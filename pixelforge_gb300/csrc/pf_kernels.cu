@@ -921,7 +921,8 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 //   2. each lane walks the batch in order at its own two pixels: coverage
 //      with the reference's integer edge functions, depth, depth test and
 //      depth write (triangles.c:398-438) -- which leaves, per pixel, the
-//      fragments that passed;
+//      fragments that passed (bit k of a 32-bit mask: the record's place in
+//      the batch);
 //   3. the passing fragments are listed pixel by pixel in submission order
 //      and shaded densely over the warp (texture, Gouraud / Phong colour:
 //      the source colour does not depend on the destination);
@@ -1032,7 +1033,7 @@ __device__ __forceinline__ float tile_depth(const QEdge &E, const PFPrim &P, uin
     wn[0] = (float)w1 * P.wInvSum; wn[1] = (float)w2 * P.wInvSum; wn[2] = (float)w3 * P.wInvSum;
     float zs = P.z1 * wn[0] + P.z2 * wn[1];
     zs = zs + P.z3 * wn[2];
-    return 1.0f / zs;
+    return __frcp_rn(zs);          // 1 / zs, correctly rounded
 }
 
 // Source colour of one fragment (triangles.c:500-521): colour interpolation,
@@ -1336,37 +1337,6 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
     levelEnd[0] = nQueue;
     uint32_t claim = 0;
     if (lane == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
-    // tiles with an empty bin only get their fused clear, if any: warp w of
-    // the grid takes the groups of 32 tiles w, w + warps of the grid, ...;
-    // the queue's dynamic schedule absorbs the time this costs
-    for (uint32_t t0 = (blockIdx.x * RASTER_WARPS + (uint32_t)warp) * 32u; t0 < a.totalTiles;
-         t0 += gridDim.x * RASTER_THREADS) {
-        const uint32_t t = t0 + (uint32_t)lane;
-        int ti = 0;
-        bool clear = false;
-        if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
-            int tlo = 0, thi = a.nTargets - 1;
-            while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= t) tlo = mid; else thi = mid - 1; }
-            ti = tlo;
-            clear = a.targets[tlo].clearMode != 0;
-        }
-        for (uint32_t m = __ballot_sync(0xffffffffu, clear); m; m &= m - 1) {
-            const int src = __ffs(m) - 1;
-            const PFTarget &T = a.targets[__shfl_sync(0xffffffffu, ti, src)];
-            const uint32_t tile = t0 + (uint32_t)src - T.tileBase;
-            const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
-            for (uint32_t p = (uint32_t)lane; p < PF_TILE_PIXELS; p += 32) {
-                const uint32_t px = ox + p % PF_TILE, py = oy + p / PF_TILE;
-                if (px >= T.W || py >= T.H) continue;
-                const size_t pidx = (size_t)py * T.W + px;
-                if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
-                if (GEN) pff_store(T.fmt, T.color, pidx, T.clearRaw);
-                else ((uint32_t *)T.color)[pidx] = T.clearRaw[0];
-                T.depth[pidx] = T.clearDepth;
-            }
-        }
-    }
-
     for (;;) {
     uint32_t next = 0xffffffffu;
     if (lane == 0) {
@@ -1416,6 +1386,16 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
         const uint32_t nk = n <= 32 ? 1u : n <= 64 ? 2u : 4u;    // keys a lane sorts: a power-of-two network
         for (uint32_t r = 0; r < 4; r++)
             if (32 * r + (uint32_t)lane < n) sk[r] = __ldg(bin + 32 * r + lane);
+        // keys binned by one warp of k_items arrive in order: check first
+        bool ordered = true;
+#pragma unroll
+        for (uint32_t r = 0; r < 4; r++) {
+            if (r >= nk) break;                               // uniform over the warp
+            const uint32_t o = __shfl_down_sync(0xffffffffu, sk[r], 1);
+            const uint32_t b = __shfl_sync(0xffffffffu, sk[r < 3 ? r + 1 : 3], 0);
+            ordered = ordered && (lane < 31 ? sk[r] <= o : (r + 1 < nk ? sk[r] <= b : true));
+        }
+        if (!__all_sync(0xffffffffu, ordered))
         for (uint32_t k = 2; k <= 32 * nk; k <<= 1)
             for (uint32_t j = k >> 1; j > 0; j >>= 1) {
                 if (j >= 32) {
@@ -1423,6 +1403,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
                     const uint32_t dr = j >> 5;
 #pragma unroll
                     for (uint32_t r = 0; r < 4; r++) {
+                        if (r >= nk) break;
                         if (r & dr) continue;
                         const uint32_t i = 32 * r + (uint32_t)lane;
                         const uint32_t x = sk[r], y = sk[r + dr];
@@ -1433,6 +1414,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
                 } else {
 #pragma unroll
                     for (uint32_t r = 0; r < 4; r++) {
+                        if (r >= nk) break;                       // uniform over the warp
                         const uint32_t i = 32 * r + (uint32_t)lane;
                         const uint32_t o = __shfl_xor_sync(0xffffffffu, sk[r], j);
                         sk[r] = (((i & k) == 0) == ((i & j) == 0)) ? min(sk[r], o) : max(sk[r], o);
@@ -1472,7 +1454,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
         __syncwarp();
         // 2. my two pixels walk the batch in submission order: coverage,
         //    depth, depth test, depth write
-        unsigned long long vis = 0;                     // bit 32 s + k: record k passed at my pixel of slot s
+        uint32_t vis0 = 0, vis1 = 0;                    // bit k: record k passed at my pixel of slot 0 / 1
         uint32_t cov = 0;
         for (uint32_t k = 0; k < cn; k++) {
             const int4 *e4 = reinterpret_cast<const int4 *>(&Q.edge[k]);
@@ -1490,7 +1472,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
                 uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + ly * (uint32_t)q2.x;
                 const float4 zq = reinterpret_cast<const float4 *>(&Q.rec[k].p)[3];     // wInvSum z1 z2 z3
                 const float zRej = __int_as_float(q2.w);
-                auto test = [&](float &d, bool rowOK, int s) {
+                auto test = [&](float &d, uint32_t &vis, bool rowOK) {
                     if (!rowOK || !((int32_t)(w1 | w2 | w3) > 0)) return;
                     cov++;
                     if (zRej >= d) return;                      // every fragment of it fails the depth test
@@ -1498,42 +1480,42 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
                     const float wn3 = (float)(int32_t)w3 * zq.x;
                     float zs = zq.y * wn1 + zq.z * wn2;
                     zs = zs + zq.w * wn3;
-                    const float z = 1.0f / zs;
+                    const float z = __frcp_rn(zs);
                     if (!(rs & PFS_DEPTH_TEST) || depth_simd(func, z, d)) {
-                        vis |= 1ull << (32 * s + (int)k);
+                        vis |= 1u << k;
                         if (rs & PFS_DEPTH_MASK) d = z;
                     }
                 };
-                test(dep0, r0, 0);
+                test(dep0, vis0, r0);
                 w1 += 4u * (uint32_t)q1.z; w2 += 4u * (uint32_t)q1.w; w3 += 4u * (uint32_t)q2.x;
-                test(dep1, r1, 1);
+                test(dep1, vis1, r1);
             } else {
                 // a point, line or rectangle set up on the host: its own
                 // coverage and depth, the scalar depth test
                 const PFPrim &P = Q.rec[k].p;
                 const bool counted = ((box >> 16) & 3u) != (PFP_BLIT >> 6);   // rectangles are not fragments
-                auto test = [&](float &d, bool rowOK, uint32_t Y, int s) {
+                auto test = [&](float &d, uint32_t &vis, bool rowOK, uint32_t Y) {
                     if (!rowOK || !lp_covers(P, (int32_t)X0, (int32_t)Y)) return;
                     if (counted) cov++;
                     const float z = lp_depth(P, (int32_t)X0, (int32_t)Y);
                     if (!(rs & PFS_DEPTH_TEST) || depth_sisd(func, z, d)) {
-                        vis |= 1ull << (32 * s + (int)k);
+                        vis |= 1u << k;
                         if (rs & PFS_DEPTH_MASK) d = z;
                     }
                 };
-                test(dep0, r0, Y0, 0);
-                test(dep1, r1, Y1, 1);
+                test(dep0, vis0, r0, Y0);
+                test(dep1, vis1, r1, Y1);
             }
         }
         frags += cov;
         // 3+4. shade the fragments that passed, densely over the warp, and
         //      blend each pixel's in submission order
         uint32_t totalv;
-        const uint32_t cntv = __popcll(vis);
+        const uint32_t cntv = __popc(vis0) + __popc(vis1);
         const uint32_t offv = warp_offsets(cntv, totalv);
         for (uint32_t b0 = 0; b0 < totalv; b0 += QFW) {
             const uint32_t bEnd = min(totalv, b0 + QFW);
-            tile_list(vis, offv, b0, bEnd, Q.fdesc);
+            tile_list(vis0 | ((unsigned long long)vis1 << 32), offv, b0, bEnd, Q.fdesc);
             __syncwarp();
             for (uint32_t f = b0 + (uint32_t)lane; f < bEnd; f += 32) {
                 const uint32_t d = Q.fdesc[f - b0], p = d >> 5, k = d & 31u;
@@ -1563,8 +1545,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
                         c.set(lpk, frag);
                     }
                 };
-                blend(col0, (uint32_t)vis);
-                blend(col1, (uint32_t)(vis >> 32));
+                blend(col0, vis0);
+                blend(col1, vis1);
             }
             __syncwarp();                                  // the window's lists are free
         }
@@ -1573,6 +1555,39 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
     if (in0) { col0.store(T, pidx0); T.depth[pidx0] = dep0; }
     if (in1) { col1.store(T, pidx1); T.depth[pidx1] = dep1; }
     }   // tile loop
+
+    // tiles with an empty bin only get their fused clear, if any: warp w of
+    // the grid takes the groups of 32 tiles w, w + warps of the grid, ...,
+    // once the queue is empty (in the tail of the launch, when warps would
+    // otherwise wait for the last tiles)
+    for (uint32_t t0 = (blockIdx.x * RASTER_WARPS + (uint32_t)warp) * 32u; t0 < a.totalTiles;
+         t0 += gridDim.x * RASTER_THREADS) {
+        const uint32_t t = t0 + (uint32_t)lane;
+        int ti = 0;
+        bool clear = false;
+        if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
+            int tlo = 0, thi = a.nTargets - 1;
+            while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= t) tlo = mid; else thi = mid - 1; }
+            ti = tlo;
+            clear = a.targets[tlo].clearMode != 0;
+        }
+        for (uint32_t m = __ballot_sync(0xffffffffu, clear); m; m &= m - 1) {
+            const int src = __ffs(m) - 1;
+            const PFTarget &T = a.targets[__shfl_sync(0xffffffffu, ti, src)];
+            const uint32_t tile = t0 + (uint32_t)src - T.tileBase;
+            const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
+            for (uint32_t p = (uint32_t)lane; p < PF_TILE_PIXELS; p += 32) {
+                const uint32_t px = ox + p % PF_TILE, py = oy + p / PF_TILE;
+                if (px >= T.W || py >= T.H) continue;
+                const size_t pidx = (size_t)py * T.W + px;
+                if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
+                if (GEN) pff_store(T.fmt, T.color, pidx, T.clearRaw);
+                else ((uint32_t *)T.color)[pidx] = T.clearRaw[0];
+                T.depth[pidx] = T.clearDepth;
+            }
+        }
+    }
+
 
     // fragment counter: one atomic per CTA (same-address atomics serialise)
     __shared__ unsigned long long sFrags;
