@@ -354,7 +354,12 @@ PF_API void pfDepthMask(PFboolean flag);
 typedef enum {
     PF_HOOK_IDENTITY   = 0,  /* params: none */
     PF_HOOK_FOG_LINEAR = 1,  /* params: PFhookfog */
-    PF_HOOK_GRAYSCALE  = 2   /* params: none */
+    PF_HOOK_GRAYSCALE  = 2,  /* params: none */
+    PF_HOOK_DITHER     = 3   /* params: none.  The ordered 3x3 dither of the reference's post-process
+                                example (examples/raylib/raylib_PostProcess.c:7-19): the pixel at
+                                column x, row y becomes white (all four channels 255) when
+                                (r + g + b) / 3 >= M[x % 3][y % 3], else 0, with
+                                M = {{230, 51, 128}, {25, 102, 179}, {154, 205, 77}} */
 } PFhookid;
 
 /* Linear fog on the stored depth.  d = (depth + znear) / (zfar + znear)
@@ -426,9 +431,14 @@ PF_API PFfloat   pfgbBatchReplay(PFgbbatch batch, PFuint n);
 PF_API void      pfgbBatchGetStats(PFgbbatch batch, PFstats* stats);
 PF_API void      pfgbBatchEnableTiming(PFgbbatch batch, PFboolean enable);
 /* Tuning knobs (set by the project's autotuner): tile-bin capacity (a power
- * of two, 32..16384; bins still grow on overflow) and persistent raster CTAs
- * per SM (1..8).  batch == NULL tunes the current context. */
+ * of two, 32..16384; bins still grow on overflow; other values leave the
+ * setting) and persistent raster CTAs per SM (1..32, at most as many as fit;
+ * 0: as many as fit, the default; larger values leave the setting).
+ * batch == NULL tunes the current context. */
 PF_API void      pfgbBatchTune(PFgbbatch batch, PFuint binCapacity, PFuint rasterCtasPerSM);
+/* The raster's block shape: warps per CTA, 2, 4 (the default) or 8; each
+ * warp rasterizes one 8x8 tile at a time.  Other values leave the setting. */
+PF_API void      pfgbBatchTuneShape(PFgbbatch batch, PFuint rasterWarpsPerCta);
 /* The same graph replay for the current context's last render. */
 PF_API PFfloat   pfgbReplay(PFuint n);
 

@@ -2451,6 +2451,17 @@ static PFcolor hook_gray(PFint x, PFint y, PFfloat depth, PFcolor c)
     return c;
 }
 static PFcolor hook_identity(PFint x, PFint y, PFfloat depth, PFcolor c) { (void)x; (void)y; (void)depth; return c; }
+/* examples/raylib/raylib_PostProcess.c:7-19 */
+static PFcolor hook_dither(PFint x, PFint y, PFfloat depth, PFcolor c)
+{
+    static const uint8_t m[3][3] = { { 230, 51, 128 }, { 25, 102, 179 }, { 154, 205, 77 } };
+    (void)depth;
+    const uint8_t dv = m[x % 3][y % 3];
+    const uint8_t avg = (uint8_t)((c.r + c.g + c.b) / 3);
+    const uint32_t v = (avg >= dv) ? 0xffffffffu : 0u;
+    memcpy(&c, &v, 4);
+    return c;
+}
 
 void pfPostProcessDevice(PFuint hookId, const void *params, PFsizei size)
 {
@@ -2460,6 +2471,7 @@ void pfPostProcessDevice(PFuint hookId, const void *params, PFsizei size)
         if (!params || size < sizeof(PFhookfog)) { G->err = PF_INVALID_VALUE; return; }
         memcpy(&g_fog, params, sizeof g_fog); pfPostProcess(hook_fog); break;
     case PF_HOOK_GRAYSCALE: pfPostProcess(hook_gray); break;
+    case PF_HOOK_DITHER: pfPostProcess(hook_dither); break;
     default: G->err = PF_INVALID_ENUM; break;
     }
 }
@@ -2468,6 +2480,8 @@ void pfPostProcessDevice(PFuint hookId, const void *params, PFsizei size)
  * with the same definition. */
 PFcolor pfref_fog_hook(PFint x, PFint y, PFfloat depth, PFcolor c) { return hook_fog(x, y, depth, c); }
 void pfref_set_fog(const PFhookfog *f) { g_fog = *f; }
+/* The dither hook as a host callback. */
+PFcolor pfref_dither_hook(PFint x, PFint y, PFfloat depth, PFcolor c) { return hook_dither(x, y, depth, c); }
 
 void pfGetStats(PFstats *s) { *s = G->stats; }
 void pfResetStats(void) { memset(&G->stats, 0, sizeof G->stats); }

@@ -88,7 +88,7 @@ def pixel_bytes(fmt: int, typ: int) -> int:
  PF_POLYGON_MODE, PF_POINT_SIZE, PF_LINE_WIDTH, PF_MATRIX_MODE, PF_PROJECTION_MATRIX, PF_MODELVIEW_MATRIX,
  PF_TEXTURE_MATRIX, PF_MAX_PROJECTION_STACK_DEPTH, PF_MAX_MODELVIEW_STACK_DEPTH, PF_MAX_TEXTURE_STACK_DEPTH,
  PF_SHADE_MODEL) = range(10000, 10021)
-PF_HOOK_IDENTITY, PF_HOOK_FOG_LINEAR, PF_HOOK_GRAYSCALE = 0, 1, 2
+PF_HOOK_IDENTITY, PF_HOOK_FOG_LINEAR, PF_HOOK_GRAYSCALE, PF_HOOK_DITHER = 0, 1, 2, 3
 
 _V = None
 _FP = C.POINTER(C.c_float)
@@ -242,6 +242,7 @@ PROTOTYPES = {
     "pfgbBatchGetStats": (_V, [PFptr, C.POINTER(PFstats)]),
     "pfgbBatchEnableTiming": (_V, [PFptr, PFbool]),
     "pfgbBatchTune": (_V, [PFptr, PFuint, PFuint]),
+    "pfgbBatchTuneShape": (_V, [PFptr, PFuint]),
     "pfgbReplay": (PFfloat, [PFuint]),
 }
 

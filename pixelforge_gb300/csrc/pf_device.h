@@ -14,6 +14,7 @@ struct PFHookParams {
     uint32_t color;
     uint32_t mode;                /* pfFogProcess: PF_LINEAR, PF_EXP, PF_EXP2 (others: no fog term) */
     float density;
+    uint32_t width;               /* framebuffer width (hooks that depend on the pixel's column and row) */
 };
 
 /* Device pointers and sizes of one raster batch (a run of draw segments on
@@ -40,6 +41,7 @@ struct PFBatchLaunch {
     int nTargets;
     uint32_t totalTiles;
     int rasterCtasPerSM;      /* persistent raster grid: SMs x this, at most as many as fit (0: as many as fit) */
+    int rasterWarps;          /* warps (tiles in flight) per raster CTA: 2, 4 (default) or 8 */
     int anyPhong;             /* some state of the launch lights per fragment */
     int generic;              /* some target is not RGBA / unsigned byte */
     PFDevCounters *cnt;

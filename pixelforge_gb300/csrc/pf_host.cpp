@@ -274,6 +274,7 @@ struct Renderer {
     DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters;
     uint32_t cap = 256, poolCap = 4096;
     int rasterCtasPerSM = 0;                // 0: as many raster CTAs per SM as fit
+    int rasterWarps = 4;                    // warps per raster CTA
     PFDevCounters *hostCounters = nullptr;
     PFstats stats{};
     PFuint devStatus = 0;
@@ -1733,6 +1734,7 @@ bool flush(Renderer *r)
                 rop.n = m->w * m->h; rop.color = m->dColor; rop.fmt = m->fmt; rop.depth = m->dDepth;
                 clear_raw(m->fmt, cmd, rop.cc);
                 rop.cd = cmd.depth; rop.all = cmd.kind == CMD_FILL; rop.hook = cmd.hook; rop.hp = cmd.hp;
+                rop.hp.width = (uint32_t)m->w;
                 r->stats.kernel_launches += 1;
                 e = (o.kind == 1) ? pfd_launch_clear(rop.color, rop.fmt, rop.depth, rop.n, rop.cc, rop.cd, rop.all, dcnt, (uint32_t)oi, st)
                                   : pfd_launch_hook(rop.color, rop.fmt, rop.depth, rop.n, rop.hook, rop.hp, dcnt, (uint32_t)oi, st);
@@ -1745,6 +1747,7 @@ bool flush(Renderer *r)
                 L.listStride = (uint32_t)(((size_t)maxTiles + 31) & ~(size_t)31);
                 L.tileList = (uint32_t *)r->binCount.p + L.listStride;
                 L.rasterCtasPerSM = r->rasterCtasPerSM;
+                L.rasterWarps = r->rasterWarps;
                 L.anyPhong = anyPhong ? 1 : 0;
                 L.cnt = dcnt;
                 rop.L = L;
@@ -3035,6 +3038,7 @@ void pfPostProcessDevice(PFuint hookId, const void *params, PFsizei size)
     cmd.kind = CMD_HOOK; cmd.fb = G->current; cmd.hook = (int)hookId;
     switch (hookId) {
     case PF_HOOK_IDENTITY: case PF_HOOK_GRAYSCALE: break;
+    case PF_HOOK_DITHER: cmd.hook = 4; break;        // device hook 3 is pfFogProcess
     case PF_HOOK_FOG_LINEAR: {
         if (!params || size < sizeof(PFhookfog)) { G->err = PF_INVALID_VALUE; return; }
         PFhookfog f; std::memcpy(&f, params, sizeof f);
@@ -3098,7 +3102,14 @@ void pfgbBatchTune(PFgbbatch batch, PFuint binCapacity, PFuint rasterCtasPerSM)
     Renderer *r = batch ? &((Batch *)batch)->r : (G ? &G->own : nullptr);
     if (!r) return;
     if (binCapacity >= 32 && binCapacity <= kCapMax && (binCapacity & (binCapacity - 1)) == 0) r->cap = binCapacity;
-    if (rasterCtasPerSM >= 1 && rasterCtasPerSM <= 8) r->rasterCtasPerSM = (int)rasterCtasPerSM;
+    if (rasterCtasPerSM <= 32) r->rasterCtasPerSM = (int)rasterCtasPerSM;
+}
+
+void pfgbBatchTuneShape(PFgbbatch batch, PFuint rasterWarpsPerCta)
+{
+    Renderer *r = batch ? &((Batch *)batch)->r : (G ? &G->own : nullptr);
+    if (!r) return;
+    if (rasterWarpsPerCta == 2 || rasterWarpsPerCta == 4 || rasterWarpsPerCta == 8) r->rasterWarps = (int)rasterWarpsPerCta;
 }
 
 PFfloat pfgbReplay(PFuint n) { return G ? replay(&G->own, n) : -1.0f; }

@@ -929,8 +929,8 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 //   4. every pixel blends its listed fragments in order into its colour,
 //      held in registers with its depth for the whole tile.
 // ---------------------------------------------------------------------------
-#define RASTER_THREADS 128          // four independent warps
-#define RASTER_WARPS (RASTER_THREADS / 32)
+// k_raster's CTAs group 2, 4 or 8 independent warps (the block shape, a
+// tuning knob); each warp owns one tile at a time
 #define QCHN 32                     // records per batch (bit k of a pixel's 32-bit masks)
 #define QFW 128                     // fragment window of a warp
 #define SORT_THREADS 256
@@ -1311,13 +1311,13 @@ __device__ __forceinline__ uint32_t warp_offsets(uint32_t v, uint32_t &total)
     return s - v;
 }
 
-template <bool GEN>
-__global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
+template <bool GEN, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
 {
     extern __shared__ __align__(16) unsigned char rsmem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     QWarp &Q = reinterpret_cast<QWarp *>(rsmem)[warp];
-    PFPrimPhong *const ph = reinterpret_cast<PFPrimPhong *>(rsmem + RASTER_WARPS * sizeof(QWarp)) + warp * QCHN;
+    PFPrimPhong *const ph = reinterpret_cast<PFPrimPhong *>(rsmem + WARPS * sizeof(QWarp)) + warp * QCHN;
 
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_binsort is done
     if (a.cnt->abortCommand <= a.command) return;
@@ -1560,8 +1560,8 @@ __global__ void __launch_bounds__(RASTER_THREADS, 6) k_raster(RasterArgs a)
     // the grid takes the groups of 32 tiles w, w + warps of the grid, ...,
     // once the queue is empty (in the tail of the launch, when warps would
     // otherwise wait for the last tiles)
-    for (uint32_t t0 = (blockIdx.x * RASTER_WARPS + (uint32_t)warp) * 32u; t0 < a.totalTiles;
-         t0 += gridDim.x * RASTER_THREADS) {
+    for (uint32_t t0 = (blockIdx.x * WARPS + (uint32_t)warp) * 32u; t0 < a.totalTiles;
+         t0 += gridDim.x * (WARPS * 32)) {
         const uint32_t t = t0 + (uint32_t)lane;
         int ti = 0;
         bool clear = false;
@@ -1679,6 +1679,14 @@ __global__ void k_hook(void *color, uint32_t fmt, const float *depth, size_t n, 
         } else if (hook == 2) {   // grayscale
             uint32_t gy = (77u * chn(c, 0) + 150u * chn(c, 1) + 29u * chn(c, 2)) >> 8;
             c = gy | (gy << 8) | (gy << 16) | (c & 0xff000000u);
+        } else if (hook == 4) {   // ordered 3x3 dither (examples/raylib/raylib_PostProcess.c:7-19)
+            const uint32_t x = (uint32_t)(i % hp.width), y = (uint32_t)(i / hp.width);
+            // the matrix {{230, 51, 128}, {25, 102, 179}, {154, 205, 77}}, row
+            // x % 3, column y % 3: its first eight bytes packed low to high
+            const uint32_t m = x % 3u * 3u + y % 3u;
+            const uint32_t dv = m < 8u ? (uint32_t)((0xCD9AB366198033E6ull >> (8u * m)) & 255u) : 77u;
+            const uint32_t avg = (chn(c, 0) + chn(c, 1) + chn(c, 2)) / 3u;
+            c = (avg >= dv) ? 0xffffffffu : 0u;
         }
         if (write) {
             pff_set_sisd(fmt, c, raw);
@@ -1771,9 +1779,9 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 
 // Dynamic shared memory of k_raster: the warps' batch buffers and their
 // per-fragment lighting records when the launch has any.
-static size_t raster_smem(bool anyPhong)
+static size_t raster_smem(bool anyPhong, int warps)
 {
-    return RASTER_WARPS * sizeof(QWarp) + (anyPhong ? RASTER_WARPS * QCHN * sizeof(PFPrimPhong) : 0);
+    return (size_t)warps * (sizeof(QWarp) + (anyPhong ? QCHN * sizeof(PFPrimPhong) : 0));
 }
 
 static RasterArgs raster_args(const PFBatchLaunch &L)
@@ -1810,16 +1818,19 @@ cudaError_t pfd_launch_binsort(const PFBatchLaunch &L, cudaStream_t st)
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
-    const size_t smem = raster_smem(L.anyPhong != 0);
-    void (*kernel)(RasterArgs) = L.generic ? k_raster<true> : k_raster<false>;
+    const int warps = (L.rasterWarps == 2 || L.rasterWarps == 8) ? L.rasterWarps : 4;
+    const size_t smem = raster_smem(L.anyPhong != 0, warps);
+    void (*kernel)(RasterArgs) =
+        L.generic ? (warps == 2 ? k_raster<true, 2> : warps == 8 ? k_raster<true, 8> : k_raster<true, 4>)
+                  : (warps == 2 ? k_raster<false, 2> : warps == 8 ? k_raster<false, 8> : k_raster<false, 4>);
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)     // the CTAs' shared memory, not L1, bounds how many fit on an SM
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     uint32_t grid = 0;
-    if (e == cudaSuccess) e = persistent_grid((const void *)kernel, RASTER_THREADS, smem, L.rasterCtasPerSM,
-                                              (L.totalTiles + RASTER_WARPS - 1) / RASTER_WARPS, grid);
+    if (e == cudaSuccess) e = persistent_grid((const void *)kernel, warps * 32, smem, L.rasterCtasPerSM,
+                                              (L.totalTiles + (uint32_t)warps - 1) / (uint32_t)warps, grid);
     if (e != cudaSuccess) return e;
-    return launch_serialized(kernel, grid, RASTER_THREADS, smem, st, raster_args(L));
+    return launch_serialized(kernel, grid, (unsigned)(warps * 32), smem, st, raster_args(L));
 }
 
 cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,

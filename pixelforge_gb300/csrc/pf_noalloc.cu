@@ -151,7 +151,7 @@ extern "C" int pfgbDrawTrianglesStatic(const float *positions, const uint32_t *c
     L.binCount = (uint32_t *)(s + kOffBinCount); L.bins = (uint32_t *)(s + kOffBins); L.cap = kBinCap;
     L.listStride = kListStride; L.tileList = L.binCount + kListStride;
     L.targets = (const PFTarget *)(s + kOffTarget); L.nTargets = 1; L.totalTiles = T.tilesX * T.tilesY;
-    L.rasterCtasPerSM = 0;
+    L.rasterCtasPerSM = 0; L.rasterWarps = 4;
     L.cnt = (PFDevCounters *)(s + kOffCnt); L.command = 0;
     e = pfd_launch_vertex(L, st);
     if (e == cudaSuccess) e = pfd_launch_items(L, st);

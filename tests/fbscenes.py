@@ -65,8 +65,8 @@ def _soup(lib, r, n):
 def run_fb(lib: A.PixelForgeLib, case: dict, device_hook: bool = True) -> dict:
     """Render the case; returns the framebuffer's raw pixels and depth and
     what the per-pixel functions and pfReadPixels returned.  device_hook:
-    run the grayscale device post-process on every third seed (libraries
-    that have pfPostProcessDevice)."""
+    run the grayscale device post-process on every third seed and the
+    dither one on the next (libraries that have pfPostProcessDevice)."""
     r = np.random.default_rng(case["seed"] + 505)
     W, H, fmt = case["W"], case["H"], case["fmt"]
     init = _init_pixels(fmt, W, H, r) if case["target"] == "main" else None
@@ -124,6 +124,8 @@ def run_fb(lib: A.PixelForgeLib, case: dict, device_hook: bool = True) -> dict:
         lib.pfFogProcess()
         if device_hook and case["seed"] % 3 == 0:
             lib.pfPostProcessDevice(A.PF_HOOK_GRAYSCALE, None, 0)
+        elif device_hook and case["seed"] % 3 == 1:
+            lib.pfPostProcessDevice(A.PF_HOOK_DITHER, None, 0)
         _soup(lib, r, 4)
         # per-pixel framebuffer functions (framebuffer objects only)
         if tg.fb is not None:

@@ -36,6 +36,29 @@ def test_batch_equals_per_context(gpu):
         sc.destroy(gpu)
 
 
+def test_batch_block_shapes_and_capacities_agree(gpu):
+    """Every tuning point the autotuner may pick (warps per raster CTA, bin
+    capacity, CTAs per SM) renders the same images."""
+    sc = BatchScene(n=24, max_side=256, tri_clip=(100, 3000), seed=33)
+    sc.create(gpu)
+    try:
+        batch = gpu.pfgbBatchCreate()
+        try:
+            first = None
+            for warps, cap, per in ((4, 256, 0), (2, 1024, 0), (8, 4096, 0), (4, 64, 3), (8, 256, 1)):
+                gpu.pfgbBatchTune(batch, cap, per)
+                gpu.pfgbBatchTuneShape(batch, warps)
+                got = sc.render_batch(gpu, batch)
+                if first is None:
+                    first = got
+                else:
+                    assert _images_equal(first, got), f"{warps} warps, capacity {cap}, {per} CTAs/SM"
+        finally:
+            gpu.pfgbBatchDelete(batch)
+    finally:
+        sc.destroy(gpu)
+
+
 def test_batch_vs_oracle(gpu, oracle):
     sc_g = BatchScene(n=12, max_side=192, tri_clip=(100, 900), seed=32)
     sc_o = BatchScene(n=12, max_side=192, tri_clip=(100, 900), seed=32)

@@ -92,3 +92,31 @@ def test_oracle_equals_reference_ragged_framebuffers(oracle, ref_shim):
         for key in ("color", "depth", "read", "get"):
             if key in a:
                 assert np.array_equal(a[key].view(np.uint8), b[key].view(np.uint8)), f"{case}: {key} differs"
+
+
+def _soup_then_hook(lib, hook, width=250, height=131):
+    from pixelforge_gb300.scenes import Target
+    sc = SoupScene(width=width, height=height, ntris=400)
+    tg = Target(lib, width, height, "fbo")
+    try:
+        sc.record(lib)
+        hook(lib)
+        return tg.finish()
+    finally:
+        tg.close()
+
+
+def test_oracle_dither_hook_equals_reference_post_process(oracle, ref_shim):
+    """The dither device hook (examples/raylib/raylib_PostProcess.c:7-19)
+    against the reference's own pfPostProcess driving the same per-pixel
+    function: pixel order, column/row arguments and the scalar getter and
+    setter around the hook."""
+    import ctypes as C
+    fn = C.cast(oracle.raw("pfref_dither_hook"), C.c_void_p).value
+    post = ref_shim.raw("pfPostProcess")
+    post.argtypes = [C.c_void_p]
+    post.restype = None
+    a = _soup_then_hook(oracle, lambda lib: lib.pfPostProcessDevice(A.PF_HOOK_DITHER, None, 0))
+    b = _soup_then_hook(ref_shim, lambda lib: post(fn))
+    assert 0 < int((a.color[..., 0] == 255).sum()) < a.color.shape[0] * a.color.shape[1]
+    same(a, b, "dither")

@@ -53,6 +53,25 @@ def test_soup_variants(gpu, oracle, kw):
     assert_parity(sc.render(gpu), sc.render(oracle), exact_color=True, label=str(kw))
 
 
+@pytest.mark.parametrize("hook", [A.PF_HOOK_DITHER, A.PF_HOOK_GRAYSCALE])
+def test_device_hooks_on_odd_width(gpu, oracle, hook):
+    """Device post-process hooks after a soup on a 250x131 framebuffer
+    (the dither hook depends on each pixel's column and row)."""
+    from pixelforge_gb300.scenes import Target
+    out = []
+    for lib in (gpu, oracle):
+        sc = SoupScene(width=250, height=131, ntris=400)
+        tg = Target(lib, 250, 131, "fbo")
+        try:
+            sc.record(lib)
+            lib.pfPostProcessDevice(hook, None, 0)
+            out.append(tg.finish())
+        finally:
+            tg.close()
+    assert gpu.pfGetDeviceStatus() == 0
+    assert_parity(out[0], out[1], exact_color=True, label=f"hook {hook}")
+
+
 def test_soup_main_target(gpu, oracle):
     sc = SoupScene(ntris=700)
     got, ref = sc.render(gpu, "main"), sc.render(oracle, "main")
