@@ -182,8 +182,9 @@ def run_gpu(args):
     # immediate-mode bytes: per fragment depth read + write and colour write
     # (12 B), 16 texel bytes (bilinear), colour read when blending (4 B)
     immediate = f_all * (12 + 16) + (f_all - f_opaque) * 4
-    # each draw copies what it references: positions, normals, uvs, indices, texture
-    h2d = 2 * (scene.pos.nbytes * 2 + scene.uv.nbytes + scene.idx.nbytes + scene.tex.nbytes)
+    # each draw copies what it references: positions (the normals are the same
+    # array, copied once), uvs, indices, texture
+    h2d = 2 * (scene.pos.nbytes + scene.uv.nbytes + scene.idx.nbytes + scene.tex.nbytes)
     d2h = scene.width * scene.height * 4
     out = {
         "metric": "fragments/s",

@@ -126,6 +126,8 @@ struct Tex {
     bool ownsPinned;     // colour of a pfGenFramebuffer framebuffer (pinned host memory)
     bool depthPinned;    // its depth buffer is pinned host memory (else malloc)
     bool isMain;         // a context's main framebuffer (its depth is internal)
+    uint32_t drawUses = 0;         // draw-time snapshots taken of the texels
+    bool hostRegistered = false;   // the texels were page-locked by the library (cudaHostRegister)
 };
 
 struct Light {
@@ -801,10 +803,26 @@ int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
 
 // RGBA8 snapshot of a texture: its own bytes, or the converted texels of
 // another format (from a snapshot of its bytes, converted once per recording).
+// A texture drawn with a second time and large enough that its draw-time
+// copy pays for page-locking: its texels are registered with the driver
+// (until pfDeleteTexture), so that every later snapshot is a DMA rather
+// than a copy through the driver's pageable staging.
+constexpr size_t kPinTextureMin = (size_t)1 << 20;
+void pin_texture(Renderer *r, Tex *t, size_t bytes)
+{
+    if (t->hostRegistered || t->ownsPinned || ++t->drawUses < 2 || bytes < kPinTextureMin || !device_init(r)) return;
+    if (!is_pageable(t->pixels)) return;                          // page-locked by someone else already
+    if (cudaHostRegister(t->pixels, bytes, cudaHostRegisterDefault) == cudaSuccess) t->hostRegistered = true;
+    else cudaGetLastError();
+}
+
 int64_t snapshot_texture(Renderer *r, const Tex *t)
 {
     const size_t n = (size_t)t->w * t->h;
-    if (t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE) return snapshot(r, t->pixels, n * 4);
+    if (t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE) {
+        pin_texture(r, const_cast<Tex *>(t), n * 4);
+        return snapshot(r, t->pixels, n * 4);
+    }
     const int64_t raw = snapshot(r, t->pixels, n * (size_t)texel_bytes(t->format, t->type), false);   // read here
     for (auto &cv : r->conversions)
         if (cv.rawOff == raw && cv.format == t->format && cv.type == t->type) return cv.off;
@@ -2490,7 +2508,11 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
 
     SegRec &r = c->rend->segs[si];
     r.posOff = stage_float_attr(c, c->positions, c->positions.size, (size_t)first, nverts);
-    if (useN) r.nrmOff = stage_float_attr(c, c->normals, 3, (size_t)first, nverts);
+    // the normals are often the positions' own array (unit spheres): one copy
+    // taken in the same call serves both
+    if (useN) r.nrmOff = (c->normals.buf == c->positions.buf && c->normals.type == PF_FLOAT &&
+                          c->positions.type == PF_FLOAT && c->positions.size == 3)
+                             ? r.posOff : stage_float_attr(c, c->normals, 3, (size_t)first, nverts);
     if (useT) r.uvOff = stage_float_attr(c, c->texcoords, 2, (size_t)first, nverts);
     if (useC) r.colOff = stage_color_attr(c, c->colors, (size_t)first, nverts);
     r.idxOff = idxOff;
@@ -3222,6 +3244,7 @@ void pfDeleteTexture(PFtexture *tex, PFboolean freeBuffer)
     Tex *t = (Tex *)*tex;
     if (!t) return;
     if (G && G->texture == t) G->texture = nullptr;   // snapshots already hold the texels
+    if (t->hostRegistered) cudaHostUnregister(t->pixels);
     if (freeBuffer) std::free(t->pixels);
     delete t;
     *tex = nullptr;
