@@ -1328,30 +1328,72 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
 
     // persistent: warps take tiles from a shared work queue -- the tiles the
     // binning listed as non-empty, those of the heaviest level first, then
-    // of each lighter level, then the rest; a tile is rasterized from the
-    // first list it is on and skipped on the later ones
+    // of each lighter level, then the rest (a tile is rasterized from the
+    // first list it is on and skipped on the later ones); then the groups of
+    // 32 tiles whose empty bins only get their fused clear, if any, one tile
+    // a lane
     uint32_t levelEnd[PF_HEAVY_LEVELS + 1];           // queue index past level l's entries, heaviest first
     uint32_t nQueue = 0;
     for (int l = PF_HEAVY_LEVELS; l >= 1; l--) { nQueue += min(a.cnt->heavyCount[l - 1], a.totalTiles); levelEnd[l] = nQueue; }
     nQueue += min(a.cnt->tileListCount, a.totalTiles);
     levelEnd[0] = nQueue;
+    const uint32_t nClear = (a.totalTiles + 31u) / 32u;
     uint32_t claim = 0;
     if (lane == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
     for (;;) {
     uint32_t next = 0xffffffffu;
     if (lane == 0) {
         const uint32_t q = claim;
-        if (q < nQueue) {
+        if (q < nQueue + nClear) {
             claim = atomicAdd(&a.cnt->tileQueue, 1u);
-            uint32_t level = PF_HEAVY_LEVELS, begin = 0;
-            while (q >= levelEnd[level]) { begin = levelEnd[level]; level--; }
-            next = __ldg(a.tileList + (size_t)level * a.listStride + (q - begin));
-            if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
+            if (q >= nQueue) next = 0x80000000u | (q - nQueue);      // a group of tiles to clear
+            else {
+                uint32_t level = PF_HEAVY_LEVELS, begin = 0;
+                while (q >= levelEnd[level]) { begin = levelEnd[level]; level--; }
+                next = __ldg(a.tileList + (size_t)level * a.listStride + (q - begin));
+                if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
+            }
         }
     }
     const uint32_t gt = __shfl_sync(0xffffffffu, next, 0);
     if (gt == 0xffffffffu) break;
     if (gt == 0xfffffffeu) continue;
+    if (gt & 0x80000000u) {
+        // the fused clear of the empty tiles of group gt: one tile a lane,
+        // each row of RGBA8 pixels and depths as two 16-byte stores
+        const uint32_t t = 32u * (gt & 0x7fffffffu) + (uint32_t)lane;
+        if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
+            int clo = 0, chi = a.nTargets - 1;
+            while (clo < chi) { int mid = (clo + chi + 1) >> 1; if (a.targets[mid].tileBase <= t) clo = mid; else chi = mid - 1; }
+            const PFTarget &C = a.targets[clo];
+            if (C.clearMode != 0) {
+                const uint32_t tile = t - C.tileBase;
+                const uint32_t cx = (tile % C.tilesX) * PF_TILE, cy = (tile / C.tilesX) * PF_TILE;
+                const uint32_t xe = min(cx + PF_TILE, C.W);
+                for (uint32_t py = cy; py < min(cy + PF_TILE, C.H); py++) {
+                    const size_t row = (size_t)py * C.W;
+                    if (!GEN && xe == cx + 8u && ((row + cx) & 3u) == 0 && !(C.clearMode == 1 && row + cx < 8) &&
+                        (((uintptr_t)C.color | (uintptr_t)C.depth) & 15u) == 0) {
+                        const uint32_t cr = C.clearRaw[0];
+                        const float cd = C.clearDepth;
+                        uint4 *cp = reinterpret_cast<uint4 *>((uint32_t *)C.color + row + cx);
+                        float4 *dp = reinterpret_cast<float4 *>(C.depth + row + cx);
+                        cp[0] = make_uint4(cr, cr, cr, cr); cp[1] = make_uint4(cr, cr, cr, cr);
+                        dp[0] = make_float4(cd, cd, cd, cd); dp[1] = make_float4(cd, cd, cd, cd);
+                        continue;
+                    }
+                    for (uint32_t px = cx; px < xe; px++) {
+                        const size_t pidx = row + px;
+                        if (C.clearMode == 1 && pidx < 8) continue;  // pfClear keeps pixels 0..7
+                        if (GEN) pff_store(C.fmt, C.color, pidx, C.clearRaw);
+                        else ((uint32_t *)C.color)[pidx] = C.clearRaw[0];
+                        C.depth[pidx] = C.clearDepth;
+                    }
+                }
+            }
+        }
+        continue;
+    }
     int tlo = 0, thi = a.nTargets - 1;
     while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gt) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
@@ -1555,39 +1597,6 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     if (in0) { col0.store(T, pidx0); T.depth[pidx0] = dep0; }
     if (in1) { col1.store(T, pidx1); T.depth[pidx1] = dep1; }
     }   // tile loop
-
-    // tiles with an empty bin only get their fused clear, if any: warp w of
-    // the grid takes the groups of 32 tiles w, w + warps of the grid, ...,
-    // once the queue is empty (in the tail of the launch, when warps would
-    // otherwise wait for the last tiles)
-    for (uint32_t t0 = (blockIdx.x * WARPS + (uint32_t)warp) * 32u; t0 < a.totalTiles;
-         t0 += gridDim.x * (WARPS * 32)) {
-        const uint32_t t = t0 + (uint32_t)lane;
-        int ti = 0;
-        bool clear = false;
-        if (t < a.totalTiles && __ldg(a.binCount + t) == 0) {
-            int tlo = 0, thi = a.nTargets - 1;
-            while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= t) tlo = mid; else thi = mid - 1; }
-            ti = tlo;
-            clear = a.targets[tlo].clearMode != 0;
-        }
-        for (uint32_t m = __ballot_sync(0xffffffffu, clear); m; m &= m - 1) {
-            const int src = __ffs(m) - 1;
-            const PFTarget &T = a.targets[__shfl_sync(0xffffffffu, ti, src)];
-            const uint32_t tile = t0 + (uint32_t)src - T.tileBase;
-            const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
-            for (uint32_t p = (uint32_t)lane; p < PF_TILE_PIXELS; p += 32) {
-                const uint32_t px = ox + p % PF_TILE, py = oy + p / PF_TILE;
-                if (px >= T.W || py >= T.H) continue;
-                const size_t pidx = (size_t)py * T.W + px;
-                if (T.clearMode == 1 && pidx < 8) continue;     // pfClear keeps pixels 0..7
-                if (GEN) pff_store(T.fmt, T.color, pidx, T.clearRaw);
-                else ((uint32_t *)T.color)[pidx] = T.clearRaw[0];
-                T.depth[pidx] = T.clearDepth;
-            }
-        }
-    }
-
 
     // fragment counter: one atomic per CTA (same-address atomics serialise)
     __shared__ unsigned long long sFrags;
