@@ -1268,12 +1268,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_binsort(RasterArgs a)
                 __syncthreads();
                 for (uint32_t k = 2; k <= N; k <<= 1)
                     for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                        for (uint32_t i = tid; i < N; i += SORT_THREADS) {
-                            const uint32_t ixj = i ^ j;
-                            if (ixj > i) {
-                                const uint32_t x = sbuf[i], y = sbuf[ixj];
-                                if ((x > y) == ((i & k) == 0)) { sbuf[i] = y; sbuf[ixj] = x; }
-                            }
+                        // pair p: places i (bit j clear) and i + j
+                        for (uint32_t p = tid; p < N / 2; p += SORT_THREADS) {
+                            const uint32_t i = ((p & ~(j - 1)) << 1) | (p & (j - 1)), ixj = i | j;
+                            const uint32_t x = sbuf[i], y = sbuf[ixj];
+                            if ((x > y) == ((i & k) == 0)) { sbuf[i] = y; sbuf[ixj] = x; }
                         }
                         __syncthreads();
                     }
@@ -1819,7 +1818,7 @@ cudaError_t pfd_launch_binsort(const PFBatchLaunch &L, cudaStream_t st)
     const size_t smem = (size_t)N * sizeof(uint32_t);
     cudaError_t e = cudaFuncSetAttribute(k_binsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     uint32_t grid = 0;
-    if (e == cudaSuccess) e = persistent_grid((const void *)k_binsort, SORT_THREADS, smem, 4, L.totalTiles, grid);
+    if (e == cudaSuccess) e = persistent_grid((const void *)k_binsort, SORT_THREADS, smem, 0, L.totalTiles, grid);
     if (e != cudaSuccess) return e;
     return launch_serialized(k_binsort, grid, SORT_THREADS, smem, st, raster_args(L));
 }
