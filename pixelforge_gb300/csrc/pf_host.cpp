@@ -812,6 +812,9 @@ void pin_texture(Renderer *r, Tex *t, size_t bytes)
 {
     if (t->hostRegistered || t->ownsPinned || ++t->drawUses < 2 || bytes < kPinTextureMin || !device_init(r)) return;
     if (!is_pageable(t->pixels)) return;                          // page-locked by someone else already
+    // registering pins the pages (the kernel may move them first): no copy
+    // of this or a neighbouring array may still be reading them
+    if (cudaDeviceSynchronize() != cudaSuccess) { cudaGetLastError(); return; }
     if (cudaHostRegister(t->pixels, bytes, cudaHostRegisterDefault) == cudaSuccess) t->hostRegistered = true;
     else cudaGetLastError();
 }
@@ -1381,6 +1384,8 @@ FBMirror *mirror_for(Renderer *r, PFframebuffer *fb)
     m.hostDepth = fb->zbuffer;
     m.depthUserVisible = !t->isMain;
     if (m.registered != t->pixels && !t->ownsPinned) {
+        // (no copy may be in flight on the pages being pinned or released)
+        if (cudaDeviceSynchronize() != cudaSuccess) cudaGetLastError();
         if (m.registered) cudaHostUnregister(m.registered);
         m.registered = nullptr;
         if (cudaHostRegister(t->pixels, w * h * bpp, cudaHostRegisterDefault) == cudaSuccess) m.registered = t->pixels;
@@ -1401,6 +1406,7 @@ void drop_mirror(const void *tex)
     std::lock_guard<std::mutex> lk(gMirrorMutex);
     auto it = gMirrors.find(tex);
     if (it == gMirrors.end()) return;
+    if (cudaDeviceSynchronize() != cudaSuccess) cudaGetLastError();   // its write-back may be in flight
     if (it->second.registered) cudaHostUnregister(it->second.registered);
     if (it->second.dColor) cudaFree(it->second.dColor);
     if (it->second.dDepth) cudaFree(it->second.dDepth);
@@ -3244,7 +3250,10 @@ void pfDeleteTexture(PFtexture *tex, PFboolean freeBuffer)
     Tex *t = (Tex *)*tex;
     if (!t) return;
     if (G && G->texture == t) G->texture = nullptr;   // snapshots already hold the texels
-    if (t->hostRegistered) cudaHostUnregister(t->pixels);
+    if (t->hostRegistered) {
+        if (cudaDeviceSynchronize() != cudaSuccess) cudaGetLastError();   // no upload from it in flight
+        cudaHostUnregister(t->pixels);
+    }
     if (freeBuffer) std::free(t->pixels);
     delete t;
     *tex = nullptr;
