@@ -25,6 +25,7 @@
 #include <cstring>
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <functional>
 #include <mutex>
@@ -266,8 +267,22 @@ struct Renderer {
     struct UpChunk { void *p; size_t cap; };
     std::vector<UpChunk> up;
     size_t upChunk = 0, upOff = 0, upBytes = 0;
+    // page-locked host chunks that pageable caller arrays are copied into
+    // (by the worker pool) for their DMA: the GPU never reads pageable memory
+    std::vector<UpChunk> hostUp;
+    size_t hostChunk = 0, hostOff = 0;
+    // uploads of this recording from pageable memory, for reuse by a later
+    // draw that references the same unchanged array
+    struct UpSnap { const void *p; size_t bytes; const uint8_t *copy; int64_t ref; int64_t maxU32; };
+    std::vector<UpSnap> upSnaps;
     cudaStream_t upStream = nullptr;
     cudaEvent_t upDone = nullptr;
+    // copies from page-locked caller memory (a pinned texture): DMAs on their
+    // own stream, under way while the call takes its other copies, waited
+    // for when the outermost API call that took them returns (CopyScope)
+    cudaStream_t pinStream = nullptr;
+    bool pinPending = false;
+    int copyScope = 0;
     unsigned *dMax = nullptr, *hMax = nullptr;   // largest uploaded index: device word, page-locked result
 
     // device
@@ -541,7 +556,12 @@ Tex *tex_new(void *pixels, PFsizei w, PFsizei h, PFpixelformat f, PFdatatype t, 
 
 // ---------------------------------------------------------------------------
 // host worker pool: large snapshots (vertex arrays, indices, textures) are
-// copied and compared by several threads, the caller taking a share
+// copied and compared by several threads, the caller taking a share.
+// A drawing call makes several such loops of a few microseconds each, so
+// dispatch must cost less than the work: items are claimed from one atomic
+// word that also carries the loop's generation and size, completions are
+// counted atomically, and an idle worker spins on the word for a while
+// (kSpinUs) before it sleeps on a condition variable.
 // ---------------------------------------------------------------------------
 class Pool {
 public:
@@ -550,24 +570,31 @@ public:
     // run fn(i) for i in [0, n); returns when all are done
     void run(int n, const std::function<void(int)> &fn)
     {
-        if (n <= 1 || threads_.empty()) { for (int i = 0; i < n; i++) fn(i); return; }
+        if (n <= 1 || threads_.empty() || n > (int)kMaxItems) { for (int i = 0; i < n; i++) fn(i); return; }
         std::lock_guard<std::mutex> one(runMutex_);      // one parallel loop at a time
-        std::unique_lock<std::mutex> lk(m_);
-        fn_.store(&fn); n_ = n; next_.store(0); done_ = 0; gen_++;
-        lk.unlock();
-        cv_.notify_all();
-        work();
-        lk.lock();
-        doneCv_.wait(lk, [&] { return done_ == n_; });
-        fn_.store(nullptr);
+        // every item of the previous loop is done, so no worker still reads fn_
+        fn_ = &fn;
+        done_.store(0, std::memory_order_relaxed);
+        gen_ = (gen_ + 1) & kGenMask;
+        claim_.store(pack(gen_, (uint64_t)n, 0), std::memory_order_seq_cst);
+        wake_one();                                      // a woken worker wakes the next
+        work(gen_);
+        while (done_.load(std::memory_order_acquire) != n) std::this_thread::yield();
     }
     ~Pool()
     {
-        { std::lock_guard<std::mutex> lk(m_); stop_ = true; gen_++; }
+        stop_.store(true);
+        { std::lock_guard<std::mutex> lk(m_); }
         cv_.notify_all();
         for (auto &t : threads_) t.join();
     }
 private:
+    // claim word: generation (24 bits) | items (20 bits) | next item (20 bits)
+    static constexpr uint64_t kGenMask = (1u << 24) - 1, kMaxItems = (1u << 20) - 1;
+    static constexpr int kSpinUs = 1000;          // about a frame's flush: the next draw finds the workers awake
+    static uint64_t pack(uint64_t g, uint64_t n, uint64_t next) { return (g << 40) | (n << 20) | next; }
+    static uint64_t gen_of(uint64_t c) { return c >> 40; }
+
     Pool()
     {
         // all cores but the caller's: the copies into staging are bound by
@@ -576,40 +603,68 @@ private:
         int n = (int)std::min(15u, hw > 1 ? hw - 1 : 0u);
         for (int i = 0; i < n; i++) threads_.emplace_back([this] { loop(); });
     }
-    void work()
+    // claim and run items of loop `g` until none is left (or a newer loop began)
+    void work(uint64_t g)
     {
         for (;;) {
-            int i = next_.fetch_add(1);
-            const std::function<void(int)> *f = fn_.load();
-            if (i >= n_ || !f) break;
-            (*f)(i);
+            uint64_t c = claim_.load(std::memory_order_acquire);
+            int item = -1;
+            while (gen_of(c) == g && (c & kMaxItems) < ((c >> 20) & kMaxItems)) {
+                if (claim_.compare_exchange_weak(c, c + 1, std::memory_order_acq_rel)) { item = (int)(c & kMaxItems); break; }
+            }
+            if (item < 0) return;
+            (*fn_)(item);
+            done_.fetch_add(1, std::memory_order_release);
+        }
+    }
+    void wake_one()
+    {
+        if (sleepers_.load(std::memory_order_seq_cst) > 0) {
             std::lock_guard<std::mutex> lk(m_);
-            if (++done_ == n_) doneCv_.notify_all();
+            cv_.notify_one();
         }
     }
     void loop()
     {
         uint64_t seen = 0;
         for (;;) {
-            std::unique_lock<std::mutex> lk(m_);
-            cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
-            if (stop_) return;
-            seen = gen_;
-            lk.unlock();
-            work();
+            // spin for a new loop, then sleep
+            const auto t0 = std::chrono::steady_clock::now();
+            uint64_t g = gen_of(claim_.load(std::memory_order_acquire));
+            for (int k = 0; g == seen && !stop_.load(std::memory_order_relaxed); k++) {
+                if ((k & 255) == 255) {
+                    if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(kSpinUs)) break;
+                    std::this_thread::yield();
+                }
+                g = gen_of(claim_.load(std::memory_order_acquire));
+            }
+            if (g == seen && !stop_.load()) {
+                sleepers_.fetch_add(1, std::memory_order_seq_cst);
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return stop_.load() || gen_of(claim_.load(std::memory_order_seq_cst)) != seen; });
+                sleepers_.fetch_sub(1, std::memory_order_relaxed);
+                lk.unlock();
+                const uint64_t c = claim_.load(std::memory_order_acquire);
+                g = gen_of(c);
+                if ((c & kMaxItems) < ((c >> 20) & kMaxItems)) wake_one();   // items left: pass the wake on
+            }
+            if (stop_.load()) return;
+            seen = g;
+            work(g);
         }
     }
     std::vector<std::thread> threads_;
     std::mutex m_, runMutex_;
-    std::condition_variable cv_, doneCv_;
-    std::atomic<const std::function<void(int)> *> fn_{ nullptr };
-    std::atomic<int> next_{ 0 };
-    int n_ = 0, done_ = 0;
+    std::condition_variable cv_;
+    const std::function<void(int)> *fn_ = nullptr;
+    std::atomic<uint64_t> claim_{ 0 };
+    std::atomic<int> done_{ 0 };
+    std::atomic<int> sleepers_{ 0 };
+    std::atomic<bool> stop_{ false };
     uint64_t gen_ = 0;
-    bool stop_ = false;
 };
 
-constexpr size_t kParallelChunk = (size_t)1 << 17;     // 128 KiB
+constexpr size_t kParallelChunk = (size_t)1 << 16;     // 64 KiB
 
 void par_memcpy(void *dst, const void *src, size_t bytes)
 {
@@ -659,9 +714,17 @@ uint32_t par_copy_max_u32(uint32_t *dst, const uint32_t *src, size_t count)
     std::vector<uint32_t> mx((size_t)std::max(n, 1), 0u);
     Pool::get().run(n, [&](int i) {
         size_t o = (size_t)i * chunk, len = std::min(chunk, count - o);
-        uint32_t m = 0;
-        for (size_t k = 0; k < len; k++) { uint32_t v = src[o + k]; dst[o + k] = v; m = v > m ? v : m; }
-        mx[(size_t)i] = m;
+        const uint32_t *s = src + o;
+        uint32_t *d = dst + o;
+        uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+        size_t k = 0;
+        for (; k + 4 <= len; k += 4) {
+            const uint32_t a = s[k], b = s[k + 1], c = s[k + 2], e = s[k + 3];
+            d[k] = a; d[k + 1] = b; d[k + 2] = c; d[k + 3] = e;
+            m0 = std::max(m0, a); m1 = std::max(m1, b); m2 = std::max(m2, c); m3 = std::max(m3, e);
+        }
+        for (; k < len; k++) { d[k] = s[k]; m0 = std::max(m0, s[k]); }
+        mx[(size_t)i] = std::max(std::max(m0, m1), std::max(m2, m3));
     });
     uint32_t m = 0;
     for (uint32_t v : mx) m = std::max(m, v);
@@ -675,22 +738,18 @@ bool device_init(Renderer *r);
 
 inline int64_t dev_ref(const void *p) { return -(int64_t)(uintptr_t)p; }
 
-constexpr size_t kUploadMin = (size_t)64 << 10;          // smaller arrays go through staging
+#ifndef PF_UPLOAD_MIN_BYTES
+#define PF_UPLOAD_MIN_BYTES ((size_t)64 << 10)
+#endif
+constexpr size_t kUploadMin = PF_UPLOAD_MIN_BYTES;        // smaller arrays go through staging
 constexpr size_t kUploadBudget = (size_t)8 << 30;        // per recording; beyond it, staging with de-duplication
 constexpr size_t kUploadChunk = (size_t)64 << 20;
 
-// Copy `bytes` of caller memory to the device now, straight from where it
-// lies (one cudaMemcpyAsync; on this platform that is several times faster
-// than a host copy into pinned staging followed by the upload).  From
-// pageable memory the call returns only once the bytes are read, which is
-// the snapshot the reference's draw-time read implies; from page-locked or
-// device memory it would return earlier, so the copy is waited for.
-// Returns the device reference, or -1 (the caller takes the staging path).
 // Room for `bytes` in the upload chunks, or nullptr (the caller takes the
 // staging path); upload_commit takes it.
 uint8_t *upload_room(Renderer *r, size_t bytes)
 {
-    if (bytes < kUploadMin || r->upBytes + bytes > kUploadBudget || !device_init(r)) return nullptr;
+    if (r->upBytes + bytes > kUploadBudget) return nullptr;
     if (r->upBytes == 0) {               // a new recording: the last flush's device data is overwritten
         r->lastOps.clear();
         r->graphValid = false;
@@ -718,16 +777,85 @@ bool is_pageable(const void *p)
     return pageable;
 }
 
-int64_t upload(Renderer *r, const void *p, size_t bytes)
+// Room for `bytes` in the page-locked host chunks (kept from one recording
+// to the next; a new chunk at least doubles what the renderer holds).
+uint8_t *host_room(Renderer *r, size_t bytes)
 {
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    while (r->hostChunk < r->hostUp.size() && r->hostOff + need > r->hostUp[r->hostChunk].cap) {
+        r->hostChunk++; r->hostOff = 0;
+    }
+    if (r->hostChunk == r->hostUp.size()) {
+        size_t held = 0;
+        for (auto &c : r->hostUp) held += c.cap;
+        Renderer::UpChunk c{ nullptr, std::max(std::max(need, held), (size_t)4 << 20) };
+        if (cudaMallocHost(&c.p, c.cap) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        r->hostUp.push_back(c);
+        r->hostOff = 0;
+    }
+    uint8_t *h = (uint8_t *)r->hostUp[r->hostChunk].p + r->hostOff;
+    r->hostOff += need;
+    return h;
+}
+
+// Copy `bytes` of caller memory to the device now (large arrays; the caller
+// may change them once the drawing call returns).  Pageable memory is
+// copied by the worker pool into a page-locked host chunk (u32 arrays: their
+// largest element found in the same pass, into *maxU32) and sent from
+// there by an asynchronous DMA; a later draw of the same recording that
+// references the same unchanged array reuses that copy.  Page-locked and
+// device memory is copied by a DMA straight from where it lies, waited for
+// before the drawing call returns.  Returns the device reference, or -1
+// (the caller takes the staging path).
+int64_t upload(Renderer *r, const void *p, size_t bytes, int64_t *maxU32 = nullptr)
+{
+    if (bytes < kUploadMin || !device_init(r)) return -1;
+    const bool pageable = is_pageable(p);
+    if (pageable)
+        for (const auto &u : r->upSnaps)
+            if (u.p == p && u.bytes == bytes && (!maxU32 || u.maxU32 >= 0) && par_equal(u.copy, p, bytes)) {
+                if (maxU32) *maxU32 = u.maxU32;
+                return u.ref;
+            }
     uint8_t *dst = upload_room(r, bytes);
     if (!dst) return -1;
-    const bool pageable = is_pageable(p);
-    if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
-    if (!pageable) cudaStreamSynchronize(r->upStream);
+    if (pageable) {
+        uint8_t *h = host_room(r, bytes);
+        if (!h) return -1;
+        int64_t mx = -1;
+        if (maxU32) mx = (int64_t)par_copy_max_u32((uint32_t *)h, (const uint32_t *)p, bytes / 4);
+        else par_memcpy(h, p, bytes);
+        if (cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, r->upStream) != cudaSuccess) { cudaGetLastError(); return -1; }
+        if (maxU32) *maxU32 = mx;
+        r->upSnaps.push_back({ p, bytes, h, dev_ref(dst), mx });
+    } else {
+        if (cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDefault, r->pinStream) != cudaSuccess) { cudaGetLastError(); return -1; }
+        // (an index maximum is then reduced on the device, on the upload
+        // stream: the copy must have landed)
+        if (r->copyScope > 0 && !maxU32) r->pinPending = true;      // waited for as the API call returns
+        else cudaStreamSynchronize(r->pinStream);
+    }
     upload_commit(r, bytes);
     return dev_ref(dst);
 }
+
+// Scope of an API call that takes snapshots of caller memory: copies from
+// page-locked memory started inside it are complete when the outermost
+// scope ends (before the call returns to the caller, who may then change
+// the memory).
+void settle_pinned(Renderer *r)
+{
+    if (!r->pinPending) return;
+    if (cudaStreamSynchronize(r->pinStream) != cudaSuccess) cudaGetLastError();
+    r->pinPending = false;
+}
+struct CopyScope {
+    Renderer *r;
+    explicit CopyScope(Renderer *rr) : r(rr) { r->copyScope++; }
+    ~CopyScope() { if (--r->copyScope == 0) settle_pinned(r); }
+    CopyScope(const CopyScope &) = delete;
+    CopyScope &operator=(const CopyScope &) = delete;
+};
 
 // Copy `bytes` of caller memory for the device: uploaded now (large arrays;
 // device_ok), or into staging, reusing an identical snapshot taken earlier
@@ -784,9 +912,11 @@ int64_t snapshot_u32(Renderer *r, const uint32_t *p, size_t count, uint32_t &mx)
 {
     const size_t bytes = count * 4;
     if (bytes >= kUploadMin) {
-        const int64_t ref = upload(r, p, bytes);
+        int64_t hm = -1;
+        const int64_t ref = upload(r, p, bytes, &hm);
         if (ref != -1) {
-            if (!device_max_u32(r, (const uint32_t *)(uintptr_t)(-ref), count, mx)) mx = par_max_u32(p, count);
+            if (hm >= 0) mx = (uint32_t)hm;                  // found while copying
+            else if (!device_max_u32(r, (const uint32_t *)(uintptr_t)(-ref), count, mx)) mx = par_max_u32(p, count);
             return ref;
         }
     }
@@ -990,6 +1120,7 @@ void push_draw(Renderer *r, PFframebuffer *fb, int si)
 int new_segment(Ctx *c, int srcKind, int itemKind)
 {
     Renderer *r = c->rend;
+    CopyScope scope(r);
     SegRec rec;
     std::memset(&rec.seg, 0, sizeof rec.seg);
     rec.seg.state = snapshot_state(c);
@@ -1328,6 +1459,7 @@ bool device_init(Renderer *r)
     }
     e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->upStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->pinStream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->upDone, cudaEventDisableTiming);
     if (e != cudaSuccess) { report_device_failure("cudaStreamCreate", e); r->devStatus |= PF_DEVICE_NO_GPU; return false; }
     if (!r->counters.ensure(sizeof(PFDevCounters))) { r->devStatus |= PF_DEVICE_ALLOC_FAIL; return false; }
@@ -1349,12 +1481,15 @@ void release_renderer(Renderer *r)
         for (auto &pr : r->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
         if (r->stream) cudaStreamDestroy(r->stream);
         if (r->upStream) cudaStreamDestroy(r->upStream);
+        if (r->pinStream) cudaStreamDestroy(r->pinStream);
         if (r->upDone) cudaEventDestroy(r->upDone);
         if (r->dMax) cudaFree(r->dMax);
         if (r->hMax) cudaFreeHost(r->hMax);
         r->dMax = r->hMax = nullptr;
         for (auto &u : r->up) cudaFree(u.p);
         r->up.clear();
+        for (auto &u : r->hostUp) cudaFreeHost(u.p);
+        r->hostUp.clear();
         for (void *q : r->splitMem) cudaFree(q);
         r->splitMem.clear();
     }
@@ -1417,9 +1552,12 @@ void discard_recording(Renderer *r)
 {
     r->states.clear(); r->segs.clear(); r->cmds.clear(); r->snaps.clear(); r->conversions.clear();
     r->staging.used = 0;
+    settle_pinned(r);
+    r->upSnaps.clear();
     if (r->upBytes) {
-        cudaStreamSynchronize(r->upStream);
+        cudaStreamSynchronize(r->upStream);            // (the host chunks' DMAs too)
         r->upChunk = r->upOff = r->upBytes = 0;
+        r->hostChunk = r->hostOff = 0;
     }
 }
 
@@ -1622,6 +1760,7 @@ bool flush(Renderer *r)
         maxVerts = std::max(maxVerts, v); maxItems = std::max(maxItems, it); maxTiles = std::max(maxTiles, tiles);
     }
     cudaError_t e = cudaMemcpyAsync(dbase, r->staging.base, total, cudaMemcpyHostToDevice, st);
+    settle_pinned(r);                               // (a flush inside a drawing call)
     if (e == cudaSuccess && r->upBytes) {            // the record-time uploads come first
         e = cudaEventRecord(r->upDone, r->upStream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, r->upDone, 0);
@@ -2463,6 +2602,7 @@ static void assemble_arrays(Ctx *c, PFdrawmode mode, PFsizei count, const void *
 static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first)
 {
     Ctx *c = G;
+    CopyScope scope(c->rend);
     update_matrices(c, !(mode == PF_POINTS || mode == PF_LINES));     // pfBegin inside the draw
     c->drawMode = mode; c->vcount = 0;
     c->stateDirty = true;
