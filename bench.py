@@ -219,17 +219,41 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, samples=2)
     tg.close()
-    if not args.no_soup:
-        out["soup256"] = run_soup(lib)
-    if not args.no_phong:
-        out["phong"] = run_phong(lib)
-    if not args.no_formats:
-        out["framebuffer_formats"] = run_formats(lib)
-    if not args.no_batched:
-        out["batched"] = run_batched(lib)
-    if not args.no_adjoint:
-        out["adjoint"] = run_adjoint(args)
+    # the other workloads, each in a process of its own: a failure there is
+    # reported in its section and leaves the headline line intact
+    for name, skip in (("soup256", args.no_soup), ("phong", args.no_phong), ("framebuffer_formats", args.no_formats),
+                       ("batched", args.no_batched), ("adjoint", args.no_adjoint)):
+        if not skip:
+            out[name] = run_section(name)
     return out
+
+
+SECTION_TIMEOUT_S = 900
+
+
+def run_section(name: str) -> dict:
+    """Run one secondary workload (``--section NAME``) in a child process and
+    return its JSON object, or {"error": ...} when the child failed."""
+    import subprocess
+    cmd = [sys.executable, os.path.abspath(__file__), "--section", name]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=SECTION_TIMEOUT_S)
+    except subprocess.TimeoutExpired:
+        return {"error": f"timed out after {SECTION_TIMEOUT_S} s"}
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        tail = " | ".join((r.stderr or r.stdout).strip().splitlines()[-3:])
+        return {"error": f"exit code {r.returncode}: {tail}"}
+    return json.loads(lines[-1])
+
+
+def section_main(name: str) -> dict:
+    from pixelforge_gb300 import load_library
+    if name == "adjoint":
+        return run_adjoint(argparse.Namespace())
+    lib = load_library()
+    return {"soup256": run_soup, "phong": run_phong, "framebuffer_formats": run_formats,
+            "batched": run_batched}[name](lib)
 
 
 SPHERE_WORKLOAD = ("sphere1080: 1920x1080 textured Gouraud UV sphere 256x128, two draws "
@@ -569,7 +593,13 @@ def main():
     ap.add_argument("--no-phong", action="store_true", help="skip the Phong 1080p measurement")
     ap.add_argument("--no-formats", action="store_true", help="skip the framebuffer-format measurement")
     ap.add_argument("--no-soup", action="store_true", help="skip the 256x256 soup measurement")
+    ap.add_argument("--section", default=None,
+                    choices=["soup256", "phong", "framebuffer_formats", "batched", "adjoint"],
+                    help="run one secondary workload alone and print its JSON object")
     args = ap.parse_args()
+    if args.section:
+        print(json.dumps(section_main(args.section)))
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
         out = run_reference(args)
