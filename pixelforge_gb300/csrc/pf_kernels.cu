@@ -932,6 +932,10 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 // k_raster's CTAs group 2, 4 or 8 independent warps (the block shape, a
 // tuning knob); each warp owns one tile at a time
 #define QCHN 32                     // records per batch (bit k of a pixel's 32-bit masks)
+// work-queue entries of a half tile: the tile index with one of these set
+#define TILE_TOP 0x40000000u
+#define TILE_BOTTOM 0x60000000u
+#define TILE_HALF_MASK 0x60000000u
 #define QFW 128                     // fragment window of a warp
 #define SORT_THREADS 256
 #define REG_SORT_MAX 128            // bins shorter than this are sorted by the raster warp (four keys a lane)
@@ -1333,7 +1337,20 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     // a lane
     uint32_t levelEnd[PF_HEAVY_LEVELS + 1];           // queue index past level l's entries, heaviest first
     uint32_t nQueue = 0;
-    for (int l = PF_HEAVY_LEVELS; l >= 1; l--) { nQueue += min(a.cnt->heavyCount[l - 1], a.totalTiles); levelEnd[l] = nQueue; }
+    // A heavy level with few tiles against the grid's warps sets the end of
+    // the launch (its tiles start first but run longest): each of its tiles
+    // is then two work items, its top and bottom halves, each a warp with
+    // one pixel a lane, which take about half as long.  Where heavy tiles
+    // are many the launch is bound by the total work, which halves would
+    // only add to (each half walks the whole bin).
+    uint32_t splitLevels = 0;
+    for (int l = PF_HEAVY_LEVELS; l >= 1; l--) {
+        const uint32_t c = min(a.cnt->heavyCount[l - 1], a.totalTiles);
+        const bool split = 4u * c <= gridDim.x * (uint32_t)WARPS;
+        splitLevels |= split ? 1u << l : 0u;
+        nQueue += split ? 2u * c : c;
+        levelEnd[l] = nQueue;
+    }
     nQueue += min(a.cnt->tileListCount, a.totalTiles);
     levelEnd[0] = nQueue;
     const uint32_t nClear = (a.totalTiles + 31u) / 32u;
@@ -1349,8 +1366,11 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             else {
                 uint32_t level = PF_HEAVY_LEVELS, begin = 0;
                 while (q >= levelEnd[level]) { begin = levelEnd[level]; level--; }
-                next = __ldg(a.tileList + (size_t)level * a.listStride + (q - begin));
+                const uint32_t e = q - begin;
+                const bool split = (splitLevels >> level) & 1u;
+                next = __ldg(a.tileList + (size_t)level * a.listStride + (split ? e >> 1 : e));
                 if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
+                else if (split) next |= (e & 1u) ? TILE_BOTTOM : TILE_TOP;
             }
         }
     }
@@ -1393,19 +1413,24 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
         }
         continue;
     }
+    // whole tile: my pixels are rows ly and ly + 4; half tile: row ly of
+    // the top half or ly + 4 of the bottom half only
+    const uint32_t gtile = gt & ~TILE_HALF_MASK;
+    const bool whole = (gt & TILE_HALF_MASK) == 0;
+    const uint32_t rowA = ly + ((gt & TILE_HALF_MASK) == TILE_BOTTOM ? 4u : 0u);
     int tlo = 0, thi = a.nTargets - 1;
-    while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gt) tlo = mid; else thi = mid - 1; }
+    while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gtile) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
-    const uint32_t tile = gt - T.tileBase;
-    const uint32_t n = min(__ldg(a.binCount + gt), a.cap);
+    const uint32_t tile = gtile - T.tileBase;
+    const uint32_t n = min(__ldg(a.binCount + gtile), a.cap);
     if (n == 0 && T.clearMode == 0) continue;
     const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
     const uint32_t W = T.W, H = T.H;
 
     FbPixel<GEN> col0{}, col1{};
     float dep0 = 0.0f, dep1 = 0.0f;
-    const uint32_t X0 = ox + lx, Y0 = oy + ly, Y1 = Y0 + 4u;
-    const bool in0 = X0 < W && Y0 < H, in1 = X0 < W && Y1 < H;
+    const uint32_t X0 = ox + lx, Y0 = oy + rowA, Y1 = Y0 + 4u;
+    const bool in0 = X0 < W && Y0 < H, in1 = whole && X0 < W && Y1 < H;
     const size_t pidx0 = (size_t)Y0 * W + X0, pidx1 = (size_t)Y1 * W + X0;
     {
         auto init = [&](FbPixel<GEN> &c, float &d, bool in, size_t pi) {
@@ -1420,7 +1445,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     // a bin shorter than REG_SORT_MAX is put into submission order here, in
     // registers: a bitonic network over 32, 64 or 128 places, place
     // 32 r + lane in key r of the lane; longer bins were sorted by k_binsort
-    const uint32_t *bin = a.bins + (size_t)gt * a.cap;
+    const uint32_t *bin = a.bins + (size_t)gtile * a.cap;
     const bool regSort = n < REG_SORT_MAX;
     uint32_t sk[4] = { 0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu };
     if (regSort) {
@@ -1502,15 +1527,15 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             const int4 q2 = e4[2];
             const uint32_t box = (uint32_t)q2.y;
             const uint32_t bx0 = box & 15u, bw = (box >> 4) & 15u, by0 = (box >> 8) & 15u, bh = (box >> 12) & 15u;
-            const bool r0 = ly - by0 < bh, r1 = ly + 4u - by0 < bh;
+            const bool r0 = rowA - by0 < bh, r1 = whole && ly + 4u - by0 < bh;
             if (lx - bx0 >= bw || !(r0 || r1)) continue;
             const uint32_t rs = (uint32_t)q2.z;
             const int func = (int)((rs >> 16) & 255u);
             if (((box >> 16) & 3u) == 0) {
                 const int4 q0 = e4[0], q1 = e4[1];
-                uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + ly * (uint32_t)q1.z;
-                uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + ly * (uint32_t)q1.w;
-                uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + ly * (uint32_t)q2.x;
+                uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + rowA * (uint32_t)q1.z;
+                uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + rowA * (uint32_t)q1.w;
+                uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + rowA * (uint32_t)q2.x;
                 const float4 zq = reinterpret_cast<const float4 *>(&Q.rec[k].p)[3];     // wInvSum z1 z2 z3
                 const float zRej = __int_as_float(q2.w);
                 auto test = [&](float &d, uint32_t &vis, bool rowOK) {
@@ -1560,7 +1585,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             __syncwarp();
             for (uint32_t f = b0 + (uint32_t)lane; f < bEnd; f += 32) {
                 const uint32_t d = Q.fdesc[f - b0], p = d >> 5, k = d & 31u;
-                const uint32_t X = p & 7u, Y = p >> 3;
+                const uint32_t X = p & 7u, Y = (p >> 3) + (rowA - ly);     // (a bottom half's slot 0 is row ly + 4)
                 const PFPrim &P = Q.rec[k].p;
                 if (anyLP && (P.flags & PFP_KIND)) {
                     Q.fc[f - b0] = lp_color(P, (int32_t)(ox + X), (int32_t)(oy + Y));
