@@ -1518,10 +1518,11 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
         }
         const bool anyLP = __any_sync(0xffffffffu, kind != 0);
         __syncwarp();
-        // 2. my two pixels walk the batch in submission order: coverage,
-        //    depth, depth test, depth write
-        uint32_t vis0 = 0, vis1 = 0;                    // bit k: record k passed at my pixel of slot 0 / 1
-        uint32_t cov = 0;
+        // 2a. coverage: bit k of cm0 / cm1 -- record k covers my pixel of
+        //     slot 0 / 1 (triangles: the integer edge functions; points,
+        //     lines and rectangles: their own rule).  Cheap per record, so
+        //     that the costly depth below runs for covering records only.
+        uint32_t cm0 = 0, cm1 = 0;
         for (uint32_t k = 0; k < cn; k++) {
             const int4 *e4 = reinterpret_cast<const int4 *>(&Q.edge[k]);
             const int4 q2 = e4[2];
@@ -1529,50 +1530,61 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             const uint32_t bx0 = box & 15u, bw = (box >> 4) & 15u, by0 = (box >> 8) & 15u, bh = (box >> 12) & 15u;
             const bool r0 = rowA - by0 < bh, r1 = whole && ly + 4u - by0 < bh;
             if (lx - bx0 >= bw || !(r0 || r1)) continue;
-            const uint32_t rs = (uint32_t)q2.z;
-            const int func = (int)((rs >> 16) & 255u);
             if (((box >> 16) & 3u) == 0) {
                 const int4 q0 = e4[0], q1 = e4[1];
-                uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + rowA * (uint32_t)q1.z;
-                uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + rowA * (uint32_t)q1.w;
-                uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + rowA * (uint32_t)q2.x;
-                const float4 zq = reinterpret_cast<const float4 *>(&Q.rec[k].p)[3];     // wInvSum z1 z2 z3
-                const float zRej = __int_as_float(q2.w);
-                auto test = [&](float &d, uint32_t &vis, bool rowOK) {
-                    if (!rowOK || !((int32_t)(w1 | w2 | w3) > 0)) return;
+                const uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + rowA * (uint32_t)q1.z;
+                const uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + rowA * (uint32_t)q1.w;
+                const uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + rowA * (uint32_t)q2.x;
+                if (r0 && (int32_t)(w1 | w2 | w3) > 0) cm0 |= 1u << k;
+                if (r1 && (int32_t)((w1 + 4u * (uint32_t)q1.z) | (w2 + 4u * (uint32_t)q1.w) | (w3 + 4u * (uint32_t)q2.x)) > 0)
+                    cm1 |= 1u << k;
+            } else {
+                const PFPrim &P = Q.rec[k].p;
+                if (r0 && lp_covers(P, (int32_t)X0, (int32_t)Y0)) cm0 |= 1u << k;
+                if (r1 && lp_covers(P, (int32_t)X0, (int32_t)Y1)) cm1 |= 1u << k;
+            }
+        }
+        // 2b. depth: each of my pixels walks its covering records in
+        //     submission order -- depth (the correctly rounded reciprocal),
+        //     the depth-test rejection bound, the depth test and write
+        uint32_t vis0 = 0, vis1 = 0;                    // bit k: record k passed at my pixel of slot 0 / 1
+        uint32_t cov = 0;
+        auto depth_walk = [&](uint32_t cm, float &d, uint32_t &vis, uint32_t row, uint32_t Y) {
+            for (; cm; cm &= cm - 1) {
+                const uint32_t k = (uint32_t)(__ffs(cm) - 1);
+                const int4 *e4 = reinterpret_cast<const int4 *>(&Q.edge[k]);
+                const int4 q2 = e4[2];
+                const uint32_t box = (uint32_t)q2.y, rs = (uint32_t)q2.z;
+                const int func = (int)((rs >> 16) & 255u);
+                float z;
+                if (((box >> 16) & 3u) == 0) {
                     cov++;
-                    if (zRej >= d) return;                      // every fragment of it fails the depth test
+                    if (__int_as_float(q2.w) >= d) continue;  // every fragment of it fails the depth test
+                    const int4 q0 = e4[0], q1 = e4[1];
+                    const uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + row * (uint32_t)q1.z;
+                    const uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + row * (uint32_t)q1.w;
+                    const uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + row * (uint32_t)q2.x;
+                    const float4 zq = reinterpret_cast<const float4 *>(&Q.rec[k].p)[3];     // wInvSum z1 z2 z3
                     const float wn1 = (float)(int32_t)w1 * zq.x, wn2 = (float)(int32_t)w2 * zq.x;
                     const float wn3 = (float)(int32_t)w3 * zq.x;
                     float zs = zq.y * wn1 + zq.z * wn2;
                     zs = zs + zq.w * wn3;
-                    const float z = __frcp_rn(zs);
-                    if (!(rs & PFS_DEPTH_TEST) || depth_simd(func, z, d)) {
-                        vis |= 1u << k;
-                        if (rs & PFS_DEPTH_MASK) d = z;
-                    }
-                };
-                test(dep0, vis0, r0);
-                w1 += 4u * (uint32_t)q1.z; w2 += 4u * (uint32_t)q1.w; w3 += 4u * (uint32_t)q2.x;
-                test(dep1, vis1, r1);
-            } else {
-                // a point, line or rectangle set up on the host: its own
-                // coverage and depth, the scalar depth test
-                const PFPrim &P = Q.rec[k].p;
-                const bool counted = ((box >> 16) & 3u) != (PFP_BLIT >> 6);   // rectangles are not fragments
-                auto test = [&](float &d, uint32_t &vis, bool rowOK, uint32_t Y) {
-                    if (!rowOK || !lp_covers(P, (int32_t)X0, (int32_t)Y)) return;
-                    if (counted) cov++;
-                    const float z = lp_depth(P, (int32_t)X0, (int32_t)Y);
-                    if (!(rs & PFS_DEPTH_TEST) || depth_sisd(func, z, d)) {
-                        vis |= 1u << k;
-                        if (rs & PFS_DEPTH_MASK) d = z;
-                    }
-                };
-                test(dep0, vis0, r0, Y0);
-                test(dep1, vis1, r1, Y1);
+                    z = __frcp_rn(zs);
+                    if ((rs & PFS_DEPTH_TEST) && !depth_simd(func, z, d)) continue;
+                } else {
+                    // a point, line or rectangle set up on the host: its own
+                    // depth, the scalar depth test (rectangles are not fragments)
+                    const PFPrim &P = Q.rec[k].p;
+                    if (((box >> 16) & 3u) != (PFP_BLIT >> 6)) cov++;
+                    z = lp_depth(P, (int32_t)X0, (int32_t)Y);
+                    if ((rs & PFS_DEPTH_TEST) && !depth_sisd(func, z, d)) continue;
+                }
+                vis |= 1u << k;
+                if (rs & PFS_DEPTH_MASK) d = z;
             }
-        }
+        };
+        depth_walk(cm0, dep0, vis0, rowA, Y0);
+        depth_walk(cm1, dep1, vis1, ly + 4u, Y1);
         frags += cov;
         // 3+4. shade the fragments that passed, densely over the warp, and
         //      blend each pixel's in submission order
