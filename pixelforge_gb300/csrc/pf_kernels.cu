@@ -402,10 +402,12 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
 {
     __shared__ __align__(16) PFSegment sSeg;
     __shared__ __align__(16) PFDrawState sState;
-    __shared__ int sUniform;
+    __shared__ int sUniform, sAborted;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // (no-op unless launched programmatically serialized)
-    if (cnt->abortCommand != 0xffffffffu) return;
+    if (threadIdx.x == 0) sAborted = cnt->abortCommand != 0xffffffffu;     // one decision per block
+    __syncthreads();
+    if (sAborted) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
     if (g == 0) {
         cnt->clipCount = 0; cnt->batchRasterized = 0; cnt->tileQueue = 0; cnt->sortQueue = 0;
@@ -862,10 +864,15 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 {
     __shared__ __align__(16) PFSegment sSeg;
     __shared__ __align__(16) PFDrawState sState;
-    __shared__ int sUniform;
+    __shared__ int sUniform, sAborted;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_vertex is done
-    if (B.cnt->abortCommand != 0xffffffffu) return;
+    // An overflow in this launch flags the abort while other blocks run: the
+    // block takes one decision (a thread that returned alone would leave
+    // the rest of the block with unset shared state).
+    if (threadIdx.x == 0) sAborted = B.cnt->abortCommand != 0xffffffffu;
+    __syncthreads();
+    if (sAborted) return;
     const uint32_t g0 = blockIdx.x * blockDim.x;
     if (threadIdx.x == 0) {
         const int a = seg_of_item(segs, nSegs, g0), b = seg_of_item(segs, nSegs, min(g0 + blockDim.x, nItems) - 1);
@@ -1354,14 +1361,17 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     nQueue += min(a.cnt->tileListCount, a.totalTiles);
     levelEnd[0] = nQueue;
     const uint32_t nClear = (a.totalTiles + 31u) / 32u;
-    uint32_t claim = 0;
-    if (lane == 0) claim = atomicAdd(&a.cnt->tileQueue, 1u);
+    // each warp's first entry is its own index in the grid; the counter
+    // hands out the entries after those (3,648 warps claiming their first
+    // entry with one atomic each would serialise at the start)
+    const uint32_t gridWarps = gridDim.x * (uint32_t)WARPS;
+    uint32_t claim = blockIdx.x * (uint32_t)WARPS + (uint32_t)warp;
     for (;;) {
     uint32_t next = 0xffffffffu;
     if (lane == 0) {
         const uint32_t q = claim;
         if (q < nQueue + nClear) {
-            claim = atomicAdd(&a.cnt->tileQueue, 1u);
+            claim = gridWarps + atomicAdd(&a.cnt->tileQueue, 1u);
             if (q >= nQueue) next = 0x80000000u | (q - nQueue);      // a group of tiles to clear
             else {
                 uint32_t level = PF_HEAVY_LEVELS, begin = 0;
