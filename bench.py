@@ -247,10 +247,10 @@ def run_section(name: str) -> dict:
     return json.loads(lines[-1])
 
 
-def section_main(name: str) -> dict:
+def section_main(name: str, args) -> dict:
     from pixelforge_gb300 import load_library
     if name == "adjoint":
-        return run_adjoint(argparse.Namespace())
+        return run_adjoint(args)
     lib = load_library()
     return {"soup256": run_soup, "phong": run_phong, "framebuffer_formats": run_formats,
             "batched": run_batched}[name](lib)
@@ -598,7 +598,7 @@ def main():
                     help="run one secondary workload alone and print its JSON object")
     args = ap.parse_args()
     if args.section:
-        print(json.dumps(section_main(args.section)))
+        print(json.dumps(section_main(args.section, args)))
         return
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
