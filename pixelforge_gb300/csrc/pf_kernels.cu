@@ -947,7 +947,6 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
 #define SORT_THREADS 256
 #define REG_SORT_MAX 128            // bins shorter than this are sorted by the raster warp (four keys a lane)
 #define REG_SORT_LEVEL 2            // the heavy-level list of bins that reached REG_SORT_MAX entries
-#define RANK_SORT_MAX 256           // k_binsort: bins up to this size are rank-sorted, longer ones bitonic-sorted
 
 static_assert(PF_TILE == 8 && PF_TILE_PIXELS == 64, "a warp owns a tile: two pixels per lane");
 static_assert(REG_SORT_MAX == (PF_HEAVY_BASE << (2 * (REG_SORT_LEVEL - 1))), "k_binsort takes one heavy-level list");
@@ -1240,16 +1239,36 @@ template <> struct FbPixel<true> {
 
 // k_binsort: one CTA per bin that reached REG_SORT_MAX entries (a
 // heavy-level list), taken from a queue: its keys are put back into
-// submission order in place -- rank sort up to RANK_SORT_MAX entries,
-// bitonic sort in shared memory beyond.
+// submission order in place by a merge sort in shared memory.  A bin is a
+// concatenation of runs that are each in order already (a warp of k_items
+// appends its lanes' entries of a tile in lane order): each warp first
+// sorts 32-key chunks in registers, then chunks are merged pairwise, level
+// by level -- a key's place in the merged run is its place in its own run
+// plus the number of smaller keys in the partner run, found by binary
+// search.  Keys are unique (item << PF_SUB_BITS | sub-triangle, below 2^31);
+// the padding to a whole chunk is unique too (2^31 + place), so every level
+// is a permutation.
+__device__ __forceinline__ uint32_t warp_sort32(uint32_t key)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t k = 2; k <= 32; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t o = __shfl_xor_sync(0xffffffffu, key, (int)j);
+            const bool asc = (lane & k) == 0, low = (lane & j) == 0;
+            key = (asc == low) ? min(key, o) : max(key, o);
+        }
+    return key;
+}
+
 __global__ void __launch_bounds__(SORT_THREADS) k_binsort(RasterArgs a)
 {
-    extern __shared__ uint32_t sbuf[];                // a bin's keys (room for a bitonic sort)
+    extern __shared__ uint32_t sbuf[];                // two buffers of a bin's keys (merge source and target)
     __shared__ uint32_t sTile;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_items is done
     if (a.cnt->abortCommand <= a.command) return;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nList = min(a.cnt->heavyCount[REG_SORT_LEVEL - 1], a.totalTiles);
+    uint32_t capPad = 32; while (capPad < a.cap) capPad <<= 1;   // each buffer's room
     for (;;) {
         if (tid == 0) {
             const uint32_t q = atomicAdd(&a.cnt->sortQueue, 1u);
@@ -1259,38 +1278,37 @@ __global__ void __launch_bounds__(SORT_THREADS) k_binsort(RasterArgs a)
         const uint32_t t = sTile;
         if (t == 0xffffffffu) break;
         const uint32_t n = min(__ldg(a.binCount + t), a.cap);
+        const uint32_t nPad = (n + 31u) & ~31u;
         uint32_t *bin = a.bins + (size_t)t * a.cap;
-        for (uint32_t i = tid; i < n; i += SORT_THREADS) sbuf[i] = bin[i];
-        __syncthreads();
+        // 1. chunks of 32 keys sorted in registers (padding 2^31 + place);
+        //    whether the bin is in order already
         int unsorted = 0;
-        for (uint32_t i = tid; i + 1 < n; i += SORT_THREADS) unsorted |= (sbuf[i] > sbuf[i + 1]);
-        if (__syncthreads_or(unsorted)) {
-            if (n <= RANK_SORT_MAX) {
-                // keys are unique: a key's place is the number of smaller keys
-                for (uint32_t i = tid; i < n; i += SORT_THREADS) {
-                    const uint32_t k = sbuf[i];
-                    uint32_t r = 0;
-                    for (uint32_t j = 0; j < n; j++) r += (sbuf[j] < k);
-                    bin[r] = k;
-                }
-            } else {
-                uint32_t N = 1; while (N < n) N <<= 1;
-                for (uint32_t i = n + tid; i < N; i += SORT_THREADS) sbuf[i] = 0xffffffffu;
-                __syncthreads();
-                for (uint32_t k = 2; k <= N; k <<= 1)
-                    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                        // pair p: places i (bit j clear) and i + j
-                        for (uint32_t p = tid; p < N / 2; p += SORT_THREADS) {
-                            const uint32_t i = ((p & ~(j - 1)) << 1) | (p & (j - 1)), ixj = i | j;
-                            const uint32_t x = sbuf[i], y = sbuf[ixj];
-                            if ((x > y) == ((i & k) == 0)) { sbuf[i] = y; sbuf[ixj] = x; }
-                        }
-                        __syncthreads();
-                    }
-                for (uint32_t i = tid; i < n; i += SORT_THREADS) bin[i] = sbuf[i];
-            }
+        for (uint32_t c = (uint32_t)warp * 32u; c < nPad; c += SORT_THREADS) {
+            const uint32_t i = c + (uint32_t)lane;
+            const uint32_t key = i < n ? bin[i] : 0x80000000u + i;
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+            unsorted |= (lane > 0 && prev > key) || (lane == 0 && c > 0 && i < n && bin[i - 1] > key);
+            sbuf[i] = warp_sort32(key);
         }
-        __syncthreads();                               // sTile and sbuf are free
+        if (__syncthreads_or(unsorted)) {
+            // 2. merge levels: runs of w keys, pairwise, into the other buffer
+            uint32_t *src = sbuf, *dst = sbuf + capPad;
+            for (uint32_t w = 32; w < nPad; w <<= 1) {
+                for (uint32_t i = tid; i < nPad; i += SORT_THREADS) {
+                    const uint32_t run = i / w, s0 = run * w;
+                    const uint32_t oStart = (run & 1u) ? s0 - w : s0 + w;      // the partner run
+                    const uint32_t oLen = oStart < nPad ? min(w, nPad - oStart) : 0u;
+                    const uint32_t key = src[i];
+                    uint32_t lo = 0, hi = oLen;                                  // partner keys below key
+                    while (lo < hi) { const uint32_t mid = (lo + hi) >> 1; if (src[oStart + mid] < key) lo = mid + 1; else hi = mid; }
+                    dst[(run & ~1u) * w + (i - s0) + lo] = key;
+                }
+                __syncthreads();
+                uint32_t *tmp = src; src = dst; dst = tmp;
+            }
+            for (uint32_t i = tid; i < n; i += SORT_THREADS) bin[i] = src[i];
+        }
+        __syncthreads();                               // sTile and the buffers are free
     }
 }
 
@@ -1861,8 +1879,8 @@ static cudaError_t persistent_grid(const void *kernel, int block, size_t smem, i
 cudaError_t pfd_launch_binsort(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
-    uint32_t N = 1; while (N < L.cap) N <<= 1;
-    const size_t smem = (size_t)N * sizeof(uint32_t);
+    uint32_t N = 32; while (N < L.cap) N <<= 1;
+    const size_t smem = 2 * (size_t)N * sizeof(uint32_t);             // merge source and target
     cudaError_t e = cudaFuncSetAttribute(k_binsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     uint32_t grid = 0;
     if (e == cudaSuccess) e = persistent_grid((const void *)k_binsort, SORT_THREADS, smem, 0, L.totalTiles, grid);
