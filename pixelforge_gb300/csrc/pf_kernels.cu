@@ -976,7 +976,8 @@ struct RasterArgs {
 // bank 0).
 struct __align__(16) SPrim {
     PFPrim p;
-    int4 pad;
+    const PFPrimPhong *ph;     // its per-fragment lighting record (read when a fragment is shaded)
+    uint64_t pad;
 };
 
 // A batch record's coverage view, three 16-byte words: edge functions at the
@@ -1078,10 +1079,12 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
     }
     if (fl & PFS_PHONG) {
         const PFDrawState &S = states[P.flags >> 8];
+        PFPrimPhong q;                                  // (80 bytes, five 16-byte loads)
+        for (int i = 0; i < 5; i++) reinterpret_cast<float4 *>(&q)[i] = __ldg(reinterpret_cast<const float4 *>(Q) + i);
         float N[3], Pp[3];
         for (int i = 0; i < 3; i++) {
-            float t0 = Q->n1[i] * wn1 + Q->n2[i] * wn2; N[i] = t0 + Q->n3[i] * wn3;
-            float t1 = Q->p1[i] * wn1 + Q->p2[i] * wn2; Pp[i] = t1 + Q->p3[i] * wn3;
+            float t0 = q.n1[i] * wn1 + q.n2[i] * wn2; N[i] = t0 + q.n3[i] * wn3;
+            float t1 = q.p1[i] * wn1 + q.p2[i] * wn2; Pp[i] = t1 + q.p3[i] * wn3;
         }
         frag = light_phong(S, frag, S.mat[P.flags & 1], Pp, N);
     }
@@ -1345,7 +1348,6 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     extern __shared__ __align__(16) unsigned char rsmem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     QWarp &Q = reinterpret_cast<QWarp *>(rsmem)[warp];
-    PFPrimPhong *const ph = reinterpret_cast<PFPrimPhong *>(rsmem + WARPS * sizeof(QWarp)) + warp * QCHN;
 
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_binsort is done
     if (a.cnt->abortCommand <= a.command) return;
@@ -1534,11 +1536,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             for (int i = 0; i < 8; i++) r[i] = __ldg(s4 + i);
             int4 *d4 = reinterpret_cast<int4 *>(&Q.rec[lane].p);
             for (int i = 0; i < 8; i++) d4[i] = r[i];
-            if (a.anyPhong) {
-                const int4 *p4 = reinterpret_cast<const int4 *>(sub != 0 ? &a.poolPh[pi] : &a.primsPh[item]);
-                int4 *q4 = reinterpret_cast<int4 *>(&ph[lane]);
-                for (int i = 0; i < 5; i++) q4[i] = __ldg(p4 + i);
-            }
+            Q.rec[lane].ph = a.anyPhong ? (sub != 0 ? &a.poolPh[pi] : &a.primsPh[item]) : nullptr;
             QEdge E;
             tile_edge(r[0], r[1], r[2], (uint32_t)r[4].w, __int_as_float(r[6].z), ox, oy, W, H, E);
             Q.edge[lane] = E;
@@ -1633,7 +1631,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
                 }
                 float wn[3];
                 const float z = tile_depth(Q.edge[k], P, X, Y, wn);
-                Q.fc[f - b0] = shade_fragment(P, &ph[k], a.states, wn[0], wn[1], wn[2], z);
+                Q.fc[f - b0] = shade_fragment(P, Q.rec[k].ph, a.states, wn[0], wn[1], wn[2], z);
             }
             __syncwarp();
             if (cntv && offv < bEnd && offv + cntv > b0) {
@@ -1850,11 +1848,12 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
                              (const PFVertexOut *)L.vout, L.nItems, O, B);
 }
 
-// Dynamic shared memory of k_raster: the warps' batch buffers and their
-// per-fragment lighting records when the launch has any.
-static size_t raster_smem(bool anyPhong, int warps)
+// Dynamic shared memory of k_raster: the warps' batch buffers (a record's
+// per-fragment lighting data is read through L1 when a fragment is shaded,
+// not staged: the CTAs' shared memory would bound how many fit on an SM).
+static size_t raster_smem(int warps)
 {
-    return (size_t)warps * (sizeof(QWarp) + (anyPhong ? QCHN * sizeof(PFPrimPhong) : 0));
+    return (size_t)warps * sizeof(QWarp);
 }
 
 static RasterArgs raster_args(const PFBatchLaunch &L)
@@ -1892,7 +1891,7 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.totalTiles == 0) return cudaSuccess;
     const int warps = (L.rasterWarps == 2 || L.rasterWarps == 8) ? L.rasterWarps : 4;
-    const size_t smem = raster_smem(L.anyPhong != 0, warps);
+    const size_t smem = raster_smem(warps);
     void (*kernel)(RasterArgs) =
         L.generic ? (warps == 2 ? k_raster<true, 2> : warps == 8 ? k_raster<true, 8> : k_raster<true, 4>)
                   : (warps == 2 ? k_raster<false, 2> : warps == 8 ? k_raster<false, 8> : k_raster<false, 4>);
