@@ -1272,9 +1272,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_binsort(RasterArgs a)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nList = min(a.cnt->heavyCount[REG_SORT_LEVEL - 1], a.totalTiles);
     uint32_t capPad = 32; while (capPad < a.cap) capPad <<= 1;   // each buffer's room
-    for (;;) {
+    // a CTA's first entry is its index in the grid, the counter hands out
+    // the entries after those (no atomics at all when no bin needs sorting)
+    for (uint32_t first = 1;; first = 0) {
         if (tid == 0) {
-            const uint32_t q = atomicAdd(&a.cnt->sortQueue, 1u);
+            const uint32_t q = first ? blockIdx.x : (blockIdx.x < nList ? gridDim.x + atomicAdd(&a.cnt->sortQueue, 1u) : nList);
             sTile = q < nList ? __ldg(a.tileList + (size_t)REG_SORT_LEVEL * a.listStride + q) : 0xffffffffu;
         }
         __syncthreads();
