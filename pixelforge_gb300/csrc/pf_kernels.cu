@@ -1334,6 +1334,22 @@ __device__ __forceinline__ void tile_list(unsigned long long m, uint32_t off, ui
     }
 }
 
+// 32x32 bit matrix held one row a lane (bit j of lane k) -> one column a
+// lane: lane j gets bit k = bit j of lane k.  Five exchange steps, each
+// swapping the off-diagonal s x s blocks between lanes k and k ^ s.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t masks[5] = { 0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u };
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        const uint32_t s = 16u >> i, m = masks[i];
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, (int)s);
+        x = (lane & s) ? ((x & ~m) | ((y >> s) & m)) : ((x & m) | ((y << s) & ~m));
+    }
+    return x;
+}
+
 // Warp-wide exclusive prefix sum of v; total gets the sum over the warp.
 __device__ __forceinline__ uint32_t warp_offsets(uint32_t v, uint32_t &total)
 {
@@ -1523,8 +1539,9 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
 
     for (uint32_t c0 = 0; c0 < n; c0 += QCHN) {
         const uint32_t cn = min((uint32_t)QCHN, n - c0);
-        // 1. my record: load, stage, derive its tile set-up
+        // 1. my record: load, stage, derive its tile set-up and coverage
         uint32_t kind = 0;
+        unsigned long long covMask = 0;
         if ((uint32_t)lane < cn) {
             uint32_t key;
             if (!regSort) key = __ldg(bin + c0 + lane);
@@ -1543,35 +1560,38 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             tile_edge(r[0], r[1], r[2], (uint32_t)r[4].w, __int_as_float(r[6].z), ox, oy, W, H, E);
             Q.edge[lane] = E;
             kind = (uint32_t)r[2].z & PFP_KIND;
+            // my record's coverage of the tile, bit 8 y + x: the pixels of its
+            // box that pass the integer edge test (triangles.c:398-424) or,
+            // for a point, line or rectangle, its own rule
+            const uint32_t bx0 = E.box & 15u, bw = (E.box >> 4) & 15u, by0 = (E.box >> 8) & 15u, bh = (E.box >> 12) & 15u;
+            if (kind == 0) {
+                for (uint32_t y = by0; y < by0 + bh; y++) {
+                    uint32_t w1 = (uint32_t)E.e0[0] + bx0 * (uint32_t)E.ex0 + y * (uint32_t)E.ey0;
+                    uint32_t w2 = (uint32_t)E.e0[1] + bx0 * (uint32_t)E.ex1 + y * (uint32_t)E.ey1;
+                    uint32_t w3 = (uint32_t)E.e0[2] + bx0 * (uint32_t)E.ex2 + y * (uint32_t)E.ey2;
+                    uint32_t row = 0;
+                    for (uint32_t x = 0; x < bw; x++) {
+                        row |= ((int32_t)(w1 | w2 | w3) > 0 ? 1u : 0u) << x;
+                        w1 += (uint32_t)E.ex0; w2 += (uint32_t)E.ex1; w3 += (uint32_t)E.ex2;
+                    }
+                    covMask |= (unsigned long long)(row << bx0) << (8u * y);
+                }
+            } else {
+                const PFPrim &P = Q.rec[lane].p;
+                for (uint32_t y = by0; y < by0 + bh; y++)
+                    for (uint32_t x = bx0; x < bx0 + bw; x++)
+                        if (lp_covers(P, (int32_t)(ox + x), (int32_t)(oy + y))) covMask |= 1ull << (8u * y + x);
+            }
         }
         const bool anyLP = __any_sync(0xffffffffu, kind != 0);
         __syncwarp();
-        // 2a. coverage: bit k of cm0 / cm1 -- record k covers my pixel of
-        //     slot 0 / 1 (triangles: the integer edge functions; points,
-        //     lines and rectangles: their own rule).  Cheap per record, so
-        //     that the costly depth below runs for covering records only.
-        uint32_t cm0 = 0, cm1 = 0;
-        for (uint32_t k = 0; k < cn; k++) {
-            const int4 *e4 = reinterpret_cast<const int4 *>(&Q.edge[k]);
-            const int4 q2 = e4[2];
-            const uint32_t box = (uint32_t)q2.y;
-            const uint32_t bx0 = box & 15u, bw = (box >> 4) & 15u, by0 = (box >> 8) & 15u, bh = (box >> 12) & 15u;
-            const bool r0 = rowA - by0 < bh, r1 = whole && ly + 4u - by0 < bh;
-            if (lx - bx0 >= bw || !(r0 || r1)) continue;
-            if (((box >> 16) & 3u) == 0) {
-                const int4 q0 = e4[0], q1 = e4[1];
-                const uint32_t w1 = (uint32_t)q0.x + lx * (uint32_t)q0.w + rowA * (uint32_t)q1.z;
-                const uint32_t w2 = (uint32_t)q0.y + lx * (uint32_t)q1.x + rowA * (uint32_t)q1.w;
-                const uint32_t w3 = (uint32_t)q0.z + lx * (uint32_t)q1.y + rowA * (uint32_t)q2.x;
-                if (r0 && (int32_t)(w1 | w2 | w3) > 0) cm0 |= 1u << k;
-                if (r1 && (int32_t)((w1 + 4u * (uint32_t)q1.z) | (w2 + 4u * (uint32_t)q1.w) | (w3 + 4u * (uint32_t)q2.x)) > 0)
-                    cm1 |= 1u << k;
-            } else {
-                const PFPrim &P = Q.rec[k].p;
-                if (r0 && lp_covers(P, (int32_t)X0, (int32_t)Y0)) cm0 |= 1u << k;
-                if (r1 && lp_covers(P, (int32_t)X0, (int32_t)Y1)) cm1 |= 1u << k;
-            }
-        }
+        // 2a. coverage per pixel: bit k of cm0 / cm1 -- record k covers my
+        //     pixel of slot 0 / 1 -- the records' masks transposed over the
+        //     warp (rows 0-3 of the tile are bits 0-31: bit 8 y + x is lane
+        //     8 y + x's pixel of slot 0; rows 4-7 its pixel of slot 1)
+        const uint32_t cmLo = warp_transpose32((uint32_t)covMask);
+        const uint32_t cmHi = warp_transpose32((uint32_t)(covMask >> 32));
+        const uint32_t cm0 = (rowA == ly) ? cmLo : cmHi, cm1 = whole ? cmHi : 0u;
         // 2b. depth: each of my pixels walks its covering records in
         //     submission order -- depth (the correctly rounded reciprocal),
         //     the depth-test rejection bound, the depth test and write
