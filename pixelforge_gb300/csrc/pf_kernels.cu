@@ -996,6 +996,7 @@ struct __align__(16) QEdge {
 struct QWarp {
     SPrim rec[QCHN];
     QEdge edge[QCHN];
+    uint32_t keys[REG_SORT_MAX];   // a short bin's keys in submission order (sorted in registers)
     uint16_t fdesc[QFW];       // listed fragments: tile pixel << 5 | record
     uint32_t fc[QFW];          // their colour
 };
@@ -1535,6 +1536,9 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
                     }
                 }
             }
+        // (kept in shared memory for the batches: the registers are free)
+        for (uint32_t r = 0; r < 4; r++) Q.keys[32 * r + (uint32_t)lane] = sk[r];
+        __syncwarp();
     }
 
     for (uint32_t c0 = 0; c0 < n; c0 += QCHN) {
@@ -1545,7 +1549,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
         if ((uint32_t)lane < cn) {
             uint32_t key;
             if (!regSort) key = __ldg(bin + c0 + lane);
-            else key = c0 == 0 ? sk[0] : c0 == 32 ? sk[1] : c0 == 64 ? sk[2] : sk[3];
+            else key = Q.keys[c0 + (uint32_t)lane];
             const uint32_t item = key >> PF_SUB_BITS, sub = key & ((1u << PF_SUB_BITS) - 1);
             const PFPrim *src = &a.prims[item];
             uint32_t pi = item;
