@@ -899,15 +899,11 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
         T = tile_space(B, sg.target);
         kept = item_setup(sg, su >= 0 ? &sState : nullptr, states, vout, g, O, B, T, P);
     }
-    // one counter update per block: same-address atomics serialise in L2
-    __shared__ unsigned sKept;
-    if (threadIdx.x == 0) sKept = 0;
-    __syncthreads();
+    // one counter update per warp, its result unused (a reduction in L2, no
+    // round trip, no block barrier)
     const unsigned wk = __popc(__ballot_sync(0xffffffffu, kept));
-    if ((threadIdx.x & 31) == 0 && wk) atomicAdd(&sKept, wk);
+    if ((threadIdx.x & 31) == 0 && wk) atomicAdd(&B.cnt->batchRasterized, (unsigned long long)wk);
     bin_prim_warp(B, T, kept, P, g << PF_SUB_BITS);
-    __syncthreads();
-    if (threadIdx.x == 0 && sKept) atomicAdd(&B.cnt->batchRasterized, (unsigned long long)sKept);
 }
 
 // ---------------------------------------------------------------------------
@@ -1406,7 +1402,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     const uint32_t gridWarps = gridDim.x * (uint32_t)WARPS;
     uint32_t claim = blockIdx.x * (uint32_t)WARPS + (uint32_t)warp;
     for (;;) {
-    uint32_t next = 0xffffffffu;
+    uint32_t next = 0xffffffffu, nextCount = 0;
     if (lane == 0) {
         const uint32_t q = claim;
         if (q < nQueue + nClear) {
@@ -1418,12 +1414,14 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
                 const uint32_t e = q - begin;
                 const bool split = (splitLevels >> level) & 1u;
                 next = __ldg(a.tileList + (size_t)level * a.listStride + (split ? e >> 1 : e));
-                if (heavy_level(__ldg(a.binCount + next)) != level) next = 0xfffffffeu;   // rasterized from an earlier list
+                nextCount = __ldg(a.binCount + next);
+                if (heavy_level(nextCount) != level) next = 0xfffffffeu;   // rasterized from an earlier list
                 else if (split) next |= (e & 1u) ? TILE_BOTTOM : TILE_TOP;
             }
         }
     }
     const uint32_t gt = __shfl_sync(0xffffffffu, next, 0);
+    const uint32_t gtCount = __shfl_sync(0xffffffffu, nextCount, 0);   // (its bin count, read for the check)
     if (gt == 0xffffffffu) break;
     if (gt == 0xfffffffeu) continue;
     if (gt & 0x80000000u) {
@@ -1471,7 +1469,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gtile) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
     const uint32_t tile = gtile - T.tileBase;
-    const uint32_t n = min(__ldg(a.binCount + gtile), a.cap);
+    const uint32_t n = min(gtCount, a.cap);
     if (n == 0 && T.clearMode == 0) continue;
     const uint32_t ox = (tile % T.tilesX) * PF_TILE, oy = (tile / T.tilesX) * PF_TILE;
     const uint32_t W = T.W, H = T.H;
