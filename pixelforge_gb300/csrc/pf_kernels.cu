@@ -400,12 +400,22 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
                          PFVertexOut *__restrict__ out, uint32_t nVerts, PFDevCounters *cnt,
                          uint32_t *__restrict__ binCount, uint32_t nTiles)
 {
-    __shared__ __align__(16) PFSegment sSeg;
-    __shared__ __align__(16) PFDrawState sState;
     __shared__ int sUniform, sAborted;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // (no-op unless launched programmatically serialized)
-    if (threadIdx.x == 0) sAborted = cnt->abortCommand != 0xffffffffu;     // one decision per block
+    // thread 0 takes the block's decisions, behind one barrier: the abort
+    // (one decision per block) and the segment of the block's vertices when
+    // they share one (the usual case; the others search)
+    const uint32_t g0 = blockIdx.x * blockDim.x;
+    if (threadIdx.x == 0) {
+        sAborted = cnt->abortCommand != 0xffffffffu;
+        int su = -1;
+        if (g0 < nVerts) {
+            const int a = seg_of_vertex(segs, nSegs, g0), b = seg_of_vertex(segs, nSegs, min(g0 + blockDim.x, nVerts) - 1);
+            su = (a == b) ? a : -1;
+        }
+        sUniform = su;
+    }
     __syncthreads();
     if (sAborted) return;
     for (uint32_t t = g; t < nTiles; t += gridDim.x * blockDim.x) binCount[t] = 0;
@@ -414,29 +424,12 @@ __global__ void k_vertex(const PFSegment *__restrict__ segs, int nSegs, const PF
         cnt->tileListCount = 0;
         for (int l = 0; l < PF_HEAVY_LEVELS; l++) cnt->heavyCount[l] = 0;
     }
-    const uint32_t g0 = blockIdx.x * blockDim.x;
-    if (g0 >= nVerts) return;
-    // the block's vertices usually belong to one segment: stage it and its
-    // draw state in shared memory instead of reading both field by field
-    if (threadIdx.x == 0) {
-        const int a = seg_of_vertex(segs, nSegs, g0), b = seg_of_vertex(segs, nSegs, min(g0 + blockDim.x, nVerts) - 1);
-        sUniform = (a == b) ? a : -1;
-    }
-    __syncthreads();
-    const int su = sUniform;
-    if (su >= 0) {
-        const int4 *src0 = reinterpret_cast<const int4 *>(&segs[su]);
-        const int4 *src1 = reinterpret_cast<const int4 *>(&states[segs[su].state]);
-        constexpr int n0 = sizeof(PFSegment) / 16, n1 = sizeof(PFDrawState) / 16;
-        for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
-            if (i < n0) reinterpret_cast<int4 *>(&sSeg)[i] = __ldg(src0 + i);
-            else reinterpret_cast<int4 *>(&sState)[i - n0] = __ldg(src1 + (i - n0));
-        }
-        __syncthreads();
-    }
     if (g >= nVerts) return;
-    const PFSegment &sg = (su >= 0) ? sSeg : segs[seg_of_vertex(segs, nSegs, g)];
-    const PFDrawState &S = (su >= 0) ? sState : states[sg.state];
+    // the segment and its draw state are read in place (one address for the
+    // block: L1 serves it after the first access)
+    const int su = sUniform;
+    const PFSegment &sg = segs[su >= 0 ? su : seg_of_vertex(segs, nSegs, g)];
+    const PFDrawState &S = states[sg.state];
     const uint32_t j = g - sg.vtxBase;
     float pos[4], nrm[3], uv[2];
     uint32_t col;
@@ -862,42 +855,33 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
 __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
                         const PFVertexOut *__restrict__ vout, uint32_t nItems, ItemOut O, BinArgs B)
 {
-    __shared__ __align__(16) PFSegment sSeg;
-    __shared__ __align__(16) PFDrawState sState;
     __shared__ int sUniform, sAborted;
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_vertex is done
-    // An overflow in this launch flags the abort while other blocks run: the
-    // block takes one decision (a thread that returned alone would leave
-    // the rest of the block with unset shared state).
-    if (threadIdx.x == 0) sAborted = B.cnt->abortCommand != 0xffffffffu;
-    __syncthreads();
-    if (sAborted) return;
+    // Thread 0 takes the block's decisions, behind one barrier: whether an
+    // overflow in this launch has flagged the abort (other blocks set it
+    // while this one runs; a thread that returned alone would leave the rest
+    // of the block with unset shared state), and the segment of the block's
+    // items when they share one (the usual case; the others search).
     const uint32_t g0 = blockIdx.x * blockDim.x;
     if (threadIdx.x == 0) {
+        sAborted = B.cnt->abortCommand != 0xffffffffu;
         const int a = seg_of_item(segs, nSegs, g0), b = seg_of_item(segs, nSegs, min(g0 + blockDim.x, nItems) - 1);
         sUniform = (a == b) ? a : -1;
     }
     __syncthreads();
+    if (sAborted) return;
     const int su = sUniform;
-    if (su >= 0) {
-        const int4 *src0 = reinterpret_cast<const int4 *>(&segs[su]);
-        const int4 *src1 = reinterpret_cast<const int4 *>(&states[segs[su].state]);
-        constexpr int n0 = sizeof(PFSegment) / 16, n1 = sizeof(PFDrawState) / 16;
-        for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
-            if (i < n0) reinterpret_cast<int4 *>(&sSeg)[i] = __ldg(src0 + i);
-            else reinterpret_cast<int4 *>(&sState)[i - n0] = __ldg(src1 + (i - n0));
-        }
-        __syncthreads();
-    }
     // every lane stays to the end: binning below is warp-cooperative
     PFPrim P;
     bool kept = false;
     TileSpace T{ 0, 0, 0, 0 };
     if (g < nItems) {
-        const PFSegment &sg = su >= 0 ? sSeg : segs[seg_of_item(segs, nSegs, g)];
+        // the segment and its draw state are read in place (one address for
+        // the block: L1 serves it after the first access)
+        const PFSegment &sg = segs[su >= 0 ? su : seg_of_item(segs, nSegs, g)];
         T = tile_space(B, sg.target);
-        kept = item_setup(sg, su >= 0 ? &sState : nullptr, states, vout, g, O, B, T, P);
+        kept = item_setup(sg, nullptr, states, vout, g, O, B, T, P);
     }
     // one counter update per warp, its result unused (a reduction in L2, no
     // round trip, no block barrier)
