@@ -49,7 +49,7 @@ __device__ __forceinline__ void v3_normalize(float *v)          // pfm.h:1183-11
 {
     float sq = v[0]*v[0] + v[1]*v[1] + v[2]*v[2];
     if (sq == 0.0f) return;
-    float inv = 1.0f / sqrtf(sq);
+    float inv = __frcp_rn(sqrtf(sq));
     v[0] = v[0] * inv; v[1] = v[1] * inv; v[2] = v[2] * inv;
 }
 __device__ __forceinline__ float v3_dot(const float *a, const float *b) { return a[0]*b[0] + a[1]*b[1] + a[2]*b[2]; }
@@ -158,7 +158,7 @@ __device__ bool setup_prim(const PFDrawState &S, int face, bool is3D, const SVer
     P.xMin = mnx; P.yMin = mny; P.xMax = mxx; P.yMax = mxy;
     P.flags = (uint32_t)face | (is3D ? 2u : 0u) | ((uint32_t)stateIdx << 8);
     P.poolBase = -1;
-    P.wInvSum = 1.0f / (float)(int32_t)(r1 + r2 + r3);
+    P.wInvSum = __frcp_rn((float)(int32_t)(r1 + r2 + r3));
     P.z1 = a.z; P.z2 = b.z; P.z3 = c.z;
     P.c1 = a.c; P.c2 = b.c; P.c3 = c.c;
     P.rstate = raster_state(S);

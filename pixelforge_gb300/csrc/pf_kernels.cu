@@ -71,7 +71,7 @@ __device__ uint32_t light_gouraud(const PFDrawState &S, const PFDevMaterial &m, 
     {
         float lsq = 0.0f;
         for (int i = 0; i < 3; i++) { V[i] = S.viewPos[i] - P[i]; lsq += V[i]*V[i]; }
-        float inv = 1.0f / sqrtf(lsq);
+        float inv = __frcp_rn(sqrtf(lsq));
         for (int i = 0; i < 3; i++) V[i] = V[i] * inv;
     }
     const float shin = m.shininess;
@@ -83,7 +83,7 @@ __device__ uint32_t light_gouraud(const PFDrawState &S, const PFDevMaterial &m, 
         float dist = 0.0f;
         if (dsq != 0.0f) {
             dist = sqrtf(dsq);
-            float inv = 1.0f / dist;
+            float inv = __frcp_rn(dist);
             L[0] = L[0] * inv; L[1] = L[1] * inv; L[2] = L[2] * inv;
         }
         uint32_t intensity = 255;
@@ -311,7 +311,7 @@ __device__ __forceinline__ void dir_simd(float *d, const float *a, const float *
     float lsq = d[0]*d[0] + d[1]*d[1];
     lsq = lsq + d[2]*d[2];
     lsq = x86_max(lsq, 1e-5f);
-    float inv = 1.0f / sqrtf(lsq);
+    float inv = __frcp_rn(sqrtf(lsq));
     d[0] = d[0] * inv; d[1] = d[1] * inv; d[2] = d[2] * inv;
 }
 __device__ __forceinline__ float dot_simd(const float *a, const float *b)
@@ -350,7 +350,7 @@ __device__ uint32_t light_phong(const PFDrawState &S, uint32_t frag, const PFDev
         float H[3] = { L[0] + V[0], L[1] + V[1], L[2] + V[2] };
         float hs = H[0]*H[0] + H[1]*H[1];
         hs = hs + H[2]*H[2];
-        float hinv = 1.0f / sqrtf(hs);
+        float hinv = __frcp_rn(sqrtf(hs));
         for (int i = 0; i < 3; i++) H[i] = H[i] * hinv;
         float spec = x86_max(dot_simd(N, H), 0.0f);
         spec = cephes_exp(cephes_log(spec) * m.shininess);
@@ -368,7 +368,7 @@ __device__ uint32_t light_phong(const PFDrawState &S, uint32_t frag, const PFDev
             float d0 = l.pos[0] - P[0], d1 = l.pos[1] - P[1], d2 = l.pos[1] - P[1];
             float dsq = d0*d0 + (d1*d1 + d2*d2);
             float dist = sqrtf(dsq);
-            float att = 1.0f / (l.attC + (l.attL*dist + l.attQ*dsq));
+            float att = __frcp_rn(l.attC + (l.attL*dist + l.attQ*dsq));
             for (int i = 0; i < 3; i++) { amb[i] = amb[i] * att; dif[i] = dif[i] * att; spe[i] = spe[i] * att; }
         }
         for (int i = 0; i < 3; i++) { acc[i] = acc[i] + amb[i]; acc[i] = acc[i] + dif[i]; acc[i] = acc[i] + spe[i]; }
@@ -747,9 +747,9 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
     if (n < 3) return;
     SVert s[PF_CLIP_MAXV];
     for (int i = 0; i < n; i++) {
-        float hz = 1.0f / poly[i].h[2];
+        float hz = __frcp_rn(poly[i].h[2]);
         s[i].u = poly[i].uv[0] * hz; s[i].v = poly[i].uv[1] * hz;
-        float invW = 1.0f / poly[i].h[3];
+        float invW = __frcp_rn(poly[i].h[3]);
         to_screen(S, poly[i].h[0] * invW, poly[i].h[1] * invW, s[i].sx, s[i].sy);
         s[i].z = hz;
         s[i].c = poly[i].c;
@@ -837,9 +837,9 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
             to_screen(S, h.x, h.y, s[m].sx, s[m].sy);
             s[m].z = h.z; s[m].u = uv.x; s[m].v = uv.y;
         } else {
-            float hz = 1.0f / h.z;
+            float hz = __frcp_rn(h.z);
             s[m].u = uv.x * hz; s[m].v = uv.y * hz;
-            float invW = 1.0f / h.w;
+            float invW = __frcp_rn(h.w);
             to_screen(S, h.x * invW, h.y * invW, s[m].sx, s[m].sy);
             s[m].z = hz;
         }
@@ -1748,7 +1748,7 @@ __global__ void k_hook(void *color, uint32_t fmt, const float *depth, size_t n, 
                 c = alpha == 255u ? f : blend_sisd(1, f, c);
             } else if (d > hp.start) {
                 float t = 0.0f;
-                const float invLen = 1.0f / (hp.end - hp.start);
+                const float invLen = __frcp_rn(hp.end - hp.start);
                 if (hp.mode == 0) t = (d - hp.start) * invLen;
                 else if (hp.mode == 1) t = 1.0f - (float)exp((double)(-hp.density * (d - hp.start)));
                 else if (hp.mode == 2) t = 1.0f - (float)exp2((double)(-hp.density * (d - hp.start)));
