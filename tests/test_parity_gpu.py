@@ -285,11 +285,11 @@ def _aligned(n_bytes: int, misalign: int) -> np.ndarray:
 
 @pytest.mark.parametrize("misalign", [0, 4])
 def test_draw_time_snapshot_of_large_arrays(gpu, oracle, misalign):
-    """Arrays of 64 KiB and more are copied to the device during the draw
-    call (in place from 16-byte-aligned pageable memory, else by
-    cudaMemcpyAsync): the caller overwrites positions, colours, texcoords,
-    indices and texture right after each draw, and the image must be the
-    one the reference draws from the contents at each call."""
+    """Arrays of 64 KiB and more are copied during the draw call (from
+    pageable memory into page-locked memory by the host workers, then by
+    DMA): the caller overwrites positions, colours, texcoords, indices and
+    texture right after each draw, and the image must be the one the
+    reference draws from the contents at each call."""
     from pixelforge_gb300.scenes import Target, _ptr
     ntri, W, H = 20000, 256, 192
     nv = ntri * 3
@@ -339,6 +339,64 @@ def test_draw_time_snapshot_of_large_arrays(gpu, oracle, misalign):
     assert gpu.pfGetDeviceStatus() == 0
     assert (ref.depth < 1e30).sum() > 10000
     assert_parity(got, ref, exact_color=True, label=f"snapshot misalign={misalign}")
+
+
+def test_draw_time_snapshot_reuse_and_pinned_texture(gpu, oracle):
+    """Within one recording a later draw reuses the copy of an array it
+    references again unchanged (here the indices, and positions on some
+    draws) and copies again what changed; a texture of 1 MiB and more is
+    page-locked on its second draw and copied by DMA from then on -- the
+    caller changes it between draws too.  Every draw must see the contents
+    at its own call."""
+    from pixelforge_gb300.scenes import Target, _ptr
+    import ctypes as C
+    ntri, W, H = 20000, 256, 192
+    nv = ntri * 3
+    r0 = np.random.default_rng(7)
+    pos = r0.uniform(-1.1, 1.1, (nv, 3)).astype(np.float32) * np.float32([1, 1, 0.8])
+    uv = r0.uniform(-1, 2, (nv, 2)).astype(np.float32)
+    idx = r0.permutation(nv).astype(np.uint32)
+    tex = r0.integers(0, 256, (512, 512, 4)).astype(np.uint8)      # 1 MiB
+
+    def run(lib):
+        tg = Target(lib, W, H, "fbo")
+        th = None
+        try:
+            lib.pfDisable(A.PF_CULL_FACE)
+            lib.pfEnable(A.PF_DEPTH_TEST)
+            lib.pfEnable(A.PF_BLEND)
+            lib.pfBlendFunc(A.PF_BLEND_ALPHA)
+            lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+            th = lib.pfGenTexture(_ptr(tex), 512, 512, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+            lib.pfBindTexture(th)
+            lib.pfEnable(A.PF_TEXTURE_2D)
+            lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_TEXTURE_COORD_ARRAY)
+            lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(pos))
+            lib.pfTexCoordPointer(A.PF_FLOAT, 0, _ptr(uv))
+            r = np.random.default_rng(11)
+            for k in range(5):
+                # indices never change; positions on draws 2 and 4; the
+                # texture's top rows on every draw after the first
+                if k in (2, 4):
+                    pos[:, 2] = r.uniform(-0.8, 0.8, nv).astype(np.float32)
+                if k > 0:
+                    tex[: 16 * k] = r.integers(0, 256, (16 * k, 512, 4)).astype(np.uint8)
+                lib.pfColor4ub(255, 255 - 40 * k, 255, 160)
+                lib.pfDrawElements(A.PF_TRIANGLES, nv, A.PF_UNSIGNED_INT, _ptr(idx))
+            return tg.finish()
+        finally:
+            if th:
+                h = C.c_void_p(th)
+                lib.pfDeleteTexture(C.byref(h), False)
+            tg.close()
+
+    saved = (pos.copy(), tex.copy())
+    got = run(gpu)
+    pos[...], tex[...] = saved
+    ref = run(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    assert (ref.depth < 1e30).sum() > 10000
+    assert_parity(got, ref, exact_color=True, label="snapshot reuse and pinned texture")
 
 
 def test_ragged_framebuffers(gpu, oracle):
