@@ -497,19 +497,20 @@ static uint16_t float_to_half(float x);
  * read the texel three places on, or the next texel, pixel.h:2253-2420),
  * single-channel and luminance half / float (their SIMD setters rewrite,
  * requantised, the pixels of the vector that the mask leaves out,
- * pixel.h:905-970, 1219-1490) and BGRA unsigned byte (lane-dependent
- * shuffle, pixel.h:2070-2078, 2916-2921). */
+ * pixel.h:905-970, 1219-1490).  BGRA unsigned byte, whose SIMD getter and
+ * setter shuffle a half vector with its first pixel's bytes, is accepted:
+ * raster_tri follows the halves. */
 static int fb_format_ok(PFpixelformat f, PFdatatype t)
 {
     if (!texel_bytes(f, t)) return 0;
     switch (f) {
-    case PF_RGB: case PF_BGR: case PF_RGBA: return 1;
-    case PF_BGRA: return t != PF_UNSIGNED_BYTE;
+    case PF_RGB: case PF_BGR: case PF_RGBA: case PF_BGRA: return 1;
     case PF_LUMINANCE_ALPHA: return t == PF_HALF_FLOAT || t == PF_FLOAT;
     default: return 0;
     }
 }
 static inline int fb_rgba8(const RTex *t) { return t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE; }
+static inline int fb_bgra8(const RTex *t) { return t->format == PF_BGRA && t->type == PF_UNSIGNED_BYTE; }
 
 /* Destination colour as the SIMD getter reads it (blending of triangles). */
 static inline uint32_t fb_get_simd(const RTex *t, size_t o)
@@ -543,7 +544,11 @@ static void fb_set_simd(RTex *t, size_t o, uint32_t col)
     case PF_UNSIGNED_SHORT_4_4_4_4:
         p16[o] = (uint16_t)(((c0 * 15u) >> 8) << 12 | ((g * 15u) >> 8) << 8 | ((c2 * 15u) >> 8) << 4 | ((a * 15u) >> 8));
         return;
-    case PF_UNSIGNED_BYTE:                                  /* RGB, BGR */
+    case PF_UNSIGNED_BYTE:                                  /* RGB, BGR, BGRA */
+        if (f == PF_BGRA) {
+            p8[4 * o] = (uint8_t)b; p8[4 * o + 1] = (uint8_t)g; p8[4 * o + 2] = (uint8_t)r; p8[4 * o + 3] = (uint8_t)a;
+            return;
+        }
         p8[3 * o] = (uint8_t)c0; p8[3 * o + 1] = (uint8_t)g; p8[3 * o + 2] = (uint8_t)c2;
         return;
     default: break;
@@ -759,6 +764,64 @@ static uint32_t light_phong(const RCtx *c, uint32_t frag, const RMat *m,
 /* rasterizer (src/internal/primitives/triangles.c:287-558)                  */
 /* ------------------------------------------------------------------------ */
 
+/* What a triangle's fragments are shaded with (triangles.c:356-397). */
+typedef struct {
+    const RCtx *c;
+    int is3D;
+    const RVert *v1, *v2, *v3;
+    const float *viewPos;
+    uint32_t c1, c2, c3;
+    const RTex *tex;
+    int phong;
+    const RMat *fm;
+    int smooth;
+} TriFrag;
+
+/* Source colour of a fragment with normalised weights wn1..wn3 and depth z
+ * (triangles.c:500-521): colour interpolation, texturing, per-fragment
+ * lighting.  texOn 0: the fragment is outside the mask, whose texture
+ * coordinates the reference replaces by zero before sampling
+ * (triangles.c:508-513). */
+static uint32_t tri_frag(const TriFrag *s, float wn1, float wn2, float wn3, float z, int texOn)
+{
+    const RVert *v1 = s->v1, *v2 = s->v2, *v3 = s->v3;
+    uint32_t frag;
+    if (s->smooth) {
+        int32_t u1 = ox_cvt_rne(wn1 * 255.0f), u2 = ox_cvt_rne(wn2 * 255.0f), u3 = ox_cvt_rne(wn3 * 255.0f);
+        int32_t o[4];
+        for (int i = 0; i < 4; i++) {
+            uint32_t t = (uint32_t)u1*(uint32_t)ch(s->c1, i) + (uint32_t)u2*(uint32_t)ch(s->c2, i);
+            t = t + (uint32_t)u3*(uint32_t)ch(s->c3, i);
+            o[i] = (int32_t)((t * 257u) >> 16);
+        }
+        frag = pack4(o);
+    } else {
+        float mx = ox_max(wn1, ox_max(wn2, wn3));
+        frag = ((mx == wn1) ? s->c1 : 0u) | (((mx == wn2) ? s->c2 : 0u) | ((mx == wn3) ? s->c3 : 0u));
+    }
+    if (s->tex) {
+        float tu = 0.0f, tv = 0.0f;
+        if (texOn) {
+            tu = v1->texcoord[0]*wn1 + v2->texcoord[0]*wn2;
+            tu = tu + v3->texcoord[0]*wn3;
+            tv = v1->texcoord[1]*wn1 + v2->texcoord[1]*wn2;
+            tv = tv + v3->texcoord[1]*wn3;
+            if (s->is3D) { tu = tu * z; tv = tv * z; }
+        }
+        uint32_t texel = tex_sample(s->tex, tu, tv);
+        frag = blend_simd(PF_BLEND_MUL, texel, frag);
+    }
+    if (s->phong) {
+        float N[3], P[3];
+        for (int i = 0; i < 3; i++) {
+            float a = v1->normal[i]*wn1 + v2->normal[i]*wn2; N[i] = a + v3->normal[i]*wn3;
+            float b = v1->position[i]*wn1 + v2->position[i]*wn2; P[i] = b + v3->position[i]*wn3;
+        }
+        frag = light_phong(s->c, frag, s->fm, s->viewPos, P, N);
+    }
+    return frag;
+}
+
 static void raster_tri(RCtx *c, PFface face, int is3D, const RVert *v1, const RVert *v2,
                        const RVert *v3, const float *viewPos)
 {
@@ -804,6 +867,57 @@ static void raster_tri(RCtx *c, PFface face, int is3D, const RVert *v1, const RV
     const int smooth = c->shade == PF_SMOOTH;
     const long area_bb = (long)(yMax - yMin) * (long)(xMax - xMin);
     uint64_t frags = 0;
+    const TriFrag sh = { c, is3D, v1, v2, v3, viewPos, c1, c2, c3, tex, phong, fm, smooth };
+
+    if (fb_bgra8(fbt)) {
+        /* BGRA / unsigned byte: the SIMD getter and setter shuffle every
+         * 4-pixel half of the 8-pixel vector with the bytes of its first
+         * pixel (pixel.h:2070-2078, 2916-2921; simd.h:564-583), so each
+         * pixel the mask lets through takes the value computed for that
+         * first pixel -- its own colour (texture coordinates zeroed when
+         * the first pixel is outside the mask), blended with its own
+         * destination.  The halves start at xMin + 4k (x steps by 8 from
+         * xMin, triangles.c:409); rows are independent. */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4) reduction(+:frags) if (area_bb >= 32*32)
+#endif
+        for (long yy = (long)yMin; yy <= (long)yMax; yy++) {
+            uint32_t y = (uint32_t)yy;
+            if (y >= H) continue;   /* memory guard: undefined in the reference */
+            for (uint32_t xf = xMin; xf < xMax; xf += 4) {
+                int m[4] = { 0, 0, 0, 0 }, any = 0;
+                float zl[4] = { 0, 0, 0, 0 };
+                float wf[3] = { 0, 0, 0 }, zf = 0.0f;
+                for (uint32_t j = 0; j < 4; j++) {
+                    const uint32_t x = xf + j;
+                    int32_t w1 = (int32_t)(w1Row + (y - yMin)*(uint32_t)w1Y + (x - xMin)*(uint32_t)w1X);
+                    int32_t w2 = (int32_t)(w2Row + (y - yMin)*(uint32_t)w2Y + (x - xMin)*(uint32_t)w2X);
+                    int32_t w3 = (int32_t)(w3Row + (y - yMin)*(uint32_t)w3Y + (x - xMin)*(uint32_t)w3X);
+                    float wn1 = (float)w1 * wInvSum, wn2 = (float)w2 * wInvSum, wn3 = (float)w3 * wInvSum;
+                    float zs = z1*wn1 + z2*wn2;
+                    zs = zs + z3*wn3;
+                    float z = 1.0f / zs;
+                    if (j == 0) { wf[0] = wn1; wf[1] = wn2; wf[2] = wn3; zf = z; }
+                    if (x >= xMax || (w1 | w2 | w3) <= 0 || x >= W) continue;
+                    frags++;
+                    if (depthTest && !depth_simd(c->depthFunc, z, zb[(size_t)y * W + x])) continue;
+                    m[j] = 1; zl[j] = z; any = 1;
+                }
+                if (!any) continue;
+                uint32_t frag = tri_frag(&sh, wf[0], wf[1], wf[2], zf, m[0]);
+                if (blending) frag = blend_simd(c->blend, frag, fb_get_simd(fbt, (size_t)y * W + xf));
+                for (uint32_t j = 0; j < 4; j++) {
+                    if (!m[j]) continue;
+                    const size_t p = (size_t)y * W + xf + j;
+                    fb_set_simd(fbt, p, frag);
+                    if (c->depthMask) zb[p] = zl[j];
+                }
+            }
+        }
+        c->stats.fragments += frags;
+        c->stats.rasterized += 1;
+        return;
+    }
 
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 4) reduction(+:frags) if (area_bb >= 32*32)
@@ -823,37 +937,7 @@ static void raster_tri(RCtx *c, PFface face, int is3D, const RVert *v1, const RV
             float z = 1.0f / zs;
             size_t p = (size_t)y * W + x;
             if (depthTest && !depth_simd(c->depthFunc, z, zb[p])) continue;
-            uint32_t frag;
-            if (smooth) {
-                int32_t u1 = ox_cvt_rne(wn1 * 255.0f), u2 = ox_cvt_rne(wn2 * 255.0f), u3 = ox_cvt_rne(wn3 * 255.0f);
-                int32_t o[4];
-                for (int i = 0; i < 4; i++) {
-                    uint32_t s = (uint32_t)u1*(uint32_t)ch(c1, i) + (uint32_t)u2*(uint32_t)ch(c2, i);
-                    s = s + (uint32_t)u3*(uint32_t)ch(c3, i);
-                    o[i] = (int32_t)((s * 257u) >> 16);
-                }
-                frag = pack4(o);
-            } else {
-                float mx = ox_max(wn1, ox_max(wn2, wn3));
-                frag = ((mx == wn1) ? c1 : 0u) | (((mx == wn2) ? c2 : 0u) | ((mx == wn3) ? c3 : 0u));
-            }
-            if (tex) {
-                float tu = v1->texcoord[0]*wn1 + v2->texcoord[0]*wn2;
-                tu = tu + v3->texcoord[0]*wn3;
-                float tv = v1->texcoord[1]*wn1 + v2->texcoord[1]*wn2;
-                tv = tv + v3->texcoord[1]*wn3;
-                if (is3D) { tu = tu * z; tv = tv * z; }
-                uint32_t texel = tex_sample(tex, tu, tv);
-                frag = blend_simd(PF_BLEND_MUL, texel, frag);
-            }
-            if (phong) {
-                float N[3], P[3];
-                for (int i = 0; i < 3; i++) {
-                    float a = v1->normal[i]*wn1 + v2->normal[i]*wn2; N[i] = a + v3->normal[i]*wn3;
-                    float b = v1->position[i]*wn1 + v2->position[i]*wn2; P[i] = b + v3->position[i]*wn3;
-                }
-                frag = light_phong(c, frag, fm, viewPos, P, N);
-            }
+            uint32_t frag = tri_frag(&sh, wn1, wn2, wn3, z, 1);
             if (blending) frag = blend_simd(c->blend, frag, fb_get_simd(fbt, p));
             fb_set_simd(fbt, p, frag);
             if (c->depthMask) zb[p] = z;

@@ -289,6 +289,7 @@ struct Renderer {
     bool devInit = false, devOk = false;
     cudaStream_t stream = nullptr;
     DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters;
+    DevBuf subMask;                         // per item, its kept sub-triangles (launches with BGRA8 targets)
     uint32_t cap = 256, poolCap = 4096;
     int rasterCtasPerSM = 0;                // 0: as many raster CTAs per SM as fit
     int rasterWarps = 4;                    // warps per raster CTA
@@ -511,12 +512,14 @@ uint32_t texel_rgba8(PFpixelformat f, PFdatatype t, const TexelSrc &s, int64_t o
 // places on, or the next texel, src/internal/pixel.h:2253-2420),
 // single-channel and luminance half / float (their SIMD setters rewrite,
 // requantised, the pixels of the vector that the mask leaves out,
-// pixel.h:905-970, 1219-1490) and BGRA unsigned byte (lane-dependent
-// shuffle, pixel.h:2070-2078, 2916-2921).
+// pixel.h:905-970, 1219-1490).  BGRA unsigned byte, whose SIMD setter
+// writes a half vector with its first pixel's value, is rasterized row by
+// row (k_rows).
 int fb_code(PFpixelformat f, PFdatatype t)
 {
     switch (t) {
-    case PF_UNSIGNED_BYTE: return f == PF_RGBA ? PFF_RGBA8 : f == PF_RGB ? PFF_RGB8 : f == PF_BGR ? PFF_BGR8 : -1;
+    case PF_UNSIGNED_BYTE:
+        return f == PF_RGBA ? PFF_RGBA8 : f == PF_RGB ? PFF_RGB8 : f == PF_BGR ? PFF_BGR8 : f == PF_BGRA ? PFF_BGRA8 : -1;
     case PF_UNSIGNED_SHORT_5_6_5: return f == PF_RGB ? PFF_RGB565 : f == PF_BGR ? PFF_BGR565 : -1;
     case PF_UNSIGNED_SHORT_5_5_5_1: return f == PF_RGBA ? PFF_RGBA5551 : f == PF_BGRA ? PFF_BGRA5551 : -1;
     case PF_UNSIGNED_SHORT_4_4_4_4: return f == PF_RGBA ? PFF_RGBA4444 : f == PF_BGRA ? PFF_BGRA4444 : -1;
@@ -1476,6 +1479,7 @@ void release_renderer(Renderer *r)
     if (r->devOk) {
         r->arena.release(); r->vout.release(); r->prims.release(); r->primsPh.release(); r->pool.release();
         r->poolPh.release(); r->binCount.release(); r->bins.release(); r->counters.release();
+        r->subMask.release();
         if (r->hostCounters) cudaFreeHost(r->hostCounters);
         if (r->evStart) { cudaEventDestroy(r->evStart); cudaEventDestroy(r->evEnd); }
         for (auto &pr : r->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -1700,7 +1704,7 @@ bool flush(Renderer *r)
     }
     // per batch: vertex / item bases, targets, tile numbering
     uint32_t maxVerts = 0, maxItems = 0, maxTiles = 0;
-    bool anyPhong = false;
+    bool anyPhong = false, anyRows = false;
     std::vector<PFBatchLaunch> launches(ops.size());
     size_t tgCursor = 0;
     for (size_t oi = 0; oi < ops.size(); oi++) {
@@ -1742,6 +1746,7 @@ bool flush(Renderer *r)
             T.tilesX = (T.W + PF_TILE - 1) / PF_TILE; T.tilesY = (T.H + PF_TILE - 1) / PF_TILE;
             T.tileBase = tiles;
             tiles += T.tilesX * T.tilesY;
+            if (m->fmt == PFF_BGRA8) { L.rowBands += T.tilesY; anyRows = true; }   // band by band (k_rows)
             if (o.clearCmd[k] >= 0) {
                 const Cmd &cl = cmds[o.clearCmd[k]];
                 T.clearMode = (cl.kind == CMD_FILL) ? 2 : 1; T.clearDepth = cl.depth;
@@ -1872,7 +1877,8 @@ bool flush(Renderer *r)
             !r->pool.ensure((size_t)r->poolCap * sizeof(PFPrim)) ||
             !r->poolPh.ensure(anyPhong ? (size_t)r->poolCap * sizeof(PFPrimPhong) : 128) ||
             !r->binCount.ensure((size_t)(((size_t)maxTiles + 31) & ~(size_t)31) * 4 * (2 + PF_HEAVY_LEVELS)) ||   // bin counters, tile lists
-            !r->bins.ensure((size_t)maxTiles * r->cap * 4 + 64)) {
+            !r->bins.ensure((size_t)maxTiles * r->cap * 4 + 64) ||
+            !r->subMask.ensure(anyRows ? (size_t)maxItems * sizeof(uint16_t) + 64 : 64)) {
             r->devStatus |= PF_DEVICE_ALLOC_FAIL;
             return fail("cudaMalloc(scratch)", cudaErrorMemoryAllocation);
         }
@@ -1912,9 +1918,10 @@ bool flush(Renderer *r)
                 L.rasterCtasPerSM = r->rasterCtasPerSM;
                 L.rasterWarps = r->rasterWarps;
                 L.anyPhong = anyPhong ? 1 : 0;
+                L.subMask = L.rowBands ? (uint16_t *)r->subMask.p : nullptr;
                 L.cnt = dcnt;
                 rop.L = L;
-                r->stats.kernel_launches += 4;
+                r->stats.kernel_launches += L.rowBands ? 5 : 4;
                 e = pfd_launch_vertex(L, st);
                 if (e == cudaSuccess) e = pfd_launch_items(L, st);
                 if (e == cudaSuccess) e = pfd_launch_binsort(L, st);

@@ -723,12 +723,16 @@ struct ItemOut {
     PFPrim *pool;
     PFPrimPhong *poolPh;
     uint32_t poolCap;
+    uint16_t *subMask;          // launches with a row-rasterized target: per item, bit s set when its
+                                // sub-triangle s has a record (null otherwise)
 };
+static_assert(PF_MAX_SUBTRIS <= 16, "an item's sub-triangles are the bits of a 16-bit mask");
 
 __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const PFVertexOut *const *V, int face,
                                        uint32_t g, const ItemOut &O, const BinArgs &B, const TileSpace &T)
 {
     CVert poly[PF_CLIP_MAXV], tmp[PF_CLIP_MAXV];
+    if (O.subMask) O.subMask[g] = 0;
     for (int m = 0; m < 3; m++) {
         const PFVertexOut &o = *V[m];
         for (int i = 0; i < 4; i++) poly[m].h[i] = o.h[i];
@@ -767,9 +771,11 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
     }
     PFPrim first;
     bool firstSet = false;
+    uint32_t kept = 0;
     for (int i = 0; i < nsub; i++) {
         PFPrim P;
         if (!setup_prim(S, face, true, s[0], s[i + 1], s[i + 2], stateIdx, P)) continue;
+        kept |= 1u << i;
         atomicAdd(&B.cnt->batchRasterized, 1ull);
         if (i == 0) { first = P; firstSet = true; }
         else {
@@ -783,6 +789,7 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
     if (!firstSet) { first.flags = 0; first.xMin = 1; first.xMax = 0; }
     first.poolBase = (int32_t)base;
     O.prims[g] = first;
+    if (O.subMask) O.subMask[g] = (uint16_t)kept;
     if (firstSet && (S.flags & PFS_PHONG)) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
 }
 
@@ -809,6 +816,7 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
         P.rstate = (raster_state(S) & ~(uint32_t)PFP_OPS) | (P.flags & PFP_OPS);
         P.zReject = __int_as_float(0x7fffffff);
         O.prims[g] = P;
+        if (O.subMask) O.subMask[g] = 1;
         return true;
     }
     uint32_t vi[3]; int face;
@@ -847,7 +855,9 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
         if (S.flags & PFS_PHONG)
             for (int i = 0; i < 3; i++) { s[m].n[i] = o.n[i]; s[m].p[i] = o.p[i]; }
     }
-    if (!setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P)) return false;
+    const bool kept = setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P);
+    if (O.subMask) O.subMask[g] = kept ? 1 : 0;
+    if (!kept) return false;
     O.prims[g] = P;
     if (S.flags & PFS_PHONG) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
     return true;
@@ -1030,15 +1040,22 @@ __device__ __forceinline__ float tile_depth(const QEdge &E, const PFPrim &P, uin
 
 // Source colour of one fragment (triangles.c:500-521): colour interpolation,
 // texturing, per-fragment lighting.  Independent of the destination pixel.
+// texOn false: a pixel outside the mask, whose texture coordinates the
+// reference replaces by zero before sampling (triangles.c:508-513);
+// anyWeights: the pixel may lie outside the triangle (weights outside
+// [0, 1]), so the weight conversions follow CVTPS2DQ out of range too.
 __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrimPhong *Q, const PFDrawState *states,
-                                                   float wn1, float wn2, float wn3, float z)
+                                                   float wn1, float wn2, float wn3, float z,
+                                                   bool texOn = true, bool anyWeights = false)
 {
     const uint32_t fl = P.rstate;
     uint32_t frag;
     if (fl & PFS_SMOOTH) {
         // covered pixels have weights in [0, 1]: the conversions are in range
-        const uint32_t u1 = (uint32_t)__float2int_rn(wn1 * 255.0f), u2 = (uint32_t)__float2int_rn(wn2 * 255.0f);
-        const uint32_t u3 = (uint32_t)__float2int_rn(wn3 * 255.0f);
+        const float s1 = wn1 * 255.0f, s2 = wn2 * 255.0f, s3 = wn3 * 255.0f;
+        const uint32_t u1 = anyWeights ? pff_cvt_rne(s1) : (uint32_t)__float2int_rn(s1);
+        const uint32_t u2 = anyWeights ? pff_cvt_rne(s2) : (uint32_t)__float2int_rn(s2);
+        const uint32_t u3 = anyWeights ? pff_cvt_rne(s3) : (uint32_t)__float2int_rn(s3);
         int32_t o[4];
         for (int i = 0; i < 4; i++) {
             uint32_t s = u1 * chn(P.c1, i) + u2 * chn(P.c2, i);
@@ -1051,11 +1068,14 @@ __device__ __forceinline__ uint32_t shade_fragment(const PFPrim &P, const PFPrim
         frag = ((mx == wn1) ? P.c1 : 0u) | (((mx == wn2) ? P.c2 : 0u) | ((mx == wn3) ? P.c3 : 0u));
     }
     if (fl & PFS_TEXTURE) {
-        float tu = P.u1 * wn1 + P.u2 * wn2;
-        tu = tu + P.u3 * wn3;
-        float tv = P.v1 * wn1 + P.v2 * wn2;
-        tv = tv + P.v3 * wn3;
-        if (P.flags & 2) { tu = tu * z; tv = tv * z; }
+        float tu = 0.0f, tv = 0.0f;
+        if (texOn) {
+            tu = P.u1 * wn1 + P.u2 * wn2;
+            tu = tu + P.u3 * wn3;
+            tv = P.v1 * wn1 + P.v2 * wn2;
+            tv = tv + P.v3 * wn3;
+            if (P.flags & 2) { tu = tu * z; tv = tv * z; }
+        }
         frag = blend_simd(4, tex_sample(tex_desc(P, states), tu, tv), frag);
     }
     if (fl & PFS_PHONG) {
@@ -1416,7 +1436,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
             int clo = 0, chi = a.nTargets - 1;
             while (clo < chi) { int mid = (clo + chi + 1) >> 1; if (a.targets[mid].tileBase <= t) clo = mid; else chi = mid - 1; }
             const PFTarget &C = a.targets[clo];
-            if (C.clearMode != 0) {
+            if (C.clearMode != 0 && !(GEN && C.fmt == PFF_BGRA8)) {     // (k_rows clears those)
                 const uint32_t tile = t - C.tileBase;
                 const uint32_t cx = (tile % C.tilesX) * PF_TILE, cy = (tile / C.tilesX) * PF_TILE;
                 const uint32_t xe = min(cx + PF_TILE, C.W);
@@ -1452,6 +1472,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
     int tlo = 0, thi = a.nTargets - 1;
     while (tlo < thi) { int mid = (tlo + thi + 1) >> 1; if (a.targets[mid].tileBase <= gtile) tlo = mid; else thi = mid - 1; }
     const PFTarget &T = a.targets[tlo];
+    if (GEN && T.fmt == PFF_BGRA8) continue;                 // rasterized by k_rows
     const uint32_t tile = gtile - T.tileBase;
     const uint32_t n = min(gtCount, a.cap);
     if (n == 0 && T.clearMode == 0) continue;
@@ -1679,6 +1700,182 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// k_rows: targets of BGRA / unsigned-byte format, band by band in
+// submission order.
+//
+// The reference writes such a framebuffer through a SIMD getter and setter
+// that shuffle each 4-pixel half of the 8-pixel vector with the bytes of
+// the half's first pixel (pixel.h:2070-2078, 2916-2921; simd.h:564-583):
+// every pixel of a half that a triangle's mask lets through takes the value
+// computed at the half's first pixel -- that pixel's own colour (texture
+// coordinates zero when it is outside the mask, triangles.c:508-513)
+// blended with that pixel's destination.  The halves start at xMin + 4k of
+// the triangle's box (x steps by 8 from xMin, triangles.c:409), so a half's
+// first pixel may lie in the tile to the left, whose colour when the
+// triangle is drawn depends on everything drawn there before it: the tiles
+// of a row are not independent.  Rows are.  A warp owns one 8-row band of
+// such a target for the whole launch and walks the launch's items in
+// submission order (their kept sub-triangles, from the masks k_items
+// wrote), drawing each record whose box meets the band: the band's
+// (row, half) pairs of the record are spread over the lanes, each lane
+// drawing its half alone, and the warp moves to the next record when all
+// are done.  Points, lines and rectangles use the scalar getter and setter
+// (a plain R / B swap, pixel.h:356-363, 703-707), pixel by pixel.
+// ---------------------------------------------------------------------------
+#define ROW_WARPS 4
+
+// One record over the rows [y0, y1) of a BGRA / unsigned-byte target, the
+// part of lane `lane`; returns the covered pixels it counted.
+__device__ __noinline__ uint32_t row_record(const PFPrim &P, const PFPrimPhong *ph, const PFDrawState *states,
+                                            uint32_t *color, float *depth, uint32_t W, uint32_t y0, uint32_t y1,
+                                            uint32_t lane)
+{
+    // rows and columns as tile_edge clips a box: y in [yMin, yMax], x in
+    // [xMin, xMax), inside the framebuffer (unsigned)
+    const uint32_t xMin = (uint32_t)P.xMin, xMax = (uint32_t)P.xMax, yMin = (uint32_t)P.yMin, yMax = (uint32_t)P.yMax;
+    if (xMin >= xMax || yMin > yMax || yMax == 0xffffffffu) return 0;
+    const uint32_t ra = max(yMin, y0), rb = min(yMax + 1u, y1), xEnd = min(xMax, W);
+    if (ra >= rb || xMin >= xEnd) return 0;
+    const uint32_t nH = (xEnd - xMin + 3u) / 4u, tasks = (rb - ra) * nH;
+    const uint32_t kind = P.flags & PFP_KIND, rs = P.rstate;
+    const int func = (int)((rs >> 16) & 255u), mode = (int)(rs >> 24);
+    // edge functions at pixel (x, y): (x - rx) sx + (y - ry) sy, 32-bit
+    // wrapping (triangles.c:336-349, 398-420)
+    int32_t sx[3] = { P.y3 - P.y2, P.y1 - P.y3, P.y2 - P.y1 };
+    int32_t sy[3] = { P.x2 - P.x3, P.x3 - P.x1, P.x1 - P.x2 };
+    const int32_t rx[3] = { P.x2, P.x3, P.x1 }, ry[3] = { P.y2, P.y3, P.y1 };
+    if (P.flags & 1u)
+        for (int e = 0; e < 3; e++) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
+    uint32_t cov = 0;
+    for (uint32_t t = lane; t < tasks; t += 32) {
+        const uint32_t y = ra + t / nH, xf = xMin + 4u * (t % nH);
+        const size_t row = (size_t)y * W;
+        if (kind == 0) {
+            bool m[4] = { false, false, false, false }, any = false;
+            float zl[4] = { 0.0f, 0.0f, 0.0f, 0.0f }, wf[3] = { 0.0f, 0.0f, 0.0f }, zf = 0.0f;
+            for (uint32_t j = 0; j < 4; j++) {
+                const uint32_t x = xf + j;
+                uint32_t w[3];
+                for (int e = 0; e < 3; e++)
+                    w[e] = (x - (uint32_t)rx[e]) * (uint32_t)sx[e] + (y - (uint32_t)ry[e]) * (uint32_t)sy[e];
+                const float wn1 = (float)(int32_t)w[0] * P.wInvSum, wn2 = (float)(int32_t)w[1] * P.wInvSum;
+                const float wn3 = (float)(int32_t)w[2] * P.wInvSum;
+                float zs = P.z1 * wn1 + P.z2 * wn2;
+                zs = zs + P.z3 * wn3;
+                const float z = __frcp_rn(zs);
+                if (j == 0) { wf[0] = wn1; wf[1] = wn2; wf[2] = wn3; zf = z; }
+                if (x >= xEnd || (int32_t)(w[0] | w[1] | w[2]) <= 0) continue;
+                cov++;
+                if ((rs & PFS_DEPTH_TEST) && !depth_simd(func, z, depth[row + x])) continue;
+                m[j] = true; zl[j] = z; any = true;
+            }
+            if (!any) continue;
+            // the half's value: its first pixel's colour and destination
+            uint32_t frag = shade_fragment(P, ph, states, wf[0], wf[1], wf[2], zf, m[0], true);
+            if (rs & PFS_BLEND) frag = blend_simd(mode, frag, pff_swap_rb(color[row + xf]));
+            const uint32_t out = pff_swap_rb(frag);
+            for (uint32_t j = 0; j < 4; j++) {
+                if (!m[j]) continue;
+                color[row + xf + j] = out;
+                if (rs & PFS_DEPTH_MASK) depth[row + xf + j] = zl[j];
+            }
+        } else {
+            for (uint32_t j = 0; j < 4; j++) {
+                const uint32_t x = xf + j;
+                if (x >= xEnd || !lp_covers(P, (int32_t)x, (int32_t)y)) continue;
+                if (kind != PFP_BLIT) cov++;
+                const float z = lp_depth(P, (int32_t)x, (int32_t)y);
+                if ((rs & PFS_DEPTH_TEST) && !depth_sisd(func, z, depth[row + x])) continue;
+                uint32_t c = lp_color(P, (int32_t)x, (int32_t)y);
+                if (rs & PFS_BLEND) c = blend_sisd(mode, c, pff_swap_rb(color[row + x]));
+                color[row + x] = pff_swap_rb(c);
+                if (rs & PFS_DEPTH_MASK) depth[row + x] = z;
+            }
+        }
+    }
+    return cov;
+}
+
+__global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFSegment *__restrict__ segs, int nSegs,
+                                                         const uint16_t *__restrict__ subMask, uint32_t nBands)
+{
+    __shared__ __align__(16) PFPrim sRec[ROW_WARPS];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // k_raster is done
+    if (a.cnt->abortCommand <= a.command) return;
+    // my band: band b of the BGRA / unsigned-byte targets, in target order
+    uint32_t band = blockIdx.x * ROW_WARPS + warp;
+    if (band >= nBands) return;
+    int t = 0;
+    for (; t < a.nTargets; t++) {
+        if (a.targets[t].fmt != PFF_BGRA8) continue;
+        if (band < a.targets[t].tilesY) break;
+        band -= a.targets[t].tilesY;
+    }
+    if (t >= a.nTargets) return;
+    const PFTarget &T = a.targets[t];
+    const uint32_t W = T.W, y0 = band * PF_TILE, y1 = min(y0 + PF_TILE, T.H);
+    uint32_t *color = static_cast<uint32_t *>(T.color);
+    float *depth = T.depth;
+    if (T.clearMode != 0) {                            // the fused clear of the band
+        for (size_t i = (size_t)y0 * W + lane; i < (size_t)y1 * W; i += 32) {
+            if (T.clearMode == 1 && i < 8) continue;  // pfClear keeps pixels 0..7
+            color[i] = T.clearRaw[0];
+            depth[i] = T.clearDepth;
+        }
+    }
+    __syncwarp();
+    PFPrim &R = sRec[warp];
+    unsigned long long frags = 0;
+    for (int si = 0; si < nSegs; si++) {
+        if (segs[si].target != t) continue;
+        const uint32_t gBegin = segs[si].itemBase, gEnd = gBegin + segs[si].nItems;
+        for (uint32_t gb = gBegin; gb < gEnd; gb += 32) {
+            // lane i: item gb + i -- which of its records meet the band
+            const uint32_t g = gb + lane;
+            uint32_t touch = 0;
+            int32_t poolBase = 0;
+            if (g < gEnd) {
+                const uint32_t m = subMask[g];
+                if (m) {
+                    poolBase = __ldg(&a.prims[g].poolBase);
+                    for (uint32_t mm = m; mm; mm &= mm - 1) {
+                        const uint32_t sub = (uint32_t)(__ffs(mm) - 1);
+                        const PFPrim *src = sub ? &a.pool[(uint32_t)poolBase + sub - 1] : &a.prims[g];
+                        const int4 q1 = __ldg(reinterpret_cast<const int4 *>(src) + 1);     // x3 y3 xMin yMin
+                        const int4 q2 = __ldg(reinterpret_cast<const int4 *>(src) + 2);     // xMax yMax ...
+                        const uint32_t xMin = (uint32_t)q1.z, yMin = (uint32_t)q1.w;
+                        const uint32_t xMax = (uint32_t)q2.x, yMax = (uint32_t)q2.y;
+                        const bool meets = xMin < xMax && xMin < W && yMin <= yMax && yMax != 0xffffffffu &&
+                                           max(yMin, y0) < min(yMax + 1u, y1);
+                        if (meets) touch |= 1u << sub;
+                    }
+                }
+            }
+            // draw them in order: items by lane, then sub-triangles
+            for (uint32_t need = __ballot_sync(0xffffffffu, touch != 0); need; need &= need - 1) {
+                const int src = __ffs(need) - 1;
+                const uint32_t tm = __shfl_sync(0xffffffffu, touch, src);
+                const uint32_t gi = gb + (uint32_t)src;
+                const int32_t pb = __shfl_sync(0xffffffffu, poolBase, src);
+                for (uint32_t mm = tm; mm; mm &= mm - 1) {
+                    const uint32_t sub = (uint32_t)(__ffs(mm) - 1);
+                    const uint32_t pi = sub ? (uint32_t)pb + sub - 1 : gi;
+                    const PFPrim *rec = sub ? &a.pool[pi] : &a.prims[gi];
+                    if (lane < 8) reinterpret_cast<int4 *>(&R)[lane] = __ldg(reinterpret_cast<const int4 *>(rec) + lane);
+                    __syncwarp();
+                    const PFPrimPhong *ph = a.anyPhong ? (sub ? &a.poolPh[pi] : &a.primsPh[gi]) : nullptr;
+                    frags += row_record(R, ph, a.states, color, depth, W, y0, y1, lane);
+                    __syncwarp();                      // the record's pixels are written; R is free
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
+    if (lane == 0 && frags) atomicAdd(&a.cnt->fragments, frags);
+}
+
+// ---------------------------------------------------------------------------
 // framebuffer-wide passes
 // ---------------------------------------------------------------------------
 // pfClear, SIMD build (context.c:680-745): pixels [8, n - n%8) take the clear
@@ -1851,7 +2048,7 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
     BinArgs B{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.targets, L.cnt, L.command };
-    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap };
+    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, L.rowBands ? L.subMask : nullptr };
     return launch_serialized(k_items, grid_for(L.nItems, 128), 128, 0, st, L.segs, L.nSegs, L.states,
                              (const PFVertexOut *)L.vout, L.nItems, O, B);
 }
@@ -1910,7 +2107,10 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
     if (e == cudaSuccess) e = persistent_grid((const void *)kernel, warps * 32, smem, L.rasterCtasPerSM,
                                               (L.totalTiles + (uint32_t)warps - 1) / (uint32_t)warps, grid);
     if (e != cudaSuccess) return e;
-    return launch_serialized(kernel, grid, (unsigned)(warps * 32), smem, st, raster_args(L));
+    e = launch_serialized(kernel, grid, (unsigned)(warps * 32), smem, st, raster_args(L));
+    if (e != cudaSuccess || L.rowBands == 0 || !L.subMask) return e;
+    return launch_serialized(k_rows, (L.rowBands + ROW_WARPS - 1) / ROW_WARPS, ROW_WARPS * 32, 0, st, raster_args(L),
+                             L.segs, L.nSegs, (const uint16_t *)L.subMask, L.rowBands);
 }
 
 cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,

@@ -37,13 +37,14 @@ enum {
     PFF_RGBA5551, PFF_BGRA5551, PFF_RGBA4444, PFF_BGRA4444,
     PFF_LA16F, PFF_RGB16F, PFF_BGR16F, PFF_RGBA16F, PFF_BGRA16F,
     PFF_LA32F, PFF_RGB32F, PFF_BGR32F, PFF_RGBA32F, PFF_BGRA32F,
+    PFF_BGRA8,                    /* BGRA / unsigned byte: see pff_swap_rb */
     PFF_COUNT
 };
 
 PFF_HD int pff_bytes(uint32_t f)
 {
     switch (f) {
-    case PFF_RGBA8: return 4;
+    case PFF_RGBA8: case PFF_BGRA8: return 4;
     case PFF_RGB8: case PFF_BGR8: return 3;
     case PFF_LA16F: return 4;
     case PFF_RGB16F: case PFF_BGR16F: return 6;
@@ -126,6 +127,15 @@ PFF_HD void pff_put_chan(uint32_t f, uint32_t *r, int k, float v)
     else r[k] = pff_fbits(v);
 }
 
+/* BGRA / unsigned byte: a pixel's bytes are B, G, R, A; every getter and
+ * setter swaps R and B of the packed RGBA colour (pixel.h:356-363,
+ * 703-707, 2070-2078, 2916-2921).  The SIMD pair does so with one shuffle
+ * mask for the whole vector, which repeats the bytes of the first pixel of
+ * each 4-pixel half (simd.h:564-583): a triangle writes the first pixel's
+ * value to every pixel of the half its mask lets through.  That rule is the
+ * rasterizer's (k_rows); one pixel's conversion is the swap. */
+PFF_HD uint32_t pff_swap_rb(uint32_t w) { return (w & 0xff00ff00u) | ((w >> 16) & 255u) | ((w & 255u) << 16); }
+
 /* ------------------------------------------------------------------------ */
 /* raw pixels in memory                                                      */
 /* ------------------------------------------------------------------------ */
@@ -181,6 +191,7 @@ PFF_HD uint32_t pff_get_simd(uint32_t f, const uint32_t *r)
     const uint32_t w = r[0];
     switch (f) {
     case PFF_RGBA8: return w;
+    case PFF_BGRA8: return pff_swap_rb(w);
     case PFF_RGB8: return (w & 0xffffffu) | 0xff000000u;
     case PFF_BGR8: return ((w >> 16) & 255u) | (w & 0xff00u) | (w & 255u) << 16 | 0xff000000u;
     case PFF_RGB565: case PFF_BGR565: {
@@ -217,6 +228,7 @@ PFF_HD uint32_t pff_get_sisd(uint32_t f, const uint32_t *r)
     uint32_t cr = 0, cg = 0, cb = 0, ca = 255;
     switch (f) {
     case PFF_RGBA8: return w;
+    case PFF_BGRA8: return pff_swap_rb(w);
     case PFF_RGB8: return (w & 0xffffffu) | 0xff000000u;
     case PFF_BGR8: return ((w >> 16) & 255u) | (w & 0xff00u) | (w & 255u) << 16 | 0xff000000u;
     case PFF_RGB565: case PFF_BGR565: {
@@ -272,6 +284,7 @@ PFF_HD void pff_set_simd(uint32_t f, uint32_t col, uint32_t *r)
     r[0] = r[1] = r[2] = r[3] = 0u;
     switch (f) {
     case PFF_RGBA8: r[0] = col; return;
+    case PFF_BGRA8: r[0] = pff_swap_rb(col); return;
     case PFF_RGB8: case PFF_BGR8: r[0] = c0 | cg << 8 | c2 << 16; return;
     case PFF_RGB565: case PFF_BGR565: r[0] = ((c0 * 31u) >> 8) << 11 | ((cg * 63u) >> 8) << 5 | ((c2 * 31u) >> 8); return;
     case PFF_RGBA5551: case PFF_BGRA5551:
@@ -307,6 +320,7 @@ PFF_HD void pff_set_sisd(uint32_t f, uint32_t col, uint32_t *r)
     r[0] = r[1] = r[2] = r[3] = 0u;
     switch (f) {
     case PFF_RGBA8: r[0] = col; return;
+    case PFF_BGRA8: r[0] = pff_swap_rb(col); return;
     case PFF_RGB8: r[0] = cr | cg << 8 | cb << 16; return;
     case PFF_BGR8: r[0] = cb | cg << 8 | cr << 16; return;
     default: break;

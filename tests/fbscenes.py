@@ -13,21 +13,30 @@ from pixelforge_gb300.scenes import Frame, Target, _ptr
 
 from pixscenes import PIXEL_FORMATS, pixel_source
 
-# (format, type) pairs a framebuffer may have; RGBA / unsigned byte first
+# (format, type) pairs a framebuffer may have, RGBA / unsigned byte first:
+# the formats of the seeded cases (case `seed` draws into format
+# seed % 19) ...
 FB_FORMATS = [(A.PF_RGBA, 0), (A.PF_RGB, 0), (A.PF_BGR, 0),
               (A.PF_RGB, 2), (A.PF_BGR, 2), (A.PF_RGBA, 3), (A.PF_BGRA, 3), (A.PF_RGBA, 4), (A.PF_BGRA, 4)] + \
     [(f, t) for t in (A.PF_HALF_FLOAT, A.PF_FLOAT)
      for f in (A.PF_LUMINANCE_ALPHA, A.PF_RGB, A.PF_BGR, A.PF_RGBA, A.PF_BGRA)]
+# ... and BGRA / unsigned byte, whose SIMD getter and setter shuffle each
+# 4-pixel half vector with the bytes of its first pixel (its cases name it)
+FB_BGRA8 = (A.PF_BGRA, A.PF_UNSIGNED_BYTE)
+FB_ACCEPTED = FB_FORMATS + [FB_BGRA8]
+# the seeded cases of the parity tests: five per format of FB_FORMATS, then
+# twelve BGRA / unsigned byte
+FB_SEEDS = [(s, None) for s in range(5 * len(FB_FORMATS))] + [(s, FB_BGRA8) for s in range(200, 212)]
 # pairs that are valid pixel formats but not framebuffer formats
 FB_REFUSED = [(f, 0) for f in (A.PF_RED, A.PF_GREEN, A.PF_BLUE, A.PF_ALPHA, A.PF_LUMINANCE,
-                               A.PF_LUMINANCE_ALPHA, A.PF_BGRA)] + \
+                               A.PF_LUMINANCE_ALPHA)] + \
     [(f, t) for t in (A.PF_HALF_FLOAT, A.PF_FLOAT)
      for f in (A.PF_RED, A.PF_GREEN, A.PF_BLUE, A.PF_ALPHA, A.PF_LUMINANCE)]
 
 
-def fb_case(seed: int) -> dict:
+def fb_case(seed: int, fmt: tuple | None = None) -> dict:
     r = np.random.default_rng(seed)
-    fmt = FB_FORMATS[seed % len(FB_FORMATS)]
+    fmt = fmt or FB_FORMATS[seed % len(FB_FORMATS)]
     # odd sizes leave a tail of W*H % 8 pixels for pfClear to copy pixel 0 into
     W, H = [(61, 37), (64, 40), (45, 29), (80, 48)][int(r.integers(4))]
     return dict(seed=seed, fmt=fmt, W=W, H=H, target=["main", "fbo"][int(r.integers(2))],
@@ -177,10 +186,10 @@ def refused_formats(lib: A.PixelForgeLib) -> list:
         lib.pfDeleteContext(ctx)
 
 
-def fb_frame(seed: int):
+def fb_frame(seed: int, fmt: tuple | None = None):
     """A golden-vector runner: the case's framebuffer as a Frame."""
     def run(lib):
-        out = run_fb(lib, fb_case(seed), device_hook=False)
+        out = run_fb(lib, fb_case(seed, fmt), device_hook=False)
         return Frame(out["color"], out.get("depth"))
     return run
 
@@ -190,7 +199,7 @@ def fb_frame(seed: int):
 # sides that are no multiple of the 16-pixel tile
 TINY_SIZES = [(1, 1), (2, 3), (7, 1), (1, 9), (17, 5), (33, 2), (5, 31)]
 TINY_FORMATS = [(A.PF_RGBA, 0), (A.PF_RGB, 0), (A.PF_RGBA, A.PF_HALF_FLOAT), (A.PF_BGRA, A.PF_FLOAT),
-                (A.PF_RGB, 2), (A.PF_RGBA, 4)]
+                (A.PF_RGB, 2), (A.PF_RGBA, 4), (A.PF_BGRA, 0)]
 
 
 def tiny_case(k: int) -> dict:

@@ -290,9 +290,11 @@ def cases() -> dict:
         c[f"lp_{s}"] = lp(7000 + s)
     for s in range(16):
         c[f"px_{s}"] = px(9000 + s)
-    from fbscenes import FB_FORMATS, fb_frame
+    from fbscenes import FB_BGRA8, FB_FORMATS, fb_frame
     for s in range(len(FB_FORMATS)):
         c[f"fb_{s}"] = fb_frame(11000 + s)
+    for s in range(4):
+        c[f"fb_bgra8_{s}"] = fb_frame(11100 + s, FB_BGRA8)
     return c
 
 

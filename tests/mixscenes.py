@@ -70,11 +70,13 @@ def _geometry(case: dict, r: np.random.Generator):
     return pos, nrm, uv, col
 
 
-def run_mix(lib: A.PixelForgeLib, case: dict, target: str = "fbo") -> Frame:
+def run_mix(lib: A.PixelForgeLib, case: dict, target: str = "fbo",
+            fmt: tuple = (A.PF_RGBA, A.PF_UNSIGNED_BYTE)) -> Frame:
+    """fmt: the framebuffer's format, RGBA or BGRA unsigned byte."""
     r = np.random.default_rng(case["seed"] + 7919)
     W, H = case["width"], case["height"]
     init = r.integers(0, 256, (H, W, 4)).astype(np.uint8)
-    tg = Target(lib, W, H, target, init=init)
+    tg = Target(lib, W, H, target, init=init, fmt=fmt)
     texh = None
     try:
         pos, nrm, uv, col = _geometry(case, r)

@@ -190,23 +190,23 @@ def test_framebuffer_formats_refused(lib, oracle):
     """Framebuffer formats whose reference results depend on other pixels or
     on the SIMD lane are refused with PF_INVALID_ENUM, by the library and
     the oracle alike; every accepted pair is a valid pixel format."""
-    from fbscenes import FB_FORMATS, FB_REFUSED, refused_formats
+    from fbscenes import FB_ACCEPTED, FB_REFUSED, refused_formats
     for lb in (lib, oracle):
         res = refused_formats(lb)
         assert len(res) == len(FB_REFUSED)
         for pair, null, err in res:
             assert null and err == A.PF_INVALID_ENUM, pair
-    assert len(FB_FORMATS) == 19 and all(A.pixel_bytes(*p) for p in FB_FORMATS)
+    assert len(FB_ACCEPTED) == 20 and all(A.pixel_bytes(*p) for p in FB_ACCEPTED)
 
 
 def test_framebuffer_pixel_functions_every_format(lib, oracle):
     """pfSetFramebufferPixel / pfGetFramebufferPixel and the stored bytes of
     a framebuffer object of every accepted format, library against oracle
     (host-side: the scalar setter and getter of pf_pixfmt.h, no device)."""
-    from fbscenes import FB_FORMATS
+    from fbscenes import FB_ACCEPTED
     rng = np.random.default_rng(77)
     cols = rng.integers(0, 256, (64, 4)).astype(np.uint8)
-    for fmt in FB_FORMATS:
+    for fmt in FB_ACCEPTED:
         res = []
         for lb in (lib, oracle):
             buf = np.zeros((4, 4, 4), np.uint8)

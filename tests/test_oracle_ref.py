@@ -7,6 +7,7 @@ uninitialised vector)."""
 import numpy as np
 import pytest
 
+from fbscenes import FB_BGRA8, FB_SEEDS
 from mixscenes import mix_case, run_mix
 from pixelforge_gb300 import abi as A
 from pixelforge_gb300.scenes import SoupScene
@@ -67,14 +68,28 @@ def test_oracle_equals_reference_read_pixels(oracle, ref_shim, seed):
         assert np.array_equal(a[k][0], b[k][0]), f"format/type {k}: bytes differ"
 
 
-@pytest.mark.parametrize("seed", range(0, 95))
-def test_oracle_equals_reference_framebuffer_formats(oracle, ref_shim, seed):
-    """Framebuffers of every accepted format (5 seeds each): clears and
-    fills, triangles through the SIMD getter / setter, points, lines,
-    rectangles and images through the scalar ones, fog, the per-pixel
-    framebuffer functions and pfReadPixels; raw pixels bit-exact."""
+@pytest.mark.parametrize("seed", range(6000, 6040))
+def test_oracle_equals_reference_mixed_bgra(oracle, ref_shim, seed):
+    """Feature-mix scenes (projections, clipping, culling, flat / smooth,
+    texture wraps, Gouraud and Phong lighting, draw modes, blending) into a
+    BGRA / unsigned-byte framebuffer, whose SIMD setter writes each 4-pixel
+    half vector with the value computed for its first pixel."""
+    case = mix_case(seed)
+    for target in ("fbo", "main"):
+        a = run_mix(oracle, case, target, fmt=FB_BGRA8)
+        b = run_mix(ref_shim, case, target, fmt=FB_BGRA8)
+        same(a, b, f"{case} {target}")
+
+
+@pytest.mark.parametrize("seed,fmt", FB_SEEDS)
+def test_oracle_equals_reference_framebuffer_formats(oracle, ref_shim, seed, fmt):
+    """Framebuffers of every accepted format (5 seeds each, 12 for BGRA /
+    unsigned byte): clears and fills, triangles through the SIMD getter /
+    setter, points, lines, rectangles and images through the scalar ones,
+    fog, the per-pixel framebuffer functions and pfReadPixels; raw pixels
+    bit-exact."""
     from fbscenes import fb_case, run_fb
-    case = fb_case(seed)
+    case = fb_case(seed, fmt)
     a, b = run_fb(oracle, case, device_hook=False), run_fb(ref_shim, case, device_hook=False)
     assert a["err"] == b["err"]
     for k in ("color", "depth", "read", "get"):

@@ -12,6 +12,7 @@ import pytest
 
 from pixelforge_gb300 import abi as A
 from pixelforge_gb300.scenes import PhongScene, SoupScene, SphereScene
+from fbscenes import FB_BGRA8, FB_SEEDS
 from mixscenes import mix_case, run_mix
 
 pytestmark = pytest.mark.gpu
@@ -106,6 +107,87 @@ def test_phong_fog_1080_full_size(gpu, oracle):
 def test_feature_mix(gpu, oracle, seed):
     case = mix_case(seed, bilinear=True)
     assert_parity(run_mix(gpu, case), run_mix(oracle, case), label=f"mix {seed} {case}")
+
+
+@pytest.mark.parametrize("seed", range(6000, 6040))
+def test_feature_mix_bgra(gpu, oracle, seed):
+    """Feature-mix scenes into BGRA / unsigned-byte framebuffers (k_rows:
+    each 4-pixel half vector of a triangle's row takes its first pixel's
+    colour, blended with that pixel's destination), main buffer and
+    framebuffer object; fragment counts equal."""
+    case = mix_case(seed, bilinear=True)
+    for target in ("fbo", "main"):
+        got, ref = run_mix(gpu, case, target, fmt=FB_BGRA8), run_mix(oracle, case, target, fmt=FB_BGRA8)
+        assert gpu.pfGetDeviceStatus() == 0
+        assert_parity(got, ref, label=f"bgra mix {seed} {target} {case}")
+        assert got.stats["fragments"] == ref.stats["fragments"]
+
+
+def test_bgra8_tile_bins_and_splits(gpu, oracle):
+    """BGRA / unsigned byte beside RGBA8 in one flush (two framebuffer
+    objects drawn alternately, the RGBA8 one rasterized by k_raster, the
+    BGRA8 one by k_rows), with more triangles in a tile than a bin holds at
+    first (capacity retries) and clipped triangles: both bit-exact."""
+    from pixelforge_gb300.scenes import _ptr
+    import ctypes as C
+    W, H, n = 200, 120, 6000
+    r = np.random.default_rng(31)
+    pos = r.uniform(-1.3, 1.3, (n * 3, 3)).astype(np.float32) * np.float32([1, 1, 2.0])
+    col = r.integers(0, 256, (n * 3, 4)).astype(np.uint8)
+
+    def run(lib):
+        buf = np.zeros((8, 8, 4), np.uint8)
+        ctx = lib.pfCreateContext(_ptr(buf), 8, 8, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+        lib.pfMakeCurrent(ctx)
+        fbs = [lib.pfGenFramebuffer(W, H, A.PF_RGBA, A.PF_UNSIGNED_BYTE),
+               lib.pfGenFramebuffer(W, H, A.PF_BGRA, A.PF_UNSIGNED_BYTE)]
+        refs = [C.pointer(f) for f in fbs]
+        out = []
+        try:
+            lib.pfMatrixMode(A.PF_PROJECTION)
+            lib.pfLoadIdentity()
+            lib.pfFrustum(-0.1, 0.1, -0.06, 0.06, 0.1, 10.0)
+            lib.pfMatrixMode(A.PF_MODELVIEW)
+            lib.pfLoadIdentity()
+            lib.pfTranslatef(0.0, 0.0, -1.5)
+            lib.pfViewport(0, 0, W, H)                    # (the context's own buffer is 8x8)
+            lib.pfDisable(A.PF_CULL_FACE)
+            lib.pfEnable(A.PF_DEPTH_TEST)
+            lib.pfEnable(A.PF_FRAMEBUFFER)
+            lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_COLOR_ARRAY)
+            lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(pos))
+            lib.pfColorPointer(4, A.PF_UNSIGNED_BYTE, 0, _ptr(col))
+            for k in range(4):
+                lib.pfBindFramebuffer(refs[k % 2])
+                if k < 2:
+                    lib.pfClearColor(10, 20, 30, 255)
+                    lib.pfClearDepth(1e30)
+                    lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+                if k >= 2:
+                    lib.pfEnable(A.PF_BLEND)
+                    lib.pfBlendFunc(A.PF_BLEND_ADD)
+                lib.pfDrawArrays(A.PF_TRIANGLES, 0, n * 3 // (1 + k % 2))
+            if lib.has("pfFinish"):
+                lib.pfFinish()
+            px = lib.raw("pfGetTexturePixels")
+            px.restype = C.c_void_p
+            px.argtypes = [C.c_void_p] * 5
+            for f in fbs:
+                base = px(f.texture, None, None, None, None)
+                out.append(np.ctypeslib.as_array(C.cast(base, C.POINTER(C.c_uint8)), shape=(H, W, 4)).copy())
+                out.append(np.ctypeslib.as_array(f.zbuffer, shape=(H, W)).copy())
+            return out
+        finally:
+            lib.pfDisable(A.PF_FRAMEBUFFER)
+            lib.pfBindFramebuffer(None)
+            for ref in refs:
+                lib.pfDeleteFramebuffer(ref)
+            lib.pfDeleteContext(ctx)
+
+    got, ref = run(gpu), run(oracle)
+    assert gpu.pfGetDeviceStatus() == 0
+    for k, (a, b) in enumerate(zip(got, ref)):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"buffer {k} differs in {int((a != b).sum())} values"
 
 
 def test_clear_leaves_first_pixels(gpu, oracle):
@@ -243,16 +325,17 @@ def test_read_pixels_formats(gpu, oracle, seed):
         assert np.array_equal(a[k][0], b[k][0]), f"format/type {k}: bytes differ"
 
 
-@pytest.mark.parametrize("seed", range(0, 95))
-def test_framebuffer_formats(gpu, oracle, seed):
-    """Framebuffers of every accepted format (5 seeds each, main buffers and
-    framebuffer objects, odd sizes): clears and fills, triangles through the
-    format's SIMD getter / setter in k_raster, points, lines, rectangles and
-    images through the scalar ones, linear fog and the grayscale device
-    hook, the per-pixel framebuffer functions and pfReadPixels.  Raw pixels,
-    depth and every read bit-exact."""
+@pytest.mark.parametrize("seed,fmt", FB_SEEDS)
+def test_framebuffer_formats(gpu, oracle, seed, fmt):
+    """Framebuffers of every accepted format (5 seeds each, 12 for BGRA /
+    unsigned byte; main buffers and framebuffer objects, odd sizes): clears
+    and fills, triangles through the format's SIMD getter / setter (k_raster;
+    k_rows for BGRA / unsigned byte), points, lines, rectangles and images
+    through the scalar ones, linear fog and the grayscale device hook, the
+    per-pixel framebuffer functions and pfReadPixels.  Raw pixels, depth and
+    every read bit-exact."""
     from fbscenes import fb_case, run_fb
-    case = fb_case(seed)
+    case = fb_case(seed, fmt)
     a, b = run_fb(gpu, case), run_fb(oracle, case)
     assert gpu.pfGetDeviceStatus() == 0
     assert a["err"] == b["err"] == 0
@@ -263,7 +346,7 @@ def test_framebuffer_formats(gpu, oracle, seed):
 
 
 @pytest.mark.parametrize("fmt", [(A.PF_RGBA, A.PF_HALF_FLOAT), (A.PF_RGB, A.PF_UNSIGNED_SHORT_5_6_5),
-                                 (A.PF_BGRA, A.PF_FLOAT)])
+                                 (A.PF_BGRA, A.PF_FLOAT), (A.PF_BGRA, A.PF_UNSIGNED_BYTE)])
 def test_framebuffer_formats_sphere1080(gpu, oracle, fmt):
     """The textured, alpha-blended sphere at 1920x1080 (unlit: no host powf)
     into a framebuffer of another format: raw pixels and depth bit-exact
