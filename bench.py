@@ -370,14 +370,16 @@ def run_formats(lib, warmup: int = 2, steps: int = 5) -> dict:
     """The sphere frame into main buffers of other formats: device ms per
     frame, raster ms and end-to-end ms (the write-back moves the format's
     bytes); RGBA / unsigned byte runs the plain kernel, the others the
-    generic-format raster kernel."""
+    generic-format raster kernel, and BGRA / unsigned byte the band-by-band
+    raster (its raster time includes both kernels)."""
     import torch
     from pixelforge_gb300 import abi as A
     from pixelforge_gb300.scenes import SphereScene, Target
     l2_flush = torch.empty(512 << 20, dtype=torch.uint8, device=torch.device("cuda:0"))
     out = {}
     for name, fmt in (("RGBA8", (A.PF_RGBA, A.PF_UNSIGNED_BYTE)), ("RGB565", (A.PF_RGB, A.PF_UNSIGNED_SHORT_5_6_5)),
-                      ("RGBA16F", (A.PF_RGBA, A.PF_HALF_FLOAT)), ("RGBA32F", (A.PF_RGBA, A.PF_FLOAT))):
+                      ("RGBA16F", (A.PF_RGBA, A.PF_HALF_FLOAT)), ("RGBA32F", (A.PF_RGBA, A.PF_FLOAT)),
+                      ("BGRA8", (A.PF_BGRA, A.PF_UNSIGNED_BYTE))):
         sc = SphereScene()
         tg = Target(lib, sc.width, sc.height, "main", fmt=fmt)
         sc.setup(lib)

@@ -305,12 +305,14 @@ PF_API void pfPostProcess(PFpostprocessfunc postProcessFunction);              /
 
 /* ---- framebuffers (pixelforge.h:1887-2003) -----------------------------------
  * A framebuffer -- a context's main buffer or a pfGenFramebuffer object -- may
- * be RGBA, RGB or BGR unsigned byte, RGB / BGR 5-6-5, RGBA / BGRA 5-5-5-1 or
- * 4-4-4-4, or luminance-alpha, RGB, BGR, RGBA or BGRA half or float.  The
- * other pairs (single-channel and luminance formats, luminance-alpha and
- * BGRA unsigned byte) set PF_INVALID_ENUM in pfCreateContext,
- * pfSetMainBuffer and pfGenFramebuffer: in the reference a pixel of those
- * depends on its neighbours or its SIMD lane. */
+ * be RGBA, RGB, BGR or BGRA unsigned byte, RGB / BGR 5-6-5, RGBA / BGRA
+ * 5-5-5-1 or 4-4-4-4, or luminance-alpha, RGB, BGR, RGBA or BGRA half or
+ * float.  In BGRA unsigned byte a triangle writes each 4-pixel half of the
+ * reference's 8-pixel vector with the value of the half's first pixel, as
+ * the reference's SIMD setter does.  The other pairs (single-channel and
+ * luminance formats, luminance-alpha unsigned byte) set PF_INVALID_ENUM in
+ * pfCreateContext, pfSetMainBuffer and pfGenFramebuffer: in the reference
+ * a pixel of those depends on its neighbours' values. */
 PF_API PFframebuffer pfGenFramebuffer(PFsizei width, PFsizei height,
                                       PFpixelformat format, PFdatatype type);  /* pixelforge.h:1887 */
 PF_API void      pfDeleteFramebuffer(PFframebuffer* framebuffer);              /* pixelforge.h:1899 */

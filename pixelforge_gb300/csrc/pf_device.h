@@ -44,9 +44,9 @@ struct PFBatchLaunch {
     int rasterWarps;          /* warps (tiles in flight) per raster CTA: 2, 4 (default) or 8 */
     int anyPhong;             /* some state of the launch lights per fragment */
     int generic;              /* some target is not RGBA / unsigned byte */
-    uint32_t rowBands;        /* 8-row bands of the BGRA / unsigned-byte targets (k_rows, after
-                                 k_raster), 0 when there are none */
-    uint16_t *subMask;        /* rowBands > 0: nItems masks of the items' kept sub-triangles */
+    uint32_t rowCount;        /* rows of the BGRA / unsigned-byte targets (k_rows, after k_raster),
+                                 0 when there are none */
+    uint64_t *rowInfo;        /* rowCount > 0: nItems summaries of the items' records (row_info) */
     PFDevCounters *cnt;
     uint32_t command;
 };
@@ -59,7 +59,7 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st);
 cudaError_t pfd_launch_binsort(const PFBatchLaunch &L, cudaStream_t st);
 /* Persistent tile raster over every tile of every target; each target's
  * clearMode says how its tiles start (see PFTarget).  BGRA / unsigned-byte
- * targets are rasterized band by band by a second kernel (rowBands). */
+ * targets are rasterized row by row by a second kernel (rowCount). */
 cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st);
 /* Number of SMs of the current device (cached). */
 int pfd_sm_count(void);

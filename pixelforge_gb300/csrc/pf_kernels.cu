@@ -723,16 +723,36 @@ struct ItemOut {
     PFPrim *pool;
     PFPrimPhong *poolPh;
     uint32_t poolCap;
-    uint16_t *subMask;          // launches with a row-rasterized target: per item, bit s set when its
-                                // sub-triangle s has a record (null otherwise)
+    uint64_t *rowInfo;          // launches with a row-rasterized target: per item, row_info (null otherwise)
 };
 static_assert(PF_MAX_SUBTRIS <= 16, "an item's sub-triangles are the bits of a 16-bit mask");
+
+// What k_rows needs to know of an item without reading its records: bit s
+// (s < 16) set when sub-triangle s has a record that draws something, and
+// the first and last framebuffer row of those records (24 bits each, at
+// bits 16 and 40; rows are unsigned, as tile_edge reads a box).
+__device__ __forceinline__ void row_info_add(uint64_t &info, uint32_t sub, const PFPrim &P)
+{
+    const uint32_t xMin = (uint32_t)P.xMin, xMax = (uint32_t)P.xMax, lo = (uint32_t)P.yMin, hi = (uint32_t)P.yMax;
+    if (xMin >= xMax || lo > hi || hi == 0xffffffffu) return;           // an empty box: nothing drawn
+    uint64_t l = min(lo, 0xffffffu), h = min(hi, 0xffffffu);
+    if (info & 0xffffu) { l = min(l, (info >> 16) & 0xffffffu); h = max(h, info >> 40); }
+    info = (info & 0xffffu) | (1ull << sub) | (l << 16) | (h << 40);
+}
+// rowInfo[g] of an item whose only record is P (kept) or that has none;
+// out of line, so that the set-up path keeps its registers
+__device__ __noinline__ void store_row_info(uint64_t *rowInfo, uint32_t g, const PFPrim &P, bool kept)
+{
+    uint64_t rows = 0;
+    if (kept) row_info_add(rows, 0, P);
+    rowInfo[g] = rows;
+}
 
 __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const PFVertexOut *const *V, int face,
                                        uint32_t g, const ItemOut &O, const BinArgs &B, const TileSpace &T)
 {
     CVert poly[PF_CLIP_MAXV], tmp[PF_CLIP_MAXV];
-    if (O.subMask) O.subMask[g] = 0;
+    if (O.rowInfo) O.rowInfo[g] = 0;
     for (int m = 0; m < 3; m++) {
         const PFVertexOut &o = *V[m];
         for (int i = 0; i < 4; i++) poly[m].h[i] = o.h[i];
@@ -771,11 +791,11 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
     }
     PFPrim first;
     bool firstSet = false;
-    uint32_t kept = 0;
+    uint64_t rows = 0;
     for (int i = 0; i < nsub; i++) {
         PFPrim P;
         if (!setup_prim(S, face, true, s[0], s[i + 1], s[i + 2], stateIdx, P)) continue;
-        kept |= 1u << i;
+        row_info_add(rows, (uint32_t)i, P);
         atomicAdd(&B.cnt->batchRasterized, 1ull);
         if (i == 0) { first = P; firstSet = true; }
         else {
@@ -789,7 +809,7 @@ __device__ __noinline__ void clip_item(const PFDrawState &S, int stateIdx, const
     if (!firstSet) { first.flags = 0; first.xMin = 1; first.xMax = 0; }
     first.poolBase = (int32_t)base;
     O.prims[g] = first;
-    if (O.subMask) O.subMask[g] = (uint16_t)kept;
+    if (O.rowInfo) O.rowInfo[g] = rows;
     if (firstSet && (S.flags & PFS_PHONG)) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
 }
 
@@ -816,7 +836,7 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
         P.rstate = (raster_state(S) & ~(uint32_t)PFP_OPS) | (P.flags & PFP_OPS);
         P.zReject = __int_as_float(0x7fffffff);
         O.prims[g] = P;
-        if (O.subMask) O.subMask[g] = 1;
+        if (O.rowInfo) store_row_info(O.rowInfo, g, P, true);
         return true;
     }
     uint32_t vi[3]; int face;
@@ -856,7 +876,7 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
             for (int i = 0; i < 3; i++) { s[m].n[i] = o.n[i]; s[m].p[i] = o.p[i]; }
     }
     const bool kept = setup_prim(S, face, !is2D, s[0], s[1], s[2], sg.state, P);
-    if (O.subMask) O.subMask[g] = kept ? 1 : 0;
+    if (O.rowInfo) store_row_info(O.rowInfo, g, P, kept);
     if (!kept) return false;
     O.prims[g] = P;
     if (S.flags & PFS_PHONG) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
@@ -1713,14 +1733,15 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
 // the triangle's box (x steps by 8 from xMin, triangles.c:409), so a half's
 // first pixel may lie in the tile to the left, whose colour when the
 // triangle is drawn depends on everything drawn there before it: the tiles
-// of a row are not independent.  Rows are.  A warp owns one 8-row band of
-// such a target for the whole launch and walks the launch's items in
-// submission order (their kept sub-triangles, from the masks k_items
-// wrote), drawing each record whose box meets the band: the band's
-// (row, half) pairs of the record are spread over the lanes, each lane
-// drawing its half alone, and the warp moves to the next record when all
-// are done.  Points, lines and rectangles use the scalar getter and setter
-// (a plain R / B swap, pixel.h:356-363, 703-707), pixel by pixel.
+// of a row are not independent.  Rows are.  A warp owns one row of such a
+// target for the whole launch and walks the launch's items in submission
+// order -- four 8-byte summaries a lane at a time (row_info: the records an
+// item has and the rows they span), so that items off the row cost a
+// coalesced load -- drawing each record whose box meets the row: its
+// 4-pixel halves are spread over the lanes, each lane drawing its half
+// alone, and the warp moves to the next record when all are done.  Points,
+// lines and rectangles use the scalar getter and setter (a plain R / B
+// swap, pixel.h:356-363, 703-707), pixel by pixel.
 // ---------------------------------------------------------------------------
 #define ROW_WARPS 4
 
@@ -1797,28 +1818,28 @@ __device__ __noinline__ uint32_t row_record(const PFPrim &P, const PFPrimPhong *
 }
 
 __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFSegment *__restrict__ segs, int nSegs,
-                                                         const uint16_t *__restrict__ subMask, uint32_t nBands)
+                                                         const uint64_t *__restrict__ rowInfo, uint32_t nRows)
 {
     __shared__ __align__(16) PFPrim sRec[ROW_WARPS];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_raster is done
     if (a.cnt->abortCommand <= a.command) return;
-    // my band: band b of the BGRA / unsigned-byte targets, in target order
-    uint32_t band = blockIdx.x * ROW_WARPS + warp;
-    if (band >= nBands) return;
+    // my row: row y of the BGRA / unsigned-byte targets, in target order
+    uint32_t y = blockIdx.x * ROW_WARPS + warp;
+    if (y >= nRows) return;
     int t = 0;
     for (; t < a.nTargets; t++) {
         if (a.targets[t].fmt != PFF_BGRA8) continue;
-        if (band < a.targets[t].tilesY) break;
-        band -= a.targets[t].tilesY;
+        if (y < a.targets[t].H) break;
+        y -= a.targets[t].H;
     }
     if (t >= a.nTargets) return;
     const PFTarget &T = a.targets[t];
-    const uint32_t W = T.W, y0 = band * PF_TILE, y1 = min(y0 + PF_TILE, T.H);
+    const uint32_t W = T.W;
     uint32_t *color = static_cast<uint32_t *>(T.color);
     float *depth = T.depth;
-    if (T.clearMode != 0) {                            // the fused clear of the band
-        for (size_t i = (size_t)y0 * W + lane; i < (size_t)y1 * W; i += 32) {
+    if (T.clearMode != 0) {                            // the fused clear of the row
+        for (size_t i = (size_t)y * W + lane; i < (size_t)(y + 1) * W; i += 32) {
             if (T.clearMode == 1 && i < 8) continue;  // pfClear keeps pixels 0..7
             color[i] = T.clearRaw[0];
             depth[i] = T.clearDepth;
@@ -1830,43 +1851,33 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFS
     for (int si = 0; si < nSegs; si++) {
         if (segs[si].target != t) continue;
         const uint32_t gBegin = segs[si].itemBase, gEnd = gBegin + segs[si].nItems;
-        for (uint32_t gb = gBegin; gb < gEnd; gb += 32) {
-            // lane i: item gb + i -- which of its records meet the band
-            const uint32_t g = gb + lane;
-            uint32_t touch = 0;
-            int32_t poolBase = 0;
-            if (g < gEnd) {
-                const uint32_t m = subMask[g];
-                if (m) {
-                    poolBase = __ldg(&a.prims[g].poolBase);
-                    for (uint32_t mm = m; mm; mm &= mm - 1) {
-                        const uint32_t sub = (uint32_t)(__ffs(mm) - 1);
-                        const PFPrim *src = sub ? &a.pool[(uint32_t)poolBase + sub - 1] : &a.prims[g];
-                        const int4 q1 = __ldg(reinterpret_cast<const int4 *>(src) + 1);     // x3 y3 xMin yMin
-                        const int4 q2 = __ldg(reinterpret_cast<const int4 *>(src) + 2);     // xMax yMax ...
-                        const uint32_t xMin = (uint32_t)q1.z, yMin = (uint32_t)q1.w;
-                        const uint32_t xMax = (uint32_t)q2.x, yMax = (uint32_t)q2.y;
-                        const bool meets = xMin < xMax && xMin < W && yMin <= yMax && yMax != 0xffffffffu &&
-                                           max(yMin, y0) < min(yMax + 1u, y1);
-                        if (meets) touch |= 1u << sub;
-                    }
-                }
+        // 128 items a step, four a lane, loaded together; drawn in order
+        for (uint32_t gb = gBegin; gb < gEnd; gb += 128) {
+            uint64_t info[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; k++) {
+                const uint32_t g = gb + 32 * k + lane;
+                info[k] = g < gEnd ? __ldg(rowInfo + g) : 0ull;
             }
-            // draw them in order: items by lane, then sub-triangles
-            for (uint32_t need = __ballot_sync(0xffffffffu, touch != 0); need; need &= need - 1) {
-                const int src = __ffs(need) - 1;
-                const uint32_t tm = __shfl_sync(0xffffffffu, touch, src);
-                const uint32_t gi = gb + (uint32_t)src;
-                const int32_t pb = __shfl_sync(0xffffffffu, poolBase, src);
-                for (uint32_t mm = tm; mm; mm &= mm - 1) {
-                    const uint32_t sub = (uint32_t)(__ffs(mm) - 1);
-                    const uint32_t pi = sub ? (uint32_t)pb + sub - 1 : gi;
-                    const PFPrim *rec = sub ? &a.pool[pi] : &a.prims[gi];
-                    if (lane < 8) reinterpret_cast<int4 *>(&R)[lane] = __ldg(reinterpret_cast<const int4 *>(rec) + lane);
-                    __syncwarp();
-                    const PFPrimPhong *ph = a.anyPhong ? (sub ? &a.poolPh[pi] : &a.primsPh[gi]) : nullptr;
-                    frags += row_record(R, ph, a.states, color, depth, W, y0, y1, lane);
-                    __syncwarp();                      // the record's pixels are written; R is free
+#pragma unroll
+            for (uint32_t k = 0; k < 4; k++) {
+                const uint64_t w = info[k];
+                const bool hit = (w & 0xffffu) && ((w >> 16) & 0xffffffu) <= y && (w >> 40) >= y;
+                for (uint32_t need = __ballot_sync(0xffffffffu, hit); need; need &= need - 1) {
+                    const int src = __ffs(need) - 1;
+                    const uint32_t gi = gb + 32 * k + (uint32_t)src;
+                    const uint32_t subs = (uint32_t)__shfl_sync(0xffffffffu, (uint32_t)w, src) & 0xffffu;
+                    const int32_t pb = (subs & ~1u) ? __ldg(&a.prims[gi].poolBase) : 0;
+                    for (uint32_t mm = subs; mm; mm &= mm - 1) {
+                        const uint32_t sub = (uint32_t)(__ffs(mm) - 1);
+                        const uint32_t pi = sub ? (uint32_t)pb + sub - 1 : gi;
+                        const PFPrim *rec = sub ? &a.pool[pi] : &a.prims[gi];
+                        if (lane < 8) reinterpret_cast<int4 *>(&R)[lane] = __ldg(reinterpret_cast<const int4 *>(rec) + lane);
+                        __syncwarp();
+                        const PFPrimPhong *ph = a.anyPhong ? (sub ? &a.poolPh[pi] : &a.primsPh[gi]) : nullptr;
+                        frags += row_record(R, ph, a.states, color, depth, W, y, y + 1, lane);
+                        __syncwarp();                  // the record's pixels are written; R is free
+                    }
                 }
             }
         }
@@ -2048,7 +2059,7 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
     BinArgs B{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.targets, L.cnt, L.command };
-    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, L.rowBands ? L.subMask : nullptr };
+    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, L.rowCount ? L.rowInfo : nullptr };
     return launch_serialized(k_items, grid_for(L.nItems, 128), 128, 0, st, L.segs, L.nSegs, L.states,
                              (const PFVertexOut *)L.vout, L.nItems, O, B);
 }
@@ -2108,9 +2119,9 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
                                               (L.totalTiles + (uint32_t)warps - 1) / (uint32_t)warps, grid);
     if (e != cudaSuccess) return e;
     e = launch_serialized(kernel, grid, (unsigned)(warps * 32), smem, st, raster_args(L));
-    if (e != cudaSuccess || L.rowBands == 0 || !L.subMask) return e;
-    return launch_serialized(k_rows, (L.rowBands + ROW_WARPS - 1) / ROW_WARPS, ROW_WARPS * 32, 0, st, raster_args(L),
-                             L.segs, L.nSegs, (const uint16_t *)L.subMask, L.rowBands);
+    if (e != cudaSuccess || L.rowCount == 0 || !L.rowInfo) return e;
+    return launch_serialized(k_rows, (L.rowCount + ROW_WARPS - 1) / ROW_WARPS, ROW_WARPS * 32, 0, st, raster_args(L),
+                             L.segs, L.nSegs, (const uint64_t *)L.rowInfo, L.rowCount);
 }
 
 cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,
