@@ -32,6 +32,19 @@ def test_oracle_equals_reference_soup(oracle, ref_shim, kw):
     same(sc.render(oracle), sc.render(ref_shim), f"soup {kw}")
 
 
+@pytest.mark.parametrize("name", ["sphere1080_nearest", "phong1080_nofog"])
+def test_oracle_equals_reference_full_size(oracle, ref_shim, name):
+    """The 1080p workloads at full size, without the library's extensions
+    (depth writes on in the sphere's second draw, no device fog): the sphere
+    with nearest filtering (the reference's bilinear lerp is unpinned) and
+    the 1.3 M-triangle Phong scene with eight lights, colour and depth
+    bit-exact."""
+    from pixelforge_gb300.scenes import PhongScene, SphereScene
+    sc = (SphereScene(filt=A.PF_NEAREST, depth_mask_off=False) if name.startswith("sphere")
+          else PhongScene(fog=False))
+    same(sc.render(oracle, "fbo"), sc.render(ref_shim, "fbo"), name)
+
+
 @pytest.mark.parametrize("k", range(4))
 def test_oracle_equals_reference_array_types(oracle, ref_shim, k):
     from mixscenes import TYPE_CASES, run_types
