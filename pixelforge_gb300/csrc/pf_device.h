@@ -47,6 +47,8 @@ struct PFBatchLaunch {
     uint32_t rowCount;        /* rows of the BGRA / unsigned-byte targets (k_rows, after k_raster),
                                  0 when there are none */
     uint64_t *rowInfo;        /* rowCount > 0: nItems summaries of the items' records (row_info) */
+    uint64_t *rowGroup;       /* and (nItems + 31) / 32 summaries of 32 items each */
+    uint32_t rowMaxW;         /* widest of those targets */
     PFDevCounters *cnt;
     uint32_t command;
 };

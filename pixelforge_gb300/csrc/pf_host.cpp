@@ -289,7 +289,7 @@ struct Renderer {
     bool devInit = false, devOk = false;
     cudaStream_t stream = nullptr;
     DevBuf arena, vout, prims, primsPh, pool, poolPh, binCount, bins, counters;
-    DevBuf rowInfo;                         // per item, its records' rows (launches with BGRA8 targets)
+    DevBuf rowInfo, rowGroup;               // per item and per 32 items, their records' rows (BGRA8 targets)
     uint32_t cap = 256, poolCap = 4096;
     int rasterCtasPerSM = 0;                // 0: as many raster CTAs per SM as fit
     int rasterWarps = 4;                    // warps per raster CTA
@@ -1479,7 +1479,7 @@ void release_renderer(Renderer *r)
     if (r->devOk) {
         r->arena.release(); r->vout.release(); r->prims.release(); r->primsPh.release(); r->pool.release();
         r->poolPh.release(); r->binCount.release(); r->bins.release(); r->counters.release();
-        r->rowInfo.release();
+        r->rowInfo.release(); r->rowGroup.release();
         if (r->hostCounters) cudaFreeHost(r->hostCounters);
         if (r->evStart) { cudaEventDestroy(r->evStart); cudaEventDestroy(r->evEnd); }
         for (auto &pr : r->rasterEv) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -1746,7 +1746,9 @@ bool flush(Renderer *r)
             T.tilesX = (T.W + PF_TILE - 1) / PF_TILE; T.tilesY = (T.H + PF_TILE - 1) / PF_TILE;
             T.tileBase = tiles;
             tiles += T.tilesX * T.tilesY;
-            if (m->fmt == PFF_BGRA8) { L.rowCount += T.H; anyRows = true; }        // row by row (k_rows)
+            if (m->fmt == PFF_BGRA8) {                                            // row by row (k_rows)
+                L.rowCount += T.H; L.rowMaxW = std::max(L.rowMaxW, T.W); anyRows = true;
+            }
             if (o.clearCmd[k] >= 0) {
                 const Cmd &cl = cmds[o.clearCmd[k]];
                 T.clearMode = (cl.kind == CMD_FILL) ? 2 : 1; T.clearDepth = cl.depth;
@@ -1878,7 +1880,8 @@ bool flush(Renderer *r)
             !r->poolPh.ensure(anyPhong ? (size_t)r->poolCap * sizeof(PFPrimPhong) : 128) ||
             !r->binCount.ensure((size_t)(((size_t)maxTiles + 31) & ~(size_t)31) * 4 * (2 + PF_HEAVY_LEVELS)) ||   // bin counters, tile lists
             !r->bins.ensure((size_t)maxTiles * r->cap * 4 + 64) ||
-            !r->rowInfo.ensure(anyRows ? (size_t)maxItems * sizeof(uint64_t) + 64 : 64)) {
+            !r->rowInfo.ensure(anyRows ? (size_t)maxItems * sizeof(uint64_t) + 64 : 64) ||
+            !r->rowGroup.ensure(anyRows ? ((size_t)maxItems / 32 + 8) * sizeof(uint64_t) : 64)) {   // every k_items warp
             r->devStatus |= PF_DEVICE_ALLOC_FAIL;
             return fail("cudaMalloc(scratch)", cudaErrorMemoryAllocation);
         }
@@ -1919,6 +1922,7 @@ bool flush(Renderer *r)
                 L.rasterWarps = r->rasterWarps;
                 L.anyPhong = anyPhong ? 1 : 0;
                 L.rowInfo = L.rowCount ? (uint64_t *)r->rowInfo.p : nullptr;
+                L.rowGroup = L.rowCount ? (uint64_t *)r->rowGroup.p : nullptr;
                 L.cnt = dcnt;
                 rop.L = L;
                 r->stats.kernel_launches += L.rowCount ? 5 : 4;

@@ -724,6 +724,7 @@ struct ItemOut {
     PFPrimPhong *poolPh;
     uint32_t poolCap;
     uint64_t *rowInfo;          // launches with a row-rasterized target: per item, row_info (null otherwise)
+    uint64_t *rowGroup;         // and per 32 items (a k_items warp), the rows their records span
 };
 static_assert(PF_MAX_SUBTRIS <= 16, "an item's sub-triangles are the bits of a 16-bit mask");
 
@@ -739,6 +740,20 @@ __device__ __forceinline__ void row_info_add(uint64_t &info, uint32_t sub, const
     if (info & 0xffffu) { l = min(l, (info >> 16) & 0xffffffu); h = max(h, info >> 40); }
     info = (info & 0xffffu) | (1ull << sub) | (l << 16) | (h << 40);
 }
+// The rows spanned by the records of a warp's 32 items (row_info words w of
+// its lanes, 0 past the end): bit 0 set when there is any, the first and
+// last row at bits 16 and 40.
+__device__ __forceinline__ uint64_t row_group(uint64_t w)
+{
+    const bool any = (w & 0xffffu) != 0;
+    uint32_t lo = any ? (uint32_t)((w >> 16) & 0xffffffu) : 0xffffffu, hi = any ? (uint32_t)(w >> 40) : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    return __any_sync(0xffffffffu, any) ? (1ull | (uint64_t)lo << 16 | (uint64_t)hi << 40) : 0ull;
+}
+
 // rowInfo[g] of an item whose only record is P (kept) or that has none;
 // out of line, so that the set-up path keeps its registers
 __device__ __noinline__ void store_row_info(uint64_t *rowInfo, uint32_t g, const PFPrim &P, bool kept)
@@ -917,6 +932,10 @@ __global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ 
     // round trip, no block barrier)
     const unsigned wk = __popc(__ballot_sync(0xffffffffu, kept));
     if ((threadIdx.x & 31) == 0 && wk) atomicAdd(&B.cnt->batchRasterized, (unsigned long long)wk);
+    if (O.rowInfo) {                                   // the warp's summary for k_rows
+        const uint64_t grp = row_group(g < nItems ? O.rowInfo[g] : 0ull);
+        if ((threadIdx.x & 31) == 0) O.rowGroup[g >> 5] = grp;
+    }
     bin_prim_warp(B, T, kept, P, g << PF_SUB_BITS);
 }
 
@@ -1745,19 +1764,18 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) k_raster(RasterArgs a)
 // ---------------------------------------------------------------------------
 #define ROW_WARPS 4
 
-// One record over the rows [y0, y1) of a BGRA / unsigned-byte target, the
-// part of lane `lane`; returns the covered pixels it counted.
+// One record over row y of a BGRA / unsigned-byte target of width W whose
+// colour and depth the row pointers crow / drow hold (in global or shared
+// memory), the part of lane `lane`; returns the covered pixels it counted.
 __device__ __noinline__ uint32_t row_record(const PFPrim &P, const PFPrimPhong *ph, const PFDrawState *states,
-                                            uint32_t *color, float *depth, uint32_t W, uint32_t y0, uint32_t y1,
-                                            uint32_t lane)
+                                            uint32_t *crow, float *drow, uint32_t W, uint32_t y, uint32_t lane)
 {
-    // rows and columns as tile_edge clips a box: y in [yMin, yMax], x in
+    // the row and columns as tile_edge clips a box: y in [yMin, yMax], x in
     // [xMin, xMax), inside the framebuffer (unsigned)
     const uint32_t xMin = (uint32_t)P.xMin, xMax = (uint32_t)P.xMax, yMin = (uint32_t)P.yMin, yMax = (uint32_t)P.yMax;
-    if (xMin >= xMax || yMin > yMax || yMax == 0xffffffffu) return 0;
-    const uint32_t ra = max(yMin, y0), rb = min(yMax + 1u, y1), xEnd = min(xMax, W);
-    if (ra >= rb || xMin >= xEnd) return 0;
-    const uint32_t nH = (xEnd - xMin + 3u) / 4u, tasks = (rb - ra) * nH;
+    const uint32_t xEnd = min(xMax, W);
+    if (xMin >= xEnd || y < yMin || y > yMax) return 0;
+    const uint32_t nH = (xEnd - xMin + 3u) / 4u;
     const uint32_t kind = P.flags & PFP_KIND, rs = P.rstate;
     const int func = (int)((rs >> 16) & 255u), mode = (int)(rs >> 24);
     // edge functions at pixel (x, y): (x - rx) sx + (y - ry) sy, 32-bit
@@ -1768,9 +1786,8 @@ __device__ __noinline__ uint32_t row_record(const PFPrim &P, const PFPrimPhong *
     if (P.flags & 1u)
         for (int e = 0; e < 3; e++) { sx[e] = -sx[e]; sy[e] = -sy[e]; }
     uint32_t cov = 0;
-    for (uint32_t t = lane; t < tasks; t += 32) {
-        const uint32_t y = ra + t / nH, xf = xMin + 4u * (t % nH);
-        const size_t row = (size_t)y * W;
+    for (uint32_t t = lane; t < nH; t += 32) {
+        const uint32_t xf = xMin + 4u * t;
         if (kind == 0) {
             bool m[4] = { false, false, false, false }, any = false;
             float zl[4] = { 0.0f, 0.0f, 0.0f, 0.0f }, wf[3] = { 0.0f, 0.0f, 0.0f }, zf = 0.0f;
@@ -1787,18 +1804,18 @@ __device__ __noinline__ uint32_t row_record(const PFPrim &P, const PFPrimPhong *
                 if (j == 0) { wf[0] = wn1; wf[1] = wn2; wf[2] = wn3; zf = z; }
                 if (x >= xEnd || (int32_t)(w[0] | w[1] | w[2]) <= 0) continue;
                 cov++;
-                if ((rs & PFS_DEPTH_TEST) && !depth_simd(func, z, depth[row + x])) continue;
+                if ((rs & PFS_DEPTH_TEST) && !depth_simd(func, z, drow[x])) continue;
                 m[j] = true; zl[j] = z; any = true;
             }
             if (!any) continue;
             // the half's value: its first pixel's colour and destination
             uint32_t frag = shade_fragment(P, ph, states, wf[0], wf[1], wf[2], zf, m[0], true);
-            if (rs & PFS_BLEND) frag = blend_simd(mode, frag, pff_swap_rb(color[row + xf]));
+            if (rs & PFS_BLEND) frag = blend_simd(mode, frag, pff_swap_rb(crow[xf]));
             const uint32_t out = pff_swap_rb(frag);
             for (uint32_t j = 0; j < 4; j++) {
                 if (!m[j]) continue;
-                color[row + xf + j] = out;
-                if (rs & PFS_DEPTH_MASK) depth[row + xf + j] = zl[j];
+                crow[xf + j] = out;
+                if (rs & PFS_DEPTH_MASK) drow[xf + j] = zl[j];
             }
         } else {
             for (uint32_t j = 0; j < 4; j++) {
@@ -1806,20 +1823,26 @@ __device__ __noinline__ uint32_t row_record(const PFPrim &P, const PFPrimPhong *
                 if (x >= xEnd || !lp_covers(P, (int32_t)x, (int32_t)y)) continue;
                 if (kind != PFP_BLIT) cov++;
                 const float z = lp_depth(P, (int32_t)x, (int32_t)y);
-                if ((rs & PFS_DEPTH_TEST) && !depth_sisd(func, z, depth[row + x])) continue;
+                if ((rs & PFS_DEPTH_TEST) && !depth_sisd(func, z, drow[x])) continue;
                 uint32_t c = lp_color(P, (int32_t)x, (int32_t)y);
-                if (rs & PFS_BLEND) c = blend_sisd(mode, c, pff_swap_rb(color[row + x]));
-                color[row + x] = pff_swap_rb(c);
-                if (rs & PFS_DEPTH_MASK) depth[row + x] = z;
+                if (rs & PFS_BLEND) c = blend_sisd(mode, c, pff_swap_rb(crow[x]));
+                crow[x] = pff_swap_rb(c);
+                if (rs & PFS_DEPTH_MASK) drow[x] = z;
             }
         }
     }
     return cov;
 }
 
+// SMEM: the warp keeps its row's colour and depth in shared memory while it
+// draws (rows up to ROW_SMEM_MAX_W pixels), else it draws in place.
+#define ROW_SMEM_MAX_W 2048
+template <bool SMEM>
 __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFSegment *__restrict__ segs, int nSegs,
-                                                         const uint64_t *__restrict__ rowInfo, uint32_t nRows)
+                                                         const uint64_t *__restrict__ rowInfo,
+                                                         const uint64_t *__restrict__ rowGroup, uint32_t nRows)
 {
+    extern __shared__ __align__(16) unsigned char rowSmem[];
     __shared__ __align__(16) PFPrim sRec[ROW_WARPS];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // k_raster is done
@@ -1836,14 +1859,20 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFS
     if (t >= a.nTargets) return;
     const PFTarget &T = a.targets[t];
     const uint32_t W = T.W;
-    uint32_t *color = static_cast<uint32_t *>(T.color);
-    float *depth = T.depth;
-    if (T.clearMode != 0) {                            // the fused clear of the row
-        for (size_t i = (size_t)y * W + lane; i < (size_t)(y + 1) * W; i += 32) {
-            if (T.clearMode == 1 && i < 8) continue;  // pfClear keeps pixels 0..7
-            color[i] = T.clearRaw[0];
-            depth[i] = T.clearDepth;
-        }
+    uint32_t *gcol = static_cast<uint32_t *>(T.color) + (size_t)y * W;
+    float *gdep = T.depth + (size_t)y * W;
+    uint32_t *crow = gcol;
+    float *drow = gdep;
+    if (SMEM) {
+        crow = reinterpret_cast<uint32_t *>(rowSmem) + (size_t)warp * 2 * ROW_SMEM_MAX_W;
+        drow = reinterpret_cast<float *>(crow + ROW_SMEM_MAX_W);
+    }
+    // the row as the draws find it: the fused clear (pfClear keeps pixels
+    // 0..7), or the framebuffer's contents
+    for (uint32_t x = lane; x < W; x += 32) {
+        const bool clr = T.clearMode == 2 || (T.clearMode == 1 && (size_t)y * W + x >= 8);
+        if (clr) { crow[x] = T.clearRaw[0]; drow[x] = T.clearDepth; }
+        else if (SMEM) { crow[x] = gcol[x]; drow[x] = gdep[x]; }
     }
     __syncwarp();
     PFPrim &R = sRec[warp];
@@ -1851,21 +1880,22 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFS
     for (int si = 0; si < nSegs; si++) {
         if (segs[si].target != t) continue;
         const uint32_t gBegin = segs[si].itemBase, gEnd = gBegin + segs[si].nItems;
-        // 128 items a step, four a lane, loaded together; drawn in order
-        for (uint32_t gb = gBegin; gb < gEnd; gb += 128) {
-            uint64_t info[4];
-#pragma unroll
-            for (uint32_t k = 0; k < 4; k++) {
-                const uint32_t g = gb + 32 * k + lane;
-                info[k] = g < gEnd ? __ldg(rowInfo + g) : 0ull;
-            }
-#pragma unroll
-            for (uint32_t k = 0; k < 4; k++) {
-                const uint64_t w = info[k];
+        if (gBegin >= gEnd) continue;
+        // groups of 32 items (one summary word each, 32 groups a step), then
+        // the items of the groups that reach the row, in order
+        const uint32_t cEnd = ((gEnd - 1) >> 5) + 1;
+        for (uint32_t cb = gBegin >> 5; cb < cEnd; cb += 32) {
+            const uint32_t c = cb + lane;
+            const uint64_t sg = c < cEnd ? __ldg(rowGroup + c) : 0ull;
+            const bool ghit = (sg & 1u) && ((sg >> 16) & 0xffffffu) <= y && (sg >> 40) >= y;
+            for (uint32_t gneed = __ballot_sync(0xffffffffu, ghit); gneed; gneed &= gneed - 1) {
+                const uint32_t gb = (cb + (uint32_t)(__ffs(gneed) - 1)) << 5;
+                const uint32_t g = gb + lane;
+                const uint64_t w = (g >= gBegin && g < gEnd) ? __ldg(rowInfo + g) : 0ull;
                 const bool hit = (w & 0xffffu) && ((w >> 16) & 0xffffffu) <= y && (w >> 40) >= y;
                 for (uint32_t need = __ballot_sync(0xffffffffu, hit); need; need &= need - 1) {
                     const int src = __ffs(need) - 1;
-                    const uint32_t gi = gb + 32 * k + (uint32_t)src;
+                    const uint32_t gi = gb + (uint32_t)src;
                     const uint32_t subs = (uint32_t)__shfl_sync(0xffffffffu, (uint32_t)w, src) & 0xffffu;
                     const int32_t pb = (subs & ~1u) ? __ldg(&a.prims[gi].poolBase) : 0;
                     for (uint32_t mm = subs; mm; mm &= mm - 1) {
@@ -1875,13 +1905,15 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RasterArgs a, const PFS
                         if (lane < 8) reinterpret_cast<int4 *>(&R)[lane] = __ldg(reinterpret_cast<const int4 *>(rec) + lane);
                         __syncwarp();
                         const PFPrimPhong *ph = a.anyPhong ? (sub ? &a.poolPh[pi] : &a.primsPh[gi]) : nullptr;
-                        frags += row_record(R, ph, a.states, color, depth, W, y, y + 1, lane);
-                        __syncwarp();                  // the record's pixels are written; R is free
+                        frags += row_record(R, ph, a.states, crow, drow, W, y, lane);
+                        __syncwarp();              // the record's pixels are written; R is free
                     }
                 }
             }
         }
     }
+    if (SMEM)
+        for (uint32_t x = lane; x < W; x += 32) { gcol[x] = crow[x]; gdep[x] = drow[x]; }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
     if (lane == 0 && frags) atomicAdd(&a.cnt->fragments, frags);
 }
@@ -2059,7 +2091,7 @@ cudaError_t pfd_launch_items(const PFBatchLaunch &L, cudaStream_t st)
 {
     if (L.nItems == 0) return cudaSuccess;
     BinArgs B{ L.binCount, L.tileList, L.listStride, L.bins, L.cap, L.targets, L.cnt, L.command };
-    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, L.rowCount ? L.rowInfo : nullptr };
+    ItemOut O{ L.prims, L.primsPh, L.pool, L.poolPh, L.poolCap, L.rowCount ? L.rowInfo : nullptr, L.rowGroup };
     return launch_serialized(k_items, grid_for(L.nItems, 128), 128, 0, st, L.segs, L.nSegs, L.states,
                              (const PFVertexOut *)L.vout, L.nItems, O, B);
 }
@@ -2119,9 +2151,17 @@ cudaError_t pfd_launch_raster(const PFBatchLaunch &L, cudaStream_t st)
                                               (L.totalTiles + (uint32_t)warps - 1) / (uint32_t)warps, grid);
     if (e != cudaSuccess) return e;
     e = launch_serialized(kernel, grid, (unsigned)(warps * 32), smem, st, raster_args(L));
-    if (e != cudaSuccess || L.rowCount == 0 || !L.rowInfo) return e;
-    return launch_serialized(k_rows, (L.rowCount + ROW_WARPS - 1) / ROW_WARPS, ROW_WARPS * 32, 0, st, raster_args(L),
-                             L.segs, L.nSegs, (const uint64_t *)L.rowInfo, L.rowCount);
+    if (e != cudaSuccess || L.rowCount == 0 || !L.rowInfo || !L.rowGroup) return e;
+    const unsigned rowGrid = (L.rowCount + ROW_WARPS - 1) / ROW_WARPS;
+    if (L.rowMaxW <= ROW_SMEM_MAX_W) {
+        const size_t rsm = (size_t)ROW_WARPS * 2 * ROW_SMEM_MAX_W * 4;          // colour and depth rows
+        e = cudaFuncSetAttribute(k_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
+        if (e != cudaSuccess) return e;
+        return launch_serialized(k_rows<true>, rowGrid, ROW_WARPS * 32, rsm, st, raster_args(L), L.segs, L.nSegs,
+                                 (const uint64_t *)L.rowInfo, (const uint64_t *)L.rowGroup, L.rowCount);
+    }
+    return launch_serialized(k_rows<false>, rowGrid, ROW_WARPS * 32, 0, st, raster_args(L), L.segs, L.nSegs,
+                             (const uint64_t *)L.rowInfo, (const uint64_t *)L.rowGroup, L.rowCount);
 }
 
 cudaError_t pfd_launch_clear(void *color, uint32_t fmt, float *depth, size_t n, const uint32_t cc[4], float cd, bool all,
