@@ -17,7 +17,7 @@ import sys
 
 
 FORMATS = {"RGBA8": (7, 0), "RGB8": (6, 0), "RGB565": (6, 2), "RGBA5551": (7, 3), "RGBA4444": (7, 4),
-           "RGBA16F": (7, 9), "RGBA32F": (7, 10), "LA16F": (5, 9)}
+           "RGBA16F": (7, 9), "RGBA32F": (7, 10), "LA16F": (5, 9), "BGRA8": (9, 0)}
 
 
 def main(argv=None) -> int:
