@@ -123,6 +123,26 @@ def test_feature_mix_bgra(gpu, oracle, seed):
         assert got.stats["fragments"] == ref.stats["fragments"]
 
 
+def test_bgra8_wide_rows(gpu, oracle):
+    """A BGRA / unsigned-byte framebuffer wider than the rows k_rows keeps
+    in shared memory (2,600 pixels: drawn in place), blended soup with
+    culling off: bit-exact, fragment counts equal."""
+    from pixelforge_gb300.scenes import Target
+    sc = SoupScene(width=2600, height=40, ntris=500, blend=A.PF_BLEND_ALPHA, cull=False)
+    outs = []
+    for lib in (gpu, oracle):
+        tg = Target(lib, sc.width, sc.height, "fbo", fmt=FB_BGRA8)
+        try:
+            sc.record(lib)
+            outs.append(tg.finish())
+        finally:
+            tg.close()
+    assert gpu.pfGetDeviceStatus() == 0
+    assert (outs[1].depth < 1e30).sum() > 20000
+    assert_parity(outs[0], outs[1], exact_color=True, label="bgra8 2600 wide")
+    assert outs[0].stats["fragments"] == outs[1].stats["fragments"]
+
+
 def test_bgra8_tile_bins_and_splits(gpu, oracle):
     """BGRA / unsigned byte beside RGBA8 in one flush (two framebuffer
     objects drawn alternately, the RGBA8 one rasterized by k_raster, the
