@@ -283,6 +283,25 @@ def test_tile_overfull_draw_is_split(gpu, oracle):
     assert_parity(got, ref, exact_color=True, label="overfull tiles")
 
 
+def test_tile_overfull_draw_is_split_bgra8(gpu, oracle):
+    """The same split into passes for a BGRA / unsigned-byte framebuffer
+    (k_rows draws each pass on top of the previous one), alpha-blended."""
+    from pixelforge_gb300.scenes import Target
+    sc = SoupScene(width=32, height=24, ntris=40000, seed=78, xy_range=(-3.0, 3.0), cull=False,
+                   blend=A.PF_BLEND_ALPHA)
+    outs = []
+    for lib in (gpu, oracle):
+        tg = Target(lib, sc.width, sc.height, "fbo", fmt=FB_BGRA8)
+        try:
+            sc.record(lib)
+            outs.append(tg.finish())
+        finally:
+            tg.close()
+    assert gpu.pfGetDeviceStatus() == 0
+    assert outs[0].stats["draw_splits"] >= 1
+    assert_parity(outs[0], outs[1], exact_color=True, label="overfull tiles bgra8")
+
+
 @pytest.mark.parametrize("fmt", [("BGRA", "UBYTE"), ("LUMINANCE_ALPHA", "UBYTE"), ("RGB", "HALF"), ("RGBA", "FLOAT"),
                                  ("BGRA", "S4444")])
 def test_texture_formats_bilinear(gpu, oracle, fmt):
