@@ -350,6 +350,39 @@ PF_API void pfFinish(void);
  * only behaviour, src/internal/primitives/triangles.c:529). */
 PF_API void pfDepthMask(PFboolean flag);
 
+/* Zero-copy vertex arrays, indices and textures in device memory.
+ *
+ * Counterparts of pfVertexPointer, pfNormalPointer, pfTexCoordPointer,
+ * pfColorPointer (pixelforge.h:1031-1069), pfDrawElements (:1082) and
+ * pfGenTexture (:2025) whose pointers are device memory of the current GPU
+ * (cudaMalloc or managed; a host pointer sets PF_INVALID_VALUE and binds
+ * nothing).  Nothing is copied when a draw is recorded: the kernels read the
+ * arrays and texels when the frame is rendered, at the next observation
+ * point, so the caller keeps that memory allocated and unchanged until then
+ * (the host-pointer calls copy at the draw call instead).  Stride is ignored,
+ * as in the reference.  Types: positions float with 2 to 4 components,
+ * normals and texture coordinates float, colours unsigned byte with 3 or 4
+ * components (other types: PF_INVALID_ENUM), every pointer but colours
+ * 4-byte aligned.  Device arrays draw triangles in every triangle draw mode
+ * with PF_FILL polygon modes; points, lines and the PF_POINT / PF_LINE
+ * polygon modes are assembled on the host and set PF_INVALID_OPERATION.
+ *
+ * pfDrawElementsDevice draws `count` unsigned-int indices read from device
+ * memory; vertexCount is the number of array elements they may reference
+ * (the largest index + 1), which the library cannot find without reading
+ * them: the vertex kernel transforms that many.  An index at or past
+ * vertexCount is clamped to vertexCount - 1 and sets PF_DEVICE_INDEX_RANGE
+ * in pfGetDeviceStatus.  vertexCount 0 sets PF_INVALID_VALUE.
+ *
+ * pfGenTextureDevice wraps width x height RGBA / unsigned-byte texels in
+ * device memory; pfDeleteTexture never frees them. */
+PF_API void pfVertexPointerDevice(PFint size, PFenum type, PFsizei stride, const void* devicePointer);
+PF_API void pfNormalPointerDevice(PFenum type, PFsizei stride, const void* devicePointer);
+PF_API void pfTexCoordPointerDevice(PFenum type, PFsizei stride, const void* devicePointer);
+PF_API void pfColorPointerDevice(PFint size, PFenum type, PFsizei stride, const void* devicePointer);
+PF_API void pfDrawElementsDevice(PFdrawmode mode, PFsizei count, PFsizei vertexCount, const PFuint* deviceIndices);
+PF_API PFtexture pfGenTextureDevice(const void* devicePixels, PFsizei width, PFsizei height);
+
 /* Built-in device post-process hooks, the GPU form of pfPostProcess.  A hook
  * is a __device__ function compiled into the library and applied to every
  * pixel of the current framebuffer, in order with the recorded draws. */
@@ -407,7 +440,8 @@ enum {
     PF_DEVICE_NO_GPU      = 1,   /* no CUDA device, or the CUDA runtime failed */
     PF_DEVICE_ALLOC_FAIL  = 2,   /* device memory allocation failed */
     PF_DEVICE_LAUNCH_FAIL = 4,   /* a kernel launch or copy reported an error */
-    PF_DEVICE_BIN_LIMIT   = 8    /* a tile bin exceeded its hard capacity */
+    PF_DEVICE_BIN_LIMIT   = 8,   /* a tile bin exceeded its hard capacity */
+    PF_DEVICE_INDEX_RANGE = 16   /* a pfDrawElementsDevice index reached its vertexCount (clamped) */
 };
 PF_API PFuint pfGetDeviceStatus(void);
 

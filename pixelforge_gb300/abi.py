@@ -89,6 +89,7 @@ def pixel_bytes(fmt: int, typ: int) -> int:
  PF_TEXTURE_MATRIX, PF_MAX_PROJECTION_STACK_DEPTH, PF_MAX_MODELVIEW_STACK_DEPTH, PF_MAX_TEXTURE_STACK_DEPTH,
  PF_SHADE_MODEL) = range(10000, 10021)
 PF_HOOK_IDENTITY, PF_HOOK_FOG_LINEAR, PF_HOOK_GRAYSCALE, PF_HOOK_DITHER = 0, 1, 2, 3
+PF_DEVICE_INDEX_RANGE = 16
 
 _V = None
 _FP = C.POINTER(C.c_float)
@@ -234,6 +235,12 @@ PROTOTYPES = {
     "pfGetDeviceStatus": (PFuint, []),
     "pfEnableTiming": (_V, [PFbool]),
     "pfGetTexturePixels": (PFptr, [PFptr, PFptr, PFptr, PFptr, PFptr]),
+    "pfVertexPointerDevice": (_V, [PFint, PFenum, PFsizei, PFptr]),
+    "pfNormalPointerDevice": (_V, [PFenum, PFsizei, PFptr]),
+    "pfTexCoordPointerDevice": (_V, [PFenum, PFsizei, PFptr]),
+    "pfColorPointerDevice": (_V, [PFint, PFenum, PFsizei, PFptr]),
+    "pfDrawElementsDevice": (_V, [PFenum_i, PFsizei, PFsizei, PFptr]),
+    "pfGenTextureDevice": (PFptr, [PFptr, PFsizei, PFsizei]),
     "pfgbBatchCreate": (PFptr, []),
     "pfgbBatchDelete": (_V, [PFptr]),
     "pfgbBatchBegin": (_V, [PFptr]),

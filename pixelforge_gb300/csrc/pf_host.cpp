@@ -129,6 +129,7 @@ struct Tex {
     bool isMain;         // a context's main framebuffer (its depth is internal)
     uint32_t drawUses = 0;         // draw-time snapshots taken of the texels
     bool hostRegistered = false;   // the texels were page-locked by the library (cudaHostRegister)
+    bool device = false;           // pfGenTextureDevice: the texels are device memory, read at the flush
 };
 
 struct Light {
@@ -144,7 +145,13 @@ struct Material {
     float shininess = 64.0f;
 };
 
-struct Attrib { const void *buf = nullptr; PFsizei stride = 0; PFint size = 0; PFenum type = 0; };
+struct Attrib {
+    const void *buf = nullptr;
+    PFsizei stride = 0;
+    PFint size = 0;
+    PFenum type = 0;
+    bool dev = false;          // buf is device memory (pf*PointerDevice): read at the flush, not copied
+};
 
 // Device mirror of one framebuffer (main or pfGenFramebuffer).
 struct FBMirror {
@@ -954,6 +961,7 @@ void pin_texture(Renderer *r, Tex *t, size_t bytes)
 
 int64_t snapshot_texture(Renderer *r, const Tex *t)
 {
+    if (t->device) return -(int64_t)(uintptr_t)t->pixels;      // the caller's device texels, as they are
     const size_t n = (size_t)t->w * t->h;
     if (t->format == PF_RGBA && t->type == PF_UNSIGNED_BYTE) {
         pin_texture(r, const_cast<Tex *>(t), n * 4);
@@ -1967,6 +1975,7 @@ bool flush(Renderer *r)
         }
         r->stats.raster_launches += nRaster;
         const PFDevCounters hc = *r->hostCounters;
+        if (hc.status & PFD_BOUNDS) r->devStatus |= PF_DEVICE_INDEX_RANGE;
         r->stats.fragments += hc.fragments;
         r->stats.rasterized += hc.rasterized;
         if (hc.abortCommand == 0xffffffffu) {
@@ -2531,6 +2540,7 @@ static float attr_f(const Attrib &a, size_t i)
 // normals, texcoords) starting at element `first`.
 static int64_t stage_float_attr(Ctx *c, const Attrib &a, int comps, size_t first, size_t count)
 {
+    if (a.dev) return -(int64_t)(uintptr_t)((const float *)a.buf + first * comps);   // read in place at the flush
     if (a.type == PF_FLOAT) return snapshot(c, (const float *)a.buf + first * comps, count * comps * 4);
     int64_t off = c->rend->staging.alloc(count * comps * 4);
     float *dst = (float *)(c->rend->staging.base + off);
@@ -2541,6 +2551,7 @@ static int64_t stage_float_attr(Ctx *c, const Attrib &a, int comps, size_t first
 static int64_t stage_color_attr(Ctx *c, const Attrib &a, size_t first, size_t count)
 {
     const size_t k = (size_t)a.size;
+    if (a.dev) return -(int64_t)(uintptr_t)((const uint8_t *)a.buf + first * k);
     if (a.type == PF_UNSIGNED_BYTE) return snapshot(c, (const uint8_t *)a.buf + first * k, count * k);
     int64_t off = c->rend->staging.alloc(count * k);
     uint8_t *dst = c->rend->staging.base + off;
@@ -2610,7 +2621,8 @@ static void assemble_arrays(Ctx *c, PFdrawmode mode, PFsizei count, const void *
 // pfDrawElements / pfDrawArrays: one segment whose vertices are the arrays'
 // elements [first, first + nverts) and whose primitives follow `indices`
 // (or the sequence 0..count-1).
-static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first)
+static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFdatatype itype, PFint first,
+                        size_t devVerts = 0)
 {
     Ctx *c = G;
     CopyScope scope(c->rend);
@@ -2625,6 +2637,13 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     bool allFill = false;
     const int nf = fill_faces(c, mode, faces, allFill);
     if (nprim == 0) return;
+    // device arrays (and device indices, devVerts > 0) are read by the
+    // kernels only: the host assembles points and lines itself
+    const bool anyDev = devVerts > 0 || c->positions.dev ||
+                        ((c->state & PF_NORMAL_ARRAY) && c->normals.buf && c->normals.dev) ||
+                        ((c->state & PF_TEXTURE_COORD_ARRAY) && c->texcoords.buf && c->texcoords.dev) ||
+                        ((c->state & PF_COLOR_ARRAY) && c->colors.buf && c->colors.dev);
+    if (anyDev && !allFill) { c->err = PF_INVALID_OPERATION; return; }
     if (!allFill) {
         assemble_arrays(c, mode, count, indices, itype, first);
         c->stateDirty = true;
@@ -2639,7 +2658,11 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     // indices: stage as u32 and find the vertex range
     int64_t idxOff = -1;
     size_t nverts;
-    if (indices) {
+    if (devVerts) {
+        idxOff = -(int64_t)(uintptr_t)indices;           // the caller's device indices, read in place
+        nverts = devVerts;
+        first = 0;
+    } else if (indices) {
         uint32_t mx = 0;
         if (itype == PF_UNSIGNED_INT) {
             idxOff = snapshot_u32(c->rend, (const uint32_t *)indices, (size_t)count, mx);
@@ -2667,8 +2690,8 @@ static void draw_arrays(PFdrawmode mode, PFsizei count, const void *indices, PFd
     r.posOff = stage_float_attr(c, c->positions, c->positions.size, (size_t)first, nverts);
     // the normals are often the positions' own array (unit spheres): one copy
     // taken in the same call serves both
-    if (useN) r.nrmOff = (c->normals.buf == c->positions.buf && c->normals.type == PF_FLOAT &&
-                          c->positions.type == PF_FLOAT && c->positions.size == 3)
+    if (useN) r.nrmOff = (c->normals.buf == c->positions.buf && c->normals.dev == c->positions.dev &&
+                          c->normals.type == PF_FLOAT && c->positions.type == PF_FLOAT && c->positions.size == 3)
                              ? r.posOff : stage_float_attr(c, c->normals, 3, (size_t)first, nverts);
     if (useT) r.uvOff = stage_float_attr(c, c->texcoords, 2, (size_t)first, nverts);
     if (useC) r.colOff = stage_color_attr(c, c->colors, (size_t)first, nverts);
@@ -2703,6 +2726,59 @@ void pfDrawArrays(PFdrawmode mode, PFint first, PFsizei count)
 {
     if (!(G->state & PF_VERTEX_ARRAY)) { G->err = PF_INVALID_OPERATION; return; }
     draw_arrays(mode, count, nullptr, PF_UNSIGNED_INT, first);
+}
+
+// --- zero-copy device arrays and textures (extension) --------------------------
+// The pointers are device memory of the current GPU (cudaMalloc or managed),
+// read by the kernels when the frame is rendered, at the next observation
+// point: nothing is copied at the call, and the caller keeps the memory
+// allocated and unchanged until then.
+static bool device_memory(Ctx *c, const void *p, size_t align)
+{
+    if (!p || ((uintptr_t)p % align) != 0 || !device_init(c->rend)) return false;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+void pfVertexPointerDevice(PFint size, PFenum type, PFsizei stride, const void *p)
+{
+    if (size < 2 || size > 4) { G->err = PF_INVALID_VALUE; return; }
+    if (type != PF_FLOAT) { G->err = PF_INVALID_ENUM; return; }
+    if (!device_memory(G, p, 4)) { G->err = PF_INVALID_VALUE; return; }
+    G->positions = Attrib{ p, stride, size, type, true };
+}
+void pfNormalPointerDevice(PFenum type, PFsizei stride, const void *p)
+{
+    if (type != PF_FLOAT) { G->err = PF_INVALID_ENUM; return; }
+    if (!device_memory(G, p, 4)) { G->err = PF_INVALID_VALUE; return; }
+    G->normals = Attrib{ p, stride, 3, type, true };
+}
+void pfTexCoordPointerDevice(PFenum type, PFsizei stride, const void *p)
+{
+    if (type != PF_FLOAT) { G->err = PF_INVALID_ENUM; return; }
+    if (!device_memory(G, p, 4)) { G->err = PF_INVALID_VALUE; return; }
+    G->texcoords = Attrib{ p, stride, 2, type, true };
+}
+void pfColorPointerDevice(PFint size, PFenum type, PFsizei stride, const void *p)
+{
+    if (size < 3 || size > 4) { G->err = PF_INVALID_VALUE; return; }
+    if (type != PF_UNSIGNED_BYTE) { G->err = PF_INVALID_ENUM; return; }
+    if (!device_memory(G, p, 1)) { G->err = PF_INVALID_VALUE; return; }
+    G->colors = Attrib{ p, stride, size, type, true };
+}
+void pfDrawElementsDevice(PFdrawmode mode, PFsizei count, PFsizei vertexCount, const PFuint *indices)
+{
+    if (!(G->state & PF_VERTEX_ARRAY)) { G->err = PF_INVALID_OPERATION; return; }
+    if (vertexCount == 0) { G->err = PF_INVALID_VALUE; return; }
+    if (!device_memory(G, indices, 4)) { G->err = PF_INVALID_VALUE; return; }
+    draw_arrays(mode, count, indices, PF_UNSIGNED_INT, 0, (size_t)vertexCount);
+}
+PFtexture pfGenTextureDevice(const void *pixels, PFsizei w, PFsizei h)
+{
+    if (w == 0 || h == 0 || !G || !device_memory(G, pixels, 4)) { set_err(PF_INVALID_VALUE); return nullptr; }
+    Tex *t = tex_new(const_cast<void *>(pixels), w, h, PF_RGBA, PF_UNSIGNED_BYTE, true);
+    if (t) t->device = true;
+    return t;
 }
 
 static void list_begin(Ctx *c, PFdrawmode mode);
@@ -3405,7 +3481,7 @@ void pfDeleteTexture(PFtexture *tex, PFboolean freeBuffer)
         if (cudaDeviceSynchronize() != cudaSuccess) cudaGetLastError();   // no upload from it in flight
         cudaHostUnregister(t->pixels);
     }
-    if (freeBuffer) std::free(t->pixels);
+    if (freeBuffer && !t->device) std::free(t->pixels);      // device texels stay the caller's
     delete t;
     *tex = nullptr;
 }

@@ -649,7 +649,7 @@ __device__ __forceinline__ void store_phong(PFPrimPhong *dst, const SVert &a, co
     *dst = q;
 }
 
-__device__ __forceinline__ void item_vertices(const PFSegment &sg, uint32_t k, uint32_t v[3], int &face)
+__device__ __forceinline__ void item_vertices(const PFSegment &sg, uint32_t k, uint32_t v[3], int &face, unsigned *status)
 {
     uint32_t s[3];
     if (sg.itemKind == PF_ITEMS_TRIS) {
@@ -662,7 +662,10 @@ __device__ __forceinline__ void item_vertices(const PFSegment &sg, uint32_t k, u
     }
     for (int m = 0; m < 3; m++) {
         uint32_t j = sg.idx ? __ldg(sg.idx + s[m]) : s[m];
-        if (j >= sg.nVerts) j = sg.nVerts - 1;        // memory guard; the host sizes nVerts from the indices
+        if (j >= sg.nVerts) {                          // the host sizes nVerts from the indices, except for
+            j = sg.nVerts - 1;                         // device indices (pfDrawElementsDevice): clamped, flagged
+            atomicOr(status, (unsigned)PFD_BOUNDS);
+        }
         v[m] = sg.vtxBase + j;
     }
 }
@@ -855,7 +858,7 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
         return true;
     }
     uint32_t vi[3]; int face;
-    item_vertices(sg, k, vi, face);
+    item_vertices(sg, k, vi, face, &B.cnt->status);
     const PFVertexOut *V[3] = { &vout[vi[0]], &vout[vi[1]], &vout[vi[2]] };
     float4 hv[3];
     for (int m = 0; m < 3; m++) hv[m] = *reinterpret_cast<const float4 *>(V[m]->h);

@@ -186,6 +186,35 @@ def test_static_entry_rejects_oversize_without_device(lib):
     assert f(dummy, dummy, 1, dummy, dummy, dummy, 64, 64, 2, 3, None) == -2       # cull mode
 
 
+def test_device_pointer_calls_refuse_host_memory(lib):
+    """The zero-copy calls take device memory only: a host pointer (or no
+    GPU at all) sets PF_INVALID_VALUE and binds nothing, other types
+    PF_INVALID_ENUM; pfGenTextureDevice returns no texture."""
+    buf = np.zeros((8, 8, 4), np.uint8)
+    arr = np.zeros(64, np.float32)
+    p = arr.ctypes.data_as(C.c_void_p)
+    ctx = lib.pfCreateContext(buf.ctypes.data_as(C.c_void_p), 8, 8, A.PF_RGBA, A.PF_UNSIGNED_BYTE)
+    lib.pfMakeCurrent(ctx)
+    try:
+        for call in (lambda: lib.pfVertexPointerDevice(3, A.PF_FLOAT, 0, p),
+                     lambda: lib.pfNormalPointerDevice(A.PF_FLOAT, 0, p),
+                     lambda: lib.pfTexCoordPointerDevice(A.PF_FLOAT, 0, p),
+                     lambda: lib.pfColorPointerDevice(4, A.PF_UNSIGNED_BYTE, 0, p)):
+            call()
+            assert lib.pfGetError() == A.PF_INVALID_VALUE
+        lib.pfVertexPointerDevice(3, A.PF_DOUBLE, 0, p)
+        assert lib.pfGetError() == A.PF_INVALID_ENUM
+        lib.pfColorPointerDevice(4, A.PF_FLOAT, 0, p)
+        assert lib.pfGetError() == A.PF_INVALID_ENUM
+        lib.pfEnable(A.PF_VERTEX_ARRAY)
+        lib.pfDrawElementsDevice(A.PF_TRIANGLES, 3, 3, p)
+        assert lib.pfGetError() == A.PF_INVALID_VALUE
+        assert not lib.pfGenTextureDevice(p, 4, 4)
+        assert lib.pfGetError() == A.PF_INVALID_VALUE
+    finally:
+        lib.pfDeleteContext(ctx)
+
+
 def test_framebuffer_formats_refused(lib, oracle):
     """Framebuffer formats whose reference results depend on other pixels or
     on the SIMD lane are refused with PF_INVALID_ENUM, by the library and
