@@ -219,6 +219,7 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, samples=2)
     tg.close()
+    out["e2e_device_inputs"] = run_device_inputs(lib, args, l2_flush)
     # the other workloads, each in a process of its own: a failure there is
     # reported in its section and leaves the headline line intact
     for name, skip in (("soup256", args.no_soup), ("phong", args.no_phong), ("framebuffer_formats", args.no_formats),
@@ -226,6 +227,44 @@ def run_gpu(args):
         if not skip:
             out[name] = run_section(name)
     return out
+
+
+def run_device_inputs(lib, args, l2_flush) -> dict:
+    """The same frames end to end with the arrays, indices and texture
+    already in device memory (the zero-copy pf*Device calls): every pf* call,
+    the kernels and the device-to-host write-back of the colour into the
+    caller's buffer; nothing is copied to the device."""
+    import torch
+    from pixelforge_gb300 import abi as A
+    from pixelforge_gb300.scenes import SphereScene, Target
+    sc = SphereScene(device_arrays=True)
+    tg = Target(lib, sc.width, sc.height, "main")
+    try:
+        sc.setup(lib)
+        lib.pfEnableTiming(True)
+        for _ in range(args.warmup):
+            sc.frame(lib)
+            lib.pfFinish()
+        lib.pfResetStats()
+        wall = 0.0
+        for _ in range(args.steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sc.frame(lib)
+            lib.pfFinish()
+            wall += time.perf_counter() - t0
+        s = A.PFstats()
+        lib.pfGetStats(s)
+        status = lib.pfGetDeviceStatus()
+        sc.teardown(lib)
+    finally:
+        tg.close()
+    if status != 0:
+        raise RuntimeError(f"device status {status:#x}")
+    return {"value": s.fragments / wall, "unit": "fragments/s", "ms_per_step": wall * 1e3 / args.steps,
+            "device_ms_per_step": s.device_ms / args.steps,
+            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": sc.width * sc.height * 4}
 
 
 SECTION_TIMEOUT_S = 900

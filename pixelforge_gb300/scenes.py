@@ -267,10 +267,12 @@ class SphereScene:
     znear: float = 0.1
     zfar: float = 100.0
     depth_mask_off: bool = True   # second draw without depth writes (extension)
+    device_arrays: bool = False   # arrays, indices and texture in device memory (zero-copy extension)
 
     def __post_init__(self):
         self.pos, self.uv, self.idx = uv_sphere(self.segments, self.rings)
         self.tex = noise_texture(self.tex_size, self.tex_seed)
+        self._dev = None
 
     @property
     def ntris(self) -> int:
@@ -298,21 +300,39 @@ class SphereScene:
             lib.pfMaterialf(A.PF_FRONT_AND_BACK, A.PF_DIFFUSE, 0.8)
             lib.pfMaterialf(A.PF_FRONT_AND_BACK, A.PF_SPECULAR, 0.5)
             lib.pfMaterialf(A.PF_FRONT_AND_BACK, A.PF_SHININESS, 32.0)
-        self.texh = lib.pfGenTexture(_ptr(self.tex), self.tex_size, self.tex_size, A.PF_RGBA,
-                                     A.PF_UNSIGNED_BYTE)
-        lib.pfTextureParameter(self.texh, self.wrap, self.filt)
-        lib.pfBindTexture(self.texh)
         lib.pfEnable(A.PF_TEXTURE_2D)
         lib.pfEnable(A.PF_VERTEX_ARRAY | A.PF_NORMAL_ARRAY | A.PF_TEXTURE_COORD_ARRAY)
-        lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(self.pos))
-        lib.pfNormalPointer(A.PF_FLOAT, 0, _ptr(self.pos))
-        lib.pfTexCoordPointer(A.PF_FLOAT, 0, _ptr(self.uv))
+        if self.device_arrays:
+            import torch
+            dev = torch.device("cuda:0")
+            self._dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+                         for k, v in (("pos", self.pos), ("uv", self.uv), ("idx", self.idx), ("tex", self.tex))}
+            torch.cuda.synchronize()
+            dp = lambda k: C.c_void_p(self._dev[k].data_ptr())
+            self.texh = lib.pfGenTextureDevice(dp("tex"), self.tex_size, self.tex_size)
+            lib.pfVertexPointerDevice(3, A.PF_FLOAT, 0, dp("pos"))
+            lib.pfNormalPointerDevice(A.PF_FLOAT, 0, dp("pos"))
+            lib.pfTexCoordPointerDevice(A.PF_FLOAT, 0, dp("uv"))
+        else:
+            self.texh = lib.pfGenTexture(_ptr(self.tex), self.tex_size, self.tex_size, A.PF_RGBA,
+                                         A.PF_UNSIGNED_BYTE)
+            lib.pfVertexPointer(3, A.PF_FLOAT, 0, _ptr(self.pos))
+            lib.pfNormalPointer(A.PF_FLOAT, 0, _ptr(self.pos))
+            lib.pfTexCoordPointer(A.PF_FLOAT, 0, _ptr(self.uv))
+        lib.pfTextureParameter(self.texh, self.wrap, self.filt)
+        lib.pfBindTexture(self.texh)
+
+    def _draw(self, lib):
+        if self._dev is not None:
+            lib.pfDrawElementsDevice(A.PF_TRIANGLES, len(self.idx), len(self.pos), C.c_void_p(self._dev["idx"].data_ptr()))
+        else:
+            lib.pfDrawElements(A.PF_TRIANGLES, len(self.idx), A.PF_UNSIGNED_INT, _ptr(self.idx))
 
     def frame(self, lib):
         """One frame: clear, opaque draw, scaled alpha-blended draw."""
         lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
         lib.pfColor4ub(255, 255, 255, 255)
-        lib.pfDrawElements(A.PF_TRIANGLES, len(self.idx), A.PF_UNSIGNED_INT, _ptr(self.idx))
+        self._draw(lib)
         if self.second_draw:
             lib.pfPushMatrix()
             lib.pfScalef(1.05, 1.05, 1.05)
@@ -322,7 +342,7 @@ class SphereScene:
             mask = self.depth_mask_off and lib.has("pfDepthMask")
             if mask:
                 lib.pfDepthMask(False)
-            lib.pfDrawElements(A.PF_TRIANGLES, len(self.idx), A.PF_UNSIGNED_INT, _ptr(self.idx))
+            self._draw(lib)
             if mask:
                 lib.pfDepthMask(True)
             lib.pfDisable(A.PF_BLEND)
@@ -331,6 +351,7 @@ class SphereScene:
     def teardown(self, lib):
         th = C.c_void_p(self.texh)
         lib.pfDeleteTexture(C.byref(th), False)
+        self._dev = None
 
     def render(self, lib, target: str = "fbo", fmt: tuple = (A.PF_RGBA, A.PF_UNSIGNED_BYTE)) -> Frame:
         tg = Target(lib, self.width, self.height, target, fmt=fmt)

@@ -218,3 +218,14 @@ def test_device_arrays_refusals(gpu):
         torch.cuda.synchronize()
     finally:
         tg.close()
+
+
+def test_sphere_device_arrays_equal_host_arrays(gpu):
+    """The 1080p sphere frame from device memory (zero-copy) and from host
+    arrays: the same image and depth, bit for bit."""
+    from pixelforge_gb300.scenes import SphereScene
+    a = SphereScene(device_arrays=True).render(gpu)
+    b = SphereScene().render(gpu)
+    assert np.array_equal(a.color, b.color)
+    assert np.array_equal(a.depth.view(np.uint32), b.depth.view(np.uint32))
+    assert a.stats["fragments"] == b.stats["fragments"] > 500000
