@@ -107,6 +107,35 @@ def test_batch_mixed_framebuffer_formats_vs_oracle(gpu, oracle):
         sc_o.destroy(oracle)
 
 
+def test_batch_bgra8_contexts_vs_oracle(gpu, oracle):
+    """A batch mixing BGRA / unsigned-byte main buffers (rasterized row by
+    row after the tile raster, several targets in one launch) with RGBA8 and
+    another format: raw pixels bit-exact against the oracle context by
+    context; a graph replay of the batch renders the same images again."""
+    fmts = ((A.PF_BGRA, A.PF_UNSIGNED_BYTE), (A.PF_RGBA, A.PF_UNSIGNED_BYTE), (A.PF_BGRA, A.PF_UNSIGNED_BYTE),
+            (A.PF_RGB, A.PF_UNSIGNED_SHORT_5_6_5))
+    sc_g = BatchScene(n=10, max_side=160, tri_clip=(100, 700), seed=35, fmts=fmts)
+    sc_o = BatchScene(n=10, max_side=160, tri_clip=(100, 700), seed=35, fmts=fmts)
+    sc_g.create(gpu)
+    sc_o.create(oracle)
+    try:
+        batch = gpu.pfgbBatchCreate()
+        try:
+            got = sc_g.render_batch(gpu, batch)
+            assert gpu.pfgbBatchReplay(batch, 2) > 0.0
+        finally:
+            gpu.pfgbBatchDelete(batch)
+        assert gpu.pfGetDeviceStatus() == 0
+        ref = sc_o.render_loop(oracle)
+        for i, (g, r) in enumerate(zip(got, ref)):
+            assert g.shape == r.shape and g.shape[2] == A.pixel_bytes(*fmts[i % len(fmts)])
+            nd = int((g != r).any(-1).sum())
+            assert nd == 0, f"context {i} {fmts[i % len(fmts)]}: {nd} pixels differ"
+    finally:
+        sc_g.destroy(gpu)
+        sc_o.destroy(oracle)
+
+
 def test_batch_replay_and_reuse(gpu):
     sc = BatchScene(n=24, max_side=192, tri_clip=(100, 2000), seed=33)
     sc.create(gpu)
