@@ -520,6 +520,61 @@ __device__ __forceinline__ bool tile_range(const TileSpace &T, const PFPrim &P, 
     return true;
 }
 
+// A triangle record's edge functions as the binning tests tiles with them:
+// w_e(x, y) = x ex_e + y ey_e + c_e (triangles.c:336-349, 398-420), set
+// only when every vertex coordinate and the box lie within (-2^13, 2^13)
+// and the framebuffer is at most 2^13 pixels a side -- there the edge
+// functions of every pixel of the box stay far inside 32 bits, where the
+// reference's wrapping arithmetic is exact (on = false otherwise, and for
+// points, lines and rectangles, which keep every tile of their box).
+struct EdgeTest {
+    int32_t ex[3], ey[3], c[3];
+    int32_t xMin, xMax, yMin, yMax;
+    bool on;
+};
+__device__ __forceinline__ EdgeTest edge_test(const PFPrim &P, uint32_t W, uint32_t H)
+{
+    EdgeTest E;
+    const int32_t L = 1 << 13;
+    const int32_t v[6] = { P.x1, P.y1, P.x2, P.y2, P.x3, P.y3 };
+    bool ok = !(P.flags & PFP_KIND) && W <= (uint32_t)L && H <= (uint32_t)L &&
+              P.xMin > -L && P.xMin < L && P.xMax > -L && P.xMax < L && P.yMin > -L && P.yMin < L && P.yMax > -L && P.yMax < L;
+    for (int k = 0; k < 6; k++) ok = ok && v[k] > -L && v[k] < L;
+    const int32_t vx[3] = { P.x2, P.x3, P.x1 }, vy[3] = { P.y2, P.y3, P.y1 };
+    const int32_t sgn = (P.flags & 1u) ? -1 : 1;
+    const int32_t sx[3] = { P.y3 - P.y2, P.y1 - P.y3, P.y2 - P.y1 }, sy[3] = { P.x2 - P.x3, P.x3 - P.x1, P.x1 - P.x2 };
+    for (int e = 0; e < 3; e++) {
+        E.ex[e] = ok ? sgn * sx[e] : 0;
+        E.ey[e] = ok ? sgn * sy[e] : 0;
+        E.c[e] = ok ? -(vx[e] * E.ex[e] + vy[e] * E.ey[e]) : 0;
+    }
+    E.xMin = P.xMin; E.xMax = P.xMax; E.yMin = P.yMin; E.yMax = P.yMax;
+    E.on = ok;
+    return E;
+}
+
+// Whether the record may cover a pixel of tile (tx, ty): no, when one of
+// its edge functions is negative on the whole rectangle where the tile and
+// the box meet -- a pixel is covered only when no edge function is negative
+// (triangles.c:415-420), and a linear function is largest at a corner.
+__device__ __forceinline__ bool tile_touched(const EdgeTest &E, uint32_t tx, uint32_t ty, uint32_t W, uint32_t H)
+{
+    if (!E.on) return true;
+    // the tile's pixels inside the box and the framebuffer (the box was
+    // found inside it by tile_range)
+    const int32_t x0 = max(E.xMin, (int32_t)(tx * PF_TILE));
+    const int32_t x1 = min(min(E.xMax, (int32_t)(tx * PF_TILE + PF_TILE)), (int32_t)W) - 1;
+    const int32_t y0 = max(E.yMin, (int32_t)(ty * PF_TILE));
+    const int32_t y1 = min(min(E.yMax, (int32_t)(ty * PF_TILE + PF_TILE - 1)), (int32_t)H - 1);
+    bool keep = true;
+    for (int e = 0; e < 3; e++) {
+        const int32_t w00 = x0 * E.ex[e] + y0 * E.ey[e] + E.c[e];
+        const int32_t hi = w00 + max((x1 - x0) * E.ex[e], 0) + max((y1 - y0) * E.ey[e], 0);
+        keep = keep && hi >= 0;
+    }
+    return keep;
+}
+
 __device__ __forceinline__ void bin_slot(const BinArgs &B, uint32_t t, uint32_t slot, uint32_t key)
 {
     if (slot < B.cap) B.bins[(size_t)t * B.cap + slot] = key;
@@ -557,8 +612,10 @@ __device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, 
 {
     uint32_t tx0, ty0, ntx, nty;
     if (!tile_range(T, P, tx0, ty0, ntx, nty)) return;
+    const EdgeTest ET = edge_test(P, T.W, T.H);
     for (uint32_t ty = ty0; ty < ty0 + nty; ty++)
         for (uint32_t tx = tx0; tx < tx0 + ntx; tx++) {
+            if (!tile_touched(ET, tx, ty, T.W, T.H)) continue;
             const uint32_t t = T.tileBase + ty * T.tilesX + tx;
             const uint32_t slot = atomicAdd(&B.binCount[t], 1u);
             list_tile(B, t, slot, 1u);
@@ -593,13 +650,27 @@ __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, co
         // the tile space of that lane's framebuffer (the lanes of a batch's
         // warp may draw into different ones)
         const uint32_t wbase = __shfl_sync(0xffffffffu, T.tileBase, src), wtx = __shfl_sync(0xffffffffu, T.tilesX, src);
+        const uint32_t wW = __shfl_sync(0xffffffffu, T.W, src), wH = __shfl_sync(0xffffffffu, T.H, src);
+        EdgeTest wb;
+        {
+            const EdgeTest mine = edge_test(P, T.W, T.H);
+            for (int e = 0; e < 3; e++) {
+                wb.ex[e] = __shfl_sync(0xffffffffu, mine.ex[e], src);
+                wb.ey[e] = __shfl_sync(0xffffffffu, mine.ey[e], src);
+                wb.c[e] = __shfl_sync(0xffffffffu, mine.c[e], src);
+            }
+            wb.xMin = __shfl_sync(0xffffffffu, mine.xMin, src); wb.xMax = __shfl_sync(0xffffffffu, mine.xMax, src);
+            wb.yMin = __shfl_sync(0xffffffffu, mine.yMin, src); wb.yMax = __shfl_sync(0xffffffffu, mine.yMax, src);
+            wb.on = __shfl_sync(0xffffffffu, (int)mine.on, src) != 0;
+        }
         for (uint32_t i0 = 0; i0 < wn; i0 += 32u * BIN_BURST) {
             uint32_t tt[BIN_BURST], bb[BIN_BURST];
 #pragma unroll
             for (int u = 0; u < BIN_BURST; u++) {
                 const uint32_t i = i0 + 32u * (uint32_t)u + lane;
-                tt[u] = i < wn ? wbase + (wy0 + i / wnx) * wtx + (wx0 + i % wnx) : 0xffffffffu;
-                bb[u] = i < wn ? atomicAdd(&B.binCount[tt[u]], 1u) : 0u;
+                const bool hit = i < wn && tile_touched(wb, wx0 + i % wnx, wy0 + i / wnx, wW, wH);
+                tt[u] = hit ? wbase + (wy0 + i / wnx) * wtx + (wx0 + i % wnx) : 0xffffffffu;
+                bb[u] = hit ? atomicAdd(&B.binCount[tt[u]], 1u) : 0u;
             }
 #pragma unroll
             for (int u = 0; u < BIN_BURST; u++) {
@@ -610,6 +681,7 @@ __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, co
         }
     }
     if (n > BIN_WIDE) n = 0;
+    const EdgeTest ET = edge_test(P, T.W, T.H);
     uint32_t most = n;
     for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
     for (uint32_t i0 = 0; i0 < most; i0 += BIN_BURST) {
@@ -619,7 +691,7 @@ __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, co
             const uint32_t i = i0 + (uint32_t)u;
             tt[u] = 0xffffffffu; gg[u] = 0; bb[u] = 0;
             if (i >= most) continue;                           // uniform over the warp
-            const bool act = i < n;
+            const bool act = i < n && tile_touched(ET, tx0 + i % ntx, ty0 + i / ntx, T.W, T.H);
             const uint32_t t = act ? T.tileBase + (ty0 + i / ntx) * T.tilesX + (tx0 + i % ntx) : 0xffffffffu;
             const uint32_t grp = __match_any_sync(0xffffffffu, t);
             tt[u] = t; gg[u] = grp;
@@ -631,7 +703,7 @@ __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, co
             if (i >= most) continue;
             const uint32_t grp = gg[u], leader = (uint32_t)(__ffs(grp) - 1);
             const uint32_t base = __shfl_sync(0xffffffffu, bb[u], leader);
-            if (i >= n) continue;
+            if (tt[u] == 0xffffffffu) continue;
             if (lane == leader) list_tile(B, tt[u], base, (uint32_t)__popc(grp));
             bin_slot(B, tt[u], base + __popc(grp & lt), key);
         }
