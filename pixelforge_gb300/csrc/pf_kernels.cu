@@ -972,7 +972,7 @@ __device__ __forceinline__ bool item_setup(const PFSegment &sg, const PFDrawStat
     if (S.flags & PFS_PHONG) store_phong(&O.primsPh[g], s[0], s[1], s[2]);
     return true;
 }
-__global__ void __launch_bounds__(128, 8) k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
+__global__ void __launch_bounds__(128, 6) k_items(const PFSegment *__restrict__ segs, int nSegs, const PFDrawState *__restrict__ states,
                         const PFVertexOut *__restrict__ vout, uint32_t nItems, ItemOut O, BinArgs B)
 {
     __shared__ int sUniform, sAborted;
