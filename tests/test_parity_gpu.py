@@ -123,6 +123,50 @@ def test_feature_mix_bgra(gpu, oracle, seed):
         assert got.stats["fragments"] == ref.stats["fragments"]
 
 
+@pytest.mark.parametrize("case", ["far_vertices", "wide_framebuffer", "slivers"])
+def test_binning_tile_test_edges(gpu, oracle, case):
+    """The binning leaves out the tiles of a box where an edge function is
+    negative on the whole tile, only where coordinates stay within 2^13:
+    triangles whose vertices lie tens of thousands of pixels off screen
+    (the 2D path, boxes clamped to the viewport: the test is off), a
+    framebuffer 9,000 pixels wide (off), and long slivers crossing many
+    tiles (on): colour and depth bit-exact, fragment counts equal."""
+    from pixelforge_gb300.scenes import Target
+    W, H = (9000, 40) if case == "wide_framebuffer" else (300, 200)
+    seed = {"far_vertices": 41, "wide_framebuffer": 42, "slivers": 43}[case]
+    outs = []
+    for lib in (gpu, oracle):
+        tg = Target(lib, W, H, "fbo")
+        try:
+            lib.pfDisable(A.PF_CULL_FACE)
+            lib.pfEnable(A.PF_DEPTH_TEST)
+            lib.pfClearDepth(1e30)
+            lib.pfClear(A.PF_COLOR_BUFFER_BIT | A.PF_DEPTH_BUFFER_BIT)
+            rr = np.random.default_rng(seed)
+            lib.pfBegin(A.PF_TRIANGLES)
+            for k in range(300):
+                lib.pfColor4ub(*[int(v) for v in rr.integers(0, 256, 3)], 255)
+                if case == "far_vertices":
+                    pts = rr.uniform(-120.0, 120.0, (3, 2))          # up to ~18,000 pixels off screen
+                    pts[rr.integers(3)] = rr.uniform(-1.0, 1.0, 2)  # one vertex on screen
+                elif case == "slivers":
+                    a = rr.uniform(-1.2, 1.2, 2)
+                    b = rr.uniform(-1.2, 1.2, 2)
+                    pts = np.stack([a, b, b + rr.uniform(-0.02, 0.02, 2)])
+                else:
+                    pts = rr.uniform(-1.1, 1.1, (3, 2))
+                for p in pts:
+                    lib.pfVertex3f(float(p[0]), float(p[1]), float(rr.uniform(-0.9, 0.9)))
+            lib.pfEnd()
+            outs.append(tg.finish())
+        finally:
+            tg.close()
+    got, ref = outs
+    assert (ref.depth < 1e30).sum() > 1000
+    assert_parity(got, ref, exact_color=True, label=case)
+    assert got.stats["fragments"] == ref.stats["fragments"]
+
+
 def test_bgra8_wide_rows(gpu, oracle):
     """A BGRA / unsigned-byte framebuffer wider than the rows k_rows keeps
     in shared memory (2,600 pixels: drawn in place), blended soup with
