@@ -865,7 +865,8 @@ static void raster_tri(RCtx *c, PFface face, int is3D, const RVert *v1, const RV
     const int phong = (c->state & PF_LIGHTING) && c->lightMode == PF_PHONG && c->nActive > 0;
     const RMat *fm = &c->mat[face];
     const int smooth = c->shade == PF_SMOOTH;
-    const long area_bb = (long)(yMax - yMin) * (long)(xMax - xMin);
+    const long area_bb = (long)(yMax - yMin) * (long)(xMax - xMin);   /* (OpenMP threshold) */
+    (void)area_bb;
     uint64_t frags = 0;
     const TriFrag sh = { c, is3D, v1, v2, v3, viewPos, c1, c2, c3, tex, phong, fm, smooth };
 

@@ -1347,7 +1347,7 @@ void lp_thin_line(LPOut &o, float sx1, float sy1, float sx2, float sy2, const LP
     PFPrim P;
     std::memset(&P, 0, sizeof P);
     P.x1 = x1; P.y1 = y1; P.x2 = endVal; P.y2 = decInc; P.x3 = sgnInc;
-    P.flags = PFP_LINE | ops | (yLonger ? PFP_Y_LONGER : 0u);
+    P.flags = (uint32_t)PFP_LINE | ops | (yLonger ? (uint32_t)PFP_Y_LONGER : 0u);
     P.wInvSum = invEndVal;
     P.z1 = a.h[2]; P.z2 = b.h[2];
     P.c1 = a.col; P.c2 = b.col;
