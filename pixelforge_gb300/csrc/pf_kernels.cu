@@ -631,7 +631,7 @@ __device__ void bin_prim(const BinArgs &B, const TileSpace &T, const PFPrim &P, 
 // BIN_WIDE tiles is binned by the whole warp, 32 of its tiles at a time.
 // Every lane of the warp must call it (lanes with nothing to bin pass
 // has = false).
-#define BIN_BURST 8
+#define BIN_BURST 4
 #define BIN_WIDE 32
 __device__ void bin_prim_warp(const BinArgs &B, const TileSpace &T, bool has, const PFPrim &P, uint32_t key)
 {
